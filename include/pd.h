@@ -1,0 +1,261 @@
+/*
+ * pd.h — C ABI of the GB300 peridynamics engine (libpd_gb300.so).
+ *
+ * The reference (XiaoMmingW/PD_Gpu1) exposes no plugin layer: its operator API
+ * is a set of free host launchers over raw SoA device pointers plus a global
+ * `__constant__ device_parameter dp` (Base.cuh:46-70).  This header replaces
+ * those launchers one for one with status-returning entry points over an
+ * opaque context that owns the device memory.  Every entry point cites the
+ * reference interface it replaces.
+ *
+ * Conventions
+ *   - All floating point is FP64 (the reference built with -DDOUBLE_PRECISION).
+ *   - Node fields are indexed in the reference's node order; bond fields are in
+ *     CSR order: row i holds the bond family of node i sorted by ascending
+ *     neighbour id, which is exactly the row order of the reference's CPU
+ *     neighbour list (Neighbor.cu:42-80).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Every call returns PD_OK (0) or a negative PD_ERR_* code; nothing exits
+ *     the process (the reference's CHECK macro calls exit(1), Error.cuh:9-23).
+ *   - One context per host thread at a time; contexts are independent.
+ */
+#ifndef PD_GB300_H
+#define PD_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define PD_OK 0
+#define PD_ERR_ARG -1           /* bad argument (null pointer, bad size, bad enum)   */
+#define PD_ERR_CUDA -2          /* a CUDA runtime call failed (see pd_last_error)    */
+#define PD_ERR_STATE -3         /* call out of order (e.g. force before neighbours)  */
+#define PD_ERR_FAMILY -4        /* a node has more than MN neighbours (ELL overflow)  */
+#define PD_ERR_NONFINITE -5     /* NaN/Inf found by pd_check_finite                   */
+#define PD_ERR_NOMEM -6         /* device allocation failed                           */
+#define PD_ERR_TIMEOUT -7       /* a bounded device-side wait gave up                 */
+#define PD_ERR_UNSUPPORTED -8   /* combination not implemented (e.g. 1-D models)      */
+
+/* ---- enums ------------------------------------------------------------- */
+/* Dselect::B_S (Base.cuh:35-43) */
+#define PD_MODEL_BOND 1   /* bond-based prototype micro-elastic brittle (PMB) */
+#define PD_MODEL_STATE 2  /* ordinary state-based (LPS)                       */
+/* Dselect::Mode */
+#define PD_MODE_STATIC 1  /* quasi-static, adaptive dynamic relaxation (ADR) */
+#define PD_MODE_DYNAMIC 2 /* explicit velocity-Verlet                         */
+
+/* Field identifiers for pd_get_field / pd_set_field / pd_field_ptr.
+ * Node fields hold N doubles per component (x, y[, z] stored as separate
+ * arrays, like BAtom, Base.cuh:186-225); bond fields hold B entries. */
+typedef enum pd_field {
+    PD_F_X = 0, PD_F_Y, PD_F_Z,                  /* reference coordinates          */
+    PD_F_UX, PD_F_UY, PD_F_UZ,                   /* displacement disp_*            */
+    PD_F_VX, PD_F_VY, PD_F_VZ,                   /* velocity vel_*                 */
+    PD_F_AX, PD_F_AY, PD_F_AZ,                   /* acceleration acc_*             */
+    PD_F_FX, PD_F_FY, PD_F_FZ,                   /* peridynamic force pforce_*     */
+    PD_F_BX, PD_F_BY, PD_F_BZ,                   /* body force bforce_*            */
+    PD_F_VHX, PD_F_VHY, PD_F_VHZ,                /* ADR velhalfold_*               */
+    PD_F_FOX, PD_F_FOY, PD_F_FOZ,                /* ADR pforceold_*                */
+    PD_F_DMG,                                    /* damage dmg                     */
+    PD_F_M, PD_F_THETA,                          /* state-based m, theta           */
+    PD_F_FNCST_X, PD_F_FNCST_Y, PD_F_FNCST_Z,    /* surface-correction factors     */
+    /* integer node field */
+    PD_F_NN,                                     /* family size NN (int32)         */
+    /* bond fields (CSR order) */
+    PD_F_ROWPTR,                                 /* int64[N+1]                     */
+    PD_F_NL,                                     /* neighbour id, int32[B]         */
+    PD_F_IDIST,                                  /* |xi|, double[B]                */
+    PD_F_FAC,                                    /* volume correction, double[B]   */
+    PD_F_SCR,                                    /* surface correction, double[B]  */
+    PD_F_W,                                      /* influence w, double[B]         */
+    PD_F_E,                                      /* extension e, double[B]         */
+    PD_F_FAIL,                                   /* 1 intact / 0 broken, int32[B]  */
+    PD_F_COUNT
+} pd_field;
+
+/* ---- parameters -------------------------------------------------------- */
+/* The first block mirrors device_parameter (Base.cuh:46-68) field for field;
+ * the rest carries what the reference keeps in Dselect, BaseModel_Parameter
+ * or hard-codes in its kernels. */
+typedef struct pd_params {
+    double pi;
+    int32_t N, MN, N_int, nx, ny, nz;
+    double dx, emod, dens, pratio, bc, delta, critical_s, vol, dt;
+    int32_t nt;
+    int32_t dim;          /* Dselect::Dim: 2 or 3 */
+    double mass, K, G;
+    /* extensions */
+    int32_t model;        /* PD_MODEL_*  (Dselect::B_S)  */
+    int32_t mode;         /* PD_MODE_*   (Dselect::Mode) */
+    double thick, length, height, width, load;
+    double sedload;       /* surface-correction test energy: 2-D 0.5E/(1-v^2)1e-6 (Surf_Corr.cu:238), 3-D 0.6E1e-6 (:280) */
+    double break_ymin;    /* 3-D bonds break only when both ends have y >= break_ymin
+                             (Force_Bond.cu:117, Force_State.cu:280 hard-code -0.04); -1e300 disables */
+} pd_params;
+
+/* BaseModel_Parameter::cal_parameter (Base.cuh:114-183) + initialil_parameter
+ * (Base_Function.cu:14-36): derive N, MN, nx, ny, nz, delta, bc, vol, mass, K, G
+ * from the driver inputs.  fix_k3d=0 keeps the reference's 3-D state-based bulk
+ * modulus K = E/3/(1-2G) (Base.cuh:175); fix_k3d=1 uses K = E/(3(1-2v)). */
+int pd_params_derive(pd_params* p, int dim, int model, int mode, double dt, double nt, double dx,
+                     double load, double thick, double length, double height, double width,
+                     double emod, double pratio, double dens, double critical_s, int fix_k3d);
+
+/* ---- context ----------------------------------------------------------- */
+typedef struct pd_ctx pd_ctx;
+
+/* Base_Allocate (Memory.cu:139-147): allocates every node field for p->N nodes.
+ * Bond storage is allocated by pd_find_neighbor once the family size is known. */
+pd_ctx* pd_create(const pd_params* p, int* status);
+/* Base_Free (Memory.cu:276-284, which re-allocates instead of freeing). */
+int pd_destroy(pd_ctx* ctx);
+int pd_get_params(const pd_ctx* ctx, pd_params* out);
+/* Replace the parameters (same N/dim); cudaMemcpyToSymbol(dp, ...) of the drivers. */
+int pd_set_params(pd_ctx* ctx, const pd_params* p);
+const char* pd_last_error(const pd_ctx* ctx);
+const char* pd_status_string(int status);
+
+/* Copy a field between host memory and the context (count elements, checked
+ * against the field's size).  Replaces the cudaMemcpy calls of Save.cu and
+ * of the drivers' setup (Solve_Kalthoff_Winkler.cu:381-383). */
+int pd_get_field(pd_ctx* ctx, int field, void* host, size_t count, void* stream);
+int pd_set_field(pd_ctx* ctx, int field, const void* host, size_t count, void* stream);
+/* Device pointer and element count of a field (for zero-copy interop). */
+int pd_field_ptr(pd_ctx* ctx, int field, void** dev, size_t* count);
+/* Number of directed bonds B (0 before pd_find_neighbor). */
+int64_t pd_num_bonds(const pd_ctx* ctx);
+/* Wait for all work on the stream. */
+int pd_sync(pd_ctx* ctx, void* stream);
+
+/* ---- geometry (Coord.cu) ----------------------------------------------- */
+/* kernel_Initial_coord_plate / Initial_coord_plate_cpu (Coord.cu:6-28). */
+int pd_coord_plate(pd_ctx* ctx, void* stream);
+/* kernel_coord_plate_crack / coord_plate_crack_cpu (Coord.cu:34-66):
+ * interior rows, then 3 rows above and 3 rows below stored after N_int. */
+int pd_coord_plate_crack(pd_ctx* ctx, void* stream);
+/* coord_KW (Coord.cu:77-129): host-side generator for the notched slab.  Writes
+ * up to `cap` nodes into x,y,z (host arrays) and returns the node count in *n. */
+int pd_coord_kw(const pd_params* p, double rad, double* x, double* y, double* z, int64_t cap, int64_t* n);
+
+/* ---- neighbour family (Neighbor.cu) ------------------------------------ */
+/* find_neighbor_gpu (Neighbor.cu:82-90), kernel_find_neighbor_2D/3D (:7-40):
+ * cell-list build of the bond family |xj-xi|^2 < delta^2 into CSR, each row
+ * sorted ascending.  Also allocates all bond arrays and sets every fail flag
+ * to 1 (kernel_initial_fail, Initial.cu:6-14).  Returns PD_ERR_FAMILY if a
+ * row exceeds p->MN (the reference's ELL would overflow, Neighbor.cu:18). */
+int pd_find_neighbor(pd_ctx* ctx, void* stream);
+
+/* ---- setup passes ------------------------------------------------------ */
+/* kernel_vol_Corr (Surf_Corr.cu:7-35): idist and fac per bond. */
+int pd_vol_corr(pd_ctx* ctx, void* stream);
+/* surface_correct_gpu (Surf_Corr.cu:235-310): vol_Corr + per-axis strain
+ * energy factors fncst + per-bond scr, fused into two kernels. */
+int pd_surface_correct(pd_ctx* ctx, void* stream);
+/* kernel_initial_weight_2D/3D (Force_State.cu:8-54): w per bond, m per node. */
+int pd_initial_weight(pd_ctx* ctx, void* stream);
+/* kernel_set_crack_2D (Base_Function.cu:39-81): cut bonds crossing a segment
+ * of length clength centred at (loc_x, loc_y) at angle theta (radians). */
+int pd_set_crack_2d(pd_ctx* ctx, double clength, double loc_x, double loc_y, double theta, void* stream);
+/* kernel_set_crack (Solve_Kalthoff_Winkler.cu:40-63): notch cut at x = +-rad. */
+int pd_set_crack_kw(pd_ctx* ctx, double rad, void* stream);
+/* base_integrate_initial_gpu / static_initial_bond_gpu (Initial.cu:24-75):
+ * zero disp, vel, acc, bforce, pforce (+ ADR state). */
+int pd_initial_state(pd_ctx* ctx, void* stream);
+/* Build the per-bond coefficients the force kernels read (from idist, fac,
+ * scr, w, m).  Called implicitly by the first force call after setup changes. */
+int pd_prepare(pd_ctx* ctx, void* stream);
+
+/* ---- forces ------------------------------------------------------------ */
+/* bond_force_2D_gpu / bond_force_3D_gpu (Force_Bond.cu:143-157);
+ * kernel_particle_force_2D (:52-85), kernel_bond_force_3D (:87-141):
+ * PMB force density on nodes [0, N_int) and breakage s > critical_s. */
+int pd_bond_force(pd_ctx* ctx, void* stream);
+/* kernel_cal_theta_2D/3D + kernel_state_force_2D/3D (Force_State.cu:56-134,
+ * :203-306): dilatation on all N nodes, force and breakage on [0, N_int). */
+int pd_state_force(pd_ctx* ctx, void* stream);
+
+/* ---- integration and reductions (Integrate.cu, Reduce.cu) -------------- */
+/* static_integrate_gpu (Integrate.cu:130-172): kernel_cnn + cal_cn + kernel_integrate.
+ * The damping coefficient stays on the device (no host sync). ct is the step index. */
+int pd_integrate_adr(pd_ctx* ctx, int ct, void* stream);
+/* Last damping coefficient cn (Integrate.cu:108-129), copied to the host (syncs). */
+int pd_get_adr_cn(pd_ctx* ctx, double* cn, void* stream);
+/* kernel_integrate_2D_1 / 3D_1 (Integrate.cu:174-216): v += dt/2 a; u += v dt. */
+int pd_integrate_verlet1(pd_ctx* ctx, void* stream);
+/* kernel_integrate_2D_2 / 3D_2 (Integrate.cu:218-266): a = (F+b)/rho; v += dt/2 a. */
+int pd_integrate_verlet2(pd_ctx* ctx, void* stream);
+/* sum (Reduce.cu:52-65): sum of n doubles of a device array into *result
+ * (host).  Deterministic order. */
+int pd_reduce_sum(pd_ctx* ctx, const double* dev_x, int64_t n, double* result, void* stream);
+
+/* ---- damage, loads, contact ------------------------------------------- */
+/* kernel_cal_dmg_2D/3D (Base_Function.cu:149-217). */
+int pd_damage(pd_ctx* ctx, void* stream);
+/* kernel_quick_load (Solve_Plate_Crack_Grow.cu:8-19): boundary rows after
+ * N_int move by +-load*dt in y. */
+int pd_quick_load(pd_ctx* ctx, double load, void* stream);
+/* load_plate_tensile_gpu (Solve_Plate_Tensile.cu:7-17): bforce_x = -+0.001E/dx
+ * on the left and right columns. */
+int pd_load_plate_tensile(pd_ctx* ctx, void* stream);
+
+/* Rigid cylindrical impactor of the Kalthoff-Winkler driver
+ * (Cylinder_Parameter, Base.cuh:227-246). */
+typedef struct pd_cylinder {
+    double rad, mass, height, v, x, y, z;
+    double vel[3], disp[3], acc[3], force[3];
+} pd_cylinder;
+/* kernel_initial_cylinder (Solve_Kalthoff_Winkler.cu:9-22). */
+int pd_cylinder_init(pd_ctx* ctx, const pd_cylinder* cyl, void* stream);
+int pd_cylinder_get(pd_ctx* ctx, pd_cylinder* cyl, void* stream);
+/* kernel_cy_integrate_1 (Solve_Kalthoff_Winkler.cu:89-99). */
+int pd_cylinder_integrate1(pd_ctx* ctx, void* stream);
+/* kernel_contact (Solve_Kalthoff_Winkler.cu:112-175): project penetrating
+ * nodes onto the cylinder, reaction force summed on the device. */
+int pd_contact(pd_ctx* ctx, void* stream);
+/* kernel_cy_integrate_2 (Solve_Kalthoff_Winkler.cu:242-253). */
+int pd_cylinder_integrate2(pd_ctx* ctx, void* stream);
+
+/* ---- fused time stepping ---------------------------------------------- */
+/* Per-step body of solve_plate_tensile's loop (Solve_Plate_Tensile.cu:106-131)
+ * for nsteps ADR steps starting at step index ct0: force + damping + update,
+ * two kernels per step, optionally with boundary-row loading (load != 0:
+ * rows after N_int move by +-load*dt per step), captured in a CUDA graph. */
+int pd_run_adr(pd_ctx* ctx, int ct0, int nsteps, double load, void* stream);
+/* Per-step body of the explicit drivers (Solve_Plate_Crack_Grow.cu:126-163,
+ * Solve_Kalthoff_Winkler.cu:407-432) for nsteps steps: [quick_load(load)] +
+ * Verlet + force (bond- or state-based by p->model) [+ contact when a
+ * cylinder is installed], captured in a CUDA graph.  When dmg_every > 0 the
+ * damage field is refreshed every dmg_every steps. */
+int pd_run_explicit(pd_ctx* ctx, int nsteps, double load, int dmg_every, void* stream);
+
+/* ---- drivers (Solve_*.cuh:17-19) --------------------------------------- */
+typedef struct pd_result {
+    int64_t N, N_int, B;
+    double setup_ms;      /* neighbour + setup passes          */
+    double loop_ms;       /* time-step loop (CUDA events)      */
+    double bond_updates_per_s;
+} pd_result;
+/* solve_plate_tensile (Solve_Plate_Tensile.cu:30-138) with dx (<=1e-8 -> 0.01).
+ * Host arrays ux, uy, dmg (N_int each) receive the final fields when non-NULL. */
+int pd_solve_plate_tensile(double dx, int nt, double* ux, double* uy, double* dmg, pd_result* res);
+/* solve_plate_crack_grow (Solve_Plate_Crack_Grow.cu:167-308). */
+int pd_solve_plate_crack_grow(double dx, int nt, double* ux, double* uy, double* dmg, pd_result* res);
+/* solve_kalthoff_winkler (Solve_Kalthoff_Winkler.cu:268-441); the reference
+ * runs nt=0 steps, this takes nt. Arrays hold N entries (see res->N). */
+int pd_solve_kalthoff_winkler(double dx, int nt, double* ux, double* uy, double* uz, double* dmg,
+                              int64_t cap, pd_result* res);
+
+/* ---- diagnostics ------------------------------------------------------- */
+/* NaN/Inf scan of displacement and force; PD_ERR_NONFINITE if any. */
+int pd_check_finite(pd_ctx* ctx, void* stream);
+/* Number of GPU kernels this context has launched (for launch accounting). */
+int64_t pd_kernel_launches(const pd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PD_GB300_H */
