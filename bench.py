@@ -1,0 +1,411 @@
+"""Benchmark: bond-updates/s of the peridynamics step loop on GB300.
+
+Default workload: the 1.6M-node dynamic crack-branching plate (2-D PMB,
+explicit Verlet, FP64, damage field every 100 steps).  A "step" is one time
+step (force + breakage + Verlet) over the whole plate; the metric is
+B_initial * steps / loop time, where B_initial is the number of directed bonds
+of the force-computed nodes (broken bonds still count: both implementations
+visit them).  Setup (neighbour build, surface correction) is timed separately.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload crack_branching|plate_tensile|kalthoff_winkler|crack_grow]
+
+--impl reference times the oracle's OpenMP host loop (the reference's
+formulas, its padded-ELL layout) on all host cores, on a bounded sample of the
+same workload.  Under torchrun (N > 1) every rank runs an independent replica
+(the workload does not shard); value is the sum over ranks, timed as the max.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+ALG_BYTES_PER_BOND_2D = 12.125  # int32 neighbour + one FP64 coefficient + one fail bit
+ALG_BYTES_PER_NODE_2D = 48.0    # read x, y, ux, uy; write fx, fy
+ALG_BYTES_PER_BOND_3D = 12.125
+ALG_BYTES_PER_NODE_3D = 72.0
+ALG_FP64_PER_BOND_2D = 23       # 10 add/sub, 8 mul, 3 div, 1 sqrt, 1 compare (sqrt/div counted once)
+ALG_FP64_PER_BOND_3D = 31
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def build_workload(name, scale, host_only=False):
+    """Parameters, engine set-up and metadata of a named workload.  With
+    host_only the parameters come from the oracle's derivation (bit-identical,
+    pinned by tests) so the CPU arm never loads the CUDA library."""
+    from pd_gpu1_gb300 import presets
+
+    kw = {}
+    if host_only:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        kw = {"derive": orc.derive_params}
+    if name == "crack_branching":
+        return presets.build_crack_branching(scale=scale, **kw)
+    if name == "plate_tensile":
+        return presets.build_plate_tensile(scale=scale, **kw)
+    if name == "kalthoff_winkler":
+        if host_only:
+            kw["coord_fn"] = orc.coord_kw
+        return presets.build_kalthoff_winkler(scale=scale, **kw)
+    if name == "crack_grow":
+        return presets.build_crack_grow(scale=scale, **kw)
+    raise SystemExit(f"unknown workload {name}")
+
+
+def run_steps(eng, meta, k, ct0=0):
+    if meta["workload"].startswith("plate_tensile"):
+        eng.run_adr(ct0, k, load=meta["load"])
+    else:
+        eng.run_explicit(k, load=meta["load"], dmg_every=meta.get("dmg_every", 0))
+
+
+# ----------------------------------------------------------------------------------------------
+def cpu_reference(p, meta, eng_coords, max_seconds, max_steps, threads):
+    """The oracle on the host cores: setup, then timed steps until max_seconds
+    or max_steps.  Returns (bond-updates/s, steps, seconds, bonds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    orc.set_threads(threads)
+    x, y, z = eng_coords
+    m = orc.Model(p, x, y, z)
+    m.find_neighbor(brute=False)
+    w = meta["workload"]
+    if w.startswith("crack_branching"):
+        m.surface_correct()
+        m.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
+        from pd_gpu1_gb300.presets import traction_field
+
+        m.by[:] = traction_field(p, meta["sigma"])
+    elif w.startswith("plate_tensile"):
+        m.surface_correct()
+    elif w.startswith("kalthoff"):
+        m.vol_corr()
+        m.initial_weight()
+        m.set_crack_kw(meta["rad"])
+    else:
+        m.set_crack_2d(0.01 * p.length / 0.05, 0.0, 0.0, 0.0)
+        m.vol_corr()
+        m.initial_weight()
+    bonds = int(m.NN[: p.N_int].sum())
+    cyl = None
+    if w.startswith("kalthoff"):
+        c = meta["cylinder"]
+        cyl = orc.new_cylinder(c.rad, c.mass, c.height, c.v, c.x, c.y, c.z)
+    t0 = time.perf_counter()
+    n = 0
+    while n < max_steps:
+        if w.startswith("plate_tensile"):
+            m.quick_load(meta["load"])
+            m.adr_step(n)
+        else:
+            m.explicit_step(load=meta["load"], cyl=cyl)
+            if meta.get("dmg_every") and (n + 1) % meta["dmg_every"] == 0:
+                m.damage()
+        n += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return bonds * n / dt, n, dt, bonds
+
+
+def reference_arm(args):
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return 0
+    p, setup, meta = build_workload(args.workload, args.scale, host_only=True)
+    coords = host_coords(p, meta)
+    threads = os.cpu_count() or 1
+    # warm-up: a short sample; then the timed sample bounded to ~60 s
+    rate, steps, secs, bonds = cpu_reference(p, meta, coords, max_seconds=min(60.0, 2.0 + 4.0 * args.steps),
+                                             max_steps=args.warmup + args.steps, threads=threads)
+    line = {
+        "impl": "reference", "metric": "bond-updates/s", "value": rate, "unit": "bond-updates/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs / steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (deterministic lattice)",
+        "config": {"workload": meta["workload"], "nodes": p.N, "bonds": bonds, "dx": p.dx},
+        "cpu_baseline": {"value": rate, "unit": "bond-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{steps} time steps of the full {meta['workload']} plate ({p.N} nodes), "
+                                   f"{secs:.1f} s; OpenMP restatement of the reference's loops"},
+        "e2e": {"value": rate, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def host_coords(p, meta):
+    """Node coordinates of the workload, computed on the host (same formulas as the engine)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    w = meta["workload"]
+    if w.startswith("crack_branching"):
+        x, y = orc.plate_coords(p)
+        return x, y, None
+    if w.startswith("plate_tensile") or w.startswith("plate_crack"):
+        x, y = orc.plate_crack_coords(p)
+        return x, y, None
+    return meta["coords"]
+
+
+# ----------------------------------------------------------------------------------------------
+def gb300_arm(args):
+    import ctypes as C
+
+    import torch
+
+    rank, world, local = rank_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from pd_gpu1_gb300 import engine as E
+    from pd_gpu1_gb300._lib import lib
+
+    p, setup, meta = build_workload(args.workload, args.scale)
+    stream = torch.cuda.Stream()
+    eng = E.Engine(p, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        setup(eng)
+        eng.sync()
+    setup_s = time.perf_counter() - t0
+    B = int(eng.get("ROWPTR")[p.N_int])
+    is3d = p.dim == 3
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # warm-up
+    with torch.cuda.stream(stream):
+        run_steps(eng, meta, args.warmup)
+    barrier()
+    launches0 = eng.kernel_launches
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    with torch.cuda.stream(stream):
+        run_steps(eng, meta, args.steps, ct0=args.warmup)
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = eng.kernel_launches - launches0
+    ms_max = ms
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = world * B * args.steps / (ms_max * 1e-3)
+
+    # dominant kernel alone: a graph of force launches only (no damage pass)
+    kern_steps = min(100, max(10, args.steps))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        if meta["workload"].startswith("plate_tensile"):
+            eng.run_adr(1, kern_steps, load=meta["load"])
+            e0.record(stream)
+            eng.run_adr(1, kern_steps, load=meta["load"])
+            e1.record(stream)
+        else:
+            eng.run_explicit(kern_steps, load=meta["load"], dmg_every=0)
+            e0.record(stream)
+            eng.run_explicit(kern_steps, load=meta["load"], dmg_every=0)
+            e1.record(stream)
+    torch.cuda.synchronize()
+    kern_ms = e0.elapsed_time(e1) / kern_steps
+    alg_bytes = (ALG_BYTES_PER_NODE_3D if is3d else ALG_BYTES_PER_NODE_2D) * p.N_int + \
+        (ALG_BYTES_PER_BOND_3D if is3d else ALG_BYTES_PER_BOND_2D) * B
+    peaks, peak_kind = measured_peaks()
+    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    gfma = C.c_double()
+    lib().pd_probe_fp64(C.byref(gfma))
+    fp64_peak_tflops = 2.0 * gfma.value / 1e3
+    alg_flops = (ALG_FP64_PER_BOND_3D if is3d else ALG_FP64_PER_BOND_2D) * B
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            tr = json.load(f).get(meta["workload"])
+        if tr:
+            traffic = tr["bytes_per_bond"] * B + tr["bytes_per_node"] * p.N_int
+
+    # end to end through the C ABI with host buffers: the initial state and the
+    # loading go up from pinned host memory, the damage field comes back at
+    # every dump and the displacement field at the end, all inside the timed
+    # region (pd_set_field / pd_get_field, which block on their copies)
+    L = lib()
+    from pd_gpu1_gb300._abi import FIELD
+
+    n = p.N
+    names_up = ["UX", "UY", "VX", "VY", "BX", "BY"]
+    pin = {k: torch.zeros(n, dtype=torch.float64).pin_memory() for k in names_up + ["DMG"]}
+    if meta["workload"].startswith("crack_branching"):
+        from pd_gpu1_gb300.presets import traction_field
+
+        pin["BY"].copy_(torch.from_numpy(traction_field(p, meta["sigma"])))
+    else:
+        pin["BX"].copy_(torch.from_numpy(eng.get("BX")))
+        pin["BY"].copy_(torch.from_numpy(eng.get("BY")))
+    eng.initial_state()
+    if meta["workload"].startswith("crack_branching"):
+        eng.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
+    barrier()
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for k in names_up:
+        eng._c(L.pd_set_field(eng.ctx, FIELD[k], pin[k].data_ptr(), n, eng.stream), "pd_set_field")
+        h2d += n * 8
+    every = meta.get("dmg_every") or args.steps
+    done = 0
+    while done < args.steps:
+        k_run = min(every, args.steps - done)
+        run_steps(eng, meta, k_run, ct0=done)
+        done += k_run
+        if meta.get("dmg_every"):
+            eng._c(L.pd_get_field(eng.ctx, FIELD["DMG"], pin["DMG"].data_ptr(), n, eng.stream), "pd_get_field")
+            d2h += n * 8
+    for k in ["UX", "UY"]:
+        eng._c(L.pd_get_field(eng.ctx, FIELD[k], pin[k].data_ptr(), n, eng.stream), "pd_get_field")
+        d2h += n * 8
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world * B * args.steps / e2e_s, "unit": "bond-updates/s",
+           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, steps, secs, bonds = cpu_reference(p, meta, host_coords(p, meta), max_seconds=args.cpu_seconds,
+                                                 max_steps=100000, threads=os.cpu_count() or 1)
+        cpu = {"value": rate, "unit": "bond-updates/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{steps} time steps of the same {p.N}-node plate ({secs:.1f} s of host time), "
+                         f"the oracle's OpenMP loops"}
+
+    if rank == 0:
+        line = {
+            "metric": "bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (deterministic lattice, seeded nothing: the geometry fixes every input)",
+            "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "dt": p.dt,
+                       "parallelism": "replicas" if world > 1 else "single",
+                       "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 28 / 1e9),
+                       "setup_s": setup_s},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_bond_force" if p.model == 1 else "k_state_force",
+                         "kernel_ms": kern_ms, "alg_bytes_per_launch": alg_bytes,
+                         "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
+                                  "peak_tflops": fp64_peak_tflops, "frac": alg_flops / (kern_ms * 1e-3) / 1e12 /
+                                  fp64_peak_tflops, "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    eng.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1800)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="crack_branching")
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return reference_arm(args)
+    return gb300_arm(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -254,6 +254,9 @@ int pd_solve_kalthoff_winkler(double dx, int nt, double* ux, double* uy, double*
 int pd_check_finite(pd_ctx* ctx, void* stream);
 /* Number of GPU kernels this context has launched (for launch accounting). */
 int64_t pd_kernel_launches(const pd_ctx* ctx);
+/* FP64 FMA issue rate of the current device in 1e9 FMA/s (dependent-chain
+ * microbenchmark, best of 3): the denominator of the FP64 roofline. */
+int pd_probe_fp64(double* gfma_per_s);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,106 @@
+"""ctypes binding of libpd_gb300.so (the C ABI declared in include/pd.h).
+
+The library is loaded from this package's directory.  There is no fallback:
+if the shared object is missing or fails to load, importing any entry point
+raises, so a run without the CUDA engine cannot pass silently.
+"""
+import ctypes as C
+import os
+
+from ._abi import PDCylinder, PDParams, PDResult
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpd_gb300.so")
+
+_lib = None
+
+P = C.POINTER
+VP = C.c_void_p
+D = C.c_double
+I32 = C.c_int
+I64 = C.c_int64
+SZ = C.c_size_t
+
+_SIGS = {
+    "pd_status_string": (C.c_char_p, [I32]),
+    "pd_last_error": (C.c_char_p, [VP]),
+    "pd_params_derive": (I32, [P(PDParams), I32, I32, I32] + [D] * 12 + [I32]),
+    "pd_create": (VP, [P(PDParams), P(I32)]),
+    "pd_destroy": (I32, [VP]),
+    "pd_get_params": (I32, [VP, P(PDParams)]),
+    "pd_set_params": (I32, [VP, P(PDParams)]),
+    "pd_get_field": (I32, [VP, I32, VP, SZ, VP]),
+    "pd_set_field": (I32, [VP, I32, VP, SZ, VP]),
+    "pd_field_ptr": (I32, [VP, I32, P(VP), P(SZ)]),
+    "pd_num_bonds": (I64, [VP]),
+    "pd_sync": (I32, [VP, VP]),
+    "pd_coord_plate": (I32, [VP, VP]),
+    "pd_coord_plate_crack": (I32, [VP, VP]),
+    "pd_coord_kw": (I32, [P(PDParams), D, P(D), P(D), P(D), I64, P(I64)]),
+    "pd_find_neighbor": (I32, [VP, VP]),
+    "pd_vol_corr": (I32, [VP, VP]),
+    "pd_surface_correct": (I32, [VP, VP]),
+    "pd_initial_weight": (I32, [VP, VP]),
+    "pd_set_crack_2d": (I32, [VP, D, D, D, D, VP]),
+    "pd_set_crack_kw": (I32, [VP, D, VP]),
+    "pd_initial_state": (I32, [VP, VP]),
+    "pd_prepare": (I32, [VP, VP]),
+    "pd_bond_force": (I32, [VP, VP]),
+    "pd_state_force": (I32, [VP, VP]),
+    "pd_integrate_adr": (I32, [VP, I32, VP]),
+    "pd_get_adr_cn": (I32, [VP, P(D), VP]),
+    "pd_integrate_verlet1": (I32, [VP, VP]),
+    "pd_integrate_verlet2": (I32, [VP, VP]),
+    "pd_reduce_sum": (I32, [VP, VP, I64, P(D), VP]),
+    "pd_damage": (I32, [VP, VP]),
+    "pd_quick_load": (I32, [VP, D, VP]),
+    "pd_load_plate_tensile": (I32, [VP, VP]),
+    "pd_cylinder_init": (I32, [VP, P(PDCylinder), VP]),
+    "pd_cylinder_get": (I32, [VP, P(PDCylinder), VP]),
+    "pd_cylinder_integrate1": (I32, [VP, VP]),
+    "pd_contact": (I32, [VP, VP]),
+    "pd_cylinder_integrate2": (I32, [VP, VP]),
+    "pd_run_adr": (I32, [VP, I32, I32, D, VP]),
+    "pd_run_explicit": (I32, [VP, I32, D, I32, VP]),
+    "pd_solve_plate_tensile": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),
+    "pd_solve_plate_crack_grow": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),
+    "pd_solve_kalthoff_winkler": (I32, [D, I32, P(D), P(D), P(D), P(D), I64, P(PDResult)]),
+    "pd_check_finite": (I32, [VP, VP]),
+    "pd_kernel_launches": (I64, [VP]),
+    "pd_probe_fp64": (I32, [P(D)]),
+}
+
+
+def exported_symbols():
+    """Names the C ABI exports (as declared in include/pd.h)."""
+    return list(_SIGS)
+
+
+def lib():
+    """Load libpd_gb300.so; raises if it is missing (no CPU fallback exists)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -c 'import __graft_entry__ as g; g.build()'`")
+        handle = C.CDLL(LIB_PATH)
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(handle, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = handle
+    return _lib
+
+
+class PDError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(msg)
+        self.status = status
+
+
+def check(status, ctx=None, what=""):
+    if status != 0:
+        L = lib()
+        name = L.pd_status_string(status).decode()
+        detail = L.pd_last_error(ctx).decode() if ctx else ""
+        raise PDError(status, f"{what}: {name} {detail}".strip())
+    return status

@@ -1,0 +1,712 @@
+// Force kernels: bond-based PMB and ordinary state-based, 2-D and 3-D.
+//
+// Replaces kernel_particle_force_2D / kernel_bond_force_2D / kernel_bond_force_3D
+// (Force_Bond.cu:6-141) and kernel_cal_theta_2D/3D + kernel_state_force_2D/3D
+// (Force_State.cu:56-306).
+//
+// Mapping: one warp per SELL slice (32 consecutive node rows), lane l owns row
+// 32s+l and walks its bond slots k = 0..width-1.  Slot loads (neighbour id and
+// per-bond coefficients) are 32-wide coalesced; on the regular lattices of the
+// reference's drivers slot k of every interior row points at the same lattice
+// offset, so the neighbour gathers are coalesced as well.  The intact flags of
+// a slot are one 32-bit word, read once per warp and rewritten with a ballot
+// when bonds break.  Forces are summed per lane in registers (no shuffles).
+//
+// GB300's FP64 pipe issues about 1/64 of the FP32 rate, so these kernels are
+// FP64-issue-bound, not HBM-bound.  Each bond therefore costs as few FP64
+// instructions as parity allows:
+//   d = (P_c - x_i) - u_i     P = x + u kept per node, so d rounds exactly as
+//                             the reference's x_c + u_c - x_i - u_i
+//   L^2 = d.d                 one product, one FMA
+//   L, 1/(2L)                 coupled Newton iteration from the hardware
+//                             reciprocal-square-root seed, then one residual
+//                             correction of L (no divide, no IEEE sqrt call)
+//   e = L - L0, t = k2 e h    k2 = 2 vol fac bc scr / L0 precomputed per bond
+//   f += t d                  one FMA per component
+// and breakage compares e with s0 L0 (precomputed) instead of dividing.
+//
+// Epilogues fused into the same launch (one launch per explicit step):
+//   EPI_VERLET  a = (F+b)/rho; v += dt/2 a (kernel_integrate_2D_2, Integrate.cu:218-249),
+//               optional rigid-impactor contact (kernel_contact,
+//               Solve_Kalthoff_Winkler.cu:112-175) and, when do_next is set, the
+//               next step's boundary loading (kernel_quick_load,
+//               Solve_Plate_Crack_Grow.cu:8-19) and first Verlet half
+//               (kernel_integrate_2D_1, Integrate.cu:174-185) into the other
+//               position buffer.
+//   EPI_ADR     per-node damping numerator/denominator (kernel_cnn,
+//               Integrate.cu:7-49) reduced across the grid; the last block to
+//               finish forms the damping coefficient (cal_cn, :108-129) on the
+//               device, so ADR needs no host round trip.
+#include "pd_internal.cuh"
+
+namespace pdg {
+
+struct ForceArgs {
+    KParams P;
+    int64_t nslices;  // slices processed (covering [0, N) for boundary epilogues)
+    int64_t nforce;   // rows [0, nforce) get forces
+    const int* width;
+    const int64_t* base;
+    const int64_t* fbase;
+    const int* col;
+    const double* l0;
+    const double* ecrit;
+    const double* k2;
+    const double* c1;
+    const double* c2;
+    const double* cth;
+    const double* xi;
+    double* e;
+    uint32_t* bits;
+    int64_t S;
+    const int* NN;
+    const double *x, *y, *z;
+    double *ux, *uy, *uz;
+    const double *pcx, *pcy, *pcz;
+    double *pnx, *pny, *pnz;
+    double *fx, *fy, *fz;
+    double *vx, *vy, *vz;
+    double *ax, *ay, *az;
+    const double *bx, *by, *bz;
+    const double *fox, *foy, *foz;
+    const double *vhx, *vhy, *vhz;
+    double* na;        // state: theta/m
+    const double* nb;  // state: 1/m
+    const double* m;
+    double* theta;
+    const double* dmg;
+    int epi, do_next, contact, first_step;
+    double load;
+    CylDev* cyl;
+    double* partials;
+    unsigned int* ticket;
+    double* cn_out;
+};
+
+namespace {
+
+constexpr int kWarpsPerBlock = kForceBlock / 32;
+constexpr int kNewtonIters = 2;
+
+__device__ __forceinline__ double rsqrt_seed(double x) {
+    double y;
+    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+    return y;
+}
+
+// sqrt(x) and 1/(2 sqrt(x)) by the coupled Newton iteration for the square
+// root and its reciprocal (r = 1/2 - s h; s += s r; h += h r), followed by one
+// residual correction of s (s += (x - s^2) h).
+__device__ __forceinline__ void sqrt_rsqrt(double x, double& s, double& h) {
+    const double y = rsqrt_seed(x);
+    s = x * y;
+    h = 0.5 * y;
+#pragma unroll
+    for (int it = 0; it < kNewtonIters; it++) {
+        const double r = fma(-s, h, 0.5);
+        s = fma(s, r, s);
+        h = fma(h, r, h);
+    }
+    const double d = fma(-s, s, x);
+    s = fma(d, h, s);
+}
+
+__device__ __forceinline__ double sqrt_only(double x) {
+    double s, h;
+    sqrt_rsqrt(x, s, h);
+    return s;
+}
+
+// e > ecrit for ecrit > 0: ordered like the IEEE bit patterns read as signed
+// integers (a negative e has its sign bit set and compares below).  Integer
+// compare keeps the test off the FP64 pipe.
+__device__ __forceinline__ bool exceeds(double e, double ecrit) {
+    return __double_as_longlong(e) > __double_as_longlong(ecrit);
+}
+
+__device__ __forceinline__ double block_sum(double v, double* sm) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) sm[w] = v;
+    __syncthreads();
+    double r = 0.0;
+    if (threadIdx.x == 0)
+        for (int k = 0; k < kWarpsPerBlock; k++) r += sm[k];
+    return r;  // valid in thread 0
+}
+
+// Per-node contact with the rigid cylinder (Solve_Kalthoff_Winkler.cu:112-175).
+// Returns the node's reaction-force contribution in rf.
+__device__ __forceinline__ void contact_node(const KParams& P, const CylDev& cy, double xi, double yi, double zi,
+                                             double& ux, double& uy, double& uz, double& vx, double& vy, double& vz,
+                                             double rf[3]) {
+    const double dpenx = xi + ux - cy.x - cy.disp[0];
+    const double dpeny = yi + uy - cy.y - cy.disp[1];
+    const double dpenz = zi + uz - cy.z - cy.disp[2];
+    const double dpend = sqrt(dpenx * dpenx + dpenz * dpenz);
+    if (dpend <= cy.rad && fabs(dpeny) <= (cy.height / 2.0)) {
+        double dprx, dpry, dprz;
+        if (cy.rad - dpend <= cy.height / 2.0 - fabs(dpeny)) {
+            dprx = dpenx / dpend * cy.rad;
+            dpry = dpeny;
+            dprz = dpenz / dpend * cy.rad;
+        } else if (dpeny >= 0.0) {
+            dprx = dpenx;
+            dpry = cy.height / 2.0;
+            dprz = dpenz;
+        } else {
+            dprx = dpenx;
+            dpry = -cy.height / 2.0;
+            dprz = dpenz;
+        }
+        const double oux = ux, ouy = uy, ouz = uz, ovx = vx, ovy = vy, ovz = vz;
+        ux = cy.x + cy.disp[0] + dprx - xi;
+        uy = cy.y + cy.disp[1] + dpry - yi;
+        uz = cy.z + cy.disp[2] + dprz - zi;
+        vx = (ux - oux) / P.dt;
+        vy = (uy - ouy) / P.dt;
+        vz = (uz - ouz) / P.dt;
+        rf[0] += -P.dens * (vx - ovx) / P.dt * P.vol;
+        rf[1] += -P.dens * (vy - ovy) / P.dt * P.vol;
+        rf[2] += -P.dens * (vz - ovz) / P.dt * P.vol;
+    }
+}
+
+// Epilogue of one force-computed row r (r < nforce).
+template <int DIM, int EPI>
+__device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, double fxr, double fyr, double fzr,
+                                             double xi, double yi, double zi, double uxi, double uyi, double uzi,
+                                             double red[3]) {
+    const KParams& P = A.P;
+    A.fx[r] = fxr;
+    A.fy[r] = fyr;
+    if (DIM == 3) A.fz[r] = fzr;
+    if (EPI == EPI_ADR) {
+        // kernel_cnn (Integrate.cu:17-33), same operand order
+        const double vhx = A.vhx[r], vhy = A.vhy[r];
+        double cn = 0.0, disp;
+        if (vhx != 0.0) cn = -1.0 * uxi * uxi * (fxr / P.mass - A.fox[r] / P.mass) / (P.dt * vhx);
+        disp = uxi * uxi;
+        if (vhy != 0.0) cn -= 1.0 * uyi * uyi * (fyr / P.mass - A.foy[r] / P.mass) / (P.dt * vhy);
+        disp += uyi * uyi;
+        if (DIM == 3) {
+            const double vhz = A.vhz[r];
+            if (vhz != 0.0) cn -= 1.0 * uzi * uzi * (fzr / P.mass - A.foz[r] / P.mass) / (P.dt * vhz);
+            disp += uzi * uzi;
+        }
+        red[0] += cn;
+        red[1] += disp;
+        return;
+    }
+    if (EPI == EPI_VERLET) {
+        double vx = A.vx[r], vy = A.vy[r], vz = DIM == 3 ? A.vz[r] : 0.0;
+        double ux = uxi, uy = uyi, uz = uzi;
+        if (A.contact && A.dmg[r] < 1.0) contact_node(P, *A.cyl, xi, yi, zi, ux, uy, uz, vx, vy, vz, red);
+        const double hdt = P.dt / 2.0;
+        const double ax = (fxr + A.bx[r]) / P.dens;
+        const double ay = (fyr + A.by[r]) / P.dens;
+        vx = fma(hdt, ax, vx);
+        vy = fma(hdt, ay, vy);
+        A.ax[r] = ax;
+        A.ay[r] = ay;
+        double az = 0.0;
+        if (DIM == 3) {
+            az = (fzr + A.bz[r]) / P.dens;
+            vz = fma(hdt, az, vz);
+            A.az[r] = az;
+        }
+        if (A.do_next) {
+            vx = fma(hdt, ax, vx);
+            vy = fma(hdt, ay, vy);
+            ux = fma(vx, P.dt, ux);
+            uy = fma(vy, P.dt, uy);
+            if (DIM == 3) {
+                vz = fma(hdt, az, vz);
+                uz = fma(vz, P.dt, uz);
+            }
+        }
+        A.vx[r] = vx;
+        A.vy[r] = vy;
+        if (DIM == 3) A.vz[r] = vz;
+        if (A.do_next || A.contact) {
+            A.ux[r] = ux;
+            A.uy[r] = uy;
+            if (DIM == 3) A.uz[r] = uz;
+        }
+        if (A.do_next) {
+            A.pnx[r] = xi + ux;
+            A.pny[r] = yi + uy;
+            if (DIM == 3) A.pnz[r] = zi + uz;
+        }
+    }
+}
+
+// Boundary rows [N_int, N): the next step's prescribed motion
+// (kernel_quick_load: the first 3 nx rows move up, the next 3 nx down).
+template <int DIM>
+__device__ __forceinline__ void boundary_row(const ForceArgs& A, int64_t r) {
+    const KParams& P = A.P;
+    double uy = A.uy[r];
+    if (A.load != 0.0) {
+        const int64_t k = r - P.N_int;
+        if (k < 3 * (int64_t)P.nx)
+            uy += A.load * P.dt;
+        else if (k < 6 * (int64_t)P.nx)
+            uy -= A.load * P.dt;
+        A.uy[r] = uy;
+    }
+    A.pnx[r] = A.pcx[r];
+    A.pny[r] = A.y[r] + uy;
+    if (DIM == 3) A.pnz[r] = A.pcz[r];
+}
+
+// Grid-level reduction of red[0..nred) into partials; the last block to finish
+// forms the result (ADR damping or contact reaction + cylinder update).
+// mode: EPI_ADR -> damping coefficient; EPI_VERLET -> contact reaction and
+// impactor update; EPI_NONE -> contact reaction accumulated only.
+template <int EPI>
+__device__ void finish_reduction(const ForceArgs& A, double red[3], int nred) {
+    __shared__ double sm[kWarpsPerBlock];
+    __shared__ bool last;
+    for (int k = 0; k < nred; k++) {
+        const double v = block_sum(red[k], sm);
+        if (threadIdx.x == 0) A.partials[(int64_t)blockIdx.x * 4 + k] = v;
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(A.ticket, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double tot[3] = {0.0, 0.0, 0.0};
+    for (int k = 0; k < nred; k++) {
+        double v = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x) v += __ldcg(A.partials + (int64_t)b * 4 + k);
+        tot[k] = block_sum(v, sm);
+    }
+    if (threadIdx.x != 0) return;
+    *A.ticket = 0u;
+    const KParams& P = A.P;
+    if (EPI == EPI_ADR) {
+        // cal_cn (Integrate.cu:108-129)
+        const double cn1 = tot[0], cn2 = tot[1];
+        double cn = 0.0;
+        if (cn2 != 0.0) cn = (cn1 / cn2 > 0.0) ? 2.0 * sqrt(cn1 / cn2) : 0.0;
+        if (cn > 2.0) cn = 1.9;
+        *A.cn_out = cn;
+    } else if (EPI == EPI_NONE) {
+        for (int a = 0; a < 3; a++) A.cyl->force[a] += tot[a];
+    } else {
+        // kernel_cy_integrate_2 (Solve_Kalthoff_Winkler.cu:242-253), then the
+        // next step's kernel_cy_integrate_1 (:89-99)
+        CylDev& cy = *A.cyl;
+        for (int a = 0; a < 3; a++) {
+            cy.force[a] = tot[a];
+            cy.acc[a] = cy.force[a] / cy.mass;
+            cy.vel[a] = fma(P.dt / 2.0, cy.acc[a], cy.vel[a]);
+            cy.force[a] = 0.0;
+            if (A.do_next) {
+                cy.vel[a] = fma(P.dt / 2.0, cy.acc[a], cy.vel[a]);
+                cy.disp[a] = fma(cy.vel[a], P.dt, cy.disp[a]);
+            }
+        }
+    }
+}
+
+template <int DIM, int EPI>
+__global__ void __launch_bounds__(kForceBlock) k_bond_force(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
+         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+        const int64_t r = s * 32 + lane;
+        const bool force_row = r < A.nforce;
+        if (s * 32 < A.nforce) {
+            const int64_t rr = force_row ? r : A.nforce - 1;
+            const double xi = A.x[rr], yi = A.y[rr], zi = DIM == 3 ? A.z[rr] : 0.0;
+            const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
+            double fxr = 0.0, fyr = 0.0, fzr = 0.0;
+            const int W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            for (int k = 0; k < W; k++) {
+                const int64_t slot = b + (int64_t)k * 32 + lane;
+                const uint32_t word = wbits[k];
+                const bool alive = force_row && ((word >> lane) & 1u);
+                bool brk = false;
+                if (alive) {
+                    const int c = A.col[slot];
+                    const double dx = (A.pcx[c] - xi) - uxi;
+                    const double dy = (A.pcy[c] - yi) - uyi;
+                    double L2 = dx * dx;
+                    L2 = fma(dy, dy, L2);
+                    double dz = 0.0;
+                    if (DIM == 3) {
+                        dz = (A.pcz[c] - zi) - uzi;
+                        L2 = fma(dz, dz, L2);
+                    }
+                    double L, h;
+                    sqrt_rsqrt(L2, L, h);
+                    const double e = L - A.l0[slot];
+                    const double t = (A.k2[slot] * e) * h;
+                    fxr = fma(t, dx, fxr);
+                    fyr = fma(t, dy, fyr);
+                    if (DIM == 3) fzr = fma(t, dz, fzr);
+                    brk = exceeds(e, A.ecrit[slot]);
+                }
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && lane == 0) wbits[k] = word & ~broke;
+            }
+            if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+        }
+        if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
+    }
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 2);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
+// Dilatation pass (kernel_cal_theta_2D/3D): every row of [0, N).  Stores the
+// extension e per bond with the reference's operand order for this pass,
+// ((x_c - x_i) + u_c) - u_i, and theta/m per node.  The 2-D pass counts every
+// bond of the family, intact or not (Force_State.cu:65); the 3-D pass intact
+// ones only (:214).
+template <int DIM>
+__global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const KParams& P = A.P;
+    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
+         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+        const int64_t r = s * 32 + lane;
+        const bool row = r < P.N;
+        const int64_t rr = row ? r : P.N - 1;
+        const int nn = row ? A.NN[rr] : 0;
+        const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
+        const bool check_bits = DIM == 3 && r < P.N_int;
+        const int W = A.width[s];
+        const int64_t b = A.base[s];
+        const uint32_t* wbits = A.bits + A.fbase[s];
+        double acc = 0.0;
+        for (int k = 0; k < W; k++) {
+            const int64_t slot = b + (int64_t)k * 32 + lane;
+            bool use = k < nn;
+            if (check_bits) use = use && ((wbits[k] >> lane) & 1u);
+            if (use) {
+                const int c = A.col[slot];
+                const double dx = (A.xi[slot] + A.ux[c]) - uxi;
+                const double dy = (A.xi[A.S + slot] + A.uy[c]) - uyi;
+                double L2 = dx * dx;
+                L2 = fma(dy, dy, L2);
+                if (DIM == 3) {
+                    const double dz = (A.xi[2 * A.S + slot] + A.uz[c]) - uzi;
+                    L2 = fma(dz, dz, L2);
+                }
+                const double e = sqrt_only(L2) - A.l0[slot];
+                A.e[slot] = e;
+                acc = fma(A.cth[slot], e, acc);
+            }
+        }
+        if (row) {
+            const double th = acc / A.m[r];
+            A.theta[r] = th;
+            A.na[r] = th / A.m[r];
+        }
+    }
+}
+
+// State-based force pass (kernel_state_force_2D/3D) on rows [0, N_int):
+// t_i + t_j = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j) per bond.
+template <int DIM, int EPI>
+__global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
+         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+        const int64_t r = s * 32 + lane;
+        const bool force_row = r < A.nforce;
+        if (s * 32 < A.nforce) {
+            const int64_t rr = force_row ? r : A.nforce - 1;
+            const double xi = A.x[rr], yi = A.y[rr], zi = DIM == 3 ? A.z[rr] : 0.0;
+            const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
+            const double nai = A.na[rr], nbi = A.nb[rr];
+            double fxr = 0.0, fyr = 0.0, fzr = 0.0;
+            const int W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            for (int k = 0; k < W; k++) {
+                const int64_t slot = b + (int64_t)k * 32 + lane;
+                const uint32_t word = wbits[k];
+                const bool alive = force_row && ((word >> lane) & 1u);
+                bool brk = false;
+                if (alive) {
+                    const int c = A.col[slot];
+                    const double dx = (A.pcx[c] - xi) - uxi;
+                    const double dy = (A.pcy[c] - yi) - uyi;
+                    double L2 = dx * dx;
+                    L2 = fma(dy, dy, L2);
+                    double dz = 0.0;
+                    if (DIM == 3) {
+                        // the reference's 3-D force kernel takes the z term of the
+                        // length in the dilatation pass's operand order (Force_State.cu:272)
+                        const double dzl = (A.xi[2 * A.S + slot] + A.uz[c]) - uzi;
+                        dz = (A.pcz[c] - zi) - uzi;
+                        L2 = fma(dzl, dzl, L2);
+                    }
+                    double L, h;
+                    sqrt_rsqrt(L2, L, h);
+                    const double ef = L - A.l0[slot];
+                    const double T = fma(A.c2[slot] * A.e[slot], nbi + A.nb[c], A.c1[slot] * (nai + A.na[c]));
+                    const double t = T * h;
+                    fxr = fma(t, dx, fxr);
+                    fyr = fma(t, dy, fyr);
+                    if (DIM == 3) fzr = fma(t, dz, fzr);
+                    brk = exceeds(ef, A.ecrit[slot]);
+                }
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && lane == 0) wbits[k] = word & ~broke;
+            }
+            if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+        }
+        if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
+    }
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 2);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
+
+// Standalone kernel_cnn + cal_cn (Integrate.cu:7-49, :108-129) on the current forces.
+template <int DIM>
+__global__ void __launch_bounds__(kForceBlock) k_adr_cnn(const ForceArgs A) {
+    double red[3] = {0.0, 0.0, 0.0};
+    const KParams& P = A.P;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.N_int; r += (int64_t)gridDim.x * blockDim.x) {
+        const double uxi = A.ux[r], uyi = A.uy[r], uzi = DIM == 3 ? A.uz[r] : 0.0;
+        double cn = 0.0, disp;
+        if (A.vhx[r] != 0.0) cn = -1.0 * uxi * uxi * (A.fx[r] / P.mass - A.fox[r] / P.mass) / (P.dt * A.vhx[r]);
+        disp = uxi * uxi;
+        if (A.vhy[r] != 0.0) cn -= 1.0 * uyi * uyi * (A.fy[r] / P.mass - A.foy[r] / P.mass) / (P.dt * A.vhy[r]);
+        disp += uyi * uyi;
+        if (DIM == 3) {
+            if (A.vhz[r] != 0.0) cn -= 1.0 * uzi * uzi * (A.fz[r] / P.mass - A.foz[r] / P.mass) / (P.dt * A.vhz[r]);
+            disp += uzi * uzi;
+        }
+        red[0] += cn;
+        red[1] += disp;
+    }
+    finish_reduction<EPI_ADR>(A, red, 2);
+}
+
+// Standalone kernel_contact (Solve_Kalthoff_Winkler.cu:112-175) on nodes [0, N).
+__global__ void __launch_bounds__(kForceBlock) k_contact(const ForceArgs A) {
+    double red[3] = {0.0, 0.0, 0.0};
+    const KParams& P = A.P;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.N; r += (int64_t)gridDim.x * blockDim.x) {
+        if (!(A.dmg[r] < 1.0)) continue;
+        double ux = A.ux[r], uy = A.uy[r], uz = A.uz[r], vx = A.vx[r], vy = A.vy[r], vz = A.vz[r];
+        const double ox = ux, oy = uy, oz = uz;
+        contact_node(P, *A.cyl, A.x[r], A.y[r], A.z[r], ux, uy, uz, vx, vy, vz, red);
+        if (ux != ox || uy != oy || uz != oz || vx != A.vx[r] || vy != A.vy[r] || vz != A.vz[r]) {
+            A.ux[r] = ux;
+            A.uy[r] = uy;
+            A.uz[r] = uz;
+            A.vx[r] = vx;
+            A.vy[r] = vy;
+            A.vz[r] = vz;
+        }
+    }
+    finish_reduction<EPI_NONE>(A, red, 3);
+}
+
+// Node pass after a force-only launch: the Verlet epilogue (contact, second
+// half-kick, next step's loading and first half) for kernels whose gathers
+// read u itself, which the fused epilogue must then not overwrite.
+template <int DIM>
+__global__ void __launch_bounds__(kForceBlock) k_node_post(const ForceArgs A) {
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.N; r += (int64_t)gridDim.x * blockDim.x) {
+        if (r < A.nforce) {
+            const double xi = A.x[r], yi = A.y[r], zi = DIM == 3 ? A.z[r] : 0.0;
+            row_epilogue<DIM, EPI_VERLET>(A, r, A.fx[r], A.fy[r], DIM == 3 ? A.fz[r] : 0.0, xi, yi, zi, A.ux[r],
+                                          A.uy[r], DIM == 3 ? A.uz[r] : 0.0, red);
+        } else if (A.do_next) {
+            boundary_row<DIM>(A, r);
+        }
+    }
+    if (A.contact) finish_reduction<EPI_VERLET>(A, red, 3);
+}
+
+}  // namespace
+
+static ForceArgs make_args(pd_ctx* c) {
+    ForceArgs A{};
+    A.P = kparams(c->p);
+    const Sell& S = c->sell;
+    A.nslices = S.nslices;
+    A.nforce = c->p.N_int;
+    A.width = S.width;
+    A.base = S.base;
+    A.fbase = S.fbase;
+    A.col = S.col;
+    A.l0 = S.l0;
+    A.ecrit = S.ecrit;
+    A.k2 = S.k2;
+    A.c1 = S.c1;
+    A.c2 = S.c2;
+    A.cth = S.cth;
+    A.xi = S.xi;
+    A.e = S.e;
+    A.bits = S.bits;
+    A.S = S.S;
+    A.NN = c->NN;
+    A.x = c->nf[PD_F_X];
+    A.y = c->nf[PD_F_Y];
+    A.z = c->nf[PD_F_Z];
+    A.ux = c->nf[PD_F_UX];
+    A.uy = c->nf[PD_F_UY];
+    A.uz = c->nf[PD_F_UZ];
+    A.pcx = c->pos[c->parity][0];
+    A.pcy = c->pos[c->parity][1];
+    A.pcz = c->pos[c->parity][2];
+    A.pnx = c->pos[c->parity ^ 1][0];
+    A.pny = c->pos[c->parity ^ 1][1];
+    A.pnz = c->pos[c->parity ^ 1][2];
+    A.fx = c->nf[PD_F_FX];
+    A.fy = c->nf[PD_F_FY];
+    A.fz = c->nf[PD_F_FZ];
+    A.vx = c->nf[PD_F_VX];
+    A.vy = c->nf[PD_F_VY];
+    A.vz = c->nf[PD_F_VZ];
+    A.ax = c->nf[PD_F_AX];
+    A.ay = c->nf[PD_F_AY];
+    A.az = c->nf[PD_F_AZ];
+    A.bx = c->nf[PD_F_BX];
+    A.by = c->nf[PD_F_BY];
+    A.bz = c->nf[PD_F_BZ];
+    A.fox = c->nf[PD_F_FOX];
+    A.foy = c->nf[PD_F_FOY];
+    A.foz = c->nf[PD_F_FOZ];
+    A.vhx = c->nf[PD_F_VHX];
+    A.vhy = c->nf[PD_F_VHY];
+    A.vhz = c->nf[PD_F_VHZ];
+    A.na = c->node_a;
+    A.nb = c->node_b;
+    A.m = c->nf[PD_F_M];
+    A.theta = c->nf[PD_F_THETA];
+    A.dmg = c->nf[PD_F_DMG];
+    A.cyl = c->cyl;
+    A.partials = c->partials;
+    A.ticket = c->ticket;
+    A.cn_out = c->cn;
+    return A;
+}
+
+static unsigned force_grid(pd_ctx* c, int64_t nslices) {
+    const int64_t want = (nslices + kWarpsPerBlock - 1) / kWarpsPerBlock;
+    const int64_t cap = (int64_t)c->num_sms * 8;  // resident blocks per SM at 256 threads
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(want, cap), kMaxPartials));
+}
+
+int launch_theta(pd_ctx* c, cudaStream_t s) {
+    ForceArgs A = make_args(c);
+    const unsigned g = force_grid(c, A.nslices);
+    if (A.P.dim == 2)
+        k_theta<2><<<g, kForceBlock, 0, s>>>(A);
+    else
+        k_theta<3><<<g, kForceBlock, 0, s>>>(A);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "theta");
+}
+
+int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
+    ForceArgs A = make_args(c);
+    A.epi = f.epi;
+    A.do_next = f.do_next;
+    A.load = f.load;
+    A.contact = f.contact;
+    if (f.epi != EPI_VERLET || !f.do_next) {
+        // without the next step's half-kick only the force rows are visited
+        A.nslices = (A.nforce + 31) / 32;
+    }
+    const bool state = A.P.model == PD_MODEL_STATE;
+    const bool d3 = A.P.dim == 3;
+    if (state && d3 && f.epi == EPI_VERLET && (f.do_next || f.contact)) {
+        // 3-D state force gathers u_z of the neighbours: force first, then the node pass
+        StepFlags g0 = f;
+        g0.epi = EPI_NONE;
+        int rc = launch_force(c, g0, s);
+        if (rc) return rc;
+        ForceArgs B = make_args(c);
+        B.epi = EPI_VERLET;
+        B.do_next = f.do_next;
+        B.load = f.load;
+        B.contact = f.contact;
+        const unsigned gp = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>((B.P.N + kForceBlock - 1) / kForceBlock, std::min<int64_t>(c->num_sms * 8, kMaxPartials)));
+        k_node_post<3><<<gp, kForceBlock, 0, s>>>(B);
+        c->launches++;
+        if (f.do_next) c->parity ^= 1;
+        if (f.contact && !f.do_next) c->pos_valid = false;
+        return cuda_err(c, cudaGetLastError(), "node post");
+    }
+    const unsigned g = force_grid(c, A.nslices);
+#define PD_LAUNCH(KER, D, E) KER<D, E><<<g, kForceBlock, 0, s>>>(A)
+#define PD_DISPATCH(KER)                                  \
+    do {                                                  \
+        if (!d3) {                                        \
+            if (f.epi == EPI_NONE) PD_LAUNCH(KER, 2, EPI_NONE);   \
+            else if (f.epi == EPI_VERLET) PD_LAUNCH(KER, 2, EPI_VERLET); \
+            else PD_LAUNCH(KER, 2, EPI_ADR);              \
+        } else {                                          \
+            if (f.epi == EPI_NONE) PD_LAUNCH(KER, 3, EPI_NONE);   \
+            else if (f.epi == EPI_VERLET) PD_LAUNCH(KER, 3, EPI_VERLET); \
+            else PD_LAUNCH(KER, 3, EPI_ADR);              \
+        }                                                 \
+    } while (0)
+    if (state)
+        PD_DISPATCH(k_state_force);
+    else
+        PD_DISPATCH(k_bond_force);
+#undef PD_DISPATCH
+#undef PD_LAUNCH
+    c->launches++;
+    if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
+    if (f.epi == EPI_VERLET && f.contact && !f.do_next) c->pos_valid = false;  // contact moved u, not P
+    c->csr_fail_current = false;
+    return cuda_err(c, cudaGetLastError(), "force");
+}
+
+}  // namespace pdg
+
+namespace pdg {
+
+int launch_adr_cnn(pd_ctx* c, cudaStream_t s) {
+    ForceArgs A = make_args(c);
+    const unsigned g = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((A.P.N_int + kForceBlock - 1) / kForceBlock, std::min<int64_t>(c->num_sms * 8, kMaxPartials)));
+    if (A.P.dim == 2)
+        k_adr_cnn<2><<<g, kForceBlock, 0, s>>>(A);
+    else
+        k_adr_cnn<3><<<g, kForceBlock, 0, s>>>(A);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "adr_cnn");
+}
+
+int launch_contact(pd_ctx* c, cudaStream_t s) {
+    if (!c->has_cyl) return set_err(c, PD_ERR_STATE, "contact needs an impactor (pd_cylinder_init)");
+    if (c->p.dim != 3) return set_err(c, PD_ERR_UNSUPPORTED, "contact is 3-D only");
+    ForceArgs A = make_args(c);
+    const unsigned g = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>((A.P.N + kForceBlock - 1) / kForceBlock, std::min<int64_t>(c->num_sms * 8, kMaxPartials)));
+    k_contact<<<g, kForceBlock, 0, s>>>(A);
+    c->launches++;
+    c->pos_valid = false;
+    return cuda_err(c, cudaGetLastError(), "contact");
+}
+
+}  // namespace pdg

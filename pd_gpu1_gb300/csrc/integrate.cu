@@ -1,0 +1,370 @@
+// Node-parallel passes: time integration, loading, damage, reductions.
+//
+//   launch_prologue     kernel_quick_load + kernel_integrate_2D_1/3D_1 +
+//                       kernel_cy_integrate_1 of the first step of a run, and the
+//                       current-position buffer P = x + u
+//   launch_adr_update   kernel_integrate (Integrate.cu:54-106) with the damping
+//                       coefficient read from device memory, the next step's
+//                       boundary loading, and P
+//   launch_verlet1/2    kernel_integrate_2D_1/_2, 3D_1/_2 (Integrate.cu:174-266)
+//   launch_damage       kernel_cal_dmg_2D/3D (Base_Function.cu:149-217)
+//   reduce_sum          sum (Reduce.cu:52-65) with a fixed summation order
+//
+// Every loop over rows < N_int stops at N_int; the reference's Verlet launches
+// are sized for N_int but test i < N (Integrate.cu:178, :206), which only
+// touches boundary rows whose force and acceleration are zero.
+#include "pd_internal.cuh"
+
+namespace pdg {
+namespace {
+
+constexpr int T = 256;
+
+inline unsigned grid_for(pd_ctx* c, int64_t n) {
+    return (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + T - 1) / T, (int64_t)c->num_sms * 16));
+}
+
+struct NodeArgs {
+    KParams P;
+    double *x, *y, *z, *ux, *uy, *uz, *vx, *vy, *vz, *ax, *ay, *az, *fx, *fy, *fz, *bx, *by, *bz;
+    double *vhx, *vhy, *vhz, *fox, *foy, *foz;
+    double *px, *py, *pz;
+    const double* cn;
+    CylDev* cyl;
+};
+
+NodeArgs node_args(pd_ctx* c) {
+    NodeArgs a;
+    a.P = kparams(c->p);
+    double** f = c->nf;
+    a.x = f[PD_F_X], a.y = f[PD_F_Y], a.z = f[PD_F_Z];
+    a.ux = f[PD_F_UX], a.uy = f[PD_F_UY], a.uz = f[PD_F_UZ];
+    a.vx = f[PD_F_VX], a.vy = f[PD_F_VY], a.vz = f[PD_F_VZ];
+    a.ax = f[PD_F_AX], a.ay = f[PD_F_AY], a.az = f[PD_F_AZ];
+    a.fx = f[PD_F_FX], a.fy = f[PD_F_FY], a.fz = f[PD_F_FZ];
+    a.bx = f[PD_F_BX], a.by = f[PD_F_BY], a.bz = f[PD_F_BZ];
+    a.vhx = f[PD_F_VHX], a.vhy = f[PD_F_VHY], a.vhz = f[PD_F_VHZ];
+    a.fox = f[PD_F_FOX], a.foy = f[PD_F_FOY], a.foz = f[PD_F_FOZ];
+    a.px = c->pos[c->parity][0], a.py = c->pos[c->parity][1], a.pz = c->pos[c->parity][2];
+    a.cn = c->cn;
+    a.cyl = c->cyl;
+    return a;
+}
+
+__global__ void k_refresh_pos(NodeArgs A) {
+    const KParams& P = A.P;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
+        A.px[i] = A.x[i] + A.ux[i];
+        A.py[i] = A.y[i] + A.uy[i];
+        if (P.dim == 3) A.pz[i] = A.z[i] + A.uz[i];
+    }
+}
+
+__device__ __forceinline__ void quick_load_row(const KParams& P, int64_t i, double load, double* uy) {
+    const int64_t k = i - P.N_int;
+    if (k < 3 * (int64_t)P.nx)
+        uy[i] += load * P.dt;
+    else if (k < 6 * (int64_t)P.nx)
+        uy[i] -= load * P.dt;
+}
+
+// First step of a run: boundary loading, first Verlet half, impactor advance, P.
+__global__ void k_prologue(NodeArgs A, double load, int first_verlet, int cyl_step) {
+    const KParams& P = A.P;
+    const double hdt = P.dt / 2.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i >= P.N_int) {
+            if (load != 0.0) quick_load_row(P, i, load, A.uy);
+        } else if (first_verlet) {
+            A.vx[i] = fma(hdt, A.ax[i], A.vx[i]);
+            A.vy[i] = fma(hdt, A.ay[i], A.vy[i]);
+            if (P.dim == 3) A.vz[i] = fma(hdt, A.az[i], A.vz[i]);
+            A.ux[i] = fma(A.vx[i], P.dt, A.ux[i]);
+            A.uy[i] = fma(A.vy[i], P.dt, A.uy[i]);
+            if (P.dim == 3) A.uz[i] = fma(A.vz[i], P.dt, A.uz[i]);
+        }
+        A.px[i] = A.x[i] + A.ux[i];
+        A.py[i] = A.y[i] + A.uy[i];
+        if (P.dim == 3) A.pz[i] = A.z[i] + A.uz[i];
+    }
+    if (cyl_step && blockIdx.x == 0 && threadIdx.x == 0) {
+        CylDev& cy = *A.cyl;
+        for (int a = 0; a < 3; a++) {
+            cy.vel[a] = fma(hdt, cy.acc[a], cy.vel[a]);
+            cy.disp[a] = fma(cy.vel[a], P.dt, cy.disp[a]);
+        }
+    }
+}
+
+// kernel_integrate (Integrate.cu:54-106), same operand order.
+__global__ void k_adr_update(NodeArgs A, int ct, int do_next, double load) {
+    const KParams& P = A.P;
+    const double cn = *A.cn;
+    const double c0 = 1.0 * P.dt / P.mass;       // ct == 0
+    const double c1 = 2.0 * P.dt / P.mass;
+    const double num = 2.0 - cn * P.dt, den = 2.0 + cn * P.dt;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
+        if (i < P.N_int) {
+            double* vh[3] = {A.vhx, A.vhy, A.vhz};
+            double* v[3] = {A.vx, A.vy, A.vz};
+            double* u[3] = {A.ux, A.uy, A.uz};
+            double* fo[3] = {A.fox, A.foy, A.foz};
+            const double* f[3] = {A.fx, A.fy, A.fz};
+            const double* b[3] = {A.bx, A.by, A.bz};
+            for (int a = 0; a < P.dim; a++) {
+                const double vho = vh[a][i];
+                const double fb = f[a][i] + b[a][i];
+                double vhn;
+                if (ct == 0)
+                    vhn = c0 * fb / 2.0;
+                else
+                    vhn = (num * vho + c1 * fb) / den;
+                v[a][i] = 0.5 * (vho + vhn);
+                u[a][i] = fma(vhn, P.dt, u[a][i]);
+                vh[a][i] = vhn;
+                fo[a][i] = f[a][i];
+            }
+        } else if (do_next && load != 0.0) {
+            quick_load_row(P, i, load, A.uy);
+        }
+        A.px[i] = A.x[i] + A.ux[i];
+        A.py[i] = A.y[i] + A.uy[i];
+        if (P.dim == 3) A.pz[i] = A.z[i] + A.uz[i];
+    }
+}
+
+__global__ void k_verlet1(NodeArgs A) {
+    const KParams& P = A.P;
+    const double hdt = P.dt / 2.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N_int;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        A.vx[i] = fma(hdt, A.ax[i], A.vx[i]);
+        A.vy[i] = fma(hdt, A.ay[i], A.vy[i]);
+        if (P.dim == 3) A.vz[i] = fma(hdt, A.az[i], A.vz[i]);
+        A.ux[i] = fma(A.vx[i], P.dt, A.ux[i]);
+        A.uy[i] = fma(A.vy[i], P.dt, A.uy[i]);
+        if (P.dim == 3) A.uz[i] = fma(A.vz[i], P.dt, A.uz[i]);
+    }
+}
+
+__global__ void k_verlet2(NodeArgs A) {
+    const KParams& P = A.P;
+    const double hdt = P.dt / 2.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N_int;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        A.ax[i] = (A.fx[i] + A.bx[i]) / P.dens;
+        A.ay[i] = (A.fy[i] + A.by[i]) / P.dens;
+        A.vx[i] = fma(hdt, A.ax[i], A.vx[i]);
+        A.vy[i] = fma(hdt, A.ay[i], A.vy[i]);
+        if (P.dim == 3) {
+            A.az[i] = (A.fz[i] + A.bz[i]) / P.dens;
+            A.vz[i] = fma(hdt, A.az[i], A.vz[i]);
+        }
+    }
+}
+
+__global__ void k_quick_load(NodeArgs A, double load) {
+    const KParams& P = A.P;
+    const int64_t n = 6 * (int64_t)P.nx;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = P.N_int + k;
+        if (i < P.N) quick_load_row(P, i, load, A.uy);
+    }
+}
+
+__global__ void k_load_tensile(NodeArgs A) {
+    const KParams& P = A.P;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < P.ny) {
+        A.bx[i * P.nx] = -0.001 * P.emod / P.dx;
+        A.bx[i * P.nx + P.nx - 1] = 0.001 * P.emod / P.dx;
+    }
+}
+
+// kernel_cal_dmg_2D/3D on CSR rows; one warp per node.
+__global__ void k_damage(KParams P, const int64_t* __restrict__ rowptr, const int* __restrict__ fail,
+                         const double* __restrict__ fac, double* __restrict__ dmg) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N_int) return;
+    double d1 = 0.0, d2 = 0.0;
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        d1 += fail[q] * P.vol * fac[q];
+        d2 += P.vol * fac[q];
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+        d1 += __shfl_down_sync(0xffffffffu, d1, off);
+        d2 += __shfl_down_sync(0xffffffffu, d2, off);
+    }
+    if (lane == 0) dmg[i] = 1.0 - d1 / d2;
+}
+
+// Deterministic two-pass sum: block partials in block order, then one block.
+__global__ void k_sum_partials(const double* __restrict__ x, int64_t n, double* __restrict__ part) {
+    __shared__ double sm[T / 32];
+    double v = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v += x[i];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int k = 0; k < T / 32; k++) r += sm[k];
+        part[blockIdx.x] = r;
+    }
+}
+
+__global__ void k_sum_final(const double* __restrict__ part, int n, double* __restrict__ out) {
+    __shared__ double sm[T / 32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[i];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int k = 0; k < T / 32; k++) r += sm[k];
+        *out = r;
+    }
+}
+
+__global__ void k_finite(NodeArgs A, int* bad) {
+    const KParams& P = A.P;
+    int b = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
+        b |= !isfinite(A.ux[i]) | !isfinite(A.uy[i]) | !isfinite(A.fx[i]) | !isfinite(A.fy[i]);
+        if (P.dim == 3) b |= !isfinite(A.uz[i]) | !isfinite(A.fz[i]);
+    }
+    if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+}
+
+// Dependent FMA chains, 8 per thread: the FP64 issue rate of this GPU.
+__global__ void k_fp64_probe(double* out, double a, double b, int iters) {
+    double x0 = threadIdx.x * 1e-9, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,
+           x7 = x0 + 7;
+    for (int i = 0; i < iters; ++i) {
+        x0 = fma(x0, a, b);
+        x1 = fma(x1, a, b);
+        x2 = fma(x2, a, b);
+        x3 = fma(x3, a, b);
+        x4 = fma(x4, a, b);
+        x5 = fma(x5, a, b);
+        x6 = fma(x6, a, b);
+        x7 = fma(x7, a, b);
+    }
+    out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+}  // namespace
+
+int fp64_probe(double* gfma_per_s) {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int blocks = sms * 8, iters = 4096;
+    double* out = nullptr;
+    if (cudaMalloc(&out, (size_t)blocks * T * 8) != cudaSuccess) return PD_ERR_NOMEM;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    float best = 1e30f;
+    for (int rep = 0; rep < 3; rep++) {
+        cudaEventRecord(a);
+        k_fp64_probe<<<blocks, T>>>(out, 0.999999, 1e-7, iters);
+        cudaEventRecord(b);
+        cudaEventSynchronize(b);
+        float ms = 0;
+        cudaEventElapsedTime(&ms, a, b);
+        best = std::min(best, ms);
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    cudaFree(out);
+    *gfma_per_s = (double)blocks * T * iters * 8 / (best * 1e-3) / 1e9;
+    return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
+
+int refresh_pos(pd_ctx* c, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_refresh_pos<<<grid_for(c, A.P.N), T, 0, s>>>(A);
+    c->launches++;
+    c->pos_valid = true;
+    return cuda_err(c, cudaGetLastError(), "refresh_pos");
+}
+
+int launch_prologue(pd_ctx* c, double load, int first_verlet, int cyl_step, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_prologue<<<grid_for(c, A.P.N), T, 0, s>>>(A, load, first_verlet, cyl_step);
+    c->launches++;
+    c->pos_valid = true;
+    return cuda_err(c, cudaGetLastError(), "prologue");
+}
+
+int launch_adr_update(pd_ctx* c, int ct, int do_next, double load, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_adr_update<<<grid_for(c, A.P.N), T, 0, s>>>(A, ct, do_next, load);
+    c->launches++;
+    c->pos_valid = true;
+    return cuda_err(c, cudaGetLastError(), "adr_update");
+}
+
+int launch_verlet1(pd_ctx* c, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_verlet1<<<grid_for(c, A.P.N_int), T, 0, s>>>(A);
+    c->launches++;
+    c->pos_valid = false;
+    return cuda_err(c, cudaGetLastError(), "verlet1");
+}
+
+int launch_verlet2(pd_ctx* c, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_verlet2<<<grid_for(c, A.P.N_int), T, 0, s>>>(A);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "verlet2");
+}
+
+int launch_quick_load(pd_ctx* c, double load, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_quick_load<<<grid_for(c, 6 * (int64_t)A.P.nx), T, 0, s>>>(A, load);
+    c->launches++;
+    c->pos_valid = false;
+    return cuda_err(c, cudaGetLastError(), "quick_load");
+}
+
+int launch_load_tensile(pd_ctx* c, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_load_tensile<<<grid_for(c, A.P.ny), T, 0, s>>>(A);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "load_plate_tensile");
+}
+
+int launch_damage(pd_ctx* c, cudaStream_t s) {
+    int rc = sync_fail_to_csr(c, s);
+    if (rc) return rc;
+    const KParams P = kparams(c->p);
+    k_damage<<<(unsigned)((P.N_int * 32 + T - 1) / T), T, 0, s>>>(P, c->rowptr, c->fail, c->fac, c->nf[PD_F_DMG]);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "damage");
+}
+
+int reduce_sum(pd_ctx* c, const double* x, int64_t n, double* out_dev, cudaStream_t s) {
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((n + T - 1) / T, 1024));
+    k_sum_partials<<<g, T, 0, s>>>(x, n, c->partials);
+    k_sum_final<<<1, T, 0, s>>>(c->partials, (int)g, out_dev);
+    c->launches += 2;
+    return cuda_err(c, cudaGetLastError(), "reduce_sum");
+}
+
+int check_finite(pd_ctx* c, cudaStream_t s, int* bad_host) {
+    int* d = reinterpret_cast<int*>(c->ticket) + 1;  // spare word after the ticket
+    cudaMemsetAsync(d, 0, sizeof(int), s);
+    NodeArgs A = node_args(c);
+    k_finite<<<grid_for(c, A.P.N), T, 0, s>>>(A, d);
+    c->launches++;
+    cudaError_t e = cudaMemcpyAsync(bad_host, d, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    return cuda_err(c, e, "check_finite");
+}
+
+}  // namespace pdg

@@ -1,0 +1,186 @@
+// Internal declarations of the GB300 peridynamics engine (not part of the C ABI).
+//
+// Layout in HBM
+//   node fields   SoA double arrays of N entries (the reference's BAtom,
+//                 Base.cuh:186-225), plus two ping-pong copies of the current
+//                 position P = x + u that the force kernels gather.
+//   bond family   CSR: rowptr (int64, N+1), NL (int32, B) with ascending rows,
+//                 and the reference's per-bond arrays idist, fac, scr, w, e
+//                 (double, B) and fail (int32, B) in CSR order.
+//   force layout  SELL-32: node rows are grouped into slices of 32 consecutive
+//                 rows; slot k of row 32s+l lives at sbase[s] + 32k + l, padded
+//                 to the slice's widest row.  One warp owns a slice, so every
+//                 per-bond load is a coalesced 32-wide access and the intact
+//                 flags of a slot are one 32-bit word (bit l = lane l).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "pd.h"
+
+namespace pdg {
+
+constexpr int kWarp = 32;
+constexpr int kForceBlock = 256;       // threads per block in the slice kernels
+constexpr int kMaxPartials = 8192;     // block partial sums of one reduction
+
+// Parameters the kernels read, passed by value (graph-capture friendly).
+struct KParams {
+    int64_t N, N_int;
+    int nx, ny, nz, dim, model;
+    double dx, emod, dens, pratio, bc, delta, critical_s, vol, dt, mass, K, G, pi, break_ymin;
+};
+
+// Rigid impactor state kept in device memory (Cylinder, Base.cuh:237-242).
+struct CylDev {
+    double rad, mass, height, v, x, y, z;
+    double vel[3], disp[3], acc[3], force[3];
+};
+
+// Per-bond coefficient arrays of the SELL layout.
+struct Sell {
+    int64_t nslices = 0;     // ceil(N / 32)
+    int64_t S = 0;           // total slots (sum of 32 * width)
+    int64_t F = 0;           // total flag words (sum of width)
+    int* width = nullptr;    // [nslices]
+    int64_t* base = nullptr; // [nslices] slot offset
+    int64_t* fbase = nullptr;// [nslices] flag-word offset
+    int* col = nullptr;      // [S] neighbour id (self for padding)
+    int* csr = nullptr;      // [S] CSR index of the slot (-1 for padding)
+    double* l0 = nullptr;    // [S] reference length |xi|
+    double* ecrit = nullptr; // [S] break threshold on e = L - l0 (s0 * l0; +inf: never)
+    double* k2 = nullptr;    // [S] bond-based: 2 * vol*fac*bc*scr / l0
+    double* c1 = nullptr;    // [S] state-based: dilatation coefficient of t
+    double* c2 = nullptr;    // [S] state-based: extension coefficient of t
+    double* cth = nullptr;   // [S] state-based: dilatation weight of e
+    double* xi = nullptr;    // [S*dim] state-based: x_c - x_i per component (SoA blocks)
+    double* e = nullptr;     // [S] state-based: extension (dilatation-pass operand order)
+    uint32_t* bits = nullptr;// [F] intact flags
+};
+
+}  // namespace pdg
+
+struct GraphEntry {
+    int kind, nsteps, parity, flags;
+    double load;
+    int dmg_every;
+    cudaGraphExec_t exec;
+    int64_t kernels;
+};
+
+struct pd_ctx {
+    pd_params p{};
+    std::string err;
+    int64_t launches = 0;
+    int device = 0;
+    int num_sms = 0;
+
+    // node fields, indexed by pd_field for ids < PD_F_NN (N doubles each)
+    double* nf[PD_F_NN] = {};
+    double* pos[2][3] = {};  // ping-pong current position P = x + u
+    int parity = 0;          // pos[parity] is current
+    bool pos_valid = false;  // pos[parity] == x + u
+    int* NN = nullptr;
+    double* node_a = nullptr;  // state-based: theta/m
+    double* node_b = nullptr;  // state-based: 1/m
+
+    // CSR bond family
+    int64_t B = 0;
+    int64_t* rowptr = nullptr;
+    int* NL = nullptr;
+    double *idist = nullptr, *fac = nullptr, *scr = nullptr, *w = nullptr, *e = nullptr;
+    int* fail = nullptr;
+
+    pdg::Sell sell;
+
+    // scratch
+    double* partials = nullptr;  // [kMaxPartials * 4]
+    unsigned int* ticket = nullptr;
+    double* cn = nullptr;        // ADR damping coefficient (device scalar)
+    double* red_out = nullptr;   // reduction result (device scalar)
+    pdg::CylDev* cyl = nullptr;
+    bool has_cyl = false;
+
+    // stage flags
+    bool family = false, volcorr = false, surfcorr = false, weights = false;
+    bool prepared = false;        // SELL arrays match the CSR coefficients
+    bool bits_current = false;    // SELL bits are the authoritative fail flags
+    bool csr_fail_current = true; // CSR fail array is current
+
+    std::vector<GraphEntry> graphs;
+};
+
+namespace pdg {
+
+inline KParams kparams(const pd_params& p) {
+    KParams k;
+    k.N = p.N;
+    k.N_int = p.N_int;
+    k.nx = p.nx;
+    k.ny = p.ny;
+    k.nz = p.nz;
+    k.dim = p.dim;
+    k.model = p.model;
+    k.dx = p.dx;
+    k.emod = p.emod;
+    k.dens = p.dens;
+    k.pratio = p.pratio;
+    k.bc = p.bc;
+    k.delta = p.delta;
+    k.critical_s = p.critical_s;
+    k.vol = p.vol;
+    k.dt = p.dt;
+    k.mass = p.mass;
+    k.K = p.K;
+    k.G = p.G;
+    k.pi = p.pi;
+    k.break_ymin = p.break_ymin;
+    return k;
+}
+
+int set_err(pd_ctx* c, int status, const std::string& msg);
+int cuda_err(pd_ctx* c, cudaError_t e, const char* what);
+inline cudaStream_t st(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// neighbour.cu
+int build_family(pd_ctx* c, cudaStream_t s);
+// setup.cu
+int vol_corr(pd_ctx* c, cudaStream_t s);
+int surface_correct(pd_ctx* c, cudaStream_t s);
+int initial_weight(pd_ctx* c, cudaStream_t s);
+int set_crack_2d(pd_ctx* c, double clength, double lx, double ly, double theta, cudaStream_t s);
+int set_crack_kw(pd_ctx* c, double rad, cudaStream_t s);
+int prepare(pd_ctx* c, cudaStream_t s);
+int sync_fail_to_csr(pd_ctx* c, cudaStream_t s);
+int sync_fail_to_bits(pd_ctx* c, cudaStream_t s);
+// force.cu
+enum Epi { EPI_NONE = 0, EPI_VERLET = 1, EPI_ADR = 2 };
+struct StepFlags {
+    int epi = EPI_NONE;
+    int do_next = 0;      // apply the next step's loading + first Verlet half
+    double load = 0.0;    // boundary-row speed of the next step (quick_load)
+    int contact = 0;      // rigid impactor contact in the epilogue
+};
+int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s);
+int launch_theta(pd_ctx* c, cudaStream_t s);
+// integrate.cu
+int refresh_pos(pd_ctx* c, cudaStream_t s);
+int launch_prologue(pd_ctx* c, double load, int first_verlet, int cyl_step, cudaStream_t s);
+int launch_adr_update(pd_ctx* c, int ct, int do_next, double load, cudaStream_t s);
+int launch_adr_cnn(pd_ctx* c, cudaStream_t s);
+int launch_verlet1(pd_ctx* c, cudaStream_t s);
+int launch_verlet2(pd_ctx* c, cudaStream_t s);
+int launch_damage(pd_ctx* c, cudaStream_t s);
+int launch_quick_load(pd_ctx* c, double load, cudaStream_t s);
+int launch_load_tensile(pd_ctx* c, cudaStream_t s);
+void release_sell(pd_ctx* c);
+int launch_contact(pd_ctx* c, cudaStream_t s);
+int launch_cyl_integrate(pd_ctx* c, int half, cudaStream_t s);
+int reduce_sum(pd_ctx* c, const double* x, int64_t n, double* out_dev, cudaStream_t s);
+int check_finite(pd_ctx* c, cudaStream_t s, int* bad_host);
+int fp64_probe(double* gfma_per_s);
+
+}  // namespace pdg

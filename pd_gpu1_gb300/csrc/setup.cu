@@ -1,0 +1,517 @@
+// Setup passes over the CSR bond family, and the build of the SELL-32 layout
+// the force kernels read.
+//
+//   vol_corr          kernel_vol_Corr (Surf_Corr.cu:7-35)
+//   surface_correct   surface_correct_gpu (Surf_Corr.cu:235-310): the reference
+//                     runs 5-8 launches with a displacement array per test
+//                     field and cudaMalloc/cudaFree temporaries; here one warp
+//                     per node computes idist, fac and the strain energy of all
+//                     test fields at once (u_axis = 0.001 x_axis is analytic),
+//                     then one pass forms scr per bond.
+//   initial_weight    kernel_initial_weight_2D/3D (Force_State.cu:8-54)
+//   set_crack_*       kernel_set_crack_2D (Base_Function.cu:39-81) and the
+//                     Kalthoff-Winkler notch cut (Solve_Kalthoff_Winkler.cu:40-63)
+//   prepare           per-bond coefficients in SELL order (see pd_internal.cuh)
+//
+// This file is compiled without FMA contraction: idist, fac, w and the crack
+// tests then round exactly like the reference's host code, so NL, idist, fac
+// and the fail flags agree bit for bit with it.
+#include <cmath>
+
+#include "pd_internal.cuh"
+
+namespace pdg {
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+__device__ __forceinline__ double bond_length(int dim, const double* x, const double* y, const double* z, int64_t i,
+                                              int64_t c) {
+    const double a = x[c] - x[i];
+    const double b = y[c] - y[i];
+    if (dim == 2) return sqrt(a * a + b * b);
+    const double d = z[c] - z[i];
+    return sqrt(a * a + b * b + d * d);
+}
+
+// idist and fac per bond (Surf_Corr.cu:17-32); one warp per node.
+__global__ void k_vol_corr(KParams P, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ z, const int64_t* __restrict__ rowptr,
+                           const int* __restrict__ NL, double* __restrict__ idist, double* __restrict__ fac) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N) return;
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        const int64_t c = NL[q];
+        const double L = bond_length(P.dim, x, y, z, i, c);
+        idist[q] = L;
+        double f;
+        if (L <= P.delta - P.dx / 2.0)
+            f = 1.0;
+        else if (L <= P.delta + P.dx / 2.0)
+            f = (P.delta + P.dx / 2.0 - L) / P.dx;
+        else
+            f = 0.0;
+        fac[q] = f;
+    }
+}
+
+// Strain energy density of node i under the test fields u_a = 0.001 x_a
+// (kernel_Disp + kernel_surface_F/_3D, Surf_Corr.cu:38-158), all axes in one
+// pass; fncst_a = sedload / energy.
+__global__ void k_surface_energy(KParams P, double sedload, const double* __restrict__ x,
+                                 const double* __restrict__ y, const double* __restrict__ z,
+                                 const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
+                                 const double* __restrict__ idist, const double* __restrict__ fac,
+                                 double* __restrict__ fx, double* __restrict__ fy, double* __restrict__ fz) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N) return;
+    const int dim = P.dim;
+    double st[3] = {0.0, 0.0, 0.0};
+    const double xi = x[i], yi = y[i], zi = dim == 3 ? z[i] : 0.0;
+    const double ui[3] = {0.001 * xi, 0.001 * yi, 0.001 * zi};
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        const int64_t c = NL[q];
+        const double xc = x[c], yc = y[c], zc = dim == 3 ? z[c] : 0.0;
+        const double L0 = idist[q];
+        for (int a = 0; a < dim; a++) {
+            // displacement only along axis a (the other components are zero,
+            // and adding zero is exact, so the reference's expression reduces
+            // to the plain coordinate difference on those axes)
+            const double uxc = a == 0 ? 0.001 * xc : 0.0, uxi = a == 0 ? ui[0] : 0.0;
+            const double uyc = a == 1 ? 0.001 * yc : 0.0, uyi = a == 1 ? ui[1] : 0.0;
+            const double ddx = xc + uxc - xi - uxi;
+            const double ddy = yc + uyc - yi - uyi;
+            double L;
+            if (dim == 2) {
+                L = sqrt(ddx * ddx + ddy * ddy);
+            } else {
+                const double uzc = a == 2 ? 0.001 * zc : 0.0, uzi = a == 2 ? ui[2] : 0.0;
+                const double ddz = zc + uzc - zi - uzi;
+                L = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+            }
+            st[a] += 0.25 * P.bc * (L - L0) * (L - L0) / L0 * P.vol * fac[q];
+        }
+    }
+    const double sx = warp_sum(st[0]);
+    const double sy = warp_sum(st[1]);
+    const double sz = warp_sum(st[2]);
+    if (lane == 0) {
+        fx[i] = sedload / sx;
+        fy[i] = sedload / sy;
+        if (dim == 3) fz[i] = sedload / sz;
+    }
+}
+
+// scr per bond (kernel_cal_surf_coff_F, Surf_Corr.cu:160-232).
+__global__ void k_surface_coeff(KParams P, const double* __restrict__ x, const double* __restrict__ y,
+                                const double* __restrict__ z, const int64_t* __restrict__ rowptr,
+                                const int* __restrict__ NL, const double* __restrict__ idist,
+                                const double* __restrict__ fnx, const double* __restrict__ fny,
+                                const double* __restrict__ fnz, double* __restrict__ scr) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N) return;
+    const double half_pi = 90.0 * P.pi / 180.0;
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        const int64_t c = NL[q];
+        const double scx = (fnx[i] + fnx[c]) / 2.0;
+        const double scy = (fny[i] + fny[c]) / 2.0;
+        const double adx = fabs(x[c] - x[i]), ady = fabs(y[c] - y[i]);
+        if (P.dim == 2) {
+            double th;
+            if (ady <= 1.0e-10)
+                th = 0.0;
+            else if (adx <= 1.0e-10)
+                th = half_pi;
+            else
+                th = atan(ady / adx);
+            scr[q] = sqrt(1.0 / (cos(th) * cos(th) / (scx * scx) + sin(th) * sin(th) / (scy * scy)));
+        } else {
+            const double scz = (fnz[i] + fnz[c]) / 2.0;
+            const double adz = fabs(z[c] - z[i]);
+            if (adz < 1.0e-10) {
+                double th;
+                if (ady < 1.0e-10)
+                    th = 0.0;
+                else if (adx < 1.0e-10)
+                    th = half_pi;
+                else
+                    th = atan(ady / adx);
+                const double phi = half_pi;
+                scr[q] = sqrt(1.0 / (cos(th) * cos(th) / (scx * scx) + sin(th) * sin(th) / (scy * scy) +
+                                     cos(phi) * cos(phi) / (scz * scz)));
+            } else if (adx < 1.0e-10 && ady < 1.0e-10) {
+                scr[q] = scz;
+            } else {
+                const double th = atan(ady / adx);
+                const double phi = acos(adz / idist[q]);
+                scr[q] = sqrt(1.0 / (cos(th) * cos(th) / (scx * scx) + sin(th) * sin(th) / (scy * scy) +
+                                     cos(phi) * cos(phi) / (scz * scz)));
+            }
+        }
+    }
+}
+
+// w per bond, m per node (Force_State.cu:8-54).
+__global__ void k_weight(KParams P, const int64_t* __restrict__ rowptr, const double* __restrict__ idist,
+                         const double* __restrict__ fac, double* __restrict__ w, double* __restrict__ m) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N) return;
+    double acc = 0.0;
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        const double L0 = idist[q];
+        const double wq = exp(-(L0 * L0) / (P.delta * P.delta));
+        w[q] = wq;
+        acc += wq * (L0 * L0) * P.vol * fac[q];
+    }
+    acc = warp_sum(acc);
+    if (lane == 0) m[i] = acc;
+}
+
+// Pre-crack segment test (Base_Function.cu:39-81) on nodes [0, N_int).
+__global__ void k_set_crack_2d(KParams P, double clength, double lx, double ly, double theta,
+                               const double* __restrict__ x, const double* __restrict__ y,
+                               const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
+                               int* __restrict__ fail) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N_int) return;
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        const int64_t c = NL[q];
+        if (fabs(theta - P.pi / 2.0) < 0.0001) {
+            if (fabs(y[c] - ly) < clength * sin(theta) / 2.0 && fabs(y[i] - ly) < clength * sin(theta) / 2.0)
+                if ((x[c] - lx) * (x[i] - lx) < 0.0) fail[q] = 0;
+        } else {
+            const double t = tan(theta);
+            const double dist_c = (y[c] - ly) * (y[c] - ly) + (x[c] - lx) * (x[c] - lx);
+            const double dist_i = (y[i] - ly) * (y[i] - ly) + (x[i] - lx) * (x[i] - lx);
+            const double vc0 = (t * x[c] - y[c] - lx * t + ly) / sqrt(1 + t * t);
+            const double vi0 = (t * x[i] - y[i] - lx * t + ly) / sqrt(1 + t * t);
+            const double len_c = sqrt(dist_c - vc0 * vc0);
+            const double len_i = sqrt(dist_i - vi0 * vi0);
+            if (len_c < clength / 2.0 && len_i < clength / 2.0) {
+                const double bcn = t * x[c] - lx * t + ly - y[c];
+                const double bi = t * x[i] - lx * t + ly - y[i];
+                if (bcn * bi <= 0) fail[q] = 0;
+            }
+        }
+    }
+}
+
+// Notch cut of the Kalthoff-Winkler slab (Solve_Kalthoff_Winkler.cu:40-63).
+__global__ void k_set_crack_kw(KParams P, double rad, const double* __restrict__ x, const double* __restrict__ y,
+                               const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
+                               int* __restrict__ fail) {
+    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= P.N_int) return;
+    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
+        const int64_t c = NL[q];
+        const bool upper = (y[c] >= -1.0e-10) | (y[i] >= -1.0e-10);
+        if (((x[c] > -rad && x[i] < -rad) | (x[i] > -rad && x[c] < -rad)) && upper) fail[q] = 0;
+        if (((x[c] > rad && x[i] < rad) | (x[i] > rad && x[c] < rad)) && upper) fail[q] = 0;
+    }
+}
+
+// ---- SELL-32 layout -------------------------------------------------------
+
+__global__ void k_slice_width(int64_t N, int64_t nslices, const int* __restrict__ NN, int* __restrict__ width) {
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    const int64_t r = s * 32 + lane;
+    int v = r < N ? NN[r] : 0;
+    for (int off = 16; off > 0; off >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, off));
+    if (lane == 0) width[s] = v;
+}
+
+// One thread per slot.  Padding slots point at their own row, carry zero
+// coefficients and a cleared intact bit, so they contribute nothing.
+__global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ width,
+                            const int64_t* __restrict__ base, const int* __restrict__ NN,
+                            const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
+                            const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
+                            const double* __restrict__ idist, const double* __restrict__ fac,
+                            const double* __restrict__ scr, const double* __restrict__ w, const double* __restrict__ m,
+                            Sell S) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int k = t >> 5, l = t & 31;
+        const int64_t r = s * 32 + l;
+        const int64_t slot = b + t;
+        const bool used = r < P.N && k < NN[r];
+        const int64_t q = used ? rowptr[r] + k : -1;
+        S.csr[slot] = (int)(used ? q : -1);
+        if (!used) {
+            S.col[slot] = (int)(r < P.N ? r : 0);
+            S.l0[slot] = 1.0;
+            S.ecrit[slot] = HUGE_VAL;
+            if (S.k2) S.k2[slot] = 0.0;
+            if (S.c1) {
+                S.c1[slot] = 0.0;
+                S.c2[slot] = 0.0;
+                S.cth[slot] = 0.0;
+                for (int a = 0; a < P.dim; a++) S.xi[a * S.S + slot] = 0.0;
+                S.e[slot] = 0.0;
+            }
+            continue;
+        }
+        const int64_t c = NL[q];
+        S.col[slot] = (int)c;
+        const double L0 = idist[q];
+        S.l0[slot] = L0;
+        // break when s = (L - L0)/L0 > s0, i.e. e = L - L0 > s0 L0; the 3-D
+        // kernels break only bonds whose ends both have y >= -0.04 (Force_Bond.cu:117)
+        bool breakable = true;
+        if (P.dim == 3) breakable = y[r] >= P.break_ymin && y[c] >= P.break_ymin;
+        S.ecrit[slot] = breakable ? P.critical_s * L0 : HUGE_VAL;
+        if (S.k2) S.k2[slot] = 2.0 * (P.vol * fac[q] * P.bc * scr[q]) / L0;
+        if (S.c1) {
+            const double pr = P.pratio;
+            double a_coef, b_coef, th_coef;
+            if (P.dim == 2) {
+                a_coef = (2.0 * pr - 1.0) / (pr - 1.0) * (2.0 * P.K - 32.0 * P.G / 9.0);
+                b_coef = 8.0 * P.G;
+                th_coef = 2.0 * (2.0 * pr - 1.0) / (pr - 1.0);
+            } else {
+                a_coef = 3.0 * P.K - 5.0 * P.G;  // 3K th w L0/m + 15G/m w (e - th L0/3)
+                b_coef = 15.0 * P.G;
+                th_coef = 3.0;
+            }
+            const double wf = w[q] * fac[q] * P.vol;
+            S.c1[slot] = 2.0 * a_coef * wf * L0;
+            S.c2[slot] = 2.0 * b_coef * wf;
+            S.cth[slot] = th_coef * w[q] * L0 * fac[q] * P.vol;
+            S.xi[slot] = x[c] - x[r];
+            S.xi[S.S + slot] = y[c] - y[r];
+            if (P.dim == 3) S.xi[2 * S.S + slot] = z[c] - z[r];
+            S.e[slot] = 0.0;
+        }
+    }
+}
+
+// Intact flags: CSR int32 <-> SELL bit words.
+__global__ void k_bits_from_csr(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
+                                const int64_t* __restrict__ fbase, const int* __restrict__ csr,
+                                const int* __restrict__ fail, int64_t n_rows_breakable, uint32_t* __restrict__ bits) {
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    const int W = width[s];
+    for (int k = 0; k < W; k++) {
+        const int64_t slot = base[s] + k * 32 + lane;
+        const int q = csr[slot];
+        // rows past N_int have no fail storage in the reference (Memory.cu:39):
+        // their bonds count as intact
+        const bool alive = q >= 0 && ((s * 32 + lane) >= n_rows_breakable || fail[q] == 1);
+        const uint32_t word = __ballot_sync(0xffffffffu, alive);
+        if (lane == 0) bits[fbase[s] + k] = word;
+    }
+}
+
+__global__ void k_csr_from_bits(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
+                                const int64_t* __restrict__ fbase, const int* __restrict__ csr,
+                                const uint32_t* __restrict__ bits, int* __restrict__ fail) {
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    const int W = width[s];
+    for (int k = 0; k < W; k++) {
+        const int64_t slot = base[s] + k * 32 + lane;
+        const int q = csr[slot];
+        if (q >= 0) fail[q] = (bits[fbase[s] + k] >> lane) & 1u;
+    }
+}
+
+__global__ void k_inv_m(int64_t N, const double* __restrict__ m, double* __restrict__ inv) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < N) inv[i] = 1.0 / m[i];
+}
+
+unsigned warps_grid(int64_t nwarps) { return (unsigned)((nwarps * 32 + 255) / 256); }
+
+template <typename T>
+void free_ptr(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+int vol_corr(pd_ctx* c, cudaStream_t s) {
+    if (!c->family) return set_err(c, PD_ERR_STATE, "vol_corr needs the bond family");
+    const KParams P = kparams(c->p);
+    k_vol_corr<<<warps_grid(P.N), 256, 0, s>>>(P, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->rowptr, c->NL,
+                                                c->idist, c->fac);
+    c->launches++;
+    c->volcorr = true;
+    c->prepared = false;
+    return cuda_err(c, cudaGetLastError(), "vol_corr");
+}
+
+int surface_correct(pd_ctx* c, cudaStream_t s) {
+    int rc = vol_corr(c, s);
+    if (rc) return rc;
+    const KParams P = kparams(c->p);
+    const double sedload = P.dim == 3 ? 0.6 * P.emod * 1.0e-6 : 0.5 * P.emod / (1.0 - P.pratio * P.pratio) * 1.0e-6;
+    double *X = c->nf[PD_F_X], *Y = c->nf[PD_F_Y], *Z = c->nf[PD_F_Z];
+    k_surface_energy<<<warps_grid(P.N), 256, 0, s>>>(P, sedload, X, Y, Z, c->rowptr, c->NL, c->idist, c->fac,
+                                                      c->nf[PD_F_FNCST_X], c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z]);
+    k_surface_coeff<<<warps_grid(P.N), 256, 0, s>>>(P, X, Y, Z, c->rowptr, c->NL, c->idist, c->nf[PD_F_FNCST_X],
+                                                     c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z], c->scr);
+    c->launches += 2;
+    c->surfcorr = true;
+    c->prepared = false;
+    return cuda_err(c, cudaGetLastError(), "surface_correct");
+}
+
+int initial_weight(pd_ctx* c, cudaStream_t s) {
+    if (!c->volcorr) {
+        int rc = vol_corr(c, s);
+        if (rc) return rc;
+    }
+    const KParams P = kparams(c->p);
+    k_weight<<<warps_grid(P.N), 256, 0, s>>>(P, c->rowptr, c->idist, c->fac, c->w, c->nf[PD_F_M]);
+    c->launches++;
+    c->weights = true;
+    c->prepared = false;
+    return cuda_err(c, cudaGetLastError(), "initial_weight");
+}
+
+int sync_fail_to_csr(pd_ctx* c, cudaStream_t s) {
+    if (c->csr_fail_current) return PD_OK;
+    const Sell& S = c->sell;
+    k_csr_from_bits<<<warps_grid(S.nslices), 256, 0, s>>>(S.nslices, S.width, S.base, S.fbase, S.csr, S.bits,
+                                                           c->fail);
+    c->launches++;
+    c->csr_fail_current = true;
+    return cuda_err(c, cudaGetLastError(), "fail flags to CSR");
+}
+
+int sync_fail_to_bits(pd_ctx* c, cudaStream_t s) {
+    if (c->bits_current) return PD_OK;
+    const Sell& S = c->sell;
+    k_bits_from_csr<<<warps_grid(S.nslices), 256, 0, s>>>(S.nslices, S.width, S.base, S.fbase, S.csr, c->fail,
+                                                           c->p.N_int, S.bits);
+    c->launches++;
+    c->bits_current = true;
+    return cuda_err(c, cudaGetLastError(), "fail flags to bits");
+}
+
+int set_crack_2d(pd_ctx* c, double clength, double lx, double ly, double theta, cudaStream_t s) {
+    if (!c->family) return set_err(c, PD_ERR_STATE, "set_crack needs the bond family");
+    int rc = sync_fail_to_csr(c, s);
+    if (rc) return rc;
+    const KParams P = kparams(c->p);
+    k_set_crack_2d<<<warps_grid(P.N_int), 256, 0, s>>>(P, clength, lx, ly, theta, c->nf[PD_F_X], c->nf[PD_F_Y],
+                                                        c->rowptr, c->NL, c->fail);
+    c->launches++;
+    c->bits_current = false;
+    return cuda_err(c, cudaGetLastError(), "set_crack_2d");
+}
+
+int set_crack_kw(pd_ctx* c, double rad, cudaStream_t s) {
+    if (!c->family) return set_err(c, PD_ERR_STATE, "set_crack needs the bond family");
+    int rc = sync_fail_to_csr(c, s);
+    if (rc) return rc;
+    const KParams P = kparams(c->p);
+    k_set_crack_kw<<<warps_grid(P.N_int), 256, 0, s>>>(P, rad, c->nf[PD_F_X], c->nf[PD_F_Y], c->rowptr, c->NL,
+                                                        c->fail);
+    c->launches++;
+    c->bits_current = false;
+    return cuda_err(c, cudaGetLastError(), "set_crack_kw");
+}
+
+static void free_sell(Sell& S) {
+    free_ptr(S.width);
+    free_ptr(S.base);
+    free_ptr(S.fbase);
+    free_ptr(S.col);
+    free_ptr(S.csr);
+    free_ptr(S.l0);
+    free_ptr(S.ecrit);
+    free_ptr(S.k2);
+    free_ptr(S.c1);
+    free_ptr(S.c2);
+    free_ptr(S.cth);
+    free_ptr(S.xi);
+    free_ptr(S.e);
+    free_ptr(S.bits);
+    S.nslices = S.S = S.F = 0;
+}
+
+void release_sell(pd_ctx* c) { free_sell(c->sell); }
+
+int prepare(pd_ctx* c, cudaStream_t s) {
+    if (!c->family) return set_err(c, PD_ERR_STATE, "prepare needs the bond family");
+    int rc;
+    if (!c->volcorr && (rc = vol_corr(c, s))) return rc;
+    const bool state = c->p.model == PD_MODEL_STATE;
+    if (state && !c->weights && (rc = initial_weight(c, s))) return rc;
+    // the SELL fail bits are rebuilt from the CSR flags
+    if ((rc = sync_fail_to_csr(c, s))) return rc;
+    const KParams P = kparams(c->p);
+    Sell& S = c->sell;
+    free_sell(S);
+    S.nslices = (P.N + 31) / 32;
+    cudaError_t e;
+    if ((e = cudaMalloc(&S.width, S.nslices * sizeof(int))) || (e = cudaMalloc(&S.base, S.nslices * 8)) ||
+        (e = cudaMalloc(&S.fbase, (S.nslices + 1) * 8)))
+        return set_err(c, PD_ERR_NOMEM, "slice tables");
+    k_slice_width<<<warps_grid(S.nslices), 256, 0, s>>>(P.N, S.nslices, c->NN, S.width);
+    c->launches++;
+    std::vector<int> w((size_t)S.nslices);
+    if ((e = cudaMemcpyAsync(w.data(), S.width, w.size() * sizeof(int), cudaMemcpyDeviceToHost, s)) ||
+        (e = cudaStreamSynchronize(s)))
+        return cuda_err(c, e, "slice widths");
+    std::vector<int64_t> fb((size_t)S.nslices + 1), bs((size_t)S.nslices);
+    int64_t acc = 0;
+    int wmax = 0;
+    for (int64_t k = 0; k < S.nslices; k++) {
+        fb[k] = acc;
+        bs[k] = acc * 32;
+        acc += w[k];
+        wmax = std::max(wmax, w[k]);
+    }
+    fb[S.nslices] = acc;
+    S.F = acc;
+    S.S = acc * 32;
+    cudaMemcpyAsync(S.fbase, fb.data(), fb.size() * 8, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
+    const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
+    bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.l0, n8) &&
+              !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
+    if (ok && !state) ok = !cudaMalloc(&S.k2, n8);
+    if (ok && state)
+        ok = !cudaMalloc(&S.c1, n8) && !cudaMalloc(&S.c2, n8) && !cudaMalloc(&S.cth, n8) &&
+             !cudaMalloc(&S.xi, n8 * P.dim) && !cudaMalloc(&S.e, n8);
+    if (!ok) {
+        free_sell(S);
+        return set_err(c, PD_ERR_NOMEM, "SELL bond arrays");
+    }
+    const unsigned gx = (unsigned)std::min<int64_t>(S.nslices, 65535);
+    const unsigned gy = (unsigned)((S.nslices + gx - 1) / gx);
+    k_sell_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, c->NN, c->rowptr, c->NL, c->nf[PD_F_X],
+                                              c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac, c->scr, c->w,
+                                              c->nf[PD_F_M], S);
+    c->launches++;
+    if (state) {
+        k_inv_m<<<(unsigned)((P.N + 255) / 256), 256, 0, s>>>(P.N, c->nf[PD_F_M], c->node_b);
+        c->launches++;
+    }
+    c->bits_current = false;
+    if ((rc = sync_fail_to_bits(c, s))) return rc;
+    c->prepared = true;
+    return cuda_err(c, cudaGetLastError(), "prepare");
+}
+
+}  // namespace pdg

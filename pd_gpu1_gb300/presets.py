@@ -1,0 +1,163 @@
+"""Named workloads: the benchmark configurations as engine set-ups.
+
+Each ``build_*`` function returns ``(params, setup)`` where ``setup(engine)``
+performs the set-up sequence of the matching reference driver on an
+:class:`~pd_gpu1_gb300.engine.Engine` created from ``params``.  ``scale``
+shrinks the plate (same dx) for quick tests.
+
+Critical stretch from fracture energy G0 (the reference has no such formula,
+so one published closed form is fixed here and used on every side):
+  2-D bond-based, plane stress (Ha & Bobaru 2010):  s0 = sqrt(4 pi G0 / (9 E delta))
+  3-D (Silling & Askari 2005):                      s0 = sqrt(5 G0 / (9 K delta)), K = E / (3 (1 - 2 nu))
+"""
+import math
+
+import numpy as np
+
+from ._abi import PD_MODE_DYNAMIC, PD_MODE_STATIC, PD_MODEL_BOND, PD_MODEL_STATE, PDCylinder
+
+
+def _derive(derive):
+    if derive is not None:
+        return derive
+    from .engine import derive_params
+
+    return derive_params
+
+
+def _coord_kw(fn):
+    if fn is not None:
+        return fn
+    from .engine import coord_kw
+
+    return coord_kw
+
+
+def s0_2d(G0, E, delta):
+    return math.sqrt(4.0 * math.pi * G0 / (9.0 * E * delta))
+
+
+def s0_3d(G0, E, nu, delta):
+    K = E / (3.0 * (1.0 - 2.0 * nu))
+    return math.sqrt(5.0 * G0 / (9.0 * K * delta))
+
+
+# ---- plate tensile, 2-D PMB, ADR (1000 steps) ---------------------------------------
+def build_plate_tensile(scale=1.0, dx=5e-4, nt=1000, derive=None):
+    """0.05 x 0.05 m plate, dx = 5e-4 (100 x 100 nodes) plus 3 boundary rows above
+    and below (the crack-plate layout, Coord.cu:34-45), E = 192 GPa, nu = 1/3,
+    rho = 8000, s0 = 0.04472, thickness dx, surface correction on, ADR with
+    dt = 1; the boundary rows move +-2.7e-8 m per step."""
+    L = 0.05 * scale
+    p = _derive(derive)(2, PD_MODEL_BOND, PD_MODE_STATIC, 1.0, nt, dx, 0.0, dx, L, L, 0.0, 192.0e9, 1.0 / 3.0, 8000.0,
+                      0.04472)
+    p.N = p.N_int + 6 * p.nx
+    load = 2.7e-8 / p.dt  # kernel_quick_load moves rows by load*dt per step
+
+    def setup(eng):
+        eng.coord_plate_crack()
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
+        eng.prepare()
+
+    return p, setup, dict(load=load, nt=nt, workload="plate_tensile_2d_pmb_adr")
+
+
+# ---- dynamic crack branching, 2-D PMB, Verlet (1800 steps, headline) ------------------
+def build_crack_branching(scale=1.0, dx=5e-5, nt=1800, derive=None):
+    """0.1 x 0.04 m glass plate, dx = 5e-5 (2000 x 800 = 1.6M nodes),
+    E = 72 GPa, nu = 1/3, rho = 2440, G0 = 3.8 J/m^2, pre-crack 0.05 m along
+    the mid-line from the left edge, 12 MPa traction on the top and bottom rows
+    as body force sigma/dx, dt = 2.5e-8, damage every 100 steps."""
+    Lx, Ly = 0.1 * scale, 0.04 * scale
+    E, nu, rho, G0 = 72.0e9, 1.0 / 3.0, 2440.0, 3.8
+    delta = 3.015 * dx
+    s0 = s0_2d(G0, E, delta)
+    p = _derive(derive)(2, PD_MODEL_BOND, PD_MODE_DYNAMIC, 2.5e-8, nt, dx, 0.0, dx, Lx, Ly, 0.0, E, nu, rho, s0)
+    sigma = 12.0e6
+
+    def setup(eng):
+        eng.coord_plate()
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
+        # pre-crack: half the plate length, from the left edge along y = 0
+        eng.set_crack_2d(Lx / 2.0, -Lx / 4.0, 0.0, 0.0)
+        eng.set("BY", traction_field(p, sigma))
+        eng.prepare()
+
+    return p, setup, dict(load=0.0, nt=nt, dmg_every=100, workload="crack_branching_2d_pmb_verlet", s0=s0,
+                          sigma=sigma)
+
+
+def traction_field(p, sigma):
+    """Body force sigma/dx on the top row (+y) and bottom row (-y) of a plate
+    laid out row by row, as load_plate_tensile applies its edge load
+    (Solve_Plate_Tensile.cu:12)."""
+    by = np.zeros(p.N)
+    by[(p.ny - 1) * p.nx: p.ny * p.nx] = sigma / p.dx
+    by[0: p.nx] = -sigma / p.dx
+    return by
+
+
+# ---- Kalthoff-Winkler impact, 3-D state-based, Verlet (1350 steps) -------------------
+def build_kalthoff_winkler(scale=1.0, dx=1e-3, nt=1350, model=PD_MODEL_STATE, derive=None, coord_fn=None):
+    """Notched slab of coord_KW (Coord.cu:77-129): 0.2 x 0.1 x 0.009 m, dx = 1e-3
+    (201 x 101 x 9 grid points minus the two notch strips at x = +-0.025 in the
+    upper half), E = 190 GPa, nu = 0.25, rho = 8000, G0 = 22170 J/m^2, rigid
+    cylindrical impactor (mass 1.57 kg, radius 0.025 m, height 0.05 m) at 32 m/s,
+    dt = 1e-7.  Bulk modulus K = E / (3 (1 - 2 nu)) (the reference's 3-D
+    formula at Base.cuh:175 divides by (1 - 2G) instead)."""
+    L, H, W = 0.2 * scale, 0.1 * scale, 0.009
+    E, nu, rho, G0 = 190.0e9, 0.25, 8000.0, 22170.0
+    delta = 3.015 * dx
+    s0 = s0_3d(G0, E, nu, delta)
+    p = _derive(derive)(3, model, PD_MODE_DYNAMIC, 1.0e-7, nt, dx, 1.0, dx, L, H, W, E, nu, rho, s0, fix_k3d=1)
+    p.nx += 1
+    p.ny += 1
+    rad = 0.025 * scale
+    x, y, z = _coord_kw(coord_fn)(p, rad)
+    p.N = p.N_int = len(x)
+    cyl = PDCylinder()
+    cyl.rad, cyl.mass, cyl.height, cyl.v = rad, 1.57, 0.05 * scale, -32.0
+    cyl.x, cyl.y, cyl.z = 0.0, H / 2.0 + cyl.height / 2.0 + 0.1 * dx, 0.0
+    cyl.vel[1] = cyl.v
+
+    def setup(eng):
+        eng.set_coords(x, y, z)
+        eng.find_neighbor_gpu()
+        if model == PD_MODEL_BOND:
+            eng.surface_correct_gpu()
+        else:
+            eng.vol_corr()
+            eng.initial_weight()
+        eng.initial_state()
+        eng.set_crack_kw(rad)
+        eng.cylinder_init(cyl)
+        eng.prepare()
+
+    return p, setup, dict(load=0.0, nt=nt, workload="kalthoff_winkler_3d_state_verlet", cylinder=cyl, s0=s0, rad=rad,
+                          coords=(x, y, z))
+
+
+# ---- crack growth, 2-D state-based, Verlet (the reference crack-grow driver) ---------
+def build_crack_grow(scale=1.0, dx=1e-4, nt=1250, derive=None):
+    """Solve_Plate_Crack_Grow.cu:177-179: 0.05 x 0.05 m plate, dx = 1e-4,
+    state-based, E = 192 GPa, nu = 0.3, rho = 7850, s0 = 0.04472, boundary rows
+    moving +-20*dt per step, centre crack 0.01 m."""
+    L = 0.05 * scale
+    p = _derive(derive)(2, PD_MODEL_STATE, PD_MODE_DYNAMIC, 1.3367e-8, nt, dx, 1.0, dx, L, L, 0.0, 192.0e9, 0.3, 7850.0,
+                      0.04472)
+    p.N = p.N_int + 6 * p.nx
+
+    def setup(eng):
+        eng.coord_plate_crack()
+        eng.find_neighbor_gpu()
+        eng.initial_state()
+        eng.set_crack_2d(0.01 * scale, 0.0, 0.0, 0.0)
+        eng.vol_corr()
+        eng.initial_weight()
+        eng.prepare()
+
+    return p, setup, dict(load=20.0, nt=nt, workload="plate_crack_grow_2d_state_verlet")

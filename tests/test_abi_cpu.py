@@ -1,0 +1,102 @@
+"""CPU checks of the C ABI: the library loads without a GPU, exports every
+entry point include/pd.h declares, and its host-only entry points (parameter
+derivation, notched-slab coordinates) agree bit for bit with the oracle and
+the reference's derivation recorded in the golden fixtures."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+
+import oracle as orc
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    txt = open(os.path.join(ROOT, "include", "pd.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(pd_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from pd_gpu1_gb300._lib import LIB_PATH, exported_symbols
+
+    assert os.path.exists(LIB_PATH), "build the library first (__graft_entry__.build())"
+    handle = C.CDLL(LIB_PATH)
+    decl = declared_symbols()
+    assert len(decl) > 40
+    missing = [s for s in decl if not hasattr(handle, s)]
+    assert not missing, missing
+    # the Python binding covers the same set
+    assert sorted(exported_symbols()) == decl
+
+
+def test_status_strings():
+    from pd_gpu1_gb300._lib import lib
+
+    L = lib()
+    for code, name in [(0, b"PD_OK"), (-1, b"PD_ERR_ARG"), (-4, b"PD_ERR_FAMILY"), (-5, b"PD_ERR_NONFINITE")]:
+        assert L.pd_status_string(code) == name
+
+
+def test_param_derivation_matches_oracle_and_reference(golden):
+    from pd_gpu1_gb300.engine import derive_params
+
+    cases = [
+        (2, 1, 1, 1.0, 1000, 0.01, 1.0, 0.01, 1.0, 0.5, 0.0, 200e9, 1 / 3, 7850, 1.0, 0),
+        (2, 2, 2, 1.3367e-8, 1250, 1e-4, 1.0, 1e-4, 0.05, 0.05, 0.0, 192e9, 0.3, 7850, 0.04472, 0),
+        (3, 1, 2, 8.7e-8, 0, 1e-3, 1.0, 1e-3, 0.2, 0.1, 0.009, 191e9, 0.25, 8000, 0.01, 0),
+        (3, 2, 2, 1e-7, 1350, 1e-3, 1.0, 1e-3, 0.2, 0.1, 0.009, 190e9, 0.25, 8000, 0.01, 1),
+        (2, 1, 2, 2.5e-8, 1800, 5e-5, 0.0, 5e-5, 0.1, 0.04, 0.0, 72e9, 1 / 3, 2440, 7e-4, 0),
+    ]
+    for c in cases:
+        a = derive_params(*c)
+        b = orc.derive_params(*c)
+        for name, _ in a._fields_:
+            assert getattr(a, name) == getattr(b, name), (c, name)
+    g = golden("plate_tensile_bond")
+    a = derive_params(2, 1, 1, 1.0, 1000, 0.01, 1.0, 0.01, 0.2, 0.1, 0.0, 200e9, 1 / 3, 7850, 1.0)
+    for k in ["bc", "delta", "vol", "mass"]:
+        assert getattr(a, k) == float(g["p_" + k]), k
+
+
+def test_coord_kw_matches_oracle_and_reference(golden):
+    from pd_gpu1_gb300.engine import coord_kw, derive_params
+
+    g = golden("kalthoff_winkler_bond")
+    p = derive_params(3, 1, 2, 8.7e-8, 0, 0.003, 1.0, 0.003, 0.06, 0.1, 0.009, 191e9, 0.25, 8000, 0.01)
+    p.nx += 1
+    p.ny += 1
+    p.N = p.nx * p.ny * p.nz
+    x, y, z = coord_kw(p, float(g["rad"]))
+    np.testing.assert_array_equal(x, g["x"])
+    np.testing.assert_array_equal(y, g["y"])
+    np.testing.assert_array_equal(z, g["z"])
+    xo, yo, zo = orc.coord_kw(p, float(g["rad"]))
+    np.testing.assert_array_equal(x, xo)
+
+
+def test_full_size_kalthoff_winkler_node_count():
+    """coord_KW at the reference's own size gives 180,873 nodes."""
+    from pd_gpu1_gb300.engine import coord_kw, derive_params
+
+    p = derive_params(3, 1, 2, 8.7e-8, 0, 1e-3, 1.0, 1e-3, 0.2, 0.1, 0.009, 191e9, 0.25, 8000, 0.01)
+    p.nx += 1
+    p.ny += 1
+    x, _, _ = coord_kw(p, 0.025)
+    assert len(x) == 180873
+
+
+def test_abi_struct_layout_matches_header():
+    """The ctypes mirror of pd_params has the C layout (field order and offsets)."""
+    from pd_gpu1_gb300._abi import PDParams
+
+    txt = open(os.path.join(ROOT, "include", "pd.h")).read()
+    body = txt[txt.index("typedef struct pd_params {"): txt.index("} pd_params;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    names = []
+    for decl in re.findall(r"(?:double|int32_t)\s+([^;]+);", body):
+        names += [n.strip() for n in decl.split(",")]
+    assert names == [f for f, _ in PDParams._fields_]
+    assert C.sizeof(PDParams) % 8 == 0

@@ -1,0 +1,367 @@
+"""Parity of the CUDA engine (through the C ABI) with the golden vectors of the
+reference's CPU functions and with the oracle.
+
+Bars:
+  - bond family (NN, NL), idist, fac and fail flags: bit-exact;
+  - per-node forces: |f - f_ref| <= 1e-12 * max|f_ref| (norm-relative);
+  - derived per-bond coefficients (scr, w) and per-node m: 1e-13 norm-relative;
+  - displacements after many steps: stated per test.
+"""
+import numpy as np
+import pytest
+
+import oracle as orc
+from helpers import assert_close_norm, model_from_golden, params_from_golden
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def E():
+    from pd_gpu1_gb300 import engine
+
+    engine.lib()
+    return engine
+
+
+def engine_from_golden(E, g, p=None):
+    p = p or params_from_golden(g)
+    eng = E.Engine(p)
+    eng.set_coords(g["x"], g["y"], g.get("z"))
+    return eng
+
+
+def test_family_matches_reference_exactly(E, golden):
+    for name in ["plate_tensile_bond", "plate_crack_state", "kalthoff_winkler_bond"]:
+        g = golden(name)
+        with engine_from_golden(E, g) as eng:
+            eng.find_neighbor_gpu()
+            np.testing.assert_array_equal(eng.get("NN"), g["NN"], err_msg=name)
+            np.testing.assert_array_equal(eng.get("NL"), g["NL"], err_msg=name)
+            rp = eng.get("ROWPTR")
+            assert rp[-1] == len(g["NL"]) == eng.num_bonds
+    g = golden("neighbor_medium")
+    p2 = params_from_golden(g, "n2_")
+    with E.Engine(p2) as eng:
+        eng.coord_plate()
+        eng.find_neighbor_gpu()
+        np.testing.assert_array_equal(eng.get("NN"), g["n2_NN"])
+        np.testing.assert_array_equal(eng.get("NL"), g["n2_NL"])
+    p3 = params_from_golden(g, "n3_")
+    with E.Engine(p3) as eng:
+        eng.set_coords(g["n3_x"], g["n3_y"], g["n3_z"])
+        eng.find_neighbor_gpu()
+        np.testing.assert_array_equal(eng.get("NN"), g["n3_NN"])
+        np.testing.assert_array_equal(eng.get("NL"), g["n3_NL"])
+
+
+def test_family_overflow_reported(E, golden):
+    g = golden("plate_tensile_bond")
+    p = params_from_golden(g)
+    p.MN = 20  # interior families have 28 members
+    with engine_from_golden(E, g, p) as eng:
+        with pytest.raises(E.PDError) as ei:
+            eng.find_neighbor_gpu()
+        assert ei.value.status == -4
+
+
+def test_surface_correction(E, golden):
+    for name in ["plate_tensile_bond", "kalthoff_winkler_bond"]:
+        g = golden(name)
+        with engine_from_golden(E, g) as eng:
+            eng.find_neighbor_gpu()
+            eng.surface_correct_gpu()
+            np.testing.assert_array_equal(eng.get("IDIST"), g["idist"], err_msg=name)
+            np.testing.assert_array_equal(eng.get("FAC"), g["fac"], err_msg=name)
+            assert_close_norm(eng.get("SCR"), g["scr"], 1e-13, name + " scr")
+
+
+def test_weights(E, golden):
+    for name in ["plate_crack_state", "kalthoff_winkler_bond"]:
+        g = golden(name)
+        with engine_from_golden(E, g) as eng:
+            eng.find_neighbor_gpu()
+            eng.vol_corr()
+            eng.initial_weight()
+            assert_close_norm(eng.get("W"), g["w"], 1e-14, name + " w")
+            assert_close_norm(eng.get("M"), g["m"], 1e-13, name + " m")
+
+
+def test_bond_force_2d_and_breakage(E, golden):
+    g = golden("plate_tensile_bond")
+    with engine_from_golden(E, g) as eng:
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
+        eng.set("UX", g["f_ux"])
+        eng.set("UY", g["f_uy"])
+        eng.bond_force_gpu()
+        assert_close_norm(eng.get("FX"), g["f_fx"], FORCE_RTOL, "fx")
+        assert_close_norm(eng.get("FY"), g["f_fy"], FORCE_RTOL, "fy")
+        np.testing.assert_array_equal(eng.get("FAIL"), g["f_fail"])
+        p = eng.params()
+        p.critical_s = float(g["b_s0"])
+        eng.set_params(p)
+        eng.initial_state()
+        eng.set("UX", g["f_ux"])
+        eng.set("UY", g["f_uy"])
+        eng.bond_force_gpu()
+        assert_close_norm(eng.get("FX"), g["b_fx1"], FORCE_RTOL, "fx step 1")
+        assert_close_norm(eng.get("FY"), g["b_fy1"], FORCE_RTOL, "fy step 1")
+        eng.bond_force_gpu()
+        assert_close_norm(eng.get("FX"), g["b_fx2"], FORCE_RTOL, "fx step 2")
+        assert_close_norm(eng.get("FY"), g["b_fy2"], FORCE_RTOL, "fy step 2")
+        np.testing.assert_array_equal(eng.get("FAIL"), g["b_fail"])
+        eng.damage()
+        assert_close_norm(eng.get("DMG"), g["b_dmg"], 1e-14, "dmg")
+
+
+def test_bond_force_3d_kalthoff_winkler(E, golden):
+    g = golden("kalthoff_winkler_bond")
+    with engine_from_golden(E, g) as eng:
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
+        eng.set_crack_kw(float(g["rad"]))
+        np.testing.assert_array_equal(eng.get("FAIL"), g["kw_fail"])
+        p = eng.params()
+        p.critical_s = float(g["f_s0"])
+        eng.set_params(p)
+        for k in ["UX", "UY", "UZ"]:
+            eng.set(k, g["f_" + k.lower()])
+        eng.bond_force_gpu()
+        for k in ["FX", "FY", "FZ"]:
+            assert_close_norm(eng.get(k), g["f_" + k.lower()], FORCE_RTOL, k)
+        np.testing.assert_array_equal(eng.get("FAIL"), g["f_fail"])
+        eng.damage()
+        assert_close_norm(eng.get("DMG"), g["f_dmg"], 1e-14, "dmg")
+
+
+def test_set_crack_2d_exact(E, golden):
+    g = golden("plate_crack_state")
+    for name in ["c0", "c90", "c30"]:
+        with engine_from_golden(E, g) as eng:
+            eng.find_neighbor_gpu()
+            eng.vol_corr()
+            eng.initial_state()
+            cl, lx, ly, th = (float(v) for v in g[name + "_args"])
+            eng.set_crack_2d(cl, lx, ly, th)
+            fail = eng.get("FAIL")
+            n_int_bonds = int(g["NN"][: int(g["p_N_int"])].sum())
+            np.testing.assert_array_equal(fail[:n_int_bonds], g[name + "_fail"], err_msg=name)
+            eng.damage()
+            assert_close_norm(eng.get("DMG")[: int(g["p_N_int"])], g[name + "_dmg"], 1e-14, name)
+
+
+def test_state_force_2d_steps(E, golden):
+    """Twelve crack-grow steps (quick_load + Verlet + state force) against the
+    reference's CPU functions, then a stretched field with breakage."""
+    g = golden("plate_crack_state")
+    with engine_from_golden(E, g) as eng:
+        eng.find_neighbor_gpu()
+        eng.vol_corr()
+        eng.initial_weight()
+        eng.initial_state()
+        eng.run_explicit(int(g["s_steps"]), load=float(g["s_load"]))
+        # 12 explicit steps: the GPU rounds the Verlet updates with FMA, the
+        # reference's host build without, so the bar is 1e-11 here
+        for k in ["UX", "UY", "VX", "VY", "AX", "AY", "FX", "FY", "THETA"]:
+            assert_close_norm(eng.get(k), g["s_" + k.lower()], 1e-11, k)
+        p = eng.params()
+        p.critical_s = float(g["t_s0"])
+        eng.set_params(p)
+        eng.initial_state()
+        eng.set("UX", g["t_ux"])
+        eng.set("UY", g["t_uy"])
+        eng.state_force_gpu()
+        n_int = int(g["p_N_int"])
+        assert_close_norm(eng.get("FX")[:n_int], g["t_fx"][:n_int], FORCE_RTOL, "fx")
+        assert_close_norm(eng.get("FY")[:n_int], g["t_fy"][:n_int], FORCE_RTOL, "fy")
+        assert_close_norm(eng.get("THETA"), g["t_theta"], FORCE_RTOL, "theta")
+        fail = eng.get("FAIL")
+        np.testing.assert_array_equal(fail[: len(g["t_fail"])], g["t_fail"])
+
+
+def _pair(E, p, coords, setup_eng, setup_orc):
+    eng = E.Engine(p)
+    eng.set_coords(*coords)
+    setup_eng(eng)
+    m = orc.Model(p, *coords)
+    setup_orc(m)
+    return eng, m
+
+
+def test_adr_loop_matches_oracle(E):
+    """ADR (kernel_cnn + cal_cn + kernel_integrate) 300 steps, small plate with
+    moving boundary rows, against the oracle's GPU-semantics restatement."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_plate_tensile(scale=0.3)
+    eng = E.Engine(p)
+    setup(eng)
+    x, y = eng.get("X"), eng.get("Y")
+    m = orc.Model(p, x, y)
+    m.find_neighbor()
+    m.surface_correct()
+    steps = 300
+    eng.run_adr(0, steps, load=meta["load"])
+    for ct in range(steps):
+        m.quick_load(meta["load"])
+        m.adr_step(ct)
+    assert eng.adr_cn() == pytest.approx(m.cn, rel=1e-9)
+    assert_close_norm(eng.get("UX")[: p.N_int], m.ux[: p.N_int], 1e-9, "ux")
+    assert_close_norm(eng.get("UY")[: p.N_int], m.uy[: p.N_int], 1e-9, "uy")
+    assert_close_norm(eng.get("FX")[: p.N_int], m.fx[: p.N_int], 1e-9, "fx")
+    eng.close()
+
+
+def test_adr_single_calls_match_fused(E):
+    """pd_bond_force + pd_integrate_adr per step equals the fused pd_run_adr."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_plate_tensile(scale=0.2)
+    a = E.Engine(p)
+    b = E.Engine(p)
+    setup(a)
+    setup(b)
+    a.run_adr(0, 40, load=meta["load"])
+    for ct in range(40):
+        b.quick_load(meta["load"])
+        b.bond_force_gpu()
+        b.static_integrate_gpu(ct)
+    for k in ["UX", "UY", "VHX", "VHY", "FX"]:
+        np.testing.assert_array_equal(a.get(k), b.get(k), err_msg=k)
+    assert a.adr_cn() == b.adr_cn()
+    a.close()
+    b.close()
+
+
+def test_explicit_bond_crack_branching_small(E):
+    """Scaled-down crack-branching plate: pre-crack + traction, 150 Verlet steps
+    with bond breakage, against the oracle."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_branching(scale=0.05, nt=150)
+    eng = E.Engine(p)
+    setup(eng)
+    x, y = eng.get("X"), eng.get("Y")
+    m = orc.Model(p, x, y)
+    m.find_neighbor()
+    m.surface_correct()
+    m.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
+    m.by[:] = eng.get("BY")
+    np.testing.assert_array_equal(eng.get("FAIL"), m.rows(m.fail))
+    # run with a large traction so that bonds break within the window
+    eng.run_explicit(meta["nt"])
+    for _ in range(meta["nt"]):
+        m.explicit_step()
+    m.damage()
+    eng.damage()
+    assert_close_norm(eng.get("UY"), m.uy, 1e-9, "uy")
+    assert_close_norm(eng.get("VY"), m.vy, 1e-9, "vy")
+    fg, fo = eng.get("FAIL"), m.rows(m.fail)
+    assert (fg != fo).sum() <= 0.001 * len(fo)
+
+
+def test_explicit_split_calls_match_fused(E):
+    """Verlet1 + force + Verlet2 per call equals the fused graph-captured loop."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_branching(scale=0.03, nt=20)
+    a, b = E.Engine(p), E.Engine(p)
+    setup(a)
+    setup(b)
+    a.run_explicit(20)
+    for _ in range(20):
+        b.integrate_verlet1()
+        b.bond_force_gpu()
+        b.integrate_verlet2()
+    for k in ["UX", "UY", "VX", "VY", "AX", "AY", "FX", "FY"]:
+        np.testing.assert_array_equal(a.get(k), b.get(k), err_msg=k)
+    np.testing.assert_array_equal(a.get("FAIL"), b.get("FAIL"))
+    a.close()
+    b.close()
+
+
+def test_kalthoff_winkler_state_with_contact(E):
+    """3-D state-based notched slab hit by the rigid cylinder: 30 steps against
+    the oracle (contact, reaction force, impactor integration)."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=30)
+    eng = E.Engine(p)
+    setup(eng)
+    x, y, z = eng.get("X"), eng.get("Y"), eng.get("Z")
+    m = orc.Model(p, x, y, z)
+    m.find_neighbor()
+    m.vol_corr()
+    m.initial_weight()
+    m.set_crack_kw(meta["rad"])
+    cyl = orc.new_cylinder(meta["cylinder"].rad, meta["cylinder"].mass, meta["cylinder"].height, -32.0,
+                           meta["cylinder"].x, meta["cylinder"].y, meta["cylinder"].z)
+    # start the impactor touching the slab so that contact acts within 30 steps
+    cyl.disp[1] = -0.1 * p.dx - 0.2 * p.dx
+    c2 = meta["cylinder"]
+    c2.disp[1] = cyl.disp[1]
+    eng.cylinder_init(c2)
+    eng.run_explicit(30)
+    for _ in range(30):
+        m.explicit_step(cyl=cyl)
+    cg = eng.cylinder()
+    assert cg.vel[1] == pytest.approx(cyl.vel[1], rel=1e-9)
+    assert cg.disp[1] == pytest.approx(cyl.disp[1], rel=1e-9)
+    assert abs(cyl.vel[1] + 32.0) > 1e-6  # the slab pushed back
+    for k in ["UX", "UY", "UZ"]:
+        assert_close_norm(eng.get(k), getattr(m, k.lower()), 1e-9, k)
+    assert_close_norm(eng.get("THETA"), m.theta, 1e-9, "theta")
+
+
+def test_kalthoff_winkler_bond_driver(E):
+    """The bond-based KW driver (the reference's own) with contact, 20 steps."""
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=20, model=PD_MODEL_BOND)
+    eng = E.Engine(p)
+    setup(eng)
+    x, y, z = eng.get("X"), eng.get("Y"), eng.get("Z")
+    m = orc.Model(p, x, y, z)
+    m.find_neighbor()
+    m.surface_correct()
+    m.set_crack_kw(meta["rad"])
+    c = meta["cylinder"]
+    c.disp[1] = -0.3 * p.dx
+    eng.cylinder_init(c)
+    cyl = orc.new_cylinder(c.rad, c.mass, c.height, -32.0, c.x, c.y, c.z)
+    cyl.disp[1] = c.disp[1]
+    eng.run_explicit(20)
+    for _ in range(20):
+        m.explicit_step(cyl=cyl)
+    for k in ["UX", "UY", "UZ", "VY"]:
+        assert_close_norm(eng.get(k), getattr(m, k.lower()), 1e-9, k)
+    assert eng.cylinder().vel[1] == pytest.approx(cyl.vel[1], rel=1e-9)
+
+
+def test_reduce_sum_and_finite(E, golden):
+    g = golden("plate_tensile_bond")
+    with engine_from_golden(E, g) as eng:
+        eng.set("UX", g["f_ux"])
+        assert eng.sum("UX") == pytest.approx(float(np.sum(g["f_ux"])), rel=1e-12, abs=1e-20)
+        eng.check_finite()
+        bad = g["f_ux"].copy()
+        bad[3] = np.nan
+        eng.set("UX", bad)
+        with pytest.raises(E.PDError) as ei:
+            eng.check_finite()
+        assert ei.value.status == -5
+
+
+def test_drivers_run(E):
+    ux, uy, dmg, res = E.solve_plate_tensile(0.02, 50)
+    assert res.B > 0 and np.all(np.isfinite(ux)) and np.abs(ux).max() > 0
+    ux, uy, dmg, res = E.solve_plate_crack_grow(0.0005, 30)
+    assert np.all(np.isfinite(uy)) and res.N_int == len(uy)
+    ux, uy, uz, dmg, res = E.solve_kalthoff_winkler(0.004, 10)
+    assert res.N == len(ux) and np.all(np.isfinite(uz))
