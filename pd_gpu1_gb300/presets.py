@@ -65,16 +65,31 @@ def build_plate_tensile(scale=1.0, dx=5e-4, nt=1000, derive=None):
 
 
 # ---- dynamic crack branching, 2-D PMB, Verlet (1800 steps, headline) ------------------
-def build_crack_branching(scale=1.0, dx=5e-5, nt=1800, derive=None):
+def critical_dt_2d(p):
+    """Explicit stability limit of 2-D PMB on a regular lattice with horizon
+    3.015 dx: dt_c = sqrt(2 rho / sum_j V_j c / |xi_j|) (Silling & Askari 2005),
+    the sum running over the 28 interior family members."""
+    dists = [1.0] * 4 + [math.sqrt(2.0)] * 4 + [2.0] * 4 + [math.sqrt(5.0)] * 8 + [math.sqrt(8.0)] * 4 + [3.0] * 4
+    return math.sqrt(2.0 * p.dens / sum(p.vol * p.bc / (r * p.dx) for r in dists))
+
+
+def build_crack_branching(scale=1.0, dx=5e-5, nt=1800, derive=None, dt=1.0e-8):
     """0.1 x 0.04 m glass plate, dx = 5e-5 (2000 x 800 = 1.6M nodes),
     E = 72 GPa, nu = 1/3, rho = 2440, G0 = 3.8 J/m^2, pre-crack 0.05 m along
     the mid-line from the left edge, 12 MPa traction on the top and bottom rows
-    as body force sigma/dx, dt = 2.5e-8, damage every 100 steps."""
+    as body force sigma/dx, damage every 100 steps.
+
+    Time step: 2.5e-8 s is the usual step of this benchmark on a grid four to
+    five times coarser; on this grid the explicit limit is 1.03e-8 s
+    (critical_dt_2d) and at 2.5e-8 s the plate shatters numerically within 50
+    steps (83 % of bonds broken), after which both implementations skip most
+    bonds.  The default is therefore 1.0e-8 s, so that every step does the full
+    bond work; pass dt=2.5e-8 to run the unstable setting."""
     Lx, Ly = 0.1 * scale, 0.04 * scale
     E, nu, rho, G0 = 72.0e9, 1.0 / 3.0, 2440.0, 3.8
     delta = 3.015 * dx
     s0 = s0_2d(G0, E, delta)
-    p = _derive(derive)(2, PD_MODEL_BOND, PD_MODE_DYNAMIC, 2.5e-8, nt, dx, 0.0, dx, Lx, Ly, 0.0, E, nu, rho, s0)
+    p = _derive(derive)(2, PD_MODEL_BOND, PD_MODE_DYNAMIC, dt, nt, dx, 0.0, dx, Lx, Ly, 0.0, E, nu, rho, s0)
     sigma = 12.0e6
 
     def setup(eng):
