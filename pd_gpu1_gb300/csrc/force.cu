@@ -37,6 +37,7 @@
 //               Integrate.cu:7-49) reduced across the grid; the last block to
 //               finish forms the damping coefficient (cal_cn, :108-129) on the
 //               device, so ADR needs no host round trip.
+#include "ff.cuh"
 #include "pd_internal.cuh"
 
 namespace pdg {
@@ -52,6 +53,8 @@ struct ForceArgs {
     const double* l0;
     const double* ecrit;
     const double* k2;
+    const float2* k2f;  // k2 * 2^-S as a float pair
+    double kscale;      // 2^S
     const double* c1;
     const double* c2;
     const double* cth;
@@ -86,35 +89,87 @@ struct ForceArgs {
 namespace {
 
 constexpr int kWarpsPerBlock = kForceBlock / 32;
-constexpr int kNewtonIters = 2;
+// Seed of the square-root iteration: the FP32 reciprocal square root (about
+// 23 correct bits, one Newton step to ~3e-14) or the FP64 one (about 20 bits,
+// two steps).  On this GPU f64<->f32 conversion instructions issue on the FP64
+// pipe, so the FP32 seed moves between the formats with integer operations on
+// the IEEE-754 fields instead; it then costs 7 FP64 instructions against 11.
+constexpr bool kSeedFp32 = true;
+// Bond-force tail (t = k2 e h, f += t d) in pair arithmetic instead of FP64.
+constexpr bool kTailFF = true;
 
-__device__ __forceinline__ double rsqrt_seed(double x) {
+// float of a positive double whose exponent is within the float normal range:
+// rebias the 11-bit exponent to 8 bits and keep the top 23 mantissa bits
+// (truncation, relative error below 2^-23).  Integer pipe only.
+__device__ __forceinline__ float f32_of_f64(double x) {
+    const unsigned hi = (unsigned)__double2hiint(x);
+    const unsigned lo = (unsigned)__double2loint(x);
+    return __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
+}
+
+// Exact double of a positive normal float (the inverse rebias); the second
+// result is the same value halved (exponent minus one).  Integer pipe only.
+__device__ __forceinline__ void f64_of_f32(float f, double& v, double& half) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned hi = (b >> 3) + (896u << 20);
+    const int lo = (int)(b << 29);
+    v = __hiloint2double((int)hi, lo);
+    half = __hiloint2double((int)(hi - (1u << 20)), lo);
+}
+
+__device__ __forceinline__ double rsqrt_seed64(double x) {
     double y;
     asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
     return y;
 }
 
-// sqrt(x) and 1/(2 sqrt(x)) by the coupled Newton iteration for the square
-// root and its reciprocal (r = 1/2 - s h; s += s r; h += h r), followed by one
-// residual correction of s (s += (x - s^2) h).
-__device__ __forceinline__ void sqrt_rsqrt(double x, double& s, double& h) {
-    const double y = rsqrt_seed(x);
-    s = x * y;
-    h = 0.5 * y;
-#pragma unroll
-    for (int it = 0; it < kNewtonIters; it++) {
+__device__ __forceinline__ float rsqrt_seed32(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// e = sqrt(x) - L0 and h = 1/(2 sqrt(x)) without a divide or a library sqrt:
+// the coupled Newton iteration for the square root and its reciprocal
+// (r = 1/2 - s h; s += s r; h += h r), then one residual correction of the
+// root folded into the subtraction, e = (s - L0) + (x - s^2) h, so that e
+// keeps the accuracy of an IEEE square root through the cancellation.
+__device__ __forceinline__ void extension(double x, double L0, double& e, double& h) {
+    double s;
+    if (kSeedFp32) {
+        double y;
+        f64_of_f32(rsqrt_seed32(f32_of_f64(x)), y, h);
+        s = x * y;
         const double r = fma(-s, h, 0.5);
         s = fma(s, r, s);
         h = fma(h, r, h);
+    } else {
+        const double y = rsqrt_seed64(x);
+        s = x * y;
+        h = 0.5 * y;
+#pragma unroll
+        for (int it = 0; it < 2; it++) {
+            const double r = fma(-s, h, 0.5);
+            s = fma(s, r, s);
+            h = fma(h, r, h);
+        }
     }
     const double d = fma(-s, s, x);
-    s = fma(d, h, s);
+    e = fma(d, h, s - L0);
 }
 
-__device__ __forceinline__ double sqrt_only(double x) {
-    double s, h;
-    sqrt_rsqrt(x, s, h);
-    return s;
+// The same quantities with the iteration in pair arithmetic: only the
+// residual correction and the cancelling subtraction stay in FP64 (s, its
+// square's residual and e), four FP64 instructions instead of eleven.  h is
+// returned as a pair, relative error ~2e-14.
+__device__ __forceinline__ void extension_ff(double x, double L0, double& e, ff& h) {
+    const ff xs = ff_split(x);
+    const ff y = ff_rsqrt(xs);
+    const ff sp = ff_mul(xs, y);
+    const double s = f64_of_f32s(sp.h) + f64_of_f32s(sp.l);
+    h = ff{0.5f * y.h, 0.5f * y.l};
+    const double d = fma(-s, s, x);
+    e = fma(d, f64_of_f32s(h.h), s - L0);
 }
 
 // e > ecrit for ecrit > 0: ordered like the IEEE bit patterns read as signed
@@ -202,7 +257,7 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
     if (EPI == EPI_VERLET) {
         double vx = A.vx[r], vy = A.vy[r], vz = DIM == 3 ? A.vz[r] : 0.0;
         double ux = uxi, uy = uyi, uz = uzi;
-        if (A.contact && A.dmg[r] < 1.0) contact_node(P, *A.cyl, xi, yi, zi, ux, uy, uz, vx, vy, vz, red);
+        if (DIM == 3 && A.contact && A.dmg[r] < 1.0) contact_node(P, *A.cyl, xi, yi, zi, ux, uy, uz, vx, vy, vz, red);
         const double hdt = P.dt / 2.0;
         const double ax = (fxr + A.bx[r]) / P.dens;
         const double ay = (fyr + A.by[r]) / P.dens;
@@ -329,6 +384,7 @@ __global__ void __launch_bounds__(kForceBlock) k_bond_force(const ForceArgs A) {
             const double xi = A.x[rr], yi = A.y[rr], zi = DIM == 3 ? A.z[rr] : 0.0;
             const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
+            ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
@@ -348,17 +404,33 @@ __global__ void __launch_bounds__(kForceBlock) k_bond_force(const ForceArgs A) {
                         dz = (A.pcz[c] - zi) - uzi;
                         L2 = fma(dz, dz, L2);
                     }
-                    double L, h;
-                    sqrt_rsqrt(L2, L, h);
-                    const double e = L - A.l0[slot];
-                    const double t = (A.k2[slot] * e) * h;
-                    fxr = fma(t, dx, fxr);
-                    fyr = fma(t, dy, fyr);
-                    if (DIM == 3) fzr = fma(t, dz, fzr);
+                    double e;
+                    if (kTailFF) {
+                        ff hp;
+                        extension_ff(L2, A.l0[slot], e, hp);
+                        const float2 kf = A.k2f[slot];
+                        const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, ff_split(e)), hp);
+                        fxa = ff_add(fxa, ff_mul(t, ff_split(dx)));
+                        fya = ff_add(fya, ff_mul(t, ff_split(dy)));
+                        if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_split(dz)));
+                    } else {
+                        double h;
+                        extension(L2, A.l0[slot], e, h);
+                        const double t = (A.k2[slot] * e) * h;
+                        fxr = fma(t, dx, fxr);
+                        fyr = fma(t, dy, fyr);
+                        if (DIM == 3) fzr = fma(t, dz, fzr);
+                    }
                     brk = exceeds(e, A.ecrit[slot]);
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0) wbits[k] = word & ~broke;
+            }
+            if (kTailFF) {
+                // undo the power-of-two scaling of the bond coefficient (exact)
+                fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+                fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+                if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
             }
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
@@ -404,7 +476,8 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
                     const double dz = (A.xi[2 * A.S + slot] + A.uz[c]) - uzi;
                     L2 = fma(dz, dz, L2);
                 }
-                const double e = sqrt_only(L2) - A.l0[slot];
+                double e, h;
+                extension(L2, A.l0[slot], e, h);
                 A.e[slot] = e;
                 acc = fma(A.cth[slot], e, acc);
             }
@@ -457,9 +530,8 @@ __global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) 
                         dz = (A.pcz[c] - zi) - uzi;
                         L2 = fma(dzl, dzl, L2);
                     }
-                    double L, h;
-                    sqrt_rsqrt(L2, L, h);
-                    const double ef = L - A.l0[slot];
+                    double ef, h;
+                    extension(L2, A.l0[slot], ef, h);
                     const double T = fma(A.c2[slot] * A.e[slot], nbi + A.nb[c], A.c1[slot] * (nai + A.na[c]));
                     const double t = T * h;
                     fxr = fma(t, dx, fxr);
@@ -556,6 +628,8 @@ static ForceArgs make_args(pd_ctx* c) {
     A.l0 = S.l0;
     A.ecrit = S.ecrit;
     A.k2 = S.k2;
+    A.k2f = S.k2f;
+    A.kscale = S.kscale;
     A.c1 = S.c1;
     A.c2 = S.c2;
     A.cth = S.cth;
@@ -606,19 +680,25 @@ static ForceArgs make_args(pd_ctx* c) {
     return A;
 }
 
-static unsigned force_grid(pd_ctx* c, int64_t nslices) {
+// Grid of the slice kernels: every block resident at once (blocks per SM from
+// the occupancy of this kernel instance x SM count), so the grid-stride loop
+// over slices runs in one wave with no tail; never more blocks than slices
+// need, nor more than the partial-sum buffer holds.
+static unsigned resident_grid(pd_ctx* c, const void* kernel, int64_t nslices) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kForceBlock, 0) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
     const int64_t want = (nslices + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    const int64_t cap = (int64_t)c->num_sms * 8;  // resident blocks per SM at 256 threads
+    const int64_t cap = (int64_t)c->num_sms * per_sm;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(want, cap), kMaxPartials));
 }
 
 int launch_theta(pd_ctx* c, cudaStream_t s) {
     ForceArgs A = make_args(c);
-    const unsigned g = force_grid(c, A.nslices);
     if (A.P.dim == 2)
-        k_theta<2><<<g, kForceBlock, 0, s>>>(A);
+        k_theta<2><<<resident_grid(c, (const void*)k_theta<2>, A.nslices), kForceBlock, 0, s>>>(A);
     else
-        k_theta<3><<<g, kForceBlock, 0, s>>>(A);
+        k_theta<3><<<resident_grid(c, (const void*)k_theta<3>, A.nslices), kForceBlock, 0, s>>>(A);
     c->launches++;
     return cuda_err(c, cudaGetLastError(), "theta");
 }
@@ -654,8 +734,8 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         if (f.contact && !f.do_next) c->pos_valid = false;
         return cuda_err(c, cudaGetLastError(), "node post");
     }
-    const unsigned g = force_grid(c, A.nslices);
-#define PD_LAUNCH(KER, D, E) KER<D, E><<<g, kForceBlock, 0, s>>>(A)
+#define PD_LAUNCH(KER, D, E) \
+    KER<D, E><<<resident_grid(c, (const void*)KER<D, E>, A.nslices), kForceBlock, 0, s>>>(A)
 #define PD_DISPATCH(KER)                                  \
     do {                                                  \
         if (!d3) {                                        \

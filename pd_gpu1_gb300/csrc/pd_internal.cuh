@@ -53,6 +53,10 @@ struct Sell {
     double* l0 = nullptr;    // [S] reference length |xi|
     double* ecrit = nullptr; // [S] break threshold on e = L - l0 (s0 * l0; +inf: never)
     double* k2 = nullptr;    // [S] bond-based: 2 * vol*fac*bc*scr / l0
+    float2* k2f = nullptr;   // [S] the same times 2^-kexp as a float pair (h, l)
+    int kexp = 0;            // power-of-two scale that brings k2 near one
+    double kscale = 1.0;     // 2^kexp
+    double kscale_inv = 1.0; // 2^-kexp
     double* c1 = nullptr;    // [S] state-based: dilatation coefficient of t
     double* c2 = nullptr;    // [S] state-based: extension coefficient of t
     double* cth = nullptr;   // [S] state-based: dilatation weight of e

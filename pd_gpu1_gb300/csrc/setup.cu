@@ -18,6 +18,7 @@
 // and the fail flags agree bit for bit with it.
 #include <cmath>
 
+#include "ff.cuh"
 #include "pd_internal.cuh"
 
 namespace pdg {
@@ -255,7 +256,10 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             S.col[slot] = (int)(r < P.N ? r : 0);
             S.l0[slot] = 1.0;
             S.ecrit[slot] = HUGE_VAL;
-            if (S.k2) S.k2[slot] = 0.0;
+            if (S.k2) {
+                S.k2[slot] = 0.0;
+                S.k2f[slot] = make_float2(0.0f, 0.0f);
+            }
             if (S.c1) {
                 S.c1[slot] = 0.0;
                 S.c2[slot] = 0.0;
@@ -274,7 +278,12 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         bool breakable = true;
         if (P.dim == 3) breakable = y[r] >= P.break_ymin && y[c] >= P.break_ymin;
         S.ecrit[slot] = breakable ? P.critical_s * L0 : HUGE_VAL;
-        if (S.k2) S.k2[slot] = 2.0 * (P.vol * fac[q] * P.bc * scr[q]) / L0;
+        if (S.k2) {
+            const double k2 = 2.0 * (P.vol * fac[q] * P.bc * scr[q]) / L0;
+            S.k2[slot] = k2;
+            const ff kf = ff_split(k2 * S.kscale_inv);
+            S.k2f[slot] = make_float2(kf.h, kf.l);
+        }
         if (S.c1) {
             const double pr = P.pratio;
             double a_coef, b_coef, th_coef;
@@ -440,6 +449,7 @@ static void free_sell(Sell& S) {
     free_ptr(S.l0);
     free_ptr(S.ecrit);
     free_ptr(S.k2);
+    free_ptr(S.k2f);
     free_ptr(S.c1);
     free_ptr(S.c2);
     free_ptr(S.cth);
@@ -490,7 +500,15 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
     bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.l0, n8) &&
               !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
-    if (ok && !state) ok = !cudaMalloc(&S.k2, n8);
+    if (ok && !state) ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.k2f, n8);
+    // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,
+    // so that the pair arithmetic of the force kernels stays in float range
+    {
+        const double ref = 2.0 * P.vol * P.bc / P.dx;
+        S.kexp = (ref > 0.0 && std::isfinite(ref)) ? (int)std::lround(std::log2(ref)) : 0;
+        S.kscale = std::ldexp(1.0, S.kexp);
+        S.kscale_inv = std::ldexp(1.0, -S.kexp);
+    }
     if (ok && state)
         ok = !cudaMalloc(&S.c1, n8) && !cudaMalloc(&S.c2, n8) && !cudaMalloc(&S.cth, n8) &&
              !cudaMalloc(&S.xi, n8 * P.dim) && !cudaMalloc(&S.e, n8);
