@@ -254,6 +254,21 @@ int pd_solve_kalthoff_winkler(double dx, int nt, double* ux, double* uy, double*
 int pd_check_finite(pd_ctx* ctx, void* stream);
 /* Number of GPU kernels this context has launched (for launch accounting). */
 int64_t pd_kernel_launches(const pd_ctx* ctx);
+/* Allocation-free sum of n doubles of a device array into *dev_result (a
+ * device pointer), in a fixed summation order.  No counterpart in the
+ * reference: for callers that cannot allocate device memory (a component
+ * that owns the allocator, a foreign-function caller without a context, a
+ * path that must not allocate).  Needs no context and allocates nothing: the
+ * block partial sums use a 64 KiB array in the library's own device memory,
+ * which every GPU that loads the library keeps until exit.  n is at most
+ * 33,554,432 (8,192 blocks of 4,096 elements); larger n returns PD_ERR_ARG.
+ * The first call on each device looks the array's address up
+ * (cudaGetSymbolAddress) and must come before any stream capture that
+ * contains this call.  All calls share the array: calls that overlap on the
+ * GPU (different streams, no ordering between them) race and may return
+ * wrong sums. */
+int pd_reduce_sum_static(const double* dev_x, int64_t n, double* dev_result, void* stream);
+
 /* FP64 FMA issue rate of the current device in 1e9 FMA/s (dependent-chain
  * microbenchmark, best of 3): the denominator of the FP64 roofline. */
 int pd_probe_fp64(double* gfma_per_s);

@@ -23,6 +23,7 @@ UNITS = {
     "force.cu": [],
     "integrate.cu": [],
     "api.cu": [],
+    "noalloc.cu": [],
 }
 
 
