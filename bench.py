@@ -34,6 +34,9 @@ ALG_BYTES_PER_BOND_3D = 12.125
 ALG_BYTES_PER_NODE_3D = 72.0
 ALG_FP64_PER_BOND_2D = 23       # 10 add/sub, 8 mul, 3 div, 1 sqrt, 1 compare (sqrt/div counted once)
 ALG_FP64_PER_BOND_3D = 31
+# measured DRAM bytes per bond and per node of the step kernel (ncu dram__bytes_read.sum +
+# dram__bytes_write.sum, one capture per workload)
+TRAFFIC = {"crack_branching_2d_pmb_verlet": (28.125, 139.8)}
 
 
 def rank_info():
@@ -98,6 +101,21 @@ class ClockSampler:
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def aggregate_replicas(elapsed_s, work, dist=None, device="cpu"):
+    """Replicas only: every rank times its own copy of the workload.  Returns
+    (max elapsed over ranks, total work over ranks); the job's throughput is
+    total work / max elapsed."""
+    if dist is None:
+        return elapsed_s, work
+    import torch
+
+    t = torch.tensor([elapsed_s], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    w = torch.tensor([float(work)], dtype=torch.float64, device=device)
+    dist.all_reduce(w, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(w.item())
 
 
 def build_workload(name, scale, host_only=False):
@@ -206,6 +224,12 @@ def reference_arm(args):
     return 0
 
 
+def r_inputs(eng, p):
+    """The engine context's problem in the argument order of RefGPU.setup."""
+    return (eng.get("X"), eng.get("Y"), eng.get("NN"), eng.get("ROWPTR"), eng.get("NL"), eng.get("IDIST"),
+            eng.get("SCR"), eng.get("FAC"), eng.get("FAIL"), eng.get("BX"), eng.get("BY"))
+
+
 def host_coords(p, meta):
     """Node coordinates of the workload, computed on the host (same formulas as the engine)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -270,12 +294,9 @@ def gb300_arm(args):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     launches = eng.kernel_launches - launches0
-    ms_max = ms
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = world * B * args.steps / (ms_max * 1e-3)
+    secs_max, work = aggregate_replicas(ms * 1e-3, B * args.steps, dist, "cuda")
+    ms_max = secs_max * 1e3
+    value = work / secs_max
 
     # dominant kernel alone: a graph of force launches only (no damage pass)
     kern_steps = min(100, max(10, args.steps))
@@ -301,13 +322,12 @@ def gb300_arm(args):
     lib().pd_probe_fp64(C.byref(gfma))
     fp64_peak_tflops = 2.0 * gfma.value / 1e3
     alg_flops = (ALG_FP64_PER_BOND_3D if is3d else ALG_FP64_PER_BOND_2D) * B
+    # DRAM bytes per launch from the ncu capture summarised in
+    # profiles/k_bond_force_crack_branching.md (half-size plate, scaled by bonds and nodes)
     traffic = None
-    tpath = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tr = json.load(f).get(meta["workload"])
-        if tr:
-            traffic = tr["bytes_per_bond"] * B + tr["bytes_per_node"] * p.N_int
+    tr = TRAFFIC.get(meta["workload"])
+    if tr:
+        traffic = tr[0] * B + tr[1] * p.N_int
 
     # end to end through the C ABI with host buffers: the initial state and the
     # loading go up from pinned host memory, the damage field comes back at
@@ -347,13 +367,38 @@ def gb300_arm(args):
     for k in ["UX", "UY"]:
         eng._c(L.pd_get_field(eng.ctx, FIELD[k], pin[k].data_ptr(), n, eng.stream), "pd_get_field")
         d2h += n * 8
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world * B * args.steps / e2e_s, "unit": "bond-updates/s",
+    e2e_s, e2e_work = aggregate_replicas(time.perf_counter() - t0, B * args.steps, dist, "cuda")
+    e2e = {"value": e2e_work / e2e_s, "unit": "bond-updates/s",
            "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
+
+    # the reference's own CUDA kernels on the same GPU and plate, when their
+    # cubin was built (oracle/_ref/ref_kernels.cubin, from the reference sources)
+    ref_cuda = None
+    if rank == 0 and not args.no_ref_cuda and p.dim == 2 and p.model == 1 and meta["workload"].startswith("crack"):
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import ref_gpu
+
+        if ref_gpu.available():
+            eng.initial_state()
+            eng.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
+            from pd_gpu1_gb300.presets import traction_field
+
+            eng.set("BY", traction_field(p, meta["sigma"]))
+            r, _ = ref_gpu.from_engine(eng, p)
+            kref = min(args.steps, 300)
+            rates = {}
+            for name, variant in (("kernel_particle_force_2D", ref_gpu.RefGPU.PARTICLE),
+                                  ("kernel_bond_force_2D", ref_gpu.RefGPU.WARP)):
+                r.setup(p, *r_inputs(eng, p))
+                r.run(variant, args.warmup, meta.get("dmg_every", 0))
+                ms_ref = r.run(variant, kref, meta.get("dmg_every", 0))
+                rates[name] = B * kref / (ms_ref * 1e-3)
+            r.free()
+            best = max(rates.values())
+            ref_cuda = {"unit": "bond-updates/s", "steps": kref, **rates, "best": best,
+                        "engine_over_best": value / best,
+                        "what": "the reference's kernels (compiled from its sources, FP64) in its step loop: "
+                                "integrate_2D_1, force, integrate_2D_2, damage every 100 steps"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
@@ -380,7 +425,7 @@ def gb300_arm(args):
                          "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
                                   "peak_tflops": fp64_peak_tflops, "frac": alg_flops / (kern_ms * 1e-3) / 1e12 /
                                   fp64_peak_tflops, "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},
-            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk, "reference_cuda": ref_cuda,
         }
         print(json.dumps(line), flush=True)
     eng.close()
@@ -398,6 +443,7 @@ def main():
     ap.add_argument("--workload", default="crack_branching")
     ap.add_argument("--scale", type=float, default=1.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     if args.warmup < 3:

@@ -1,0 +1,110 @@
+"""TEST/MEASUREMENT INFRASTRUCTURE ONLY: the reference's own CUDA kernels on the GPU.
+
+oracle/_ref/ref_kernels.cubin is compiled from the reference sources (make -C
+oracle ref, in a container that has them) and loaded through the CUDA driver
+API by oracle/_build/libref_gpu_runner.so.  The caller supplies the problem in
+the reference's layout; :func:`from_engine` converts an engine context's CSR
+family into the reference's padded ELL arrays.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CUBIN = os.path.join(HERE, "_ref", "ref_kernels.cubin")
+LIB = os.path.join(HERE, "_build", "libref_gpu_runner.so")
+
+D = C.POINTER(C.c_double)
+I = C.POINTER(C.c_int)
+
+
+def available():
+    return os.path.exists(CUBIN)
+
+
+def _d(a):
+    return a.ctypes.data_as(D)
+
+
+def _i(a):
+    return a.ctypes.data_as(I)
+
+
+class RefGPU:
+    PARTICLE = 0  # kernel_particle_force_2D, thread per node (the tensile driver's choice)
+    WARP = 1      # kernel_bond_force_2D, warp per node
+
+    def __init__(self):
+        if not os.path.exists(LIB):
+            subprocess.run(["make", "-s", "-C", HERE, "_build/libref_gpu_runner.so"], check=True)
+        self.lib = C.CDLL(LIB)
+        self.lib.rr_error.restype = C.c_char_p
+        self.lib.rr_run.argtypes = [C.c_int, C.c_int, C.c_int, D]
+        self._check(self.lib.rr_init(CUBIN.encode()), "rr_init")
+        self.N = self.MN = 0
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what}: {self.lib.rr_error().decode()}")
+
+    def setup(self, p, x, y, NN, rowptr, NL, idist, scr, fac, fail, bx, by):
+        """p: PDParams; bond arrays in CSR order (rowptr over N rows)."""
+        N, MN = p.N, p.MN
+        self.N, self.MN = N, MN
+        mask = (np.arange(MN)[None, :] < NN[:, None]).reshape(-1)
+
+        def ell(v, dtype, fill):
+            out = np.full(N * MN, fill, dtype=dtype)
+            out[mask] = v
+            return out
+
+        self.arrays = dict(NL=ell(NL, np.int32, 0), idist=ell(idist, np.float64, 1.0), scr=ell(scr, np.float64, 0.0),
+                           fac=ell(fac, np.float64, 0.0), fail=ell(fail, np.int32, 1))
+        dv = np.array([p.pi, p.dx, p.emod, p.dens, p.pratio, p.bc, p.delta, p.critical_s, p.vol, p.dt, p.mass, p.K,
+                       p.G])
+        iv = np.array([p.N, p.MN, p.N_int, p.nx, p.ny, p.nz, p.nt], dtype=np.int32)
+        a = self.arrays
+        self.keep = [np.ascontiguousarray(v, dtype=np.float64) for v in (x, y, bx, by)]
+        self.NNc = np.ascontiguousarray(NN, dtype=np.int32)
+        self._check(self.lib.rr_setup(_d(dv), _i(iv), _d(self.keep[0]), _d(self.keep[1]), _i(self.NNc), _i(a["NL"]),
+                                      _d(a["idist"]), _d(a["scr"]), _d(a["fac"]), _i(a["fail"]), _d(self.keep[2]),
+                                      _d(self.keep[3])), "rr_setup")
+
+    def set_disp(self, ux, uy):
+        ux = np.ascontiguousarray(ux, dtype=np.float64)
+        uy = np.ascontiguousarray(uy, dtype=np.float64)
+        self._check(self.lib.rr_set_disp(_d(ux), _d(uy)), "rr_set_disp")
+
+    def force(self, variant):
+        self._check(self.lib.rr_force(variant), "rr_force")
+
+    def run(self, variant, nsteps, dmg_every=0):
+        ms = C.c_double()
+        self._check(self.lib.rr_run(variant, nsteps, dmg_every, C.byref(ms)), "rr_run")
+        return ms.value
+
+    def get(self, NN=None):
+        N, MN = self.N, self.MN
+        out = {k: np.zeros(N) for k in ("ux", "uy", "fx", "fy", "vy")}
+        fail = np.zeros(N * MN, dtype=np.int32)
+        self._check(self.lib.rr_get(_d(out["ux"]), _d(out["uy"]), _d(out["fx"]), _d(out["fy"]), _d(out["vy"]),
+                                    _i(fail)), "rr_get")
+        if NN is not None:
+            mask = (np.arange(MN)[None, :] < NN[:, None]).reshape(-1)
+            out["fail"] = fail[mask]
+        return out
+
+    def free(self):
+        self.lib.rr_free()
+
+
+def from_engine(eng, p):
+    """A RefGPU loaded with the engine context's current problem (family,
+    coefficients, fail flags, body forces)."""
+    r = RefGPU()
+    NN = eng.get("NN")
+    r.setup(p, eng.get("X"), eng.get("Y"), NN, eng.get("ROWPTR"), eng.get("NL"), eng.get("IDIST"), eng.get("SCR"),
+            eng.get("FAC"), eng.get("FAIL"), eng.get("BX"), eng.get("BY"))
+    return r, NN
