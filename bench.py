@@ -314,14 +314,18 @@ def gb300_arm(args):
             e1.record(stream)
     torch.cuda.synchronize()
     kern_ms = e0.elapsed_time(e1) / kern_steps
-    alg_bytes = (ALG_BYTES_PER_NODE_3D if is3d else ALG_BYTES_PER_NODE_2D) * p.N_int + \
-        (ALG_BYTES_PER_BOND_3D if is3d else ALG_BYTES_PER_BOND_2D) * B
+    state = p.model == 2
+    if state:  # dilatation + force passes (SURVEY's 3-D state-based model; 2-D by the same count)
+        alg_bytes = (88.0 if is3d else 64.0) * p.N_int + 16.125 * B
+    else:
+        alg_bytes = (ALG_BYTES_PER_NODE_3D if is3d else ALG_BYTES_PER_NODE_2D) * p.N_int + \
+            (ALG_BYTES_PER_BOND_3D if is3d else ALG_BYTES_PER_BOND_2D) * B
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
     gfma = C.c_double()
     lib().pd_probe_fp64(C.byref(gfma))
     fp64_peak_tflops = 2.0 * gfma.value / 1e3
-    alg_flops = (ALG_FP64_PER_BOND_3D if is3d else ALG_FP64_PER_BOND_2D) * B
+    alg_flops = (ALG_FP64_PER_BOND_3D if is3d else ALG_FP64_PER_BOND_2D) * B * (2 if state else 1)
     # DRAM bytes per launch from the ncu capture summarised in
     # profiles/k_bond_force_crack_branching.md (half-size plate, scaled by bonds and nodes)
     traffic = None
@@ -337,18 +341,10 @@ def gb300_arm(args):
     from pd_gpu1_gb300._abi import FIELD
 
     n = p.N
-    names_up = ["UX", "UY", "VX", "VY", "BX", "BY"]
-    pin = {k: torch.zeros(n, dtype=torch.float64).pin_memory() for k in names_up + ["DMG"]}
-    if meta["workload"].startswith("crack_branching"):
-        from pd_gpu1_gb300.presets import traction_field
-
-        pin["BY"].copy_(torch.from_numpy(traction_field(p, meta["sigma"])))
-    else:
-        pin["BX"].copy_(torch.from_numpy(eng.get("BX")))
-        pin["BY"].copy_(torch.from_numpy(eng.get("BY")))
-    eng.initial_state()
-    if meta["workload"].startswith("crack_branching"):
-        eng.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
+    names_up = ["UX", "UY", "VX", "VY", "BX", "BY"] + (["UZ", "VZ", "BZ"] if is3d else [])
+    setup(eng)  # the workload's initial state (family, corrections, cracks, loads, impactor)
+    pin = {k: torch.from_numpy(eng.get(k)).pin_memory() for k in names_up}
+    pin["DMG"] = torch.zeros(n, dtype=torch.float64).pin_memory()
     barrier()
     h2d = d2h = 0
     t0 = time.perf_counter()
@@ -364,7 +360,7 @@ def gb300_arm(args):
         if meta.get("dmg_every"):
             eng._c(L.pd_get_field(eng.ctx, FIELD["DMG"], pin["DMG"].data_ptr(), n, eng.stream), "pd_get_field")
             d2h += n * 8
-    for k in ["UX", "UY"]:
+    for k in ["UX", "UY"] + (["UZ"] if is3d else []):
         eng._c(L.pd_get_field(eng.ctx, FIELD[k], pin[k].data_ptr(), n, eng.stream), "pd_get_field")
         d2h += n * 8
     e2e_s, e2e_work = aggregate_replicas(time.perf_counter() - t0, B * args.steps, dist, "cuda")
@@ -379,11 +375,7 @@ def gb300_arm(args):
         import ref_gpu
 
         if ref_gpu.available():
-            eng.initial_state()
-            eng.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
-            from pd_gpu1_gb300.presets import traction_field
-
-            eng.set("BY", traction_field(p, meta["sigma"]))
+            setup(eng)
             r, _ = ref_gpu.from_engine(eng, p)
             kref = min(args.steps, 300)
             rates = {}
@@ -420,7 +412,7 @@ def gb300_arm(args):
                        "setup_s": setup_s},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_bond_force" if p.model == 1 else "k_state_force",
+                         "kernel": "k_bond_force" if p.model == 1 else "k_theta + k_state_force",
                          "kernel_ms": kern_ms, "alg_bytes_per_launch": alg_bytes,
                          "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
                                   "peak_tflops": fp64_peak_tflops, "frac": alg_flops / (kern_ms * 1e-3) / 1e12 /

@@ -25,6 +25,14 @@ int cuda_err(pd_ctx* c, cudaError_t e, const char* what) {
 
 void release_sell(pd_ctx* c);
 
+// Every cached graph bakes in device pointers (SELL arrays, node fields,
+// position buffers) and kernel parameters by value; any reallocation or
+// parameter change must drop them before the next replay.
+void drop_graphs(pd_ctx* c) {
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
 namespace {
 
 __global__ void k_init_state(KParams P, double* const* fields, int nfields, double* cn) {
@@ -326,7 +334,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
 
 int pd_destroy(pd_ctx* c) {
     if (!c) return PD_ERR_ARG;
-    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    drop_graphs(c);
     for (int f = 0; f < kNodeDoubleFields; f++)
         if (c->nf[f]) cudaFree(c->nf[f]);
     for (int b = 0; b < 2; b++)
@@ -353,8 +361,7 @@ int pd_set_params(pd_ctx* c, const pd_params* p) {
         return set_err(c, PD_ERR_ARG, "pd_set_params cannot change N, dim or model");
     c->p = *p;
     c->prepared = false;  // coefficients depend on the parameters
-    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
-    c->graphs.clear();
+    drop_graphs(c);
     return PD_OK;
 }
 
@@ -492,6 +499,7 @@ int pd_coord_kw(const pd_params* p, double rad, double* x, double* y, double* z,
 // ---- family and setup -------------------------------------------------------
 int pd_find_neighbor(pd_ctx* c, void* stream) {
     if (!c) return PD_ERR_ARG;
+    drop_graphs(c);
     release_sell(c);
     return build_family(c, st(stream));
 }
@@ -609,7 +617,10 @@ int pd_cylinder_init(pd_ctx* c, const pd_cylinder* cyl, void* stream) {
     }
     cudaError_t e = cudaMemcpyAsync(c->cyl, &d, sizeof(d), cudaMemcpyHostToDevice, st(stream));
     if (e == cudaSuccess) e = cudaStreamSynchronize(st(stream));
-    if (e == cudaSuccess) c->has_cyl = true;
+    if (e == cudaSuccess) {
+        if (!c->has_cyl) drop_graphs(c);  // captured steps without the contact epilogue
+        c->has_cyl = true;
+    }
     return cuda_err(c, e, "pd_cylinder_init");
 }
 

@@ -476,8 +476,9 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
                     const double dz = (A.xi[2 * A.S + slot] + A.uz[c]) - uzi;
                     L2 = fma(dz, dz, L2);
                 }
-                double e, h;
-                extension(L2, A.l0[slot], e, h);
+                double e;
+                ff h;
+                extension_ff(L2, A.l0[slot], e, h);
                 A.e[slot] = e;
                 acc = fma(A.cth[slot], e, acc);
             }
@@ -508,6 +509,7 @@ __global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) 
             const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
             const double nai = A.na[rr], nbi = A.nb[rr];
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
+            ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
@@ -530,18 +532,23 @@ __global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) 
                         dz = (A.pcz[c] - zi) - uzi;
                         L2 = fma(dzl, dzl, L2);
                     }
-                    double ef, h;
-                    extension(L2, A.l0[slot], ef, h);
+                    double ef;
+                    ff h;
+                    extension_ff(L2, A.l0[slot], ef, h);
                     const double T = fma(A.c2[slot] * A.e[slot], nbi + A.nb[c], A.c1[slot] * (nai + A.na[c]));
-                    const double t = T * h;
-                    fxr = fma(t, dx, fxr);
-                    fyr = fma(t, dy, fyr);
-                    if (DIM == 3) fzr = fma(t, dz, fzr);
+                    // t = T h and f += t d in pair arithmetic (as in the bond-based kernel)
+                    const ff t = ff_mul(ff_split(T), h);
+                    fxa = ff_add(fxa, ff_mul(t, ff_split(dx)));
+                    fya = ff_add(fya, ff_mul(t, ff_split(dy)));
+                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_split(dz)));
                     brk = exceeds(ef, A.ecrit[slot]);
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0) wbits[k] = word & ~broke;
             }
+            fxr = f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l);
+            fyr = f64_of_f32s(fya.h) + f64_of_f32s(fya.l);
+            if (DIM == 3) fzr = f64_of_f32s(fza.h) + f64_of_f32s(fza.l);
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);

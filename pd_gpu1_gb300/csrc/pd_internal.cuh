@@ -181,6 +181,8 @@ int launch_damage(pd_ctx* c, cudaStream_t s);
 int launch_quick_load(pd_ctx* c, double load, cudaStream_t s);
 int launch_load_tensile(pd_ctx* c, cudaStream_t s);
 void release_sell(pd_ctx* c);
+// Destroy the cached step graphs (they hold device pointers and parameters).
+void drop_graphs(pd_ctx* c);
 int launch_contact(pd_ctx* c, cudaStream_t s);
 int launch_cyl_integrate(pd_ctx* c, int half, cudaStream_t s);
 int reduce_sum(pd_ctx* c, const double* x, int64_t n, double* out_dev, cudaStream_t s);

@@ -459,10 +459,14 @@ static void free_sell(Sell& S) {
     S.nslices = S.S = S.F = 0;
 }
 
-void release_sell(pd_ctx* c) { free_sell(c->sell); }
+void release_sell(pd_ctx* c) {
+    drop_graphs(c);
+    free_sell(c->sell);
+}
 
 int prepare(pd_ctx* c, cudaStream_t s) {
     if (!c->family) return set_err(c, PD_ERR_STATE, "prepare needs the bond family");
+    drop_graphs(c);  // the SELL arrays are reallocated below
     int rc;
     if (!c->volcorr && (rc = vol_corr(c, s))) return rc;
     const bool state = c->p.model == PD_MODEL_STATE;

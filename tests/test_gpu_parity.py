@@ -375,3 +375,24 @@ def test_drivers_run(E):
     assert np.all(np.isfinite(uy)) and res.N_int == len(uy)
     ux, uy, uz, dmg, res = E.solve_kalthoff_winkler(0.004, 10)
     assert res.N == len(ux) and np.all(np.isfinite(uz))
+
+
+def test_rebuild_after_run_recaptures_graphs(E):
+    """Re-running the set-up (new bond family and coefficient arrays) after a
+    graph-captured run must not replay graphs that point at the old arrays:
+    the second run equals a fresh context's, bit for bit."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_grow(scale=0.08, nt=20)
+    a, b = E.Engine(p), E.Engine(p)
+    setup(a)
+    a.run_explicit(20, load=meta["load"])
+    setup(a)
+    a.run_explicit(20, load=meta["load"])
+    setup(b)
+    b.run_explicit(20, load=meta["load"])
+    for k in ["UX", "UY", "VY", "THETA"]:
+        np.testing.assert_array_equal(a.get(k), b.get(k), err_msg=k)
+    np.testing.assert_array_equal(a.get("FAIL"), b.get("FAIL"))
+    a.close()
+    b.close()
