@@ -8,7 +8,11 @@ of the force-computed nodes (broken bonds still count: both implementations
 visit them).  Setup (neighbour build, surface correction) is timed separately.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload crack_branching|plate_tensile|kalthoff_winkler|crack_grow]
+                  [--workload crack_branching|plate_tensile|kalthoff_winkler|crack_grow|batch]
+
+--workload batch: 256 seeded uneven plates (6.25M interior nodes) solved
+together by ADR (1000 steps), against the same plates run one after another
+(the engine's single-plate loop, and the reference's own kernels).
 
 --impl reference times the oracle's OpenMP host loop (the reference's
 formulas, its padded-ELL layout) on all host cores, on a bounded sample of the
@@ -245,6 +249,273 @@ def host_coords(p, meta):
     return meta["coords"]
 
 
+# ---- batch of plates -------------------------------------------------------------------------
+ALG_BYTES_PER_NODE_2D_ADR = 88.0  # P (x+u: 16) ... as 2-D + vh, fo (32) + ADR mass (8) for the damping sums
+
+
+def batch_host_specimen(base, sp):
+    """Host-only parameters and coordinates of one batch specimen (oracle
+    derivation, bit-identical to the engine's, pinned by tests)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+    from pd_gpu1_gb300 import presets
+
+    p, _ = presets.build_specimen(base, sp, derive=orc.derive_params)
+    x, y = orc.plate_crack_coords(p)
+    return p, x, y
+
+
+def batch_cpu_reference(base, specs, load, max_seconds, steps_each, threads):
+    """The oracle's ADR loop on the host cores over the specimens in order,
+    steps_each steps per specimen, until max_seconds.  Returns (bond-updates/s,
+    specimens, steps, seconds)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as orc
+
+    orc.set_threads(threads)
+    work = secs = 0.0
+    done = steps = nodes = 0
+    for sp in specs:
+        p, x, y = batch_host_specimen(base, sp)
+        m = orc.Model(p, x, y)
+        m.find_neighbor(brute=False)
+        m.surface_correct()
+        if sp["crack_len"] > 0.0:
+            m.set_crack_2d(sp["crack_len"], 0.0, 0.0, sp["crack_theta"])
+        bonds = int(m.NN[: p.N_int].sum())
+        nodes += p.N_int
+        t0 = time.perf_counter()
+        for ct in range(steps_each):
+            m.quick_load(load * sp["load_scale"])
+            m.adr_step(ct)
+        secs += time.perf_counter() - t0
+        work += bonds * steps_each
+        done += 1
+        steps += steps_each
+        if secs > max_seconds:
+            break
+    # time one step of the whole batch would take at this rate (bonds per node of the sample)
+    total_nodes = sum(int(sp["nx"]) * int(sp["ny"]) for sp in specs)
+    ms_batch_step = (work / steps_each) / nodes * total_nodes / (work / secs) * 1e3
+    return work / secs, done, steps, secs, ms_batch_step
+
+
+def batch_reference_arm(args, base, specs, meta):
+    threads = os.cpu_count() or 1
+    rate, done, steps, secs, ms_step = batch_cpu_reference(base, specs, meta["load"],
+                                                           min(60.0, 2.0 + 4.0 * args.steps), max(args.warmup, 5),
+                                                           threads)
+    line = {
+        "impl": "reference", "metric": "bond-updates/s", "value": rate, "unit": "bond-updates/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": f"synthetic (seeded specimens, seed "
+                                                                       f"{meta['seed']})",
+        "config": {"workload": meta["workload"], "specimens": len(specs), "dx": base.dx},
+        "cpu_baseline": {"value": rate, "unit": "bond-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{done} specimens of the batch in order, {steps // max(done, 1)} ADR steps "
+                                   f"each ({secs:.1f} s); OpenMP restatement of the reference's loops, one plate "
+                                   f"after another"},
+        "e2e": {"value": rate, "unit": "bond-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def batch_arm(args):
+    import ctypes as C
+
+    import torch
+
+    from pd_gpu1_gb300 import presets
+
+    rank, world, local = rank_info()
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle as orc
+
+        base, specs, meta = presets.build_batch(count=args.count, nt=args.steps, derive=orc.derive_params)
+        return batch_reference_arm(args, base, specs, meta)
+    base, specs, meta = presets.build_batch(count=args.count, nt=args.steps)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    from pd_gpu1_gb300 import engine as E
+    from pd_gpu1_gb300._abi import FIELD
+    from pd_gpu1_gb300._lib import lib
+
+    L = lib()
+    load = meta["load"]
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        bat = E.Batch(base, specs, stream=stream.cuda_stream)
+        bat.sync()
+    setup_s = time.perf_counter() - t0
+    p = bat.p
+    rp = bat.get("ROWPTR")
+    B = int(rp[p.N_int])
+    fail0 = bat.get("FAIL")
+    zeros = np.zeros(p.N)
+
+    def reset():
+        for k in ["UX", "UY", "VX", "VY", "VHX", "VHY", "FOX", "FOY", "FX", "FY"]:
+            bat.set(k, zeros)
+        bat.set("FAIL", fail0)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+
+    # launch shape: the autotuner times the ADR force kernel at the initial state
+    with torch.cuda.stream(stream):
+        tuned = bat.autotune(reps=5)
+    # warm-up, then the timed steps
+    with torch.cuda.stream(stream):
+        bat.run_adr(0, args.warmup, load)
+    barrier()
+    launches0 = bat.kernel_launches
+    clocks = ClockSampler(torch.cuda.current_device())
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    ev0.record(stream)
+    with torch.cuda.stream(stream):
+        bat.run_adr(args.warmup, args.steps, load)
+    ev1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = bat.kernel_launches - launches0
+    secs_max, work = aggregate_replicas(ms * 1e-3, B * args.steps, dist, "cuda")
+    value = work / secs_max
+    broken = float((bat.get("FAIL") == 0).mean())
+
+    # force kernel alone (ADR epilogue with per-slice damping sums), timed by the
+    # autotuner with CUDA events on the launch stream: its best shape is the one used
+    kern_ms = tuned[3]
+    alg_bytes = ALG_BYTES_PER_NODE_2D_ADR * p.N_int + ALG_BYTES_PER_BOND_2D * B
+    peaks, peak_kind = measured_peaks()
+    achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
+    gfma = C.c_double()
+    L.pd_probe_fp64(C.byref(gfma))
+    fp64_peak = 2.0 * gfma.value / 1e3
+    alg_flops = ALG_FP64_PER_BOND_2D * B
+    tr = TRAFFIC.get(meta["workload"])
+    traffic = tr[0] * B + tr[1] * p.N_int if tr else None
+
+    # end to end through the C ABI with host buffers: the initial state goes up
+    # from pinned host memory, the displacement field comes back every 100 steps
+    n = p.N
+    reset()
+    names_up = ["UX", "UY", "VHX", "VHY", "FOX", "FOY"]
+    pin = {k: torch.zeros(n, dtype=torch.float64).pin_memory() for k in names_up}
+    barrier()
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for k in names_up:
+        bat._c(L.pd_set_field(bat.ctx, FIELD[k], pin[k].data_ptr(), n, bat.stream), "pd_set_field")
+        h2d += n * 8
+    done = 0
+    while done < args.steps:
+        k_run = min(100, args.steps - done)
+        bat.run_adr(done, k_run, load)
+        done += k_run
+        for k in ["UX", "UY"]:
+            bat._c(L.pd_get_field(bat.ctx, FIELD[k], pin[k].data_ptr(), n, bat.stream), "pd_get_field")
+            d2h += n * 8
+    e2e_s, e2e_work = aggregate_replicas(time.perf_counter() - t0, B * args.steps, dist, "cuda")
+    e2e = {"value": e2e_work / e2e_s, "unit": "bond-updates/s", "h2d_bytes_per_step": h2d / args.steps,
+           "d2h_bytes_per_step": d2h / args.steps}
+    bat.close()
+
+    sequential = ref_cuda = cpu = None
+    if rank == 0 and world == 1:
+        # the same plates one after another through the engine's single-plate loop
+        k_seq = min(args.steps, args.seq_steps)
+        engines, bonds = [], []
+        for sp in specs:
+            q, setup = presets.build_specimen(base, sp)
+            e = E.Engine(q, stream=stream.cuda_stream)
+            with torch.cuda.stream(stream):
+                setup(e)
+            engines.append(e)
+            bonds.append(int(e.get("ROWPTR")[q.N_int]))
+        with torch.cuda.stream(stream):
+            for e, sp in zip(engines, specs):
+                e.run_adr(0, 3, load * sp["load_scale"])
+        barrier()
+        s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s0.record(stream)
+        with torch.cuda.stream(stream):
+            for e, sp in zip(engines, specs):
+                e.run_adr(3, k_seq, load * sp["load_scale"])
+        s1.record(stream)
+        barrier()
+        seq_ms = s0.elapsed_time(s1)
+        sequential = {"value": sum(bonds) * k_seq / (seq_ms * 1e-3), "unit": "bond-updates/s", "steps_each": k_seq,
+                      "what": "the same specimens one after another, pd_run_adr per plate (CUDA graphs)"}
+        # the reference's own kernels, one plate after another
+        if not args.no_ref_cuda:
+            sys.path.insert(0, os.path.join(ROOT, "oracle"))
+            import ref_gpu
+
+            if ref_gpu.available():
+                k_ref = min(args.steps, args.seq_steps)
+                tot_ms, tot_work = 0.0, 0.0
+                for e, sp, b in zip(engines, specs, bonds):
+                    r, _ = ref_gpu.from_engine(e, e.p)
+                    r.run_adr(0, 3, load * sp["load_scale"])
+                    ms_r, _ = r.run_adr(3, k_ref, load * sp["load_scale"])
+                    tot_ms += ms_r
+                    tot_work += b * k_ref
+                    r.free()
+                best = tot_work / (tot_ms * 1e-3)
+                ref_cuda = {"unit": "bond-updates/s", "steps_each": k_ref, "best": best,
+                            "engine_over_best": value / best,
+                            "what": "the reference's kernels (compiled from its sources, FP64), its ADR loop "
+                                    "(particle force, kernel_cnn, two host-read sums, kernel_integrate) per plate, "
+                                    "one plate after another; loop time summed over plates"}
+        for e in engines:
+            e.close()
+        if not args.no_cpu:
+            rate, ndone, steps, secs, _ = batch_cpu_reference(base, specs, load, args.cpu_seconds, 100,
+                                                              os.cpu_count() or 1)
+            cpu = {"value": rate, "unit": "bond-updates/s", "cores": os.cpu_count(), "kind": "port",
+                   "sample": f"{ndone} specimens of the batch in order, 100 ADR steps each ({secs:.1f} s of "
+                             f"host time), the oracle's OpenMP loops"}
+
+    if rank == 0:
+        line = {
+            "metric": "bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs_max * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": f"synthetic (seeded specimen table, seed {meta['seed']})",
+            "config": {"workload": meta["workload"], "specimens": len(specs), "nodes": p.N, "interior": p.N_int,
+                       "bonds": B, "dx": p.dx, "dt": p.dt, "parallelism": "replicas" if world > 1 else "single",
+                       "launch": {"block": tuned[0], "chunked": tuned[1], "waves": tuned[2]},
+                       "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 28 / 1e9),
+                       "setup_s": setup_s, "broken_bond_fraction": broken},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+                         "kernel": "k_bond_force<2, ADR>", "kernel_ms": kern_ms, "alg_bytes_per_launch": alg_bytes,
+                         "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
+                                  "frac": alg_flops / (kern_ms * 1e-3) / 1e12 / fp64_peak,
+                                  "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk, "sequential": sequential,
+            "reference_cuda": ref_cuda,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
 # ----------------------------------------------------------------------------------------------
 def gb300_arm(args):
     import ctypes as C
@@ -429,7 +700,7 @@ def gb300_arm(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1800)
+    ap.add_argument("--steps", type=int, default=None, help="time steps (default: the workload's nt)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="crack_branching")
@@ -437,9 +708,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--count", type=int, default=256, help="batch workload: number of specimens")
+    ap.add_argument("--seq-steps", type=int, default=100, help="batch workload: steps per plate when run one "
+                                                                "after another")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.steps is None:
+        args.steps = {"crack_branching": 1800, "plate_tensile": 1000, "kalthoff_winkler": 1350,
+                      "crack_grow": 1250, "batch": 1000}.get(args.workload, 1800)
+    if args.workload == "batch":
+        return batch_arm(args)
     if args.impl == "reference":
         return reference_arm(args)
     return gb300_arm(args)

@@ -232,6 +232,56 @@ int pd_run_adr(pd_ctx* ctx, int ct0, int nsteps, double load, void* stream);
  * damage field is refreshed every dmg_every steps. */
 int pd_run_explicit(pd_ctx* ctx, int nsteps, double load, int dmg_every, void* stream);
 
+/* ---- batches of specimens ----------------------------------------------- */
+/* No counterpart in the reference, which solves one plate per process.  A
+ * batch packs many 2-D bond-based plates of the crack-plate layout
+ * (Coord.cu:34-45: nx*ny interior nodes, then 3 boundary rows above and 3
+ * below) into one context and solves them together with the ADR step of
+ * solve_plate_tensile (Solve_Plate_Tensile.cu:106-131), one launch per phase
+ * for all specimens. */
+typedef struct pd_specimen {
+    int32_t nx, ny;       /* interior nodes per row, interior rows (>= 4 each) */
+    double emod;          /* Young's modulus: sets bc and the ADR mass (Base.cuh:135, :150) */
+    double critical_s;    /* critical stretch s0                               */
+    double crack_len;     /* centred pre-crack length (0: none), kernel_set_crack_2D */
+    double crack_theta;   /* pre-crack angle in radians                         */
+    double load_scale;    /* boundary rows move by +-load_scale*load*dt per step */
+} pd_specimen;
+/* Builds the batch from shared parameters (dx, dt, thick, pratio, delta, MN,
+ * mode: a 2-D bond-based pd_params, e.g. from pd_params_derive) and count
+ * specimens: family (each specimen only with itself), surface correction,
+ * per-specimen pre-crack, bond arrays.  Every specimen keeps its own
+ * coordinate frame, so its coefficients and forces are those of the same
+ * plate set up alone.  Node layout: specimen k's interior nodes start at
+ * interior_offsets[k] (a multiple of 32; rows after its nx*ny nodes up to the
+ * next offset are bond-less padding), its 6*nx boundary nodes at
+ * N_int + boundary_offsets[k] (pd_batch_info).  Returns NULL and *status on
+ * failure. */
+pd_ctx* pd_batch_create(const pd_params* base, const pd_specimen* spec, int count, int* status);
+/* count, and when non-NULL the count+1 interior and boundary offsets. */
+int pd_batch_info(const pd_ctx* ctx, int* count, int64_t* interior_offsets, int64_t* boundary_offsets);
+/* pd_run_adr for every specimen of a batch: each specimen has its own damping
+ * coefficient (cal_cn over its own nodes) and ADR mass; boundary rows move by
+ * +-load_scale*load*dt per step.  Three launches per step, CUDA graphs. */
+int pd_batch_run_adr(pd_ctx* ctx, int ct0, int nsteps, double load, void* stream);
+/* The count per-specimen damping coefficients of the last step. */
+int pd_batch_get_cn(pd_ctx* ctx, double* cn, void* stream);
+
+/* ---- launch shape of the bond-force kernels ------------------------------ */
+/* Threads per block (128, 256, 512), warp-to-slice order (0: grid-strided,
+ * 1: one contiguous run of slices per warp) and grid size in waves of
+ * resident blocks (1..8).  The per-node force sums do not depend on the
+ * shape; sums over the whole grid (the single-specimen ADR damping
+ * coefficient, the impactor reaction) follow the block order and may differ
+ * in the last bits.  Default 256 / 0 / 1. */
+int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves);
+int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves);
+/* Times the bond-force kernel (reps launches per shape, at the current
+ * displacements) over the 18 shapes above and keeps the fastest; *best_ms
+ * receives its time per launch.  Intact flags and forces are restored, so a
+ * run continues exactly as without the call.  Bond-based contexts only. */
+int pd_autotune(pd_ctx* ctx, int reps, double* best_ms, void* stream);
+
 /* ---- drivers (Solve_*.cuh:17-19) --------------------------------------- */
 typedef struct pd_result {
     int64_t N, N_int, B;

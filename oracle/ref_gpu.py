@@ -42,6 +42,7 @@ class RefGPU:
         self.lib = C.CDLL(LIB)
         self.lib.rr_error.restype = C.c_char_p
         self.lib.rr_run.argtypes = [C.c_int, C.c_int, C.c_int, D]
+        self.lib.rr_run_adr.argtypes = [C.c_int, C.c_int, C.c_double, D, D]
         self._check(self.lib.rr_init(CUBIN.encode()), "rr_init")
         self.N = self.MN = 0
 
@@ -84,6 +85,13 @@ class RefGPU:
         ms = C.c_double()
         self._check(self.lib.rr_run(variant, nsteps, dmg_every, C.byref(ms)), "rr_run")
         return ms.value
+
+    def run_adr(self, ct0, nsteps, load):
+        """solve_plate_tensile's ADR loop with moving boundary rows; returns
+        (elapsed ms, last damping coefficient)."""
+        ms, cn = C.c_double(), C.c_double()
+        self._check(self.lib.rr_run_adr(ct0, nsteps, load, C.byref(ms), C.byref(cn)), "rr_run_adr")
+        return ms.value, cn.value
 
     def get(self, NN=None):
         N, MN = self.N, self.MN

@@ -13,6 +13,7 @@
 // (Solve_Plate_Crack_Grow.cu:301).
 #include <cuda.h>
 
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
@@ -32,11 +33,15 @@ struct Runner {
     CUcontext ctx = nullptr;
     CUmodule mod = nullptr;
     CUfunction f_particle = nullptr, f_bond = nullptr, f_int1 = nullptr, f_int2 = nullptr, f_dmg = nullptr;
+    CUfunction f_cnn = nullptr, f_adr = nullptr, f_reduce = nullptr, f_qload = nullptr;
+    CUdeviceptr static_y = 0;  // Reduce.cu's block partial array
     CUstream stream = nullptr;
     device_parameter p{};
     // device arrays
     CUdeviceptr x = 0, y = 0, ux = 0, uy = 0, vx = 0, vy = 0, ax = 0, ay = 0, fx = 0, fy = 0, bx = 0, by = 0,
                 dmg = 0, NN = 0, NL = 0, idist = 0, scr = 0, fac = 0, fail = 0;
+    // ADR arrays (velhalf, velhalfold, pforceold per axis; kernel_cnn's outputs)
+    CUdeviceptr vhx = 0, vhy = 0, vhox = 0, vhoy = 0, fox = 0, foy = 0, cn_xy = 0, disp_xy = 0;
     bool ready = false;
 };
 
@@ -57,8 +62,10 @@ int fail_with(CUresult r, const char* what) {
     } while (0)
 
 void free_all() {
-    CUdeviceptr* all[] = {&R.x, &R.y, &R.ux, &R.uy, &R.vx, &R.vy, &R.ax, &R.ay, &R.fx, &R.fy,
-                          &R.bx, &R.by, &R.dmg, &R.NN, &R.NL, &R.idist, &R.scr, &R.fac, &R.fail};
+    CUdeviceptr* all[] = {&R.x,     &R.y,   &R.ux,   &R.uy,   &R.vx,   &R.vy,    &R.ax,   &R.ay,
+                          &R.fx,    &R.fy,  &R.bx,   &R.by,   &R.dmg,  &R.NN,    &R.NL,   &R.idist,
+                          &R.scr,   &R.fac, &R.fail, &R.vhx,  &R.vhy,  &R.vhox,  &R.vhoy, &R.fox,
+                          &R.foy,   &R.cn_xy, &R.disp_xy};
     for (CUdeviceptr* d : all)
         if (*d) {
             cuMemFree(*d);
@@ -94,6 +101,14 @@ int rr_init(const char* cubin) {
     RR_TRY(cuModuleGetFunction(&R.f_int2, R.mod, "_Z21kernel_integrate_2D_2PdS_S_S_S_S_S_S_"),
            "kernel_integrate_2D_2");
     RR_TRY(cuModuleGetFunction(&R.f_dmg, R.mod, "_Z17kernel_cal_dmg_2DPiPdS_S0_"), "kernel_cal_dmg_2D");
+    RR_TRY(cuModuleGetFunction(&R.f_cnn, R.mod, "_Z10kernel_cnnPdS_S_S_S_S_S_S_S_S_S_S_S_S_"), "kernel_cnn");
+    RR_TRY(cuModuleGetFunction(&R.f_adr, R.mod, "_Z16kernel_integrateidPdS_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_S_"),
+           "kernel_integrate");
+    RR_TRY(cuModuleGetFunction(&R.f_reduce, R.mod, "_Z9reduce_cpPKdPdi"), "reduce_cp");
+    RR_TRY(cuModuleGetFunction(&R.f_qload, R.mod, "harness_quick_load"), "harness_quick_load");
+    size_t ys = 0;
+    RR_TRY(cuModuleGetGlobal(&R.static_y, &ys, R.mod, "static_y"), "static_y");
+    if (ys != 256 * sizeof(double)) return fail_with(CUDA_ERROR_INVALID_VALUE, "static_y size");
     RR_TRY(cuStreamCreate(&R.stream, CU_STREAM_NON_BLOCKING), "stream");
     return 0;
 }
@@ -134,7 +149,9 @@ int rr_setup(const double* dparams, const int* iparams, const double* x, const d
     RR_TRY(cuModuleGetGlobal(&dpp, &dps, R.mod, "dp"), "dp symbol");
     if (dps != sizeof(device_parameter)) return fail_with(CUDA_ERROR_INVALID_VALUE, "dp size");
     RR_TRY(cuMemcpyHtoD(dpp, &p, sizeof(p)), "dp copy");
-    CUdeviceptr* nodes[] = {&R.x, &R.y, &R.ux, &R.uy, &R.vx, &R.vy, &R.ax, &R.ay, &R.fx, &R.fy, &R.bx, &R.by, &R.dmg};
+    CUdeviceptr* nodes[] = {&R.x,   &R.y,    &R.ux,   &R.uy,  &R.vx,  &R.vy,    &R.ax,      &R.ay,   &R.fx,
+                            &R.fy,  &R.bx,   &R.by,   &R.dmg, &R.vhx, &R.vhy,   &R.vhox,    &R.vhoy, &R.fox,
+                            &R.foy, &R.cn_xy, &R.disp_xy};
     for (CUdeviceptr* d : nodes) {
         RR_TRY(cuMemAlloc(d, N * 8), "node alloc");
         RR_TRY(cuMemsetD8(*d, 0, N * 8), "node zero");
@@ -207,6 +224,73 @@ int rr_run(int variant, int nsteps, int dmg_every, double* ms) {
     float t = 0.f;
     RR_TRY(cuEventElapsedTime(&t, e0, e1), "elapsed");
     *ms = t;
+    cuEventDestroy(e0);
+    cuEventDestroy(e1);
+    return 0;
+}
+
+namespace {
+
+// sum (Reduce.cu:52-65): two reduce_cp launches into static_y, then a
+// blocking read of the result.
+int ref_sum(int n, CUdeviceptr x, double* out) {
+    int nn = n, nb = 256;
+    void* a1[] = {&x, &R.static_y, &nn};
+    void* a2[] = {&R.static_y, &R.static_y, &nb};
+    RR_TRY(cuLaunchKernel(R.f_reduce, 256, 1, 1, 256, 1, 1, 256 * 8, R.stream, a1, nullptr), "reduce_cp");
+    RR_TRY(cuLaunchKernel(R.f_reduce, 1, 1, 1, 256, 1, 1, 256 * 8, R.stream, a2, nullptr), "reduce_cp");
+    RR_TRY(cuMemcpyDtoHAsync(out, R.static_y, sizeof(double), R.stream), "sum read");
+    RR_TRY(cuStreamSynchronize(R.stream), "sum sync");
+    return 0;
+}
+
+}  // namespace
+
+// nsteps ADR steps of solve_plate_tensile's loop (Solve_Plate_Tensile.cu:106-131)
+// with the crack-plate driver's moving boundary rows before each step:
+// quick_load, kernel_particle_force_2D, kernel_cnn, cal_cn (two sums, each
+// read back by the host), kernel_integrate.  Step indices ct0.. ; the
+// elapsed time of the loop goes to *ms, the last damping coefficient to *cn.
+int rr_run_adr(int ct0, int nsteps, double load, double* ms, double* cn_out) {
+    if (!R.ready) return -1;
+    CUdeviceptr null = 0;
+    void* af[] = {&R.x, &R.ux, &R.fx, &R.y, &R.uy, &R.fy, &R.NN, &R.NL, &R.idist, &R.scr, &R.fail, &R.fac};
+    void* ac[] = {&R.cn_xy, &R.fx, &R.fox, &R.vhox, &R.ux, &R.disp_xy, &R.fy, &R.foy, &R.vhoy, &R.uy,
+                  &null,    &null, &null,  &null};
+    void* aq[] = {&load, &R.uy};
+    const unsigned gN = (unsigned)((R.p.N - 1) / 256 + 1);
+    const unsigned gQ = (unsigned)((6 * R.p.nx - 1) / 256 + 1);
+    CUevent e0, e1;
+    RR_TRY(cuEventCreate(&e0, CU_EVENT_DEFAULT), "event");
+    RR_TRY(cuEventCreate(&e1, CU_EVENT_DEFAULT), "event");
+    RR_TRY(cuEventRecord(e0, R.stream), "record");
+    double cn = 0.0;
+    for (int s = 0; s < nsteps; s++) {
+        int ct = ct0 + s;
+        if (load != 0.0 && launch(R.f_qload, gQ, aq)) return -1;
+        if (launch(R.f_particle, gN, af)) return -1;
+        if (launch(R.f_cnn, gN, ac)) return -1;
+        double cn1 = 0.0, cn2 = 0.0;
+        if (ref_sum(R.p.N_int, R.cn_xy, &cn1) || ref_sum(R.p.N_int, R.disp_xy, &cn2)) return -1;
+        cn = 0.0;  // cal_cn (Integrate.cu:108-129)
+        if (cn2 != 0.0) {
+            if (cn1 / cn2 > 0.0)
+                cn = 2.0 * std::sqrt(cn1 / cn2);
+            else
+                cn = 0.0;
+        }
+        if (cn > 2.0) cn = 1.9;
+        void* ai[] = {&ct,    &cn,   &R.fx,  &R.vhx, &R.bx, &R.vx,  &R.vhox, &R.ux,
+                      &R.fox, &R.fy, &R.vhy, &R.by,  &R.vy, &R.vhoy, &R.uy,  &R.foy,
+                      &null,  &null, &null,  &null,  &null, &null,  &null};
+        if (launch(R.f_adr, gN, ai)) return -1;
+    }
+    RR_TRY(cuEventRecord(e1, R.stream), "record");
+    RR_TRY(cuEventSynchronize(e1), "sync");
+    float t = 0.f;
+    RR_TRY(cuEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+    if (cn_out) *cn_out = cn;
     cuEventDestroy(e0);
     cuEventDestroy(e1);
     return 0;

@@ -88,3 +88,12 @@ class PDResult(C.Structure):
         ("N", C.c_int64), ("N_int", C.c_int64), ("B", C.c_int64),
         ("setup_ms", C.c_double), ("loop_ms", C.c_double), ("bond_updates_per_s", C.c_double),
     ]
+
+
+class PDSpecimen(C.Structure):
+    """pd_specimen: one plate of a batch (size, modulus, s0, pre-crack, loading rate)."""
+
+    _fields_ = [
+        ("nx", C.c_int32), ("ny", C.c_int32), ("emod", C.c_double), ("critical_s", C.c_double),
+        ("crack_len", C.c_double), ("crack_theta", C.c_double), ("load_scale", C.c_double),
+    ]

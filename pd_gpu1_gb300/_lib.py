@@ -7,7 +7,7 @@ raises, so a run without the CUDA engine cannot pass silently.
 import ctypes as C
 import os
 
-from ._abi import PDCylinder, PDParams, PDResult
+from ._abi import PDCylinder, PDParams, PDResult, PDSpecimen
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpd_gb300.so")
@@ -62,6 +62,13 @@ _SIGS = {
     "pd_cylinder_integrate2": (I32, [VP, VP]),
     "pd_run_adr": (I32, [VP, I32, I32, D, VP]),
     "pd_run_explicit": (I32, [VP, I32, D, I32, VP]),
+    "pd_batch_create": (VP, [P(PDParams), P(PDSpecimen), I32, P(I32)]),
+    "pd_batch_info": (I32, [VP, P(I32), P(I64), P(I64)]),
+    "pd_batch_run_adr": (I32, [VP, I32, I32, D, VP]),
+    "pd_batch_get_cn": (I32, [VP, P(D), VP]),
+    "pd_set_launch": (I32, [VP, I32, I32, I32]),
+    "pd_get_launch": (I32, [VP, P(I32), P(I32), P(I32)]),
+    "pd_autotune": (I32, [VP, I32, P(D), VP]),
     "pd_solve_plate_tensile": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),
     "pd_solve_plate_crack_grow": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),
     "pd_solve_kalthoff_winkler": (I32, [D, I32, P(D), P(D), P(D), P(D), I64, P(PDResult)]),

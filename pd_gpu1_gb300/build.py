@@ -24,6 +24,7 @@ UNITS = {
     "integrate.cu": [],
     "api.cu": [],
     "noalloc.cu": [],
+    "batch.cu": [],
 }
 
 

@@ -345,6 +345,7 @@ int pd_destroy(pd_ctx* c) {
     for (void* q : ptrs)
         if (q) cudaFree(q);
     release_sell(c);
+    release_batch(c);
     delete c;
     return PD_OK;
 }
@@ -556,6 +557,7 @@ int pd_state_force(pd_ctx* c, void* stream) {
 // ---- integration --------------------------------------------------------------
 int pd_integrate_adr(pd_ctx* c, int ct, void* stream) {
     if (!c) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "a batch of specimens steps with pd_batch_run_adr");
     cudaStream_t s = st(stream);
     int rc = launch_adr_cnn(c, s);
     if (rc) return rc;
@@ -564,6 +566,7 @@ int pd_integrate_adr(pd_ctx* c, int ct, void* stream) {
 
 int pd_get_adr_cn(pd_ctx* c, double* cn, void* stream) {
     if (!c || !cn) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "a batch of specimens has one cn per specimen");
     cudaError_t e = cudaMemcpyAsync(cn, c->cn, 8, cudaMemcpyDeviceToHost, st(stream));
     if (e == cudaSuccess) e = cudaStreamSynchronize(st(stream));
     return cuda_err(c, e, "pd_get_adr_cn");
@@ -592,7 +595,11 @@ int pd_damage(pd_ctx* c, void* stream) {
     return launch_damage(c, st(stream));
 }
 
-int pd_quick_load(pd_ctx* c, double load, void* stream) { return c ? launch_quick_load(c, load, st(stream)) : PD_ERR_ARG; }
+int pd_quick_load(pd_ctx* c, double load, void* stream) {
+    if (!c) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "batch boundary rows move inside pd_batch_run_adr");
+    return launch_quick_load(c, load, st(stream));
+}
 
 int pd_load_plate_tensile(pd_ctx* c, void* stream) {
     if (!c || c->p.dim != 2) return PD_ERR_ARG;
@@ -667,6 +674,7 @@ static const int kChunk = 50;
 
 int pd_run_adr(pd_ctx* c, int ct0, int nsteps, double load, void* stream) {
     if (!c || nsteps < 0 || ct0 < 0) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "a batch of specimens steps with pd_batch_run_adr");
     if (nsteps == 0) return PD_OK;
     if (c->p.mass == 0.0) return set_err(c, PD_ERR_ARG, "ADR needs the fictitious mass (bond-based parameters)");
     StreamScope sc(c, stream);
@@ -705,6 +713,7 @@ int pd_run_adr(pd_ctx* c, int ct0, int nsteps, double load, void* stream) {
 
 int pd_run_explicit(pd_ctx* c, int nsteps, double load, int dmg_every, void* stream) {
     if (!c || nsteps < 0 || dmg_every < 0) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "a batch of specimens is solved by ADR only");
     if (nsteps == 0) return PD_OK;
     StreamScope sc(c, stream);
     cudaStream_t s = sc.s;
@@ -740,6 +749,134 @@ int pd_run_explicit(pd_ctx* c, int nsteps, double load, int dmg_every, void* str
         done += len;
     }
     return cuda_err(c, cudaGetLastError(), "pd_run_explicit");
+}
+
+// Batched ADR: the loop of pd_run_adr over every specimen of a batch context,
+// three launches per step (force + per-slice damping sums, per-specimen cn,
+// update), captured in CUDA graphs of kChunk steps.
+int pd_batch_run_adr(pd_ctx* c, int ct0, int nsteps, double load, void* stream) {
+    if (!c || nsteps < 0 || ct0 < 0) return PD_ERR_ARG;
+    if (!c->batch.count) return set_err(c, PD_ERR_STATE, "not a batch context (pd_batch_create)");
+    if (nsteps == 0) return PD_OK;
+    StreamScope sc(c, stream);
+    cudaStream_t s = sc.s;
+    int rc = ensure_ready(c, s);
+    if (rc) return rc;
+    if ((rc = batch_prologue(c, load, s))) return rc;
+    int done = 0;
+    if (ct0 == 0) {
+        if ((rc = batch_step(c, 0, nsteps == 1, load, s))) return rc;
+        done = 1;
+    }
+    while (done < nsteps) {
+        const int len = std::min(kChunk, nsteps - done);
+        const int final_chunk = done + len == nsteps;
+        Key k{3, len, c->parity, final_chunk, load, 0};
+        rc = graph_chunk(c, k, s, [&]() -> int {
+            for (int t = 0; t < len; t++) {
+                int r = batch_step(c, ct0 + done + t, final_chunk && t == len - 1, load, s);
+                if (r) return r;
+            }
+            return PD_OK;
+        });
+        if (rc) return rc;
+        done += len;
+    }
+    return cuda_err(c, cudaGetLastError(), "pd_batch_run_adr");
+}
+
+int pd_set_launch(pd_ctx* c, int block, int chunked, int waves) {
+    if (!c || (block != 128 && block != 256 && block != 512) || (chunked != 0 && chunked != 1) || waves < 1 ||
+        waves > 8)
+        return PD_ERR_ARG;
+    if (block != c->tune_block || chunked != c->tune_chunked || waves != c->tune_waves) {
+        drop_graphs(c);  // captured launches carry the old shape
+        c->tune_block = block;
+        c->tune_chunked = chunked;
+        c->tune_waves = waves;
+    }
+    return PD_OK;
+}
+
+int pd_get_launch(const pd_ctx* c, int* block, int* chunked, int* waves) {
+    if (!c || !block || !chunked || !waves) return PD_ERR_ARG;
+    *block = c->tune_block;
+    *chunked = c->tune_chunked;
+    *waves = c->tune_waves;
+    return PD_OK;
+}
+
+// Times the bond-force kernel at the current displacements for every launch
+// shape (block 128/256/512 x strided/chunked slice order x 1/2/4 waves of
+// resident blocks) and keeps the fastest.  The intact flags and forces are
+// restored afterwards, so a run continues exactly as it would have.
+int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
+    if (!c || reps < 1) return PD_ERR_ARG;
+    if (c->p.model != PD_MODEL_BOND) return set_err(c, PD_ERR_UNSUPPORTED, "the launch shape applies to bond kernels");
+    StreamScope sc(c, stream);
+    cudaStream_t s = sc.s;
+    int rc = ensure_ready(c, s);
+    if (rc) return rc;
+    const Sell& S = c->sell;
+    const int64_t N = c->p.N;
+    const size_t nbits = (size_t)std::max<int64_t>(S.F, 1) * 4;
+    uint32_t* saved_bits = nullptr;
+    double* saved_f = nullptr;
+    cudaError_t e;
+    if ((e = cudaMallocAsync(&saved_bits, nbits, s)) != cudaSuccess) return cuda_err(c, e, "autotune scratch");
+    if ((e = cudaMallocAsync(&saved_f, 2 * N * sizeof(double), s)) != cudaSuccess) {
+        cudaFreeAsync(saved_bits, s);
+        return cuda_err(c, e, "autotune scratch");
+    }
+    cudaMemcpyAsync(saved_bits, S.bits, nbits, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(saved_f, c->nf[PD_F_FX], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(saved_f + N, c->nf[PD_F_FY], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    const bool csr_current = c->csr_fail_current, pos_valid = c->pos_valid;
+    const int b0 = c->tune_block, k0 = c->tune_chunked, w0 = c->tune_waves;
+    StepFlags f;
+    f.epi = c->batch.count ? EPI_ADR : EPI_NONE;  // a batch's ADR epilogue writes only per-slice scratch
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    double best = 1e300;
+    int bb = b0, bk = k0, bw = w0;
+    const int blocks[3] = {128, 256, 512}, waves[3] = {1, 2, 4};
+    for (int ib = 0; ib < 3 && !rc; ib++)
+        for (int ck = 0; ck < 2 && !rc; ck++)
+            for (int iw = 0; iw < 3 && !rc; iw++) {
+                c->tune_block = blocks[ib];
+                c->tune_chunked = ck;
+                c->tune_waves = waves[iw];
+                if ((rc = launch_force(c, f, s))) break;  // warm-up
+                cudaEventRecord(e0, s);
+                for (int r = 0; r < reps && !rc; r++) rc = launch_force(c, f, s);
+                cudaEventRecord(e1, s);
+                if (rc || (e = cudaEventSynchronize(e1)) != cudaSuccess) {
+                    if (!rc) rc = cuda_err(c, e, "autotune timing");
+                    break;
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms / reps < best) {
+                    best = ms / reps;
+                    bb = blocks[ib], bk = ck, bw = waves[iw];
+                }
+            }
+    cudaMemcpyAsync(S.bits, saved_bits, nbits, cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(c->nf[PD_F_FX], saved_f, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaMemcpyAsync(c->nf[PD_F_FY], saved_f + N, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    cudaFreeAsync(saved_bits, s);
+    cudaFreeAsync(saved_f, s);
+    e = cudaStreamSynchronize(s);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->csr_fail_current = csr_current;
+    c->pos_valid = pos_valid;
+    c->tune_block = b0, c->tune_chunked = k0, c->tune_waves = w0;
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_err(c, e, "pd_autotune");
+    if (best_ms) *best_ms = best;
+    return pd_set_launch(c, bb, bk, bw);
 }
 
 // ---- drivers ----------------------------------------------------------------

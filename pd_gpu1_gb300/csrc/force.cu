@@ -84,11 +84,17 @@ struct ForceArgs {
     double* partials;
     unsigned int* ticket;
     double* cn_out;
+    int chunked;              // contiguous slice runs per warp instead of a grid stride
+    // batch of specimens (null for a single one)
+    const double* node_mass;  // ADR fictitious mass per node
+    double* slice_part;       // per-slice damping sums (2 per slice) instead of a grid reduction
 };
 
 namespace {
 
 constexpr int kWarpsPerBlock = kForceBlock / 32;
+constexpr int kMaxBondBlock = 512;  // the bond kernels take any block size up to this
+constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
 // Seed of the square-root iteration: the FP32 reciprocal square root (about
 // 23 correct bits, one Newton step to ~3e-14) or the FP64 one (about 20 bits,
 // two steps).  On this GPU f64<->f32 conversion instructions issue on the FP64
@@ -187,7 +193,7 @@ __device__ __forceinline__ double block_sum(double v, double* sm) {
     __syncthreads();
     double r = 0.0;
     if (threadIdx.x == 0)
-        for (int k = 0; k < kWarpsPerBlock; k++) r += sm[k];
+        for (int k = 0; k < (int)(blockDim.x >> 5); k++) r += sm[k];
     return r;  // valid in thread 0
 }
 
@@ -238,16 +244,18 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
     A.fy[r] = fyr;
     if (DIM == 3) A.fz[r] = fzr;
     if (EPI == EPI_ADR) {
-        // kernel_cnn (Integrate.cu:17-33), same operand order
+        // kernel_cnn (Integrate.cu:17-33), same operand order; a batch of
+        // specimens carries its fictitious mass per node
+        const double mass = A.node_mass ? A.node_mass[r] : P.mass;
         const double vhx = A.vhx[r], vhy = A.vhy[r];
         double cn = 0.0, disp;
-        if (vhx != 0.0) cn = -1.0 * uxi * uxi * (fxr / P.mass - A.fox[r] / P.mass) / (P.dt * vhx);
+        if (vhx != 0.0) cn = -1.0 * uxi * uxi * (fxr / mass - A.fox[r] / mass) / (P.dt * vhx);
         disp = uxi * uxi;
-        if (vhy != 0.0) cn -= 1.0 * uyi * uyi * (fyr / P.mass - A.foy[r] / P.mass) / (P.dt * vhy);
+        if (vhy != 0.0) cn -= 1.0 * uyi * uyi * (fyr / mass - A.foy[r] / mass) / (P.dt * vhy);
         disp += uyi * uyi;
         if (DIM == 3) {
             const double vhz = A.vhz[r];
-            if (vhz != 0.0) cn -= 1.0 * uzi * uzi * (fzr / P.mass - A.foz[r] / P.mass) / (P.dt * vhz);
+            if (vhz != 0.0) cn -= 1.0 * uzi * uzi * (fzr / mass - A.foz[r] / mass) / (P.dt * vhz);
             disp += uzi * uzi;
         }
         red[0] += cn;
@@ -297,6 +305,21 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
     }
 }
 
+// Batch of specimens: the damping sums of one slice (one specimen's rows)
+// reduced over the warp in a fixed order and stored per slice.
+__device__ __forceinline__ void slice_partials(const ForceArgs& A, int64_t s, double red[3]) {
+    double a = red[0], b = red[1];
+    for (int off = 16; off > 0; off >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, off);
+        b += __shfl_down_sync(0xffffffffu, b, off);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        A.slice_part[2 * s] = a;
+        A.slice_part[2 * s + 1] = b;
+    }
+    red[0] = red[1] = 0.0;
+}
+
 // Boundary rows [N_int, N): the next step's prescribed motion
 // (kernel_quick_load: the first 3 nx rows move up, the next 3 nx down).
 template <int DIM>
@@ -322,7 +345,7 @@ __device__ __forceinline__ void boundary_row(const ForceArgs& A, int64_t r) {
 // impactor update; EPI_NONE -> contact reaction accumulated only.
 template <int EPI>
 __device__ void finish_reduction(const ForceArgs& A, double red[3], int nred) {
-    __shared__ double sm[kWarpsPerBlock];
+    __shared__ double sm[kMaxWarpsPerBlock];
     __shared__ bool last;
     for (int k = 0; k < nred; k++) {
         const double v = block_sum(red[k], sm);
@@ -370,13 +393,23 @@ __device__ void finish_reduction(const ForceArgs& A, double red[3], int nred) {
 }
 
 template <int DIM, int EPI>
-__global__ void __launch_bounds__(kForceBlock) k_bond_force(const ForceArgs A) {
+__global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const KParams& P = A.P;
     double red[3] = {0.0, 0.0, 0.0};
-    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
-         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+    // warp -> slice mapping: strided over the grid, or one contiguous run of
+    // slices per warp (the autotuner chooses; the per-lane sums are the same)
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    int64_t s_begin = w, s_end = A.nslices, s_step = nwarps;
+    if (A.chunked) {
+        const int64_t per = (A.nslices + nwarps - 1) / nwarps;
+        s_begin = w * per;
+        s_end = s_begin + per < A.nslices ? s_begin + per : A.nslices;
+        s_step = 1;
+    }
+    for (int64_t s = s_begin; s < s_end; s += s_step) {
         const int64_t r = s * 32 + lane;
         const bool force_row = r < A.nforce;
         if (s * 32 < A.nforce) {
@@ -433,10 +466,11 @@ __global__ void __launch_bounds__(kForceBlock) k_bond_force(const ForceArgs A) {
                 if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
             }
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+            if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
     }
-    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 2);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -684,6 +718,8 @@ static ForceArgs make_args(pd_ctx* c) {
     A.partials = c->partials;
     A.ticket = c->ticket;
     A.cn_out = c->cn;
+    A.node_mass = c->batch.node_mass;
+    A.slice_part = c->batch.slice_part;
     return A;
 }
 
@@ -691,12 +727,13 @@ static ForceArgs make_args(pd_ctx* c) {
 // the occupancy of this kernel instance x SM count), so the grid-stride loop
 // over slices runs in one wave with no tail; never more blocks than slices
 // need, nor more than the partial-sum buffer holds.
-static unsigned resident_grid(pd_ctx* c, const void* kernel, int64_t nslices) {
+static unsigned resident_grid(pd_ctx* c, const void* kernel, int64_t nslices, int block = kForceBlock,
+                              int waves = 1) {
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kForceBlock, 0) != cudaSuccess || per_sm < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    const int64_t want = (nslices + kWarpsPerBlock - 1) / kWarpsPerBlock;
-    const int64_t cap = (int64_t)c->num_sms * per_sm;
+    const int64_t want = (nslices + block / 32 - 1) / (block / 32);
+    const int64_t cap = (int64_t)c->num_sms * per_sm * waves;
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(want, cap), kMaxPartials));
 }
 
@@ -741,8 +778,12 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         if (f.contact && !f.do_next) c->pos_valid = false;
         return cuda_err(c, cudaGetLastError(), "node post");
     }
+    const bool bond = !state;
+    const int blk = bond ? c->tune_block : kForceBlock;
+    const int waves = bond ? c->tune_waves : 1;
+    A.chunked = bond ? c->tune_chunked : 0;
 #define PD_LAUNCH(KER, D, E) \
-    KER<D, E><<<resident_grid(c, (const void*)KER<D, E>, A.nslices), kForceBlock, 0, s>>>(A)
+    KER<D, E><<<resident_grid(c, (const void*)KER<D, E>, A.nslices, blk, waves), blk, 0, s>>>(A)
 #define PD_DISPATCH(KER)                                  \
     do {                                                  \
         if (!d3) {                                        \

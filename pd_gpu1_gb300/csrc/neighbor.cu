@@ -94,13 +94,22 @@ __device__ __forceinline__ void cell_of(const Grid& g, int dim, double x, double
     }
 }
 
+// Grouped 2-D builds (a batch of specimens sharing one coordinate frame):
+// the third cell axis is the node's group, so a node only visits cells of its
+// own group; padding nodes (group -1) sit in a layer of their own past the
+// last group and have no family.
+__device__ __forceinline__ void group_cell(const Grid& g, const int* __restrict__ grp, int64_t i, int64_t* c) {
+    if (grp) c[2] = grp[i] >= 0 ? grp[i] : g.nc[2] - 1;
+}
+
 __global__ void k_cell_count(const double* __restrict__ x, const double* __restrict__ y,
-                             const double* __restrict__ z, int64_t n, int dim, Grid g, int64_t* __restrict__ key,
-                             int* __restrict__ count) {
+                             const double* __restrict__ z, const int* __restrict__ grp, int64_t n, int dim, Grid g,
+                             int64_t* __restrict__ key, int* __restrict__ count) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     int64_t c[3];
     cell_of(g, dim, x[i], y[i], dim == 3 ? z[i] : 0.0, c);
+    group_cell(g, grp, i, c);
     const int64_t k = cell_key(g, dim, c[0], c[1], c[2]);
     key[i] = k;
     atomicAdd(&count[k], 1);
@@ -130,13 +139,19 @@ __device__ __forceinline__ bool in_family(const double* __restrict__ x, const do
 // One thread per node; FILL=false counts the row, FILL=true writes it.
 template <bool FILL>
 __global__ void k_family(const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
-                         int64_t n, int dim, Grid g, double delta2, const int64_t* __restrict__ start,
-                         const int* __restrict__ count, const int* __restrict__ order, int* __restrict__ NN,
-                         const int64_t* __restrict__ rowptr, int* __restrict__ NL) {
+                         const int* __restrict__ grp, int64_t n, int dim, Grid g, double delta2,
+                         const int64_t* __restrict__ start, const int* __restrict__ count,
+                         const int* __restrict__ order, int* __restrict__ NN, const int64_t* __restrict__ rowptr,
+                         int* __restrict__ NL) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (grp && grp[i] < 0) {
+        if (!FILL) NN[i] = 0;
+        return;
+    }
     int64_t c[3];
     cell_of(g, dim, x[i], y[i], dim == 3 ? z[i] : 0.0, c);
+    group_cell(g, grp, i, c);
     int cnt = 0;
     int64_t out = FILL ? rowptr[i] : 0;
     const int64_t z0 = dim == 3 ? -1 : 0, z1 = dim == 3 ? 1 : 0;
@@ -221,6 +236,8 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     double* X = c->nf[PD_F_X];
     double* Y = c->nf[PD_F_Y];
     double* Z = c->nf[PD_F_Z];
+    const int* grp = c->batch.node_group;
+    if (grp && dim != 2) return set_err(c, PD_ERR_ARG, "grouped family builds are 2-D");
     cudaError_t e;
 
     // bounding box
@@ -246,6 +263,7 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     for (int a = 0; a < 3; a++) {
         g.lo[a] = a < dim ? lo[a] : 0.0;
         g.nc[a] = a < dim ? (int64_t)std::floor((hi[a] - lo[a]) / h) + 1 : 1;
+        if (a == 2 && grp) g.nc[2] = c->batch.count + 1;  // groups, then the padding layer
         ncell *= g.nc[a];
         int b = 0;
         while ((int64_t(1) << b) < g.nc[a]) b++;
@@ -254,7 +272,7 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     if (ncell > (int64_t(1) << 31)) return set_err(c, PD_ERR_ARG, "domain too large for the cell grid");
     // Morton keys when their padded range stays small, row-major otherwise
     const int64_t mrange = int64_t(1) << (maxbits * dim);
-    g.morton = (maxbits * dim <= 30 && mrange <= 8 * ncell + 1024) ? 1 : 0;
+    g.morton = (!grp && maxbits * dim <= 30 && mrange <= 8 * ncell + 1024) ? 1 : 0;
     g.bits = maxbits;
     const int64_t nkeys = g.morton ? mrange : ncell;
 
@@ -286,7 +304,7 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     cudaMemsetAsync(dmax, 0, sizeof(int), s);
     const int T = 256;
     const unsigned gN = (unsigned)((N + T - 1) / T);
-    k_cell_count<<<gN, T, 0, s>>>(X, Y, Z, N, dim, g, key, count);
+    k_cell_count<<<gN, T, 0, s>>>(X, Y, Z, grp, N, dim, g, key, count);
     c->launches++;
     int rc = scan_counts(c, count, start, nkeys, s);
     if (rc) {
@@ -297,7 +315,7 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     c->launches++;
 
     const double delta2 = p.delta * p.delta;
-    k_family<false><<<gN, T, 0, s>>>(X, Y, Z, N, dim, g, delta2, start, count, order, c->NN, nullptr, nullptr);
+    k_family<false><<<gN, T, 0, s>>>(X, Y, Z, grp, N, dim, g, delta2, start, count, order, c->NN, nullptr, nullptr);
     c->launches++;
     rc = scan_counts(c, c->NN, c->rowptr, N, s);
     if (rc) {
@@ -333,7 +351,7 @@ int build_family(pd_ctx* c, cudaStream_t s) {
         return set_err(c, PD_ERR_NOMEM, "bond array allocation failed");
     }
     c->B = B;
-    k_family<true><<<gN, T, 0, s>>>(X, Y, Z, N, dim, g, delta2, start, count, order, nullptr, c->rowptr, c->NL);
+    k_family<true><<<gN, T, 0, s>>>(X, Y, Z, grp, N, dim, g, delta2, start, count, order, nullptr, c->rowptr, c->NL);
     k_row_sort<<<gN, T, 0, s>>>(N, c->rowptr, c->NL);
     cudaMemsetAsync(c->idist, 0, nb8, s);
     cudaMemsetAsync(c->fac, 0, nb8, s);

@@ -67,6 +67,23 @@ struct Sell {
 
 }  // namespace pdg
 
+// A batch of specimens packed into one context (see batch.cu).
+struct BatchInfo {
+    int count = 0;                     // number of specimens (0: not a batch)
+    int* node_group = nullptr;         // [N] specimen of each node (-1: padding row, no family)
+    double* node_bc = nullptr;         // [N] micro-modulus constant of the node's specimen
+    double* node_sed = nullptr;        // [N] surface-correction energy density of the node's specimen
+    double* node_s0 = nullptr;         // [N] critical stretch of the node's specimen
+    double* node_mass = nullptr;       // [N] ADR fictitious mass per node
+    double* load_sign = nullptr;       // [N] signed load factor of moving boundary rows, 0 elsewhere
+    int* slice_inst = nullptr;         // [nslices] specimen of each slice (-1: none)
+    int64_t* inst_slices = nullptr;    // [count + 1] first slice of each specimen's interior
+    double* slice_part = nullptr;      // [2 * nslices] per-slice damping sums
+    double* inst_cn = nullptr;         // [count] damping coefficient per specimen
+    std::vector<int64_t> h_inst_nodes; // host: interior node offset of each specimen (+ total)
+    std::vector<int64_t> h_inst_bnd;   // host: boundary node offset of each specimen (+ total)
+};
+
 struct GraphEntry {
     int kind, nsteps, parity, flags;
     double load;
@@ -115,6 +132,11 @@ struct pd_ctx {
     bool csr_fail_current = true; // CSR fail array is current
 
     std::vector<GraphEntry> graphs;
+    BatchInfo batch;
+    // launch shape of the bond-force kernel (pd_autotune may change it)
+    int tune_block = 256;   // threads per block: 128, 256 or 512
+    int tune_waves = 1;     // grid = resident blocks x waves
+    int tune_chunked = 0;   // 1: contiguous slice runs per warp
 };
 
 namespace pdg {
@@ -156,6 +178,9 @@ int vol_corr(pd_ctx* c, cudaStream_t s);
 int surface_correct(pd_ctx* c, cudaStream_t s);
 int initial_weight(pd_ctx* c, cudaStream_t s);
 int set_crack_2d(pd_ctx* c, double clength, double lx, double ly, double theta, cudaStream_t s);
+// the same segment test on rows [r0, r1) only
+int set_crack_2d_rows(pd_ctx* c, int64_t r0, int64_t r1, double clength, double lx, double ly, double theta,
+                      cudaStream_t s);
 int set_crack_kw(pd_ctx* c, double rad, cudaStream_t s);
 int prepare(pd_ctx* c, cudaStream_t s);
 int sync_fail_to_csr(pd_ctx* c, cudaStream_t s);
@@ -188,5 +213,9 @@ int launch_cyl_integrate(pd_ctx* c, int half, cudaStream_t s);
 int reduce_sum(pd_ctx* c, const double* x, int64_t n, double* out_dev, cudaStream_t s);
 int check_finite(pd_ctx* c, cudaStream_t s, int* bad_host);
 int fp64_probe(double* gfma_per_s);
+// batch.cu
+void release_batch(pd_ctx* c);
+int batch_prologue(pd_ctx* c, double load, cudaStream_t s);
+int batch_step(pd_ctx* c, int ct, int last, double load, cudaStream_t s);
 
 }  // namespace pdg

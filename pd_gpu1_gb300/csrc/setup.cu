@@ -62,8 +62,10 @@ __global__ void k_vol_corr(KParams P, const double* __restrict__ x, const double
 
 // Strain energy density of node i under the test fields u_a = 0.001 x_a
 // (kernel_Disp + kernel_surface_F/_3D, Surf_Corr.cu:38-158), all axes in one
-// pass; fncst_a = sedload / energy.
-__global__ void k_surface_energy(KParams P, double sedload, const double* __restrict__ x,
+// pass; fncst_a = sedload / energy.  A batch of specimens passes bc and
+// sedload per node (its specimen's values); bonds never cross specimens.
+__global__ void k_surface_energy(KParams P, double sedload, const double* __restrict__ node_bc,
+                                 const double* __restrict__ node_sed, const double* __restrict__ x,
                                  const double* __restrict__ y, const double* __restrict__ z,
                                  const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
                                  const double* __restrict__ idist, const double* __restrict__ fac,
@@ -71,6 +73,10 @@ __global__ void k_surface_energy(KParams P, double sedload, const double* __rest
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= P.N) return;
+    if (node_bc) {
+        P.bc = node_bc[i];
+        sedload = node_sed[i];
+    }
     const int dim = P.dim;
     double st[3] = {0.0, 0.0, 0.0};
     const double xi = x[i], yi = y[i], zi = dim == 3 ? z[i] : 0.0;
@@ -175,14 +181,15 @@ __global__ void k_weight(KParams P, const int64_t* __restrict__ rowptr, const do
     if (lane == 0) m[i] = acc;
 }
 
-// Pre-crack segment test (Base_Function.cu:39-81) on nodes [0, N_int).
-__global__ void k_set_crack_2d(KParams P, double clength, double lx, double ly, double theta,
-                               const double* __restrict__ x, const double* __restrict__ y,
+// Pre-crack segment test (Base_Function.cu:39-81) on nodes [r0, r1)
+// (the reference tests [0, N_int); a batch cracks one specimen at a time).
+__global__ void k_set_crack_2d(KParams P, int64_t r0, int64_t r1, double clength, double lx, double ly,
+                               double theta, const double* __restrict__ x, const double* __restrict__ y,
                                const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
                                int* __restrict__ fail) {
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int64_t i = r0 + ((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (i >= P.N_int) return;
+    if (i >= r1) return;
     for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
         const int64_t c = NL[q];
         if (fabs(theta - P.pi / 2.0) < 0.0001) {
@@ -240,7 +247,7 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                             const double* __restrict__ x, const double* __restrict__ y, const double* __restrict__ z,
                             const double* __restrict__ idist, const double* __restrict__ fac,
                             const double* __restrict__ scr, const double* __restrict__ w, const double* __restrict__ m,
-                            Sell S) {
+                            const double* __restrict__ node_bc, const double* __restrict__ node_s0, Sell S) {
     const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
     if (s >= nslices) return;
     const int W = width[s];
@@ -277,9 +284,12 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         // kernels break only bonds whose ends both have y >= -0.04 (Force_Bond.cu:117)
         bool breakable = true;
         if (P.dim == 3) breakable = y[r] >= P.break_ymin && y[c] >= P.break_ymin;
-        S.ecrit[slot] = breakable ? P.critical_s * L0 : HUGE_VAL;
+        // a batch of specimens carries bc and s0 per node (the row's specimen)
+        const double s0 = node_s0 ? node_s0[r] : P.critical_s;
+        const double bc = node_bc ? node_bc[r] : P.bc;
+        S.ecrit[slot] = breakable ? s0 * L0 : HUGE_VAL;
         if (S.k2) {
-            const double k2 = 2.0 * (P.vol * fac[q] * P.bc * scr[q]) / L0;
+            const double k2 = 2.0 * (P.vol * fac[q] * bc * scr[q]) / L0;
             S.k2[slot] = k2;
             const ff kf = ff_split(k2 * S.kscale_inv);
             S.k2f[slot] = make_float2(kf.h, kf.l);
@@ -373,7 +383,8 @@ int surface_correct(pd_ctx* c, cudaStream_t s) {
     const KParams P = kparams(c->p);
     const double sedload = P.dim == 3 ? 0.6 * P.emod * 1.0e-6 : 0.5 * P.emod / (1.0 - P.pratio * P.pratio) * 1.0e-6;
     double *X = c->nf[PD_F_X], *Y = c->nf[PD_F_Y], *Z = c->nf[PD_F_Z];
-    k_surface_energy<<<warps_grid(P.N), 256, 0, s>>>(P, sedload, X, Y, Z, c->rowptr, c->NL, c->idist, c->fac,
+    k_surface_energy<<<warps_grid(P.N), 256, 0, s>>>(P, sedload, c->batch.node_bc, c->batch.node_sed, X, Y, Z,
+                                                      c->rowptr, c->NL, c->idist, c->fac,
                                                       c->nf[PD_F_FNCST_X], c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z]);
     k_surface_coeff<<<warps_grid(P.N), 256, 0, s>>>(P, X, Y, Z, c->rowptr, c->NL, c->idist, c->nf[PD_F_FNCST_X],
                                                      c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z], c->scr);
@@ -416,16 +427,23 @@ int sync_fail_to_bits(pd_ctx* c, cudaStream_t s) {
     return cuda_err(c, cudaGetLastError(), "fail flags to bits");
 }
 
-int set_crack_2d(pd_ctx* c, double clength, double lx, double ly, double theta, cudaStream_t s) {
+int set_crack_2d_rows(pd_ctx* c, int64_t r0, int64_t r1, double clength, double lx, double ly, double theta,
+                      cudaStream_t s) {
     if (!c->family) return set_err(c, PD_ERR_STATE, "set_crack needs the bond family");
+    if (r0 < 0 || r1 > c->p.N || r0 > r1) return set_err(c, PD_ERR_ARG, "set_crack row range out of bounds");
+    if (r0 == r1) return PD_OK;
     int rc = sync_fail_to_csr(c, s);
     if (rc) return rc;
     const KParams P = kparams(c->p);
-    k_set_crack_2d<<<warps_grid(P.N_int), 256, 0, s>>>(P, clength, lx, ly, theta, c->nf[PD_F_X], c->nf[PD_F_Y],
-                                                        c->rowptr, c->NL, c->fail);
+    k_set_crack_2d<<<warps_grid(r1 - r0), 256, 0, s>>>(P, r0, r1, clength, lx, ly, theta, c->nf[PD_F_X],
+                                                        c->nf[PD_F_Y], c->rowptr, c->NL, c->fail);
     c->launches++;
     c->bits_current = false;
     return cuda_err(c, cudaGetLastError(), "set_crack_2d");
+}
+
+int set_crack_2d(pd_ctx* c, double clength, double lx, double ly, double theta, cudaStream_t s) {
+    return set_crack_2d_rows(c, 0, c->p.N_int, clength, lx, ly, theta, s);
 }
 
 int set_crack_kw(pd_ctx* c, double rad, cudaStream_t s) {
@@ -524,7 +542,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     const unsigned gy = (unsigned)((S.nslices + gx - 1) / gx);
     k_sell_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, c->NN, c->rowptr, c->NL, c->nf[PD_F_X],
                                               c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac, c->scr, c->w,
-                                              c->nf[PD_F_M], S);
+                                              c->nf[PD_F_M], c->batch.node_bc, c->batch.node_s0, S);
     c->launches++;
     if (state) {
         k_inv_m<<<(unsigned)((P.N + 255) / 256), 256, 0, s>>>(P.N, c->nf[PD_F_M], c->node_b);

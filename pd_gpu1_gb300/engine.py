@@ -13,10 +13,10 @@ import ctypes as C
 
 import numpy as np
 
-from ._abi import FIELD, FIELD_DTYPE, PDCylinder, PDParams, PDResult
+from ._abi import FIELD, FIELD_DTYPE, PDCylinder, PDParams, PDResult, PDSpecimen
 from ._lib import PDError, check, lib
 
-__all__ = ["Engine", "derive_params", "coord_kw", "solve_plate_tensile", "solve_plate_crack_grow",
+__all__ = ["Engine", "Batch", "derive_params", "coord_kw", "solve_plate_tensile", "solve_plate_crack_grow",
            "solve_kalthoff_winkler", "PDError"]
 
 
@@ -233,10 +233,86 @@ class Engine:
     def check_finite(self):
         self._c(self._lib.pd_check_finite(self.ctx, self.stream), "pd_check_finite")
 
+    # ---- launch shape of the bond-force kernel ------------------------------
+    def set_launch(self, block=256, chunked=0, waves=1):
+        self._c(self._lib.pd_set_launch(self.ctx, block, chunked, waves), "pd_set_launch")
+
+    def launch(self):
+        b, k, w = C.c_int(), C.c_int(), C.c_int()
+        self._c(self._lib.pd_get_launch(self.ctx, C.byref(b), C.byref(k), C.byref(w)), "pd_get_launch")
+        return b.value, k.value, w.value
+
+    def autotune(self, reps=5):
+        """Times the 18 launch shapes at the current state and keeps the
+        fastest; returns (block, chunked, waves, ms per launch)."""
+        ms = C.c_double()
+        self._c(self._lib.pd_autotune(self.ctx, reps, C.byref(ms), self.stream), "pd_autotune")
+        return self.launch() + (ms.value,)
+
     # ---- views -------------------------------------------------------------
     def csr(self):
         """(rowptr, NL) of the bond family."""
         return self.get("ROWPTR"), self.get("NL")
+
+
+class Batch(Engine):
+    """Many 2-D bond-based plates in one context (``pd_batch_create``).
+
+    ``specimens`` is a sequence of dicts (or :class:`PDSpecimen`) with keys
+    nx, ny, emod, critical_s and optionally crack_len, crack_theta,
+    load_scale; ``base`` carries the shared parameters (dx, dt, thickness,
+    Poisson ratio, horizon, MN)."""
+
+    def __init__(self, base, specimens, stream=None):
+        self._lib = lib()
+        n = len(specimens)
+        arr = (PDSpecimen * n)()
+        for k, sp in enumerate(specimens):
+            if isinstance(sp, PDSpecimen):
+                arr[k] = sp
+                continue
+            a = arr[k]
+            a.nx, a.ny = int(sp["nx"]), int(sp["ny"])
+            a.emod, a.critical_s = float(sp["emod"]), float(sp["critical_s"])
+            a.crack_len = float(sp.get("crack_len", 0.0))
+            a.crack_theta = float(sp.get("crack_theta", 0.0))
+            a.load_scale = float(sp.get("load_scale", 1.0))
+        self.specimens = arr
+        st = C.c_int(0)
+        b = base.copy()
+        self.ctx = self._lib.pd_batch_create(C.byref(b), arr, n, C.byref(st))
+        if not self.ctx:
+            check(st.value, None, "pd_batch_create")
+        self.stream = _stream(stream)
+        self.p = self.params()
+        cnt = C.c_int()
+        self.interior = np.zeros(n + 1, dtype=np.int64)
+        self.boundary = np.zeros(n + 1, dtype=np.int64)
+        self._c(self._lib.pd_batch_info(self.ctx, C.byref(cnt), self.interior.ctypes.data_as(C.POINTER(C.c_int64)),
+                                        self.boundary.ctypes.data_as(C.POINTER(C.c_int64))), "pd_batch_info")
+        self.count = cnt.value
+
+    def run_adr(self, ct0, nsteps, load=0.0):
+        self._c(self._lib.pd_batch_run_adr(self.ctx, ct0, nsteps, load, self.stream), "pd_batch_run_adr")
+
+    def cn(self):
+        out = np.zeros(self.count)
+        self._c(self._lib.pd_batch_get_cn(self.ctx, out.ctypes.data_as(C.POINTER(C.c_double)), self.stream),
+                "pd_batch_get_cn")
+        return out
+
+    def rows(self, k):
+        """Node indices of specimen k in the standalone order: interior rows,
+        then its 6 nx boundary rows."""
+        sp = self.specimens[k]
+        a = np.arange(self.interior[k], self.interior[k] + sp.nx * sp.ny)
+        b = self.p.N_int + np.arange(self.boundary[k], self.boundary[k + 1])
+        return np.concatenate([a, b])
+
+    def specimen_field(self, name, k, values=None):
+        """Field ``name`` of specimen k (node fields), in standalone order."""
+        v = self.get(name) if values is None else values
+        return v[self.rows(k)]
 
 
 def solve_plate_tensile(dx=0.0, nt=1000):

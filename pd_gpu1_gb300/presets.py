@@ -176,3 +176,62 @@ def build_crack_grow(scale=1.0, dx=1e-4, nt=1250, derive=None):
         eng.prepare()
 
     return p, setup, dict(load=20.0, nt=nt, workload="plate_crack_grow_2d_state_verlet")
+
+
+# ---- batch of uneven plates, 2-D PMB, ADR (256 specimens x 1000 steps) -------------
+def batch_specimens(count=256, seed=20240607, dx=5e-4, side=(50, 300), max_nodes=None):
+    """Seeded specimen table: side ~ log-uniform[50, 300] nodes (square
+    plates), E ~ U[70, 210] GPa, rho ~ U[2400, 8000] (drawn for the record;
+    ADR uses its fictitious mass, not rho), G0 ~ U[4, 22000] J/m^2 -> s0 by
+    the 2-D closed form, centred pre-crack of length U[0, 0.3] x width at an
+    angle U[0, 90) degrees.  ``max_nodes`` caps the side (quick tests)."""
+    rng = np.random.default_rng(seed)
+    delta = 3.015 * dx
+    out = []
+    for _ in range(count):
+        n = int(round(math.exp(rng.uniform(math.log(side[0]), math.log(side[1])))))
+        if max_nodes:
+            n = min(n, max_nodes)
+        E = rng.uniform(70.0e9, 210.0e9)
+        rho = rng.uniform(2400.0, 8000.0)
+        G0 = rng.uniform(4.0, 22000.0)
+        frac = rng.uniform(0.0, 0.3)
+        theta = rng.uniform(0.0, math.pi / 2.0)
+        out.append(dict(nx=n, ny=n, emod=E, dens=rho, G0=G0, critical_s=s0_2d(G0, E, delta),
+                        crack_len=frac * n * dx, crack_theta=theta, load_scale=1.0))
+    return out
+
+
+def build_batch(count=256, seed=20240607, dx=5e-4, nt=1000, derive=None, max_nodes=None):
+    """The plate-tensile ADR pipeline on a seeded batch of uneven plates
+    (batch_specimens): shared dx = 5e-4, thickness dx, nu = 1/3, ADR dt = 1,
+    boundary rows moving +-2.7e-8 m per step.  Returns (base params,
+    specimens, meta)."""
+    base = _derive(derive)(2, PD_MODEL_BOND, PD_MODE_STATIC, 1.0, nt, dx, 0.0, dx, 0.05, 0.05, 0.0, 192.0e9,
+                           1.0 / 3.0, 8000.0, 0.04472)
+    specs = batch_specimens(count, seed, dx, max_nodes=max_nodes)
+    return base, specs, dict(load=2.7e-8 / base.dt, nt=nt, workload="batch_plate_adr_2d_pmb", seed=seed,
+                             count=count)
+
+
+def build_specimen(base, sp, derive=None):
+    """One batch specimen set up alone, as the batch sets it up: the plate
+    of the crack-plate layout with the specimen's size, modulus, s0 and
+    pre-crack.  Returns (params, setup)."""
+    nx, ny = int(sp["nx"]), int(sp["ny"])
+    p = _derive(derive)(2, PD_MODEL_BOND, base.mode, base.dt, base.nt, base.dx, base.load, base.thick, nx * base.dx,
+                        ny * base.dx, 0.0, float(sp["emod"]), base.pratio, base.dens, float(sp["critical_s"]))
+    p.nx, p.ny = nx, ny
+    p.N_int = nx * ny
+    p.N = p.N_int + 6 * nx
+
+    def setup(eng):
+        eng.coord_plate_crack()
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
+        if sp.get("crack_len", 0.0) > 0.0:
+            eng.set_crack_2d(float(sp["crack_len"]), 0.0, 0.0, float(sp.get("crack_theta", 0.0)))
+        eng.prepare()
+
+    return p, setup

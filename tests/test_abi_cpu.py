@@ -3,6 +3,7 @@ entry point include/pd.h declares, and its host-only entry points (parameter
 derivation, notched-slab coordinates) agree bit for bit with the oracle and
 the reference's derivation recorded in the golden fixtures."""
 import ctypes as C
+import math
 import os
 import re
 
@@ -88,15 +89,39 @@ def test_full_size_kalthoff_winkler_node_count():
     assert len(x) == 180873
 
 
-def test_abi_struct_layout_matches_header():
-    """The ctypes mirror of pd_params has the C layout (field order and offsets)."""
-    from pd_gpu1_gb300._abi import PDParams
-
+def _header_fields(struct):
     txt = open(os.path.join(ROOT, "include", "pd.h")).read()
-    body = txt[txt.index("typedef struct pd_params {"): txt.index("} pd_params;")]
+    body = txt[txt.index(f"typedef struct {struct} {{"): txt.index(f"}} {struct};")]
     body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
     names = []
     for decl in re.findall(r"(?:double|int32_t)\s+([^;]+);", body):
         names += [n.strip() for n in decl.split(",")]
-    assert names == [f for f, _ in PDParams._fields_]
+    return names
+
+
+def test_abi_struct_layout_matches_header():
+    """The ctypes mirrors of pd_params and pd_specimen have the C layout
+    (field order; all members naturally aligned, no padding)."""
+    from pd_gpu1_gb300._abi import PDParams, PDSpecimen
+
+    assert _header_fields("pd_params") == [f for f, _ in PDParams._fields_]
     assert C.sizeof(PDParams) % 8 == 0
+    assert _header_fields("pd_specimen") == [f for f, _ in PDSpecimen._fields_]
+    assert C.sizeof(PDSpecimen) == 2 * 4 + 5 * 8
+
+
+def test_batch_specimen_table_is_seeded():
+    """The batch workload: 256 seeded specimens of about 6.25M interior nodes,
+    s0 from G0 by the 2-D closed form, cracks within 30 % of the width."""
+    from pd_gpu1_gb300 import presets
+
+    a = presets.batch_specimens()
+    b = presets.batch_specimens()
+    assert a == b and len(a) == 256
+    n = sum(s["nx"] * s["ny"] for s in a)
+    assert 5.5e6 < n < 7.0e6
+    for s in a:
+        assert 50 <= s["nx"] <= 300 and s["nx"] == s["ny"]
+        assert 70e9 <= s["emod"] <= 210e9 and 2400 <= s["dens"] <= 8000
+        assert s["critical_s"] == presets.s0_2d(s["G0"], s["emod"], 3.015 * 5e-4)
+        assert 0.0 <= s["crack_len"] <= 0.3 * s["nx"] * 5e-4 and 0.0 <= s["crack_theta"] < math.pi / 2
