@@ -396,9 +396,11 @@ def batch_arm(args):
     value = work / secs_max
     broken = float((bat.get("FAIL") == 0).mean())
 
-    # force kernel alone (ADR epilogue with per-slice damping sums), timed by the
-    # autotuner with CUDA events on the launch stream: its best shape is the one used
-    kern_ms = tuned[3]
+    # the force kernel (ADR epilogue with per-slice damping sums) inside the
+    # step loop: CUDA events on the launch stream around each step's launch
+    with torch.cuda.stream(stream):
+        kern_ms, step_ms = bat.profile_steps(0, args.warmup + args.steps, min(50, args.steps), load)
+    torch.cuda.synchronize()
     alg_bytes = ALG_BYTES_PER_NODE_2D_ADR * p.N_int + ALG_BYTES_PER_BOND_2D * B
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
@@ -503,7 +505,9 @@ def batch_arm(args):
                        "setup_s": setup_s, "broken_bond_fraction": broken},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
-                         "kernel": "k_bond_force<2, ADR>", "kernel_ms": kern_ms, "alg_bytes_per_launch": alg_bytes,
+                         "kernel": "k_bond_force<2, ADR>", "kernel_ms": kern_ms,
+                         "kernel_share_of_step": kern_ms / step_ms, "autotune_ms": tuned[3],
+                         "alg_bytes_per_launch": alg_bytes,
                          "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
                                   "frac": alg_flops / (kern_ms * 1e-3) / 1e12 / fp64_peak,
                                   "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},
@@ -569,22 +573,13 @@ def gb300_arm(args):
     ms_max = secs_max * 1e3
     value = work / secs_max
 
-    # dominant kernel alone: a graph of force launches only (no damage pass)
+    # the dominant kernel inside the step loop: CUDA events on the launch stream
+    # around every step's force launch(es), over further real steps
     kern_steps = min(100, max(10, args.steps))
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    kind = 0 if meta["workload"].startswith("plate_tensile") else 1
     with torch.cuda.stream(stream):
-        if meta["workload"].startswith("plate_tensile"):
-            eng.run_adr(1, kern_steps, load=meta["load"])
-            e0.record(stream)
-            eng.run_adr(1, kern_steps, load=meta["load"])
-            e1.record(stream)
-        else:
-            eng.run_explicit(kern_steps, load=meta["load"], dmg_every=0)
-            e0.record(stream)
-            eng.run_explicit(kern_steps, load=meta["load"], dmg_every=0)
-            e1.record(stream)
+        kern_ms, step_ms = eng.profile_steps(kind, args.warmup + args.steps, kern_steps, meta["load"])
     torch.cuda.synchronize()
-    kern_ms = e0.elapsed_time(e1) / kern_steps
     state = p.model == 2
     if state:  # dilatation + force passes (SURVEY's 3-D state-based model; 2-D by the same count)
         alg_bytes = (88.0 if is3d else 64.0) * p.N_int + 16.125 * B
@@ -684,7 +679,8 @@ def gb300_arm(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_bond_force" if p.model == 1 else "k_theta + k_state_force",
-                         "kernel_ms": kern_ms, "alg_bytes_per_launch": alg_bytes,
+                         "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / step_ms,
+                         "alg_bytes_per_launch": alg_bytes,
                          "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
                                   "peak_tflops": fp64_peak_tflops, "frac": alg_flops / (kern_ms * 1e-3) / 1e12 /
                                   fp64_peak_tflops, "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},

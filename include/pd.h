@@ -282,6 +282,16 @@ int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves);
  * run continues exactly as without the call.  Bond-based contexts only. */
 int pd_autotune(pd_ctx* ctx, int reps, double* best_ms, void* stream);
 
+/* ---- step profile --------------------------------------------------------- */
+/* Runs nsteps steps of the ADR loop (kind 0: pd_run_adr, or pd_batch_run_adr
+ * on a batch) or of the explicit loop (kind 1: pd_run_explicit without
+ * damage passes) starting at step index ct0, launched directly rather than
+ * from graphs, with CUDA events on the launch stream around each step's
+ * force kernel(s) and around each whole step.  *force_ms and *step_ms receive
+ * the averages per step.  The state advances as in those loops. */
+int pd_profile_steps(pd_ctx* ctx, int kind, int ct0, int nsteps, double load, double* force_ms, double* step_ms,
+                     void* stream);
+
 /* ---- drivers (Solve_*.cuh:17-19) --------------------------------------- */
 typedef struct pd_result {
     int64_t N, N_int, B;
@@ -298,6 +308,35 @@ int pd_solve_plate_crack_grow(double dx, int nt, double* ux, double* uy, double*
  * runs nt=0 steps, this takes nt. Arrays hold N entries (see res->N). */
 int pd_solve_kalthoff_winkler(double dx, int nt, double* ux, double* uy, double* uz, double* dmg,
                               int64_t cap, pd_result* res);
+
+/* ---- output ------------------------------------------------------------ */
+/* save_disp_gpu / save_disp_cpu (Save.cu:6-60): one line per interior node,
+ * "ux uy dmg" (uz == NULL) or "ux uy uz dmg", each value as std::ostream
+ * prints a double by default (%g, 6 significant digits). */
+int pd_write_disp_txt(const char* path, int64_t n, const double* ux, const double* uy, const double* uz,
+                      const double* dmg);
+/* save_kw_gpu / save_kw_cpu (Save.cu:62-140): the first z layer of the
+ * notched slab in grid order (p->nx x p->ny), notch cells of the upper half
+ * written as "nan nan 0 nan"; n is the number of node values available. */
+int pd_write_kw_txt(const char* path, const pd_params* p, double rad, int64_t n, const double* ux,
+                    const double* uy, const double* uz, const double* dmg);
+/* The same writers fed from a context (its N_int interior nodes). */
+int pd_save_disp(pd_ctx* ctx, const char* path, void* stream);
+int pd_save_kw(pd_ctx* ctx, double rad, const char* path, void* stream);
+/* Binary snapshot of the simulation state: displacement, velocity,
+ * acceleration, force, body force, ADR half-step velocity and old force, damage
+ * and dilatation (N doubles per component), the intact flags (B int32), the ADR
+ * damping coefficient and the impactor.  No reference counterpart (its output
+ * is text only).  Loading needs a context with the same set-up (N, N_int, B,
+ * dim, model); a run continued from a loaded snapshot repeats the saved run
+ * bit for bit. */
+int pd_snapshot_save(pd_ctx* ctx, const char* path, void* stream);
+int pd_snapshot_load(pd_ctx* ctx, const char* path, void* stream);
+/* Crack tip from the damage field: the interior node with the largest x among
+ * those with dmg > threshold (lowest index among ties); tip_xy receives its
+ * reference coordinates, NaN when no node is damaged.  The reference's tracker
+ * (commented out, Solve_Plate_Crack_Grow.cu:150-162) scans one row for dmg > 0.38. */
+int pd_crack_tip(pd_ctx* ctx, double threshold, double* tip_xy, void* stream);
 
 /* ---- diagnostics ------------------------------------------------------- */
 /* NaN/Inf scan of displacement and force; PD_ERR_NONFINITE if any. */

@@ -69,9 +69,17 @@ _SIGS = {
     "pd_set_launch": (I32, [VP, I32, I32, I32]),
     "pd_get_launch": (I32, [VP, P(I32), P(I32), P(I32)]),
     "pd_autotune": (I32, [VP, I32, P(D), VP]),
+    "pd_profile_steps": (I32, [VP, I32, I32, I32, D, P(D), P(D), VP]),
     "pd_solve_plate_tensile": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),
     "pd_solve_plate_crack_grow": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),
     "pd_solve_kalthoff_winkler": (I32, [D, I32, P(D), P(D), P(D), P(D), I64, P(PDResult)]),
+    "pd_write_disp_txt": (I32, [C.c_char_p, I64, VP, VP, VP, VP]),
+    "pd_write_kw_txt": (I32, [C.c_char_p, P(PDParams), D, I64, VP, VP, VP, VP]),
+    "pd_save_disp": (I32, [VP, C.c_char_p, VP]),
+    "pd_save_kw": (I32, [VP, D, C.c_char_p, VP]),
+    "pd_snapshot_save": (I32, [VP, C.c_char_p, VP]),
+    "pd_snapshot_load": (I32, [VP, C.c_char_p, VP]),
+    "pd_crack_tip": (I32, [VP, D, P(D), VP]),
     "pd_check_finite": (I32, [VP, VP]),
     "pd_kernel_launches": (I64, [VP]),
     "pd_probe_fp64": (I32, [P(D)]),

@@ -25,6 +25,7 @@ UNITS = {
     "api.cu": [],
     "noalloc.cu": [],
     "batch.cu": [],
+    "output.cu": [],
 }
 
 

@@ -170,11 +170,13 @@ int batch_prologue(pd_ctx* c, double load, cudaStream_t s) {
     return cuda_err(c, cudaGetLastError(), "batch prologue");
 }
 
-int batch_step(pd_ctx* c, int ct, int last, double load, cudaStream_t s) {
+int batch_force(pd_ctx* c, cudaStream_t s) {
     StepFlags f;
     f.epi = EPI_ADR;
-    int rc = launch_force(c, f, s);
-    if (rc) return rc;
+    return launch_force(c, f, s);
+}
+
+int batch_finish(pd_ctx* c, int ct, int last, double load, cudaStream_t s) {
     const BatchInfo& B = c->batch;
     k_batch_cn<<<(unsigned)(((int64_t)B.count * 32 + T - 1) / T), T, 0, s>>>(B.count, B.inst_slices, B.slice_part,
                                                                               B.inst_cn);
@@ -183,6 +185,11 @@ int batch_step(pd_ctx* c, int ct, int last, double load, cudaStream_t s) {
     c->launches += 2;
     c->pos_valid = true;
     return cuda_err(c, cudaGetLastError(), "batch step");
+}
+
+int batch_step(pd_ctx* c, int ct, int last, double load, cudaStream_t s) {
+    int rc = batch_force(c, s);
+    return rc ? rc : batch_finish(c, ct, last, load, s);
 }
 
 }  // namespace pdg

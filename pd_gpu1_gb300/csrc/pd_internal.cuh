@@ -217,5 +217,7 @@ int fp64_probe(double* gfma_per_s);
 void release_batch(pd_ctx* c);
 int batch_prologue(pd_ctx* c, double load, cudaStream_t s);
 int batch_step(pd_ctx* c, int ct, int last, double load, cudaStream_t s);
+int batch_force(pd_ctx* c, cudaStream_t s);  // first phase of batch_step
+int batch_finish(pd_ctx* c, int ct, int last, double load, cudaStream_t s);  // the rest
 
 }  // namespace pdg

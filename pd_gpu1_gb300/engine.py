@@ -233,6 +233,14 @@ class Engine:
     def check_finite(self):
         self._c(self._lib.pd_check_finite(self.ctx, self.stream), "pd_check_finite")
 
+    def profile_steps(self, kind, ct0, nsteps, load=0.0):
+        """(force ms, step ms) per step over nsteps real steps (kind 0 ADR,
+        1 explicit), timed with CUDA events on the launch stream."""
+        f, st = C.c_double(), C.c_double()
+        self._c(self._lib.pd_profile_steps(self.ctx, kind, ct0, nsteps, load, C.byref(f), C.byref(st), self.stream),
+                "pd_profile_steps")
+        return f.value, st.value
+
     # ---- launch shape of the bond-force kernel ------------------------------
     def set_launch(self, block=256, chunked=0, waves=1):
         self._c(self._lib.pd_set_launch(self.ctx, block, chunked, waves), "pd_set_launch")
@@ -248,6 +256,26 @@ class Engine:
         ms = C.c_double()
         self._c(self._lib.pd_autotune(self.ctx, reps, C.byref(ms), self.stream), "pd_autotune")
         return self.launch() + (ms.value,)
+
+    # ---- output ------------------------------------------------------------
+    def save_disp(self, path="disp.txt"):
+        """save_disp_gpu (Save.cu:6-36): ux uy [uz] dmg per interior node."""
+        self._c(self._lib.pd_save_disp(self.ctx, str(path).encode(), self.stream), "pd_save_disp")
+
+    def save_kw(self, rad, path="disp.txt"):
+        """save_kw_gpu (Save.cu:62-101)."""
+        self._c(self._lib.pd_save_kw(self.ctx, rad, str(path).encode(), self.stream), "pd_save_kw")
+
+    def snapshot_save(self, path):
+        self._c(self._lib.pd_snapshot_save(self.ctx, str(path).encode(), self.stream), "pd_snapshot_save")
+
+    def snapshot_load(self, path):
+        self._c(self._lib.pd_snapshot_load(self.ctx, str(path).encode(), self.stream), "pd_snapshot_load")
+
+    def crack_tip(self, threshold=0.38):
+        xy = (C.c_double * 2)()
+        self._c(self._lib.pd_crack_tip(self.ctx, threshold, xy, self.stream), "pd_crack_tip")
+        return xy[0], xy[1]
 
     # ---- views -------------------------------------------------------------
     def csr(self):
