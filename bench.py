@@ -40,7 +40,7 @@ ALG_FP64_PER_BOND_2D = 23       # 10 add/sub, 8 mul, 3 div, 1 sqrt, 1 compare (s
 ALG_FP64_PER_BOND_3D = 31
 # measured DRAM bytes per bond and per node of the step kernel (ncu dram__bytes_read.sum +
 # dram__bytes_write.sum, one capture per workload)
-TRAFFIC = {"crack_branching_2d_pmb_verlet": (28.125, 139.8)}
+TRAFFIC = {"crack_branching_2d_pmb_verlet": (28.125, 139.8), "batch_plate_adr_2d_pmb": (32.2, 0.0)}
 
 
 def rank_info():
