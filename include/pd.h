@@ -232,6 +232,72 @@ int pd_run_adr(pd_ctx* ctx, int ct0, int nsteps, double load, void* stream);
  * damage field is refreshed every dmg_every steps. */
 int pd_run_explicit(pd_ctx* ctx, int nsteps, double load, int dmg_every, void* stream);
 
+/* ---- quasi-static load stepping ---------------------------------------- */
+/* No counterpart in the reference, which runs a fixed number of ADR steps
+ * (Solve_Plate_Tensile.cu:106).  The residual of an iterate is |F + b|, the
+ * 2-norm over the free (interior) nodes of internal plus body force. */
+/* Residual at the current displacement: one force evaluation that leaves the
+ * intact flags unchanged, then a fixed-order sum. */
+int pd_residual(pd_ctx* ctx, double* norm, void* stream);
+/* ADR steps ct0, ct0+1, ... (pd_run_adr's step, boundary rows held) in chunks
+ * of check_every graph-captured steps, until the residual of an iterate is
+ * <= tol or max_iters steps have run.  *iters receives the steps run and
+ * *norm the last residual seen (that of the iterate the chunk's last step
+ * started from; each step's force kernel reduces it beside the damping sums). */
+int pd_adr_solve(pd_ctx* ctx, int ct0, int max_iters, int check_every, double tol, int* iters, double* norm,
+                 void* stream);
+typedef struct pd_load_step_stats {
+    int32_t iters;      /* ADR steps run                                      */
+    int32_t warm_used;  /* 1: the predicted start was kept                    */
+    double r_plain;     /* residual of the plain start (previous solution)     */
+    double r_start;     /* residual of the start used                         */
+    double r_final;     /* last residual seen                                 */
+    double ms;          /* wall time of the whole increment (CUDA events)     */
+} pd_load_step_stats;
+/* One load increment: the boundary rows move by +-delta (kernel_quick_load's
+ * rows), the ADR state restarts (half-step velocity and old force zero, step
+ * index 0), and ADR runs until the residual is <= tol_rel times the plain
+ * start's.  With dev_du (device array: N_int x increments, then N_int y
+ * increments) the start is the previous solution plus dev_du, unless that
+ * start's residual exceeds the plain start's, in which case the plain start
+ * is used: the converged answer is the plain method's either way. */
+int pd_load_step(pd_ctx* ctx, double delta, const double* dev_du, double tol_rel, int max_iters, int check_every,
+                 pd_load_step_stats* out, void* stream);
+
+/* ---- learned warm start (per-node MLP on the tensor cores) --------------- */
+/* No reference counterpart.  8 -> 128 -> 128 -> 128 -> 2, GELU on the hidden
+ * layers, 34,434 parameters: BF16 operands of tcgen05.mma with FP32
+ * accumulation; FP32 master parameters and Adam state for training.  Flat
+ * parameter order (FP32, row-major [out][in]): W1[128][8], b1[128],
+ * W2[128][128], b2[128], W3[128][128], b3[128], W4[2][128], b4[2].  Inputs
+ * are BF16 rows of 16 (8 features, 8 zeros); outputs FP32 rows of 2. */
+typedef struct pd_mlp pd_mlp;
+pd_mlp* pd_mlp_create(int64_t max_rows, int* status);  /* rows per forward/backward pass */
+int pd_mlp_destroy(pd_mlp* net);
+int pd_mlp_num_params(void);
+/* set (also resets the Adam state) / get the FP32 master parameters */
+int pd_mlp_set_params(pd_mlp* net, const float* host, int64_t count);
+int pd_mlp_get_params(pd_mlp* net, float* host, int64_t count);
+/* y[M][2] = net(x[M][16]) (device pointers; any M, processed in max_rows blocks) */
+int pd_mlp_forward(pd_mlp* net, const void* dev_x, int64_t M, float* dev_y, void* stream);
+/* Gradient of loss = sum over rows and outputs of (y - t)^2 / (2 M), t[M][2] on
+ * the device, M <= max_rows; flat gradient to host_grad (may be NULL). */
+int pd_mlp_grad(pd_mlp* net, const void* dev_x, const float* dev_t, int64_t M, float* host_grad, float* loss,
+                void* stream);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on that loss. */
+int pd_mlp_train_step(pd_mlp* net, const void* dev_x, const float* dev_t, int64_t M, float lr, float* loss,
+                      void* stream);
+/* The tensor-core product on its own: d[M][N] = a[M][K] * b[N][K]^T (BF16 in,
+ * FP32 out; a stored [K][M] when transpose_a); N = 16 or a multiple of 128. */
+int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d, int transpose_a,
+                void* stream);
+/* Features of the free nodes for a load increment (BF16 [N_int][16]): previous
+ * displacement / U, increment / U, damage, loaded-edge flag, x and y over the
+ * half sizes, family size / nn_ref; U is the accumulated boundary displacement. */
+int pd_warm_features(pd_ctx* ctx, double U, double delta, double nn_ref, void* dev_x, void* stream);
+/* Predicted increment for pd_load_step: dev_du[2*N_int] = delta * net(features). */
+int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, double nn_ref, double* dev_du, void* stream);
+
 /* ---- batches of specimens ----------------------------------------------- */
 /* No counterpart in the reference, which solves one plate per process.  A
  * batch packs many 2-D bond-based plates of the crack-plate layout

@@ -97,3 +97,15 @@ class PDSpecimen(C.Structure):
         ("nx", C.c_int32), ("ny", C.c_int32), ("emod", C.c_double), ("critical_s", C.c_double),
         ("crack_len", C.c_double), ("crack_theta", C.c_double), ("load_scale", C.c_double),
     ]
+
+
+class PDLoadStepStats(C.Structure):
+    """pd_load_step_stats: one quasi-static load increment."""
+
+    _fields_ = [
+        ("iters", C.c_int32), ("warm_used", C.c_int32), ("r_plain", C.c_double), ("r_start", C.c_double),
+        ("r_final", C.c_double), ("ms", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}

@@ -7,7 +7,7 @@ raises, so a run without the CUDA engine cannot pass silently.
 import ctypes as C
 import os
 
-from ._abi import PDCylinder, PDParams, PDResult, PDSpecimen
+from ._abi import PDCylinder, PDLoadStepStats, PDParams, PDResult, PDSpecimen
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libpd_gb300.so")
@@ -62,6 +62,20 @@ _SIGS = {
     "pd_cylinder_integrate2": (I32, [VP, VP]),
     "pd_run_adr": (I32, [VP, I32, I32, D, VP]),
     "pd_run_explicit": (I32, [VP, I32, D, I32, VP]),
+    "pd_residual": (I32, [VP, P(D), VP]),
+    "pd_adr_solve": (I32, [VP, I32, I32, I32, D, P(I32), P(D), VP]),
+    "pd_load_step": (I32, [VP, D, VP, D, I32, I32, P(PDLoadStepStats), VP]),
+    "pd_mlp_create": (VP, [I64, P(I32)]),
+    "pd_mlp_destroy": (I32, [VP]),
+    "pd_mlp_num_params": (I32, []),
+    "pd_mlp_set_params": (I32, [VP, VP, I64]),
+    "pd_mlp_get_params": (I32, [VP, VP, I64]),
+    "pd_mlp_forward": (I32, [VP, VP, I64, VP, VP]),
+    "pd_mlp_grad": (I32, [VP, VP, VP, I64, VP, P(C.c_float), VP]),
+    "pd_mlp_train_step": (I32, [VP, VP, VP, I64, C.c_float, P(C.c_float), VP]),
+    "pd_mlp_gemm": (I32, [VP, VP, I64, I64, I64, VP, I32, VP]),
+    "pd_warm_features": (I32, [VP, D, D, D, VP, VP]),
+    "pd_warm_predict": (I32, [VP, VP, D, D, D, VP, VP]),
     "pd_batch_create": (VP, [P(PDParams), P(PDSpecimen), I32, P(I32)]),
     "pd_batch_info": (I32, [VP, P(I32), P(I64), P(I64)]),
     "pd_batch_run_adr": (I32, [VP, I32, I32, D, VP]),

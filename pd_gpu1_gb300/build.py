@@ -26,6 +26,7 @@ UNITS = {
     "noalloc.cu": [],
     "batch.cu": [],
     "output.cu": [],
+    "mlp.cu": [],
 }
 
 

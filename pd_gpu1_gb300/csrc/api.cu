@@ -307,6 +307,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     ok = ok && cudaMalloc(&c->partials, (size_t)kMaxPartials * 4 * 8) == cudaSuccess;
     ok = ok && cudaMalloc(&c->ticket, 4 * sizeof(unsigned)) == cudaSuccess;
     ok = ok && cudaMalloc(&c->cn, 8) == cudaSuccess && cudaMalloc(&c->red_out, 8) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->res, 8) == cudaSuccess;
     ok = ok && cudaMalloc(&c->cyl, sizeof(CylDev)) == cudaSuccess;
     if (!ok) {
         pd_destroy(c);
@@ -322,6 +323,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     cudaMemset(c->node_b, 0, nb);
     cudaMemset(c->ticket, 0, 4 * sizeof(unsigned));
     cudaMemset(c->cn, 0, 8);
+    cudaMemset(c->res, 0, 8);
     cudaMemset(c->cyl, 0, sizeof(CylDev));
     c->pos_valid = true;
     if (cudaDeviceSynchronize() != cudaSuccess) {
@@ -341,7 +343,8 @@ int pd_destroy(pd_ctx* c) {
         for (int a = 0; a < 3; a++)
             if (c->pos[b][a]) cudaFree(c->pos[b][a]);
     void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->partials, c->ticket, c->cn, c->red_out,
-                    c->cyl, c->NL,     c->idist,  c->fac,    c->scr,      c->w,      c->e,  c->fail};
+                    c->res, c->cyl,    c->NL,     c->idist,  c->fac,      c->scr,    c->w,  c->e,
+                    c->fail};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     release_sell(c);
@@ -749,6 +752,111 @@ int pd_run_explicit(pd_ctx* c, int nsteps, double load, int dmg_every, void* str
         done += len;
     }
     return cuda_err(c, cudaGetLastError(), "pd_run_explicit");
+}
+
+// ---- quasi-static load stepping ------------------------------------------------
+static int residual_now(pd_ctx* c, cudaStream_t s, double* norm) {
+    int rc = ensure_ready(c, s);
+    if (rc) return rc;
+    StepFlags f;
+    f.nobreak = 1;
+    if (c->p.model == PD_MODEL_STATE && (rc = launch_theta(c, s))) return rc;
+    if ((rc = launch_force(c, f, s))) return rc;
+    if ((rc = residual_sq(c, c->red_out, s))) return rc;
+    double v = 0.0;
+    cudaError_t e = cudaMemcpyAsync(&v, c->red_out, sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err(c, e, "residual");
+    *norm = std::sqrt(v);
+    return PD_OK;
+}
+
+int pd_residual(pd_ctx* c, double* norm, void* stream) {
+    if (!c || !norm) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "residual of a batch: not provided");
+    StreamScope sc(c, stream);
+    return residual_now(c, sc.s, norm);
+}
+
+int pd_adr_solve(pd_ctx* c, int ct0, int max_iters, int check_every, double tol, int* iters, double* norm,
+                 void* stream) {
+    if (!c || ct0 < 0 || max_iters < 1 || check_every < 1 || !(tol >= 0.0) || !iters || !norm) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "a batch of specimens steps with pd_batch_run_adr");
+    int done = 0;
+    double r = HUGE_VAL;
+    while (done < max_iters) {
+        const int len = std::min(check_every, max_iters - done);
+        int rc = pd_run_adr(c, ct0 + done, len, 0.0, stream);
+        if (rc) return rc;
+        done += len;
+        double v = 0.0;
+        cudaError_t e = cudaMemcpyAsync(&v, c->res, sizeof(double), cudaMemcpyDeviceToHost, st(stream));
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st(stream));
+        if (e != cudaSuccess) return cuda_err(c, e, "pd_adr_solve");
+        r = std::sqrt(v);
+        if (!(r > tol)) break;  // also stops on NaN
+    }
+    *iters = done;
+    *norm = r;
+    if (!std::isfinite(r)) return set_err(c, PD_ERR_NONFINITE, "ADR residual is not finite");
+    return PD_OK;
+}
+
+int pd_load_step(pd_ctx* c, double delta, const double* dev_du, double tol_rel, int max_iters, int check_every,
+                 pd_load_step_stats* out, void* stream) {
+    if (!c || !out || !(tol_rel > 0.0) || max_iters < 1 || check_every < 1) return PD_ERR_ARG;
+    if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "load stepping of a batch: not provided");
+    if (c->p.mass == 0.0) return set_err(c, PD_ERR_ARG, "ADR needs the fictitious mass (bond-based parameters)");
+    StreamScope sc(c, stream);
+    cudaStream_t s = sc.s;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    cudaEventRecord(e0, s);
+    pd_load_step_stats st{};
+    int rc = ensure_ready(c, s);
+    const int64_t ni = c->p.N_int;
+    double* saved = nullptr;
+    // the increment: boundary rows move by +-delta (kernel_quick_load), ADR restarts
+    if (!rc) rc = launch_quick_load(c, delta / c->p.dt, s);
+    const int zero[] = {PD_F_VHX, PD_F_VHY, PD_F_VHZ, PD_F_FOX, PD_F_FOY, PD_F_FOZ};
+    for (int k = 0; k < 6 && !rc; k++)
+        rc = cuda_err(c, cudaMemsetAsync(c->nf[zero[k]], 0, c->p.N * sizeof(double), s), "ADR restart");
+    c->pos_valid = false;
+    if (!rc) rc = residual_now(c, s, &st.r_plain);
+    st.r_start = st.r_plain;
+    if (!rc && dev_du) {
+        // start from the previous solution plus the predicted increment, unless
+        // its residual is larger than the plain start's
+        cudaError_t e = cudaMallocAsync(&saved, 2 * ni * sizeof(double), s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(saved, c->nf[PD_F_UX], ni * 8, cudaMemcpyDeviceToDevice, s);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(saved + ni, c->nf[PD_F_UY], ni * 8, cudaMemcpyDeviceToDevice, s);
+        rc = cuda_err(c, e, "warm start save");
+        if (!rc) rc = add_increment(c, dev_du, s);
+        c->pos_valid = false;
+        double rw = 0.0;
+        if (!rc) rc = residual_now(c, s, &rw);
+        if (!rc && rw <= st.r_plain) {
+            st.warm_used = 1;
+            st.r_start = rw;
+        } else if (!rc) {
+            e = cudaMemcpyAsync(c->nf[PD_F_UX], saved, ni * 8, cudaMemcpyDeviceToDevice, s);
+            if (e == cudaSuccess) e = cudaMemcpyAsync(c->nf[PD_F_UY], saved + ni, ni * 8, cudaMemcpyDeviceToDevice, s);
+            rc = cuda_err(c, e, "warm start restore");
+            c->pos_valid = false;
+        }
+    }
+    if (saved) cudaFreeAsync(saved, s);
+    if (!rc) rc = pd_adr_solve(c, 0, max_iters, check_every, tol_rel * st.r_plain, &st.iters, &st.r_final, s);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    st.ms = ms;
+    *out = st;
+    return rc;
 }
 
 // Batched ADR: the loop of pd_run_adr over every specimen of a batch context,

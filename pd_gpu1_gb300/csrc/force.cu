@@ -85,6 +85,8 @@ struct ForceArgs {
     unsigned int* ticket;
     double* cn_out;
     int chunked;              // contiguous slice runs per warp instead of a grid stride
+    int nobreak;              // evaluate forces without updating the intact flags
+    double* res_out;          // ADR: sum over force rows of |F + b|^2 (device scalar)
     // batch of specimens (null for a single one)
     const double* node_mass;  // ADR fictitious mass per node
     double* slice_part;       // per-slice damping sums (2 per slice) instead of a grid reduction
@@ -260,6 +262,14 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
         }
         red[0] += cn;
         red[1] += disp;
+        // residual of the iterate: |F + b|^2 over the force rows (free nodes)
+        const double rx = fxr + A.bx[r], ry = fyr + A.by[r];
+        double rr = rx * rx + ry * ry;
+        if (DIM == 3) {
+            const double rz = fzr + A.bz[r];
+            rr += rz * rz;
+        }
+        red[2] += rr;
         return;
     }
     if (EPI == EPI_VERLET) {
@@ -317,7 +327,7 @@ __device__ __forceinline__ void slice_partials(const ForceArgs& A, int64_t s, do
         A.slice_part[2 * s] = a;
         A.slice_part[2 * s + 1] = b;
     }
-    red[0] = red[1] = 0.0;
+    red[0] = red[1] = red[2] = 0.0;
 }
 
 // Boundary rows [N_int, N): the next step's prescribed motion
@@ -373,6 +383,7 @@ __device__ void finish_reduction(const ForceArgs& A, double red[3], int nred) {
         if (cn2 != 0.0) cn = (cn1 / cn2 > 0.0) ? 2.0 * sqrt(cn1 / cn2) : 0.0;
         if (cn > 2.0) cn = 1.9;
         *A.cn_out = cn;
+        if (A.res_out) *A.res_out = tot[2];
     } else if (EPI == EPI_NONE) {
         for (int a = 0; a < 3; a++) A.cyl->force[a] += tot[a];
     } else {
@@ -457,7 +468,7 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
                     brk = exceeds(e, A.ecrit[slot]);
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
-                if (broke && lane == 0) wbits[k] = word & ~broke;
+                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
             }
             if (kTailFF) {
                 // undo the power-of-two scaling of the bond coefficient (exact)
@@ -470,7 +481,7 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
     }
-    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 2);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -578,7 +589,7 @@ __global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) 
                     brk = exceeds(ef, A.ecrit[slot]);
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
-                if (broke && lane == 0) wbits[k] = word & ~broke;
+                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
             }
             fxr = f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l);
             fyr = f64_of_f32s(fya.h) + f64_of_f32s(fya.l);
@@ -587,7 +598,7 @@ __global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) 
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
     }
-    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 2);
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -610,8 +621,15 @@ __global__ void __launch_bounds__(kForceBlock) k_adr_cnn(const ForceArgs A) {
         }
         red[0] += cn;
         red[1] += disp;
+        const double rx = A.fx[r] + A.bx[r], ry = A.fy[r] + A.by[r];
+        double rr = rx * rx + ry * ry;
+        if (DIM == 3) {
+            const double rz = A.fz[r] + A.bz[r];
+            rr += rz * rz;
+        }
+        red[2] += rr;
     }
-    finish_reduction<EPI_ADR>(A, red, 2);
+    finish_reduction<EPI_ADR>(A, red, 3);
 }
 
 // Standalone kernel_contact (Solve_Kalthoff_Winkler.cu:112-175) on nodes [0, N).
@@ -720,6 +738,7 @@ static ForceArgs make_args(pd_ctx* c) {
     A.cn_out = c->cn;
     A.node_mass = c->batch.node_mass;
     A.slice_part = c->batch.slice_part;
+    A.res_out = c->res;
     return A;
 }
 
@@ -753,6 +772,7 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
     A.do_next = f.do_next;
     A.load = f.load;
     A.contact = f.contact;
+    A.nobreak = f.nobreak;
     if (f.epi != EPI_VERLET || !f.do_next) {
         // without the next step's half-kick only the force rows are visited
         A.nslices = (A.nforce + 31) / 32;

@@ -229,6 +229,30 @@ __global__ void k_sum_final(const double* __restrict__ part, int n, double* __re
     }
 }
 
+// Squared residual |F + b|^2 of the free nodes, block partials in a fixed order.
+__global__ void k_residual_partials(NodeArgs A, double* __restrict__ part) {
+    __shared__ double sm[T / 32];
+    const KParams& P = A.P;
+    double v = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N_int;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double rx = A.fx[i] + A.bx[i], ry = A.fy[i] + A.by[i];
+        v += rx * rx + ry * ry;
+        if (P.dim == 3) {
+            const double rz = A.fz[i] + A.bz[i];
+            v += rz * rz;
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int k = 0; k < T / 32; k++) r += sm[k];
+        part[blockIdx.x] = r;
+    }
+}
+
 __global__ void k_finite(NodeArgs A, int* bad) {
     const KParams& P = A.P;
     int b = 0;
@@ -354,6 +378,33 @@ int reduce_sum(pd_ctx* c, const double* x, int64_t n, double* out_dev, cudaStrea
     k_sum_final<<<1, T, 0, s>>>(c->partials, (int)g, out_dev);
     c->launches += 2;
     return cuda_err(c, cudaGetLastError(), "reduce_sum");
+}
+
+// u += du on the free nodes (du: x components then y components, N_int each).
+__global__ void k_add_increment(NodeArgs A, const double* __restrict__ du) {
+    const KParams& P = A.P;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N_int;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        A.ux[i] += du[i];
+        A.uy[i] += du[P.N_int + i];
+    }
+}
+
+int add_increment(pd_ctx* c, const double* du, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    k_add_increment<<<grid_for(c, A.P.N_int), T, 0, s>>>(A, du);
+    c->launches++;
+    c->pos_valid = false;
+    return cuda_err(c, cudaGetLastError(), "add_increment");
+}
+
+int residual_sq(pd_ctx* c, double* out_dev, cudaStream_t s) {
+    NodeArgs A = node_args(c);
+    const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((A.P.N_int + T - 1) / T, 1024));
+    k_residual_partials<<<g, T, 0, s>>>(A, c->partials);
+    k_sum_final<<<1, T, 0, s>>>(c->partials, (int)g, out_dev);
+    c->launches += 2;
+    return cuda_err(c, cudaGetLastError(), "residual");
 }
 
 int check_finite(pd_ctx* c, cudaStream_t s, int* bad_host) {

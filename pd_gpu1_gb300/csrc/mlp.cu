@@ -1,0 +1,705 @@
+// Per-node MLP of the learned ADR warm start (no reference counterpart: the
+// reference runs a fixed number of ADR steps, Solve_Plate_Tensile.cu:106).
+//
+// Network: 8 -> 128 -> 128 -> 128 -> 2, GELU (erf form) on the hidden layers,
+// 34,434 parameters.  Weights are BF16 operands of the tensor cores with FP32
+// master copies for the optimizer; every product is a BF16 x BF16 -> FP32
+// tcgen05.mma (kind::f16) issued by one thread, operands staged in shared
+// memory in the canonical K-major layout without swizzle, accumulators in
+// tensor memory read back with tcgen05.ld for the fused epilogues:
+//   forward   Z = H W^T + b, H' = GELU(Z)            (epilogue: bias, GELU, BF16)
+//   backward  dH = dZ' W, dZ = dH * GELU'(Z)         (epilogue: GELU', BF16)
+//             dW = dZ^T H (split over row blocks)    (epilogue: FP32 partials)
+// One kernel template serves every product: D[M x N] = A[M x K] * B[N x K]^T
+// with A and B read through arbitrary element strides, so transposed operands
+// (dZ^T, H^T, W) are gathered by the loader instead of being stored twice.
+//
+// Padding: the 8 inputs are padded to K = 16 and the 2 outputs to N = 16 with
+// zero weights; tiles are 128 rows (M) by 16 or 128 columns (N).
+#include <cuda_bf16.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "pd_internal.cuh"
+
+namespace pdg {
+namespace mlp {
+
+constexpr int kIn = 8, kInPad = 16, kHid = 128, kOut = 2, kOutPad = 16;
+constexpr int kParams = kHid * kIn + kHid + 2 * (kHid * kHid + kHid) + kOut * kHid + kOut;  // 34,434
+constexpr int kTileM = 128;
+constexpr int kChunkK = 64;
+constexpr int kThreads = 128;
+constexpr long long kSpinLimit = 1ll << 24;  // bounded mbarrier wait
+
+enum Epi { E_F32 = 0, E_GELU = 1, E_BWD = 2, E_PARTIAL = 3 };
+
+struct GemmArgs {
+    const __nv_bfloat16* A;
+    int64_t sam, sak;  // element strides of A(m, k)
+    const __nv_bfloat16* B;
+    int64_t sbn, sbk;  // element strides of B(n, k)
+    int64_t M, N, K;
+    int64_t k_per_split;
+    int epi;
+    float* D;            // E_F32: [M][ldd]; E_PARTIAL: [split][M][ldd]
+    int64_t ldd;
+    const float* bias;   // E_F32 / E_GELU: [N]
+    float* Z;            // E_GELU: pre-activation [M][ldh]
+    __nv_bfloat16* H;    // E_GELU: activation [M][ldh]; E_BWD: dZ [M][ldh]
+    int64_t ldh;
+    const float* Zin;    // E_BWD: pre-activation [M][ldh]
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// Shared-memory matrix descriptor: canonical K-major layout, no swizzle.
+// Core matrices are 8 rows x 16 bytes stored contiguously (128 B); lbo is the
+// byte distance between core matrices adjacent in K, sbo between core matrices
+// adjacent in M/N (8-row groups).  Version field (bits 46-47) = 1.
+__device__ __forceinline__ uint64_t make_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr >> 4) & 0x3fffu);
+    d |= (uint64_t)((lbo >> 4) & 0x3fffu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3fffu) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;  // base offset 0, layout type 0 (no swizzle)
+}
+
+// Instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both
+// K-major, N >> 3 at bits 17-22, M >> 4 at bits 24-28.
+__host__ __device__ constexpr uint32_t make_idesc(int m, int n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(m >> 4) << 24);
+}
+
+// Byte offset of element (row r, column k) of a K-major tile with kChunkK columns.
+__device__ __forceinline__ uint32_t tile_off(int r, int k) {
+    constexpr uint32_t lbo = 128, sbo = (kChunkK / 8) * 128;
+    return (uint32_t)(r >> 3) * sbo + (uint32_t)(k >> 3) * lbo + (uint32_t)(r & 7) * 16 + (uint32_t)(k & 7) * 2;
+}
+
+// Stage rows [r0, r0 + rows) x columns [k0, k0 + kChunkK) of X(r, k) =
+// X[r * sr + k * sk] into a K-major tile, zero outside [0, R) x [0, Kmax).
+__device__ void load_tile(unsigned char* tile, const __nv_bfloat16* X, int64_t sr, int64_t sk, int64_t r0, int rows,
+                          int64_t R, int64_t k0, int64_t Kmax) {
+    const int groups = rows * (kChunkK / 8);
+    if (sk == 1) {  // 8 consecutive k per 16-byte vector
+        for (int g = threadIdx.x; g < groups; g += kThreads) {
+            const int r = g / (kChunkK / 8), kg = (g % (kChunkK / 8)) * 8;
+            const int64_t gr = r0 + r, gk = k0 + kg;
+            uint4 v = make_uint4(0, 0, 0, 0);
+            if (gr < R) {
+                const __nv_bfloat16* src = X + gr * sr + gk;
+                if (gk + 8 <= Kmax && ((reinterpret_cast<uintptr_t>(src) & 15) == 0)) {
+                    v = *reinterpret_cast<const uint4*>(src);
+                } else {
+                    unsigned short e[8];
+                    for (int j = 0; j < 8; j++)
+                        e[j] = gk + j < Kmax ? __bfloat16_as_ushort(src[j]) : (unsigned short)0;
+                    v = make_uint4(e[0] | (e[1] << 16), e[2] | (e[3] << 16), e[4] | (e[5] << 16), e[6] | (e[7] << 16));
+                }
+            }
+            *reinterpret_cast<uint4*>(tile + tile_off(r, kg)) = v;
+        }
+    } else {  // element by element (strided k)
+        for (int g = threadIdx.x; g < rows * kChunkK; g += kThreads) {
+            const int k = g / rows, r = g % rows;  // consecutive threads: consecutive rows
+            const int64_t gr = r0 + r, gk = k0 + k;
+            unsigned short e = 0;
+            if (gr < R && gk < Kmax) e = __bfloat16_as_ushort(X[gr * sr + gk * sk]);
+            *reinterpret_cast<unsigned short*>(tile + tile_off(r, k)) = e;
+        }
+    }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
+    for (long long it = 0; it < kSpinLimit; it++) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(bar), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ float gelu(float z) { return 0.5f * z * (1.0f + erff(z * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad(float z) {
+    const float cdf = 0.5f * (1.0f + erff(z * 0.70710678118654752f));
+    const float pdf = 0.39894228040143268f * expf(-0.5f * z * z);
+    return cdf + z * pdf;
+}
+
+// D[M x N] = A[M x K] * B[N x K]^T for one 128 x NT tile and one K range.
+template <int NT>
+__global__ void __launch_bounds__(kThreads) k_gemm(GemmArgs g) {
+    static_assert(NT == 16 || NT == 128, "tile width");
+    constexpr uint32_t kCols = NT < 32 ? 32 : NT;  // TMEM allocation: power of two >= 32
+    constexpr uint32_t kIdesc = make_idesc(kTileM, NT);
+    __shared__ __align__(1024) unsigned char sa[kTileM * kChunkK * 2];
+    __shared__ __align__(1024) unsigned char sb[NT * kChunkK * 2];
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int failed;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t m0 = (int64_t)blockIdx.x * kTileM, n0 = (int64_t)blockIdx.y * NT;
+    const int64_t kb = (int64_t)blockIdx.z * g.k_per_split;
+    const int64_t ke = kb + g.k_per_split < g.K ? kb + g.k_per_split : g.K;
+    const uint32_t bar_a = smem_addr(&bar);
+
+    if (threadIdx.x == 0) {
+        failed = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(kCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+
+    uint32_t phase = 0;
+    int chunks = 0;
+    for (int64_t k0 = kb; k0 < ke; k0 += kChunkK, chunks++) {
+        if (chunks > 0) {  // the previous chunk's products have read the tiles
+            if (!mbar_wait(bar_a, phase)) failed = 1;
+            phase ^= 1;
+        }
+        __syncthreads();
+        if (failed) break;
+        load_tile(sa, g.A, g.sam, g.sak, m0, kTileM, g.M, k0, ke);
+        load_tile(sb, g.B, g.sbn, g.sbk, n0, NT, g.N, k0, ke);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const int ksteps = (int)((ke - k0 < kChunkK ? ke - k0 : kChunkK) + 15) / 16;
+            for (int j = 0; j < ksteps; j++) {
+                const uint64_t da = make_desc(smem_addr(sa) + j * 256, 128, (kChunkK / 8) * 128);
+                const uint64_t db = make_desc(smem_addr(sb) + j * 256, 128, (kChunkK / 8) * 128);
+                const uint32_t acc = (chunks > 0 || j > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\t"
+                    "setp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                    "l"(da), "l"(db), "r"(kIdesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_a)
+                         : "memory");
+        }
+    }
+    if (chunks > 0 && !failed) {
+        if (!mbar_wait(bar_a, phase)) failed = 1;
+    }
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (!failed && chunks > 0) {
+        // epilogue: thread (warp w, lane l) owns row m0 + 32 w + l
+        const int64_t m = m0 + 32 * warp + lane;
+        for (int c0 = 0; c0 < NT; c0 += 16) {
+            uint32_t v[16];
+            const uint32_t taddr = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c0;
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]),
+                  "=r"(v[15])
+                : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (m >= g.M) continue;
+            for (int j = 0; j < 16; j++) {
+                const int64_t n = n0 + c0 + j;
+                if (n >= g.N) break;
+                const float d = __uint_as_float(v[j]);
+                switch (g.epi) {
+                    case E_F32:
+                        g.D[m * g.ldd + n] = d + (g.bias ? g.bias[n] : 0.0f);
+                        break;
+                    case E_PARTIAL:
+                        g.D[((int64_t)blockIdx.z * g.M + m) * g.ldd + n] = d;
+                        break;
+                    case E_GELU: {
+                        const float z = d + g.bias[n];
+                        g.Z[m * g.ldh + n] = z;
+                        g.H[m * g.ldh + n] = __float2bfloat16_rn(gelu(z));
+                        break;
+                    }
+                    default: {  // E_BWD
+                        const float z = g.Zin[m * g.ldh + n];
+                        g.H[m * g.ldh + n] = __float2bfloat16_rn(d * gelu_grad(z));
+                        break;
+                    }
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kCols) : "memory");
+    if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
+}
+
+// Sum of split-K partials [splits][rows][cols] -> out, fixed order.
+__global__ void k_reduce_splits(const float* __restrict__ part, int splits, int64_t n, float* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int k = 0; k < splits; k++) s += part[(int64_t)k * n + i];
+        out[i] = s;
+    }
+}
+
+// Column sums of a BF16 [M][cols] matrix (bias gradients), one thread per column.
+__global__ void k_colsum(const __nv_bfloat16* __restrict__ x, int64_t M, int cols, int64_t rows_per_block,
+                         float* __restrict__ part) {
+    const int c = threadIdx.x;
+    if (c >= cols) return;
+    const int64_t r0 = blockIdx.x * rows_per_block;
+    const int64_t r1 = r0 + rows_per_block < M ? r0 + rows_per_block : M;
+    float s = 0.0f;
+    for (int64_t r = r0; r < r1; r++) s += __bfloat162float(x[r * cols + c]);
+    part[(int64_t)blockIdx.x * cols + c] = s;
+}
+
+// Loss gradient of the mean squared error over the 2 outputs: dY = 2 (Y - T) / (2 M),
+// stored as BF16 [M][16] (columns 2..15 zero); per-block loss partial sums.
+__global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ T, int64_t M,
+                       __nv_bfloat16* __restrict__ dY, float* __restrict__ part) {
+    __shared__ float sm[kThreads / 32];
+    float l = 0.0f;
+    const float scale = 1.0f / (float)M;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < M; r += (int64_t)gridDim.x * blockDim.x) {
+        for (int j = 0; j < kOutPad; j++) {
+            float d = 0.0f;
+            if (j < kOut) {
+                const float e = Y[r * kOutPad + j] - T[r * kOut + j];
+                l += e * e;
+                d = e * scale;  // d/dy of sum(e^2) / (2 M)
+            }
+            dY[r * kOutPad + j] = __float2bfloat16_rn(d);
+        }
+    }
+    for (int off = 16; off > 0; off >>= 1) l += __shfl_down_sync(0xffffffffu, l, off);
+    if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = l;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float s = 0.0f;
+        for (int k = 0; k < kThreads / 32; k++) s += sm[k];
+        part[blockIdx.x] = s;
+    }
+}
+
+__global__ void k_features(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                           const double* __restrict__ ux, const double* __restrict__ uy,
+                           const double* __restrict__ dmg, const int* __restrict__ NN, double inv_u, double inc,
+                           double inv_hx, double inv_hy, double edge, double inv_nn, __nv_bfloat16* __restrict__ X) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float f[kInPad];
+        f[0] = (float)(ux[i] * inv_u);
+        f[1] = (float)(uy[i] * inv_u);
+        f[2] = (float)inc;
+        f[3] = (float)dmg[i];
+        f[4] = fabs(y[i]) > edge ? 1.0f : 0.0f;
+        f[5] = (float)(x[i] * inv_hx);
+        f[6] = (float)(y[i] * inv_hy);
+        f[7] = (float)(NN[i] * inv_nn);
+        for (int j = kIn; j < kInPad; j++) f[j] = 0.0f;
+        for (int j = 0; j < kInPad; j++) X[i * kInPad + j] = __float2bfloat16_rn(f[j]);
+    }
+}
+
+__global__ void k_scale_out(int64_t n, const float* __restrict__ y, double delta, double* __restrict__ du) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        du[i] = delta * (double)y[i * kOut];
+        du[n + i] = delta * (double)y[i * kOut + 1];
+    }
+}
+
+}  // namespace mlp
+}  // namespace pdg
+
+using namespace pdg;
+using namespace pdg::mlp;
+
+// Parameter layout (flat FP32, PyTorch order): W1[128][8], b1[128], W2[128][128],
+// b2[128], W3[128][128], b3[128], W4[2][128], b4[2].
+namespace {
+constexpr int oW1 = 0, ob1 = oW1 + kHid * kIn, oW2 = ob1 + kHid, ob2 = oW2 + kHid * kHid, oW3 = ob2 + kHid,
+              ob3 = oW3 + kHid * kHid, oW4 = ob3 + kHid, ob4 = oW4 + kOut * kHid, oEnd = ob4 + kOut;
+static_assert(oEnd == kParams, "parameter count");
+
+// master parameters -> padded BF16 operands and FP32 biases
+__global__ void k_pack(const float* __restrict__ p, __nv_bfloat16* W1, __nv_bfloat16* W2, __nv_bfloat16* W3,
+                       __nv_bfloat16* W4, float* b1, float* b2, float* b3, float* b4) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kHid * kHid; i += gridDim.x * blockDim.x) {
+        W2[i] = __float2bfloat16_rn(p[oW2 + i]);
+        W3[i] = __float2bfloat16_rn(p[oW3 + i]);
+        if (i < kHid * kInPad) {
+            const int o = i / kInPad, c = i % kInPad;
+            W1[i] = __float2bfloat16_rn(c < kIn ? p[oW1 + o * kIn + c] : 0.0f);
+        }
+        if (i < kOutPad * kHid) {
+            const int o = i / kHid, c = i % kHid;
+            W4[i] = __float2bfloat16_rn(o < kOut ? p[oW4 + o * kHid + c] : 0.0f);
+        }
+        if (i < kHid) {
+            b1[i] = p[ob1 + i];
+            b2[i] = p[ob2 + i];
+            b3[i] = p[ob3 + i];
+        }
+        if (i < kOutPad) b4[i] = i < kOut ? p[ob4 + i] : 0.0f;
+    }
+}
+
+// padded gradients -> flat gradient vector
+__global__ void k_unpack_grad(const float* gW1, const float* gb1, const float* gW2, const float* gb2,
+                              const float* gW3, const float* gb3, const float* gW4, const float* gb4, float* g) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kParams; i += gridDim.x * blockDim.x) {
+        float v;
+        if (i < ob1) v = gW1[(i / kIn) * kInPad + i % kIn];
+        else if (i < oW2) v = gb1[i - ob1];
+        else if (i < ob2) v = gW2[i - oW2];
+        else if (i < oW3) v = gb2[i - ob2];
+        else if (i < ob3) v = gW3[i - oW3];
+        else if (i < oW4) v = gb3[i - ob3];
+        else if (i < ob4) v = gW4[i - oW4];  // rows 0, 1 of the [16][128] gradient
+        else v = gb4[i - ob4];
+        g[i] = v;
+    }
+}
+
+__global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m1,
+                       float* __restrict__ m2, float lr, float b1, float b2, float eps, float c1, float c2) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < kParams; i += gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        m1[i] = b1 * m1[i] + (1.0f - b1) * gi;
+        m2[i] = b2 * m2[i] + (1.0f - b2) * gi * gi;
+        p[i] -= lr * (m1[i] / c1) / (sqrtf(m2[i] / c2) + eps);
+    }
+}
+}  // namespace
+
+struct pd_mlp {
+    int64_t max_rows = 0;
+    int* err = nullptr;
+    float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;  // master, gradient, Adam moments
+    __nv_bfloat16 *W1 = nullptr, *W2 = nullptr, *W3 = nullptr, *W4 = nullptr;
+    float *b1 = nullptr, *b2 = nullptr, *b3 = nullptr, *b4 = nullptr;
+    float *gW1 = nullptr, *gW2 = nullptr, *gW3 = nullptr, *gW4 = nullptr;
+    float *gb1 = nullptr, *gb2 = nullptr, *gb3 = nullptr, *gb4 = nullptr;
+    // activations for max_rows rows
+    float *Z1 = nullptr, *Z2 = nullptr, *Z3 = nullptr, *Y = nullptr;
+    __nv_bfloat16 *H1 = nullptr, *H2 = nullptr, *H3 = nullptr, *dY = nullptr, *dZ = nullptr, *dZb = nullptr;
+    float* part = nullptr;  // split-K partials / column-sum partials
+    int64_t part_floats = 0;
+    int64_t step = 0;
+    std::string errmsg;
+};
+
+namespace {
+
+constexpr int64_t kRowsPerSplit = 1024;
+
+int launch_gemm(pd_mlp* n, const GemmArgs& a0, int nt, cudaStream_t s, int splits = 1) {
+    GemmArgs a = a0;
+    a.err = n->err;
+    if (a.k_per_split <= 0) a.k_per_split = a.K;
+    const dim3 grid((unsigned)((a.M + kTileM - 1) / kTileM), (unsigned)((a.N + nt - 1) / nt), (unsigned)splits);
+    if (nt == 16)
+        k_gemm<16><<<grid, kThreads, 0, s>>>(a);
+    else
+        k_gemm<128><<<grid, kThreads, 0, s>>>(a);
+    return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
+
+GemmArgs gemm(const __nv_bfloat16* A, int64_t sam, int64_t sak, const __nv_bfloat16* B, int64_t sbn, int64_t sbk,
+              int64_t M, int64_t N, int64_t K) {
+    GemmArgs a{};
+    a.A = A, a.sam = sam, a.sak = sak, a.B = B, a.sbn = sbn, a.sbk = sbk, a.M = M, a.N = N, a.K = K;
+    a.k_per_split = K;
+    return a;
+}
+
+// forward over M rows of X (BF16 [M][16]); Y (FP32 [M][16]) receives the outputs
+int forward(pd_mlp* n, const __nv_bfloat16* X, int64_t M, cudaStream_t s) {
+    int rc;
+    GemmArgs a = gemm(X, kInPad, 1, n->W1, kInPad, 1, M, kHid, kInPad);
+    a.epi = E_GELU, a.bias = n->b1, a.Z = n->Z1, a.H = n->H1, a.ldh = kHid;
+    if ((rc = launch_gemm(n, a, 128, s))) return rc;
+    a = gemm(n->H1, kHid, 1, n->W2, kHid, 1, M, kHid, kHid);
+    a.epi = E_GELU, a.bias = n->b2, a.Z = n->Z2, a.H = n->H2, a.ldh = kHid;
+    if ((rc = launch_gemm(n, a, 128, s))) return rc;
+    a = gemm(n->H2, kHid, 1, n->W3, kHid, 1, M, kHid, kHid);
+    a.epi = E_GELU, a.bias = n->b3, a.Z = n->Z3, a.H = n->H3, a.ldh = kHid;
+    if ((rc = launch_gemm(n, a, 128, s))) return rc;
+    a = gemm(n->H3, kHid, 1, n->W4, kHid, 1, M, kOutPad, kHid);
+    a.epi = E_F32, a.bias = n->b4, a.D = n->Y, a.ldd = kOutPad;
+    return launch_gemm(n, a, 16, s);
+}
+
+// dW[out][in] = sum over rows of dZ[m][out] * Hin[m][in]  (split over row blocks)
+int weight_grad(pd_mlp* n, const __nv_bfloat16* dZ, int64_t ldz, int64_t nout, const __nv_bfloat16* Hin,
+                int64_t ldi, int64_t nin, int64_t M, float* out, cudaStream_t s) {
+    const int splits = (int)((M + kRowsPerSplit - 1) / kRowsPerSplit);
+    GemmArgs a = gemm(dZ, 1, ldz, Hin, 1, ldi, nout, nin, M);
+    a.epi = E_PARTIAL, a.D = n->part, a.ldd = nin, a.k_per_split = kRowsPerSplit;
+    int rc = launch_gemm(n, a, nin <= 16 ? 16 : 128, s, splits);
+    if (rc) return rc;
+    const int64_t cnt = nout * nin;
+    k_reduce_splits<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(n->part, splits, cnt, out);
+    return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
+
+int bias_grad(pd_mlp* n, const __nv_bfloat16* dZ, int64_t M, int cols, float* out, cudaStream_t s) {
+    const int64_t rpb = 256;
+    const int blocks = (int)((M + rpb - 1) / rpb);
+    k_colsum<<<blocks, 128, 0, s>>>(dZ, M, cols, rpb, n->part);
+    k_reduce_splits<<<1, 128, 0, s>>>(n->part, blocks, cols, out);
+    return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
+
+// forward + backward over M rows; gradient into n->g (flat), loss (mean of
+// squared errors over rows and outputs, halved) into *loss
+int grad(pd_mlp* n, const __nv_bfloat16* X, const float* T, int64_t M, float* loss, cudaStream_t s) {
+    int rc = forward(n, X, M, s);
+    if (rc) return rc;
+    const int lb = (int)std::min<int64_t>((M + kThreads - 1) / kThreads, 1024);
+    k_loss<<<lb, kThreads, 0, s>>>(n->Y, T, M, n->dY, n->part);
+    // layer 4: dW4 = dY^T H3, db4 = colsum dY, dH3 = dY W4 -> dZ3
+    std::vector<float> lp(lb);
+    cudaMemcpyAsync(lp.data(), n->part, lb * sizeof(float), cudaMemcpyDeviceToHost, s);
+    if ((rc = weight_grad(n, n->dY, kOutPad, kOutPad, n->H3, kHid, kHid, M, n->gW4, s))) return rc;
+    if ((rc = bias_grad(n, n->dY, M, kOutPad, n->gb4, s))) return rc;
+    GemmArgs a = gemm(n->dY, kOutPad, 1, n->W4, 1, kHid, M, kHid, kOutPad);
+    a.epi = E_BWD, a.Zin = n->Z3, a.H = n->dZ, a.ldh = kHid;
+    if ((rc = launch_gemm(n, a, 128, s))) return rc;
+    // layer 3: dW3 = dZ3^T H2, db3, dH2 = dZ3 W3 -> dZ2
+    if ((rc = weight_grad(n, n->dZ, kHid, kHid, n->H2, kHid, kHid, M, n->gW3, s))) return rc;
+    if ((rc = bias_grad(n, n->dZ, M, kHid, n->gb3, s))) return rc;
+    a = gemm(n->dZ, kHid, 1, n->W3, 1, kHid, M, kHid, kHid);
+    a.epi = E_BWD, a.Zin = n->Z2, a.H = n->dZb, a.ldh = kHid;
+    if ((rc = launch_gemm(n, a, 128, s))) return rc;
+    // layer 2: dW2 = dZ2^T H1, db2, dH1 = dZ2 W2 -> dZ1
+    if ((rc = weight_grad(n, n->dZb, kHid, kHid, n->H1, kHid, kHid, M, n->gW2, s))) return rc;
+    if ((rc = bias_grad(n, n->dZb, M, kHid, n->gb2, s))) return rc;
+    a = gemm(n->dZb, kHid, 1, n->W2, 1, kHid, M, kHid, kHid);
+    a.epi = E_BWD, a.Zin = n->Z1, a.H = n->dZ, a.ldh = kHid;
+    if ((rc = launch_gemm(n, a, 128, s))) return rc;
+    // layer 1: dW1 = dZ1^T X, db1
+    if ((rc = weight_grad(n, n->dZ, kHid, kHid, X, kInPad, kInPad, M, n->gW1, s))) return rc;
+    if ((rc = bias_grad(n, n->dZ, M, kHid, n->gb1, s))) return rc;
+    k_unpack_grad<<<64, 256, 0, s>>>(n->gW1, n->gb1, n->gW2, n->gb2, n->gW3, n->gb3, n->gW4, n->gb4, n->g);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, n->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return PD_ERR_CUDA;
+    if (herr) return PD_ERR_TIMEOUT;
+    if (loss) {
+        double l = 0.0;
+        for (float v : lp) l += v;
+        *loss = (float)(l / (2.0 * (double)M));
+    }
+    return PD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+pd_mlp* pd_mlp_create(int64_t max_rows, int* status) {
+    auto fail = [&](int st) -> pd_mlp* {
+        if (status) *status = st;
+        return nullptr;
+    };
+    if (max_rows < 1) return fail(PD_ERR_ARG);
+    pd_mlp* n = new pd_mlp();
+    n->max_rows = max_rows;
+    const int64_t R = (max_rows + kTileM - 1) / kTileM * kTileM;
+    const int64_t splits = (R + kRowsPerSplit - 1) / kRowsPerSplit;
+    n->part_floats = std::max<int64_t>(splits * kHid * kHid, (R / 128 + 1) * 128 + 1024);
+    bool ok = true;
+    auto al = [&](auto*& ptr, int64_t count) {
+        if (ok) ok = cudaMalloc(&ptr, std::max<int64_t>(count, 1) * sizeof(*ptr)) == cudaSuccess;
+        if (ok) cudaMemset(ptr, 0, std::max<int64_t>(count, 1) * sizeof(*ptr));
+    };
+    al(n->err, 1);
+    al(n->p, kParams), al(n->g, kParams), al(n->m1, kParams), al(n->m2, kParams);
+    al(n->W1, kHid * kInPad), al(n->W2, kHid * kHid), al(n->W3, kHid * kHid), al(n->W4, kOutPad * kHid);
+    al(n->b1, kHid), al(n->b2, kHid), al(n->b3, kHid), al(n->b4, kOutPad);
+    al(n->gW1, kHid * kInPad), al(n->gW2, kHid * kHid), al(n->gW3, kHid * kHid), al(n->gW4, kOutPad * kHid);
+    al(n->gb1, kHid), al(n->gb2, kHid), al(n->gb3, kHid), al(n->gb4, kOutPad);
+    al(n->Z1, R * kHid), al(n->Z2, R * kHid), al(n->Z3, R * kHid), al(n->Y, R * kOutPad);
+    al(n->H1, R * kHid), al(n->H2, R * kHid), al(n->H3, R * kHid), al(n->dY, R * kOutPad);
+    al(n->dZ, R * kHid), al(n->dZb, R * kHid);
+    al(n->part, n->part_floats);
+    if (!ok) {
+        pd_mlp_destroy(n);
+        return fail(PD_ERR_NOMEM);
+    }
+    if (status) *status = PD_OK;
+    return n;
+}
+
+int pd_mlp_destroy(pd_mlp* n) {
+    if (!n) return PD_ERR_ARG;
+    void* ptrs[] = {n->err, n->p,   n->g,   n->m1,  n->m2,  n->W1,  n->W2,  n->W3, n->W4, n->b1,
+                    n->b2,  n->b3,  n->b4,  n->gW1, n->gW2, n->gW3, n->gW4, n->gb1, n->gb2, n->gb3,
+                    n->gb4, n->Z1,  n->Z2,  n->Z3,  n->Y,   n->H1,  n->H2,  n->H3, n->dY, n->dZ,
+                    n->dZb, n->part};
+    for (void* q : ptrs)
+        if (q) cudaFree(q);
+    delete n;
+    return PD_OK;
+}
+
+int pd_mlp_num_params(void) { return kParams; }
+
+int pd_mlp_set_params(pd_mlp* n, const float* host, int64_t count) {
+    if (!n || !host || count != kParams) return PD_ERR_ARG;
+    if (cudaMemcpy(n->p, host, kParams * sizeof(float), cudaMemcpyHostToDevice) != cudaSuccess) return PD_ERR_CUDA;
+    cudaMemset(n->m1, 0, kParams * sizeof(float));
+    cudaMemset(n->m2, 0, kParams * sizeof(float));
+    n->step = 0;
+    k_pack<<<64, 256>>>(n->p, n->W1, n->W2, n->W3, n->W4, n->b1, n->b2, n->b3, n->b4);
+    return cudaDeviceSynchronize() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
+
+int pd_mlp_get_params(pd_mlp* n, float* host, int64_t count) {
+    if (!n || !host || count != kParams) return PD_ERR_ARG;
+    return cudaMemcpy(host, n->p, kParams * sizeof(float), cudaMemcpyDeviceToHost) == cudaSuccess ? PD_OK
+                                                                                                 : PD_ERR_CUDA;
+}
+
+int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* stream) {
+    if (!n || !dev_x || !dev_y || M < 1) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    for (int64_t r0 = 0; r0 < M; r0 += n->max_rows) {
+        const int64_t m = std::min<int64_t>(n->max_rows, M - r0);
+        int rc = forward(n, reinterpret_cast<const __nv_bfloat16*>(dev_x) + r0 * kInPad, m, s);
+        if (rc) return rc;
+        if (cudaMemcpy2DAsync(dev_y + r0 * kOut, kOut * sizeof(float), n->Y, kOutPad * sizeof(float),
+                              kOut * sizeof(float), m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+            return PD_ERR_CUDA;
+    }
+    int herr = 0;
+    cudaMemcpyAsync(&herr, n->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return PD_ERR_CUDA;
+    return herr ? PD_ERR_TIMEOUT : PD_OK;
+}
+
+int pd_mlp_grad(pd_mlp* n, const void* dev_x, const float* dev_t, int64_t M, float* host_grad, float* loss,
+                void* stream) {
+    if (!n || !dev_x || !dev_t || M < 1 || M > n->max_rows) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    int rc = grad(n, reinterpret_cast<const __nv_bfloat16*>(dev_x), dev_t, M, loss, s);
+    if (rc) return rc;
+    if (host_grad && cudaMemcpy(host_grad, n->g, kParams * sizeof(float), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return PD_ERR_CUDA;
+    return PD_OK;
+}
+
+int pd_mlp_train_step(pd_mlp* n, const void* dev_x, const float* dev_t, int64_t M, float lr, float* loss,
+                      void* stream) {
+    if (!n || !dev_x || !dev_t || M < 1 || M > n->max_rows || !(lr > 0.0f)) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    int rc = grad(n, reinterpret_cast<const __nv_bfloat16*>(dev_x), dev_t, M, loss, s);
+    if (rc) return rc;
+    n->step++;
+    const float b1 = 0.9f, b2 = 0.999f;
+    const float c1 = 1.0f - std::pow(b1, (float)n->step), c2 = 1.0f - std::pow(b2, (float)n->step);
+    k_adam<<<64, 256, 0, s>>>(n->p, n->g, n->m1, n->m2, lr, b1, b2, 1e-8f, c1, c2);
+    k_pack<<<64, 256, 0, s>>>(n->p, n->W1, n->W2, n->W3, n->W4, n->b1, n->b2, n->b3, n->b4);
+    return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
+
+// Warm-start features of the free nodes (BF16 [N_int][16], columns 8..15 zero):
+//   0, 1  previous displacement / accumulated boundary displacement U
+//   2     load increment / U
+//   3     damage
+//   4     1 within one horizon of a loaded edge
+//   5, 6  x / (half width), y / (half height)
+//   7     family size / nn_ref (1 in the bulk, below 1 near surfaces and cracks)
+int pd_warm_features(pd_ctx* c, double U, double delta, double nn_ref, void* dev_x, void* stream) {
+    if (!c || !dev_x || !(U > 0.0) || !(nn_ref > 0.0) || c->p.dim != 2) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    const int64_t n = c->p.N_int;
+    const double hx = c->p.nx * c->p.dx / 2.0, hy = c->p.ny * c->p.dx / 2.0;
+    k_features<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+        n, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_UX], c->nf[PD_F_UY], c->nf[PD_F_DMG], c->NN, 1.0 / U, delta / U,
+        1.0 / hx, 1.0 / hy, hy - c->p.delta, 1.0 / nn_ref, reinterpret_cast<__nv_bfloat16*>(dev_x));
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "pd_warm_features");
+}
+
+// Predicted increment of the free nodes: features, forward pass, then
+// du = delta * output (x components, then y components, as doubles).
+int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref, double* dev_du, void* stream) {
+    if (!c || !n || !dev_du) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    const int64_t ni = c->p.N_int;
+    void* x = nullptr;
+    float* y = nullptr;
+    if (cudaMallocAsync(&x, ni * kInPad * 2, s) != cudaSuccess) return set_err(c, PD_ERR_NOMEM, "warm features");
+    if (cudaMallocAsync(&y, ni * kOut * sizeof(float), s) != cudaSuccess) {
+        cudaFreeAsync(x, s);
+        return set_err(c, PD_ERR_NOMEM, "warm outputs");
+    }
+    int rc = pd_warm_features(c, U, delta, nn_ref, x, s);
+    if (!rc) rc = pd_mlp_forward(n, x, ni, y, s);
+    if (!rc) {
+        k_scale_out<<<(unsigned)std::min<int64_t>((ni + 255) / 256, 4096), 256, 0, s>>>(ni, y, delta, dev_du);
+        c->launches++;
+        rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
+    } else {
+        set_err(c, rc, rc == PD_ERR_TIMEOUT ? "tensor-core wait gave up" : "MLP forward failed");
+    }
+    cudaFreeAsync(x, s);
+    cudaFreeAsync(y, s);
+    cudaStreamSynchronize(s);
+    return rc;
+}
+
+// Self-test of the tensor-core product: D[M x N] = A[M x K] * B[N x K]^T for
+// row-major BF16 A and B (FP32 D), through the same kernel and loader.
+int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d, int transpose_a,
+                void* stream) {
+    if (!dev_a || !dev_b || !dev_d || M < 1 || N < 1 || K < 1 || (N != 16 && N % 128 != 0)) return PD_ERR_ARG;
+    pd_mlp tmp;
+    if (cudaMalloc(&tmp.err, sizeof(int)) != cudaSuccess) return PD_ERR_NOMEM;
+    cudaMemset(tmp.err, 0, sizeof(int));
+    cudaStream_t s = st(stream);
+    const __nv_bfloat16* A = reinterpret_cast<const __nv_bfloat16*>(dev_a);
+    // transpose_a: A is stored K x M (the loader gathers A(m, k) = A[k][m])
+    GemmArgs a = transpose_a ? gemm(A, 1, M, reinterpret_cast<const __nv_bfloat16*>(dev_b), K, 1, M, N, K)
+                             : gemm(A, K, 1, reinterpret_cast<const __nv_bfloat16*>(dev_b), K, 1, M, N, K);
+    a.epi = E_F32, a.D = dev_d, a.ldd = N;
+    int rc = launch_gemm(&tmp, a, N == 16 ? 16 : 128, s);
+    int herr = 0;
+    cudaMemcpyAsync(&herr, tmp.err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(tmp.err);
+    tmp.err = nullptr;
+    if (rc) return rc;
+    if (e != cudaSuccess) return PD_ERR_CUDA;
+    return herr ? PD_ERR_TIMEOUT : PD_OK;
+}
+
+}  // extern "C"

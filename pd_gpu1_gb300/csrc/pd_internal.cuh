@@ -122,6 +122,7 @@ struct pd_ctx {
     unsigned int* ticket = nullptr;
     double* cn = nullptr;        // ADR damping coefficient (device scalar)
     double* red_out = nullptr;   // reduction result (device scalar)
+    double* res = nullptr;       // ADR: |F + b|^2 over the free nodes at the last step (device scalar)
     pdg::CylDev* cyl = nullptr;
     bool has_cyl = false;
 
@@ -192,6 +193,7 @@ struct StepFlags {
     int do_next = 0;      // apply the next step's loading + first Verlet half
     double load = 0.0;    // boundary-row speed of the next step (quick_load)
     int contact = 0;      // rigid impactor contact in the epilogue
+    int nobreak = 0;      // leave the intact flags unchanged (residual evaluations)
 };
 int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s);
 int launch_theta(pd_ctx* c, cudaStream_t s);
@@ -212,6 +214,10 @@ int launch_contact(pd_ctx* c, cudaStream_t s);
 int launch_cyl_integrate(pd_ctx* c, int half, cudaStream_t s);
 int reduce_sum(pd_ctx* c, const double* x, int64_t n, double* out_dev, cudaStream_t s);
 int check_finite(pd_ctx* c, cudaStream_t s, int* bad_host);
+// |F + b|^2 summed over the free nodes [0, N_int) into *out_dev (current forces)
+int residual_sq(pd_ctx* c, double* out_dev, cudaStream_t s);
+// u += du on the free nodes (du on the device: N_int x components, then N_int y)
+int add_increment(pd_ctx* c, const double* du, cudaStream_t s);
 int fp64_probe(double* gfma_per_s);
 // batch.cu
 void release_batch(pd_ctx* c);

@@ -13,7 +13,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._abi import FIELD, FIELD_DTYPE, PDCylinder, PDParams, PDResult, PDSpecimen
+from ._abi import FIELD, FIELD_DTYPE, PDCylinder, PDLoadStepStats, PDParams, PDResult, PDSpecimen
 from ._lib import PDError, check, lib
 
 __all__ = ["Engine", "Batch", "derive_params", "coord_kw", "solve_plate_tensile", "solve_plate_crack_grow",
@@ -229,6 +229,27 @@ class Engine:
 
     def run_explicit(self, nsteps, load=0.0, dmg_every=0):
         self._c(self._lib.pd_run_explicit(self.ctx, nsteps, load, dmg_every, self.stream), "pd_run_explicit")
+
+    # ---- quasi-static load stepping -----------------------------------------
+    def residual(self):
+        """|F + b| over the free nodes at the current displacement."""
+        r = C.c_double()
+        self._c(self._lib.pd_residual(self.ctx, C.byref(r), self.stream), "pd_residual")
+        return r.value
+
+    def adr_solve(self, ct0, max_iters, check_every, tol):
+        it, r = C.c_int(), C.c_double()
+        self._c(self._lib.pd_adr_solve(self.ctx, ct0, max_iters, check_every, tol, C.byref(it), C.byref(r),
+                                       self.stream), "pd_adr_solve")
+        return it.value, r.value
+
+    def load_step(self, delta, du_ptr=None, tol_rel=1e-6, max_iters=200000, check_every=100):
+        """One load increment solved by ADR to tol_rel; du_ptr: device pointer
+        to predicted increments (2*N_int doubles) or None.  Returns the stats."""
+        st = PDLoadStepStats()
+        self._c(self._lib.pd_load_step(self.ctx, delta, du_ptr, tol_rel, max_iters, check_every, C.byref(st),
+                                       self.stream), "pd_load_step")
+        return st.as_dict()
 
     def check_finite(self):
         self._c(self._lib.pd_check_finite(self.ctx, self.stream), "pd_check_finite")

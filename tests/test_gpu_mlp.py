@@ -1,0 +1,121 @@
+"""The warm-start MLP on the tensor cores (tcgen05, BF16 operands, FP32
+accumulation) against the CPU oracle (oracle/mlp_oracle.py).
+
+Bars: products within 1e-5 of exact (FP32 accumulation of exact BF16
+products); forward outputs within 2e-3 and gradients within 1e-2
+norm-relative of the oracle, which rounds in the same places (the residual
+difference comes from BF16 roundings of activations that FP32 accumulation
+order tips the other way, and erf/exp in FP32); a short training run lowers
+the loss by 50x."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import mlp_oracle as mo
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def L():
+    from pd_gpu1_gb300._lib import lib
+
+    return lib()
+
+
+def _dev(a, dtype):
+    import torch
+
+    return torch.tensor(np.asarray(a), dtype=dtype, device="cuda")
+
+
+@pytest.mark.parametrize("M,N,K,tr", [(128, 128, 64, 0), (300, 128, 200, 0), (257, 16, 16, 0), (1000, 128, 128, 0),
+                                      (128, 128, 777, 1), (130, 256, 48, 0)])
+def test_gemm_matches_exact(L, M, N, K, tr):
+    import torch
+
+    rng = np.random.default_rng(M + N + K)
+    a = mo.bf16(rng.standard_normal((M, K)).astype(np.float32))
+    b = mo.bf16(rng.standard_normal((N, K)).astype(np.float32))
+    da = _dev(a.T.copy() if tr else a, torch.bfloat16)
+    db = _dev(b, torch.bfloat16)
+    dd = torch.zeros((M, N), dtype=torch.float32, device="cuda")
+    assert L.pd_mlp_gemm(da.data_ptr(), db.data_ptr(), M, N, K, dd.data_ptr(), tr, None) == 0
+    want = a.astype(np.float64) @ b.astype(np.float64).T
+    got = dd.cpu().numpy().astype(np.float64)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()
+
+
+def _net(L, rows):
+    st = C.c_int()
+    n = L.pd_mlp_create(rows, C.byref(st))
+    assert n, st.value
+    return n
+
+
+def _problem(seed, M):
+    rng = np.random.default_rng(seed)
+    x = np.zeros((M, 16), dtype=np.float32)
+    x[:, :8] = rng.uniform(-1, 1, (M, 8))
+    x = mo.bf16(x)
+    t = np.stack([x[:, 0] + 0.3 * np.sin(3 * x[:, 5]), x[:, 1] - 0.2 * x[:, 6] ** 2], axis=1).astype(np.float32)
+    return x, t
+
+
+def test_forward_and_gradient_match_oracle(L):
+    import torch
+
+    M = 777
+    p = mo.init_params(7)
+    rng = np.random.default_rng(11)
+    p = (p + 0.01 * rng.standard_normal(p.size)).astype(np.float32)  # nonzero biases
+    x, t = _problem(5, M)
+    n = _net(L, 1024)
+    assert L.pd_mlp_set_params(n, p.ctypes.data, p.size) == 0
+    dx, dt = _dev(x, torch.bfloat16), _dev(t, torch.float32)
+    dy = torch.zeros((M, 2), dtype=torch.float32, device="cuda")
+    assert L.pd_mlp_forward(n, dx.data_ptr(), M, dy.data_ptr(), None) == 0
+    y_or, _ = mo.forward(p, x[:, :8])
+    y = dy.cpu().numpy()
+    assert np.abs(y - y_or).max() <= 2e-3 * np.abs(y_or).max()
+    g = np.zeros(mo.N_PARAMS, dtype=np.float32)
+    loss = C.c_float()
+    assert L.pd_mlp_grad(n, dx.data_ptr(), dt.data_ptr(), M, g.ctypes.data, C.byref(loss), None) == 0
+    g_or, loss_or = mo.grad(p, x[:, :8], t)
+    assert loss.value == pytest.approx(loss_or, rel=1e-3)
+    for name, (lo, hi) in _slices().items():
+        err = np.linalg.norm(g[lo:hi] - g_or[lo:hi]) / np.linalg.norm(g_or[lo:hi])
+        assert err <= 1e-2, (name, err)
+    L.pd_mlp_destroy(n)
+
+
+def _slices():
+    out, o = {}, 0
+    for name, shape in mo.SHAPES:
+        k = int(np.prod(shape))
+        out[name] = (o, o + k)
+        o += k
+    return out
+
+
+def test_training_lowers_loss(L):
+    import torch
+
+    M = 8192
+    x, t = _problem(9, M)
+    n = _net(L, M)
+    p = mo.init_params(3)
+    assert L.pd_mlp_set_params(n, p.ctypes.data, p.size) == 0
+    dx, dt = _dev(x, torch.bfloat16), _dev(t, torch.float32)
+    loss = C.c_float()
+    first = None
+    for k in range(400):
+        assert L.pd_mlp_train_step(n, dx.data_ptr(), dt.data_ptr(), M, C.c_float(3e-3), C.byref(loss), None) == 0
+        if first is None:
+            first = loss.value
+    assert loss.value < first / 50.0, (first, loss.value)
+    q = np.zeros(mo.N_PARAMS, dtype=np.float32)
+    assert L.pd_mlp_get_params(n, q.ctypes.data, q.size) == 0
+    assert np.isfinite(q).all() and not np.array_equal(q, p)
+    L.pd_mlp_destroy(n)
