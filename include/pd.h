@@ -248,7 +248,7 @@ int pd_adr_solve(pd_ctx* ctx, int ct0, int max_iters, int check_every, double to
                  void* stream);
 typedef struct pd_load_step_stats {
     int32_t iters;      /* ADR steps run                                      */
-    int32_t warm_used;  /* 1: the predicted start was kept                    */
+    int32_t warm_used;  /* 0: plain start; k: the k-th candidate start        */
     double r_plain;     /* residual of the plain start (previous solution)     */
     double r_start;     /* residual of the start used                         */
     double r_final;     /* last residual seen                                 */
@@ -257,12 +257,13 @@ typedef struct pd_load_step_stats {
 /* One load increment: the boundary rows move by +-delta (kernel_quick_load's
  * rows), the ADR state restarts (half-step velocity and old force zero, step
  * index 0), and ADR runs until the residual is <= tol_rel times the plain
- * start's.  With dev_du (device array: N_int x increments, then N_int y
- * increments) the start is the previous solution plus dev_du, unless that
- * start's residual exceeds the plain start's, in which case the plain start
- * is used: the converged answer is the plain method's either way. */
-int pd_load_step(pd_ctx* ctx, double delta, const double* dev_du, double tol_rel, int max_iters, int check_every,
-                 pd_load_step_stats* out, void* stream);
+ * start's.  dev_du holds ncand (0..8) candidate increments on the device,
+ * each N_int x increments then N_int y increments; the start is the previous
+ * solution plus the candidate with the smallest residual, or the previous
+ * solution itself (the plain start) when no candidate's residual is smaller:
+ * the converged answer is the plain method's either way. */
+int pd_load_step(pd_ctx* ctx, double delta, const double* dev_du, int ncand, double tol_rel, int max_iters,
+                 int check_every, pd_load_step_stats* out, void* stream);
 
 /* ---- learned warm start (per-node MLP on the tensor cores) --------------- */
 /* No reference counterpart.  8 -> 128 -> 128 -> 128 -> 2, GELU on the hidden
@@ -295,7 +296,12 @@ int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int6
  * displacement / U, increment / U, damage, loaded-edge flag, x and y over the
  * half sizes, family size / nn_ref; U is the accumulated boundary displacement. */
 int pd_warm_features(pd_ctx* ctx, double U, double delta, double nn_ref, void* dev_x, void* stream);
-/* Predicted increment for pd_load_step: dev_du[2*N_int] = delta * net(features). */
+/* Candidate increments for pd_load_step (ncand = 2): dev_du[0 .. 2*N_int) =
+ * u * delta / U + delta * net(features) on nodes with damage > 0 (u * delta / U
+ * elsewhere), dev_du[2*N_int .. 4*N_int) = u * delta / U.  The skip term is
+ * the proportional (secant) increment, exact for a linear response loaded
+ * proportionally from rest; the network predicts the departure from it next
+ * to cracks (the damage field must be current: pd_damage). */
 int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, double nn_ref, double* dev_du, void* stream);
 
 /* ---- batches of specimens ----------------------------------------------- */

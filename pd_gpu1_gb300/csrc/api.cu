@@ -802,9 +802,11 @@ int pd_adr_solve(pd_ctx* c, int ct0, int max_iters, int check_every, double tol,
     return PD_OK;
 }
 
-int pd_load_step(pd_ctx* c, double delta, const double* dev_du, double tol_rel, int max_iters, int check_every,
-                 pd_load_step_stats* out, void* stream) {
-    if (!c || !out || !(tol_rel > 0.0) || max_iters < 1 || check_every < 1) return PD_ERR_ARG;
+int pd_load_step(pd_ctx* c, double delta, const double* dev_du, int ncand, double tol_rel, int max_iters,
+                 int check_every, pd_load_step_stats* out, void* stream) {
+    if (!c || !out || !(tol_rel > 0.0) || max_iters < 1 || check_every < 1 || ncand < 0 || ncand > 8 ||
+        (ncand > 0 && !dev_du))
+        return PD_ERR_ARG;
     if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "load stepping of a batch: not provided");
     if (c->p.mass == 0.0) return set_err(c, PD_ERR_ARG, "ADR needs the fictitious mass (bond-based parameters)");
     StreamScope sc(c, stream);
@@ -825,25 +827,33 @@ int pd_load_step(pd_ctx* c, double delta, const double* dev_du, double tol_rel, 
     c->pos_valid = false;
     if (!rc) rc = residual_now(c, s, &st.r_plain);
     st.r_start = st.r_plain;
-    if (!rc && dev_du) {
-        // start from the previous solution plus the predicted increment, unless
-        // its residual is larger than the plain start's
+    if (!rc && ncand > 0) {
+        // candidate starts: previous solution plus each predicted increment;
+        // the one with the smallest residual is kept, the plain start unless
+        // a candidate's residual is smaller
         cudaError_t e = cudaMallocAsync(&saved, 2 * ni * sizeof(double), s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(saved, c->nf[PD_F_UX], ni * 8, cudaMemcpyDeviceToDevice, s);
         if (e == cudaSuccess) e = cudaMemcpyAsync(saved + ni, c->nf[PD_F_UY], ni * 8, cudaMemcpyDeviceToDevice, s);
         rc = cuda_err(c, e, "warm start save");
-        if (!rc) rc = add_increment(c, dev_du, s);
-        c->pos_valid = false;
-        double rw = 0.0;
-        if (!rc) rc = residual_now(c, s, &rw);
-        if (!rc && rw <= st.r_plain) {
-            st.warm_used = 1;
-            st.r_start = rw;
-        } else if (!rc) {
-            e = cudaMemcpyAsync(c->nf[PD_F_UX], saved, ni * 8, cudaMemcpyDeviceToDevice, s);
-            if (e == cudaSuccess) e = cudaMemcpyAsync(c->nf[PD_F_UY], saved + ni, ni * 8, cudaMemcpyDeviceToDevice, s);
-            rc = cuda_err(c, e, "warm start restore");
+        auto restore = [&]() -> int {
+            cudaError_t r = cudaMemcpyAsync(c->nf[PD_F_UX], saved, ni * 8, cudaMemcpyDeviceToDevice, s);
+            if (r == cudaSuccess) r = cudaMemcpyAsync(c->nf[PD_F_UY], saved + ni, ni * 8, cudaMemcpyDeviceToDevice, s);
             c->pos_valid = false;
+            return cuda_err(c, r, "warm start restore");
+        };
+        for (int k = 0; k < ncand && !rc; k++) {
+            if (k > 0) rc = restore();
+            if (!rc) rc = add_increment(c, dev_du + (int64_t)k * 2 * ni, s);
+            double rw = 0.0;
+            if (!rc) rc = residual_now(c, s, &rw);
+            if (!rc && rw < st.r_start) {
+                st.warm_used = k + 1;
+                st.r_start = rw;
+            }
+        }
+        if (!rc && st.warm_used != ncand) {  // bring back the chosen start
+            rc = restore();
+            if (!rc && st.warm_used > 0) rc = add_increment(c, dev_du + (int64_t)(st.warm_used - 1) * 2 * ni, s);
         }
     }
     if (saved) cudaFreeAsync(saved, s);

@@ -326,10 +326,23 @@ __global__ void k_features(int64_t n, const double* __restrict__ x, const double
     }
 }
 
-__global__ void k_scale_out(int64_t n, const float* __restrict__ y, double delta, double* __restrict__ du) {
+// du = delta * net + u_prev * (delta / U): the network's output is the
+// correction to the proportional (secant) increment, which the skip term adds
+// in FP64.  The correction applies to nodes with damage (next to a crack,
+// where large crack-face rotations make the response depart from
+// proportionality); elsewhere the skip term stands alone, so BF16-level
+// output noise never reaches the undamaged bulk.  The skip term alone is
+// written as the second candidate.
+__global__ void k_scale_out(int64_t n, const float* __restrict__ y, double delta, double ratio,
+                            const double* __restrict__ ux, const double* __restrict__ uy,
+                            const double* __restrict__ dmg, double* __restrict__ du) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        du[i] = delta * (double)y[i * kOut];
-        du[n + i] = delta * (double)y[i * kOut + 1];
+        const double sx = ux[i] * ratio, sy = uy[i] * ratio;
+        const bool near_crack = dmg[i] > 0.0;
+        du[i] = near_crack ? fma(delta, (double)y[i * kOut], sx) : sx;
+        du[n + i] = near_crack ? fma(delta, (double)y[i * kOut + 1], sy) : sy;
+        du[2 * n + i] = sx;
+        du[3 * n + i] = sy;
     }
 }
 
@@ -650,7 +663,8 @@ int pd_warm_features(pd_ctx* c, double U, double delta, double nn_ref, void* dev
 }
 
 // Predicted increment of the free nodes: features, forward pass, then
-// du = delta * output (x components, then y components, as doubles).
+// du = delta * output + u * delta / U (x components, then y components): the
+// network predicts the departure from proportional loading.
 int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref, double* dev_du, void* stream) {
     if (!c || !n || !dev_du) return PD_ERR_ARG;
     cudaStream_t s = st(stream);
@@ -665,7 +679,8 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
     int rc = pd_warm_features(c, U, delta, nn_ref, x, s);
     if (!rc) rc = pd_mlp_forward(n, x, ni, y, s);
     if (!rc) {
-        k_scale_out<<<(unsigned)std::min<int64_t>((ni + 255) / 256, 4096), 256, 0, s>>>(ni, y, delta, dev_du);
+        k_scale_out<<<(unsigned)std::min<int64_t>((ni + 255) / 256, 4096), 256, 0, s>>>(
+            ni, y, delta, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], c->nf[PD_F_DMG], dev_du);
         c->launches++;
         rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
     } else {

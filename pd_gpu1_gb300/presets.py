@@ -238,21 +238,23 @@ def build_specimen(base, sp, derive=None):
 
 
 # ---- quasi-static crack-growth plate for the learned ADR warm start ----------------
-def build_warm_start_plate(scale=1.0, dx=1e-4, E=192.0e9, G0=3.0e4, derive=None):
+def build_warm_start_plate(scale=1.0, dx=1e-4, E=192.0e9, G0=2.65e3, crack_frac=0.2, derive=None):
     """0.1 x 0.1 m plate, dx = 1e-4 (1000 x 1000 nodes) plus 3 boundary rows
     above and below (the crack-plate layout, Coord.cu:34-45), 2-D PMB,
     thickness dx, nu = 1/3, s0 from G0 by the 2-D closed form, an edge
     pre-crack 0.02 m long from the left edge along the mid-line, surface
     correction on, ADR with dt = 1.  Loaded in 200 equal increments of the
     boundary rows to 1e-4 m (each increment moves the rows by +-5e-7 m).
-    ``scale`` shrinks the plate and the crack together (same dx)."""
+    ``scale`` shrinks the plate and the crack together (same dx).  G0 is
+    chosen so that the pre-crack starts to grow within the loading (bond
+    stretch at the tip ~ 8x the nominal strain; s0 = 8e-3)."""
     L = 0.1 * scale
     delta = 3.015 * dx
     s0 = s0_2d(G0, E, delta)
     p = _derive(derive)(2, PD_MODEL_BOND, PD_MODE_STATIC, 1.0, 200, dx, 0.0, dx, L, L, 0.0, E, 1.0 / 3.0, 8000.0,
                         s0)
     p.N = p.N_int + 6 * p.nx
-    crack = 0.2 * L
+    crack = crack_frac * L
 
     def setup(eng):
         eng.coord_plate_crack()

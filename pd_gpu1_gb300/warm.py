@@ -1,0 +1,253 @@
+"""Learned ADR warm start: quasi-static load stepping, training data from the
+solver's own converged states, training and inference of the per-node MLP on
+the tensor cores (``pd_mlp_*`` / ``pd_warm_*`` in include/pd.h).
+
+A load increment moves the boundary rows by +-delta and is solved by ADR to
+``|F + b| <= tol * |F + b|_plain`` (``pd_load_step``).  The plain start is the
+previous converged solution; the learned start adds the network's predicted
+increment ``delta * net(features)`` and is kept only when its residual is
+not larger than the plain start's, so the converged answer is the plain
+method's.  Features (``pd_warm_features``) and targets are normalised:
+features use the accumulated boundary displacement U of the previous
+increment.  The prediction is ``u * delta / U + delta * net(features)``: a
+skip term, the proportional (secant) increment, plus the network's output
+on the nodes with damage (next to cracks), so the target of training is the
+converged increment over delta minus ``u / U`` on those nodes — zero while
+the plate responds linearly to proportional loading, nonzero where large
+crack-face rotations make the response depart from proportionality.  Increments in which a crack advances
+(bonds break during the increment) are left out of training: no local
+predictor sees them coming.  pd_load_step receives two candidates, the
+network's prediction and the skip term alone, and keeps whichever start
+(or the plain one) has the smallest residual.
+
+No reference counterpart: the reference runs a fixed number of ADR steps
+(Solve_Plate_Tensile.cu:106-131).
+
+  python -m pd_gpu1_gb300.warm train [--out PATH]   # generate data, train, save
+"""
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import time
+
+import numpy as np
+
+from . import presets
+from ._lib import check, lib
+from .engine import Engine
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+WEIGHTS = os.path.join(HERE, "data", "warm_mlp_params.f32")
+N_PARAMS = 34434
+
+
+def init_params(seed=0):
+    """He-normal hidden weights, zero output layer (the prediction starts at
+    the skip term), zero biases, in the flat order of pd_mlp_set_params."""
+    rng = np.random.default_rng(seed)
+    parts = []
+    for fan_out, fan_in in ((128, 8), (128, 128), (128, 128), (2, 128)):
+        scale = 0.0 if fan_out == 2 else math.sqrt(2.0 / fan_in)
+        parts.append(rng.standard_normal(fan_out * fan_in) * scale)
+        parts.append(np.zeros(fan_out))
+    p = np.concatenate(parts).astype(np.float32)
+    assert p.size == N_PARAMS
+    return p
+
+
+class Net:
+    """A pd_mlp handle (parameters, optimizer state, activation buffers)."""
+
+    def __init__(self, max_rows=65536, params=None):
+        self.L = lib()
+        st = C.c_int()
+        self.h = self.L.pd_mlp_create(max_rows, C.byref(st))
+        if not self.h:
+            check(st.value, None, "pd_mlp_create")
+        self.max_rows = max_rows
+        self.set_params(init_params() if params is None else params)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.pd_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        check(self.L.pd_mlp_set_params(self.h, p.ctypes.data, p.size), None, "pd_mlp_set_params")
+
+    def params(self):
+        p = np.zeros(N_PARAMS, dtype=np.float32)
+        check(self.L.pd_mlp_get_params(self.h, p.ctypes.data, p.size), None, "pd_mlp_get_params")
+        return p
+
+    def save(self, path=WEIGHTS):
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        self.params().tofile(path)
+
+    @classmethod
+    def load(cls, path=WEIGHTS, max_rows=65536):
+        p = np.fromfile(path, dtype=np.float32)
+        if p.size != N_PARAMS:
+            raise ValueError(f"{path}: {p.size} parameters, expected {N_PARAMS}")
+        return cls(max_rows, p)
+
+    def train_step(self, x_ptr, t_ptr, rows, lr, stream=None):
+        loss = C.c_float()
+        check(self.L.pd_mlp_train_step(self.h, x_ptr, t_ptr, rows, C.c_float(lr), C.byref(loss), stream), None,
+              "pd_mlp_train_step")
+        return loss.value
+
+
+def nn_reference(eng):
+    """Bulk family size (the largest row of the free nodes)."""
+    return float(eng.get("NN")[: eng.p.N_int].max())
+
+
+def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1e-6, max_iters=400000,
+                   check_every=100, keep=1.0, seed=0, start=0):
+    """Solve n_inc load increments on a set-up engine.
+
+    mode: "plain" (previous solution); "learned" (the two candidates of
+    pd_warm_predict, network + skip term and skip term alone, against the
+    plain start; net required); "network" / "secant" (one of the two alone,
+    for ablations); "extrapolate" (previous solution plus the previous
+    increment: used to generate training states quickly).  collect: a list that receives (features, targets) device
+    tensors of a random ``keep`` fraction of the damaged free nodes per
+    increment without crack advance.
+    Returns the per-increment statistics of pd_load_step."""
+    import torch
+
+    L = lib()
+    p = eng.p
+    ni = p.N_int
+    delta = meta["delta"]
+    nnref = nn_reference(eng)
+    rng = np.random.default_rng(seed)
+    du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")  # two candidates
+    X = torch.zeros((ni, 16), dtype=torch.bfloat16, device="cuda") if collect is not None else None
+    prev = None
+    out = []
+    for k in range(start, start + n_inc):
+        U = k * delta  # accumulated boundary displacement before this increment
+        ptr = None
+        u0 = None
+        if U > 0.0 and (mode in ("learned", "network", "secant") or collect is not None):
+            eng.damage()
+        if U > 0.0 and collect is not None:
+            check(L.pd_warm_features(eng.ctx, U, delta, nnref, X.data_ptr(), eng.stream), eng.ctx,
+                  "pd_warm_features")
+        if collect is not None or mode == "extrapolate":
+            u0 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+        t0 = time.perf_counter()
+        ncand = 1
+        if collect is not None:
+            broken0 = int((eng.get("FAIL") == 0).sum())
+        if mode in ("learned", "network", "secant") and U > 0.0:
+            check(L.pd_warm_predict(eng.ctx, net.h, U, delta, nnref, du.data_ptr(), eng.stream), eng.ctx,
+                  "pd_warm_predict")
+            ptr = du.data_ptr()  # "network": the network's start against the plain start
+            if mode == "learned":  # both candidates
+                ncand = 2
+            if mode == "secant":  # the skip term alone
+                ptr = du.data_ptr() + 2 * ni * 8
+        elif mode == "extrapolate" and prev is not None:
+            du[: 2 * ni].copy_(torch.from_numpy(prev))
+            ptr = du.data_ptr()
+        st = eng.load_step(delta, ptr, tol, max_iters, check_every, ncand)
+        st["wall_ms"] = (time.perf_counter() - t0) * 1e3
+        st["increment"] = k
+        if u0 is not None:
+            u1 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+            prev = u1 - u0
+            if collect is not None and U > 0.0:
+                tt = prev / delta - u0 / U  # departure from the proportional increment
+                st["max_target"] = float(np.abs(tt).max())
+                st["advanced"] = int((eng.get("FAIL") == 0).sum()) - broken0  # bonds broken in the increment
+                if st["advanced"] == 0:
+                    # nodes next to a crack (the correction applies there only)
+                    near = np.nonzero(eng.get("DMG")[:ni] > 0.0)[0]
+                    idx = np.sort(rng.choice(near, max(1, int(keep * len(near))), replace=False))
+                    t = np.stack([tt[idx], tt[ni + idx]], axis=1).astype(np.float32)
+                    ii = torch.from_numpy(idx).cuda()
+                    collect.append((X.index_select(0, ii).clone(), torch.from_numpy(t).cuda()))
+        out.append(st)
+    return out
+
+
+def train(X, T, steps=3000, batch=16384, lr=2e-3, seed=0, log=None):
+    """Adam on the mean squared error over (X, T) device tensors (BF16 [S][16],
+    FP32 [S][2]); cosine learning-rate decay.  Returns the trained Net."""
+    import torch
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    net = Net(batch, init_params(seed))
+    S = X.shape[0]
+    for k in range(steps):
+        idx = torch.randint(0, S, (batch,), device="cuda", generator=g)
+        xb = X.index_select(0, idx).contiguous()
+        tb = T.index_select(0, idx).contiguous()
+        a = lr * 0.5 * (1.0 + math.cos(math.pi * k / steps))
+        loss = net.train_step(xb.data_ptr(), tb.data_ptr(), batch, a)
+        if log is not None and (k % 250 == 0 or k == steps - 1):
+            log.append((k, loss))
+    return net
+
+
+TRAIN_RUNS = [  # (scale, crack fraction, seed): 100k-1M-node plates of the same set-up
+    (0.32, 0.20, 1), (0.32, 0.15, 2), (0.32, 0.25, 3), (0.5, 0.20, 4),
+]
+
+
+def generate(runs=TRAIN_RUNS, n_inc=200, keep=1.0, log=print):
+    """Converged states of seeded load-stepping runs -> (X, T) device tensors."""
+    import torch
+
+    data = []
+    for scale, frac, seed in runs:
+        p, setup, meta = presets.build_warm_start_plate(scale=scale, crack_frac=frac)
+        with Engine(p) as eng:
+            setup(eng)
+            t0 = time.perf_counter()
+            st = run_increments(eng, meta, n_inc, mode="extrapolate", collect=data, keep=keep, seed=seed)
+            broken = int((eng.get("FAIL") == 0).sum())
+        jumps = [(s["increment"], s["iters"], s.get("advanced", 0), round(s.get("max_target", 0.0), 2))
+                 for s in st if s.get("advanced", 0) > 0]
+        log(json.dumps({"run": [scale, frac, seed], "nodes": p.N, "increments": n_inc,
+                        "iters": int(sum(s["iters"] for s in st)), "max_iters": int(max(s["iters"] for s in st)),
+                        "seconds": round(time.perf_counter() - t0, 1), "broken_bonds": broken,
+                        "left_out": jumps[:20], "n_left_out": len(jumps),
+                        "max_target_kept": round(max([s.get("max_target", 0.0) for s in st
+                                                      if s.get("advanced", 1) == 0] + [0.0]), 3)}))
+    X = torch.cat([d[0] for d in data])
+    T = torch.cat([d[1] for d in data])
+    return X, T
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("--out", default=WEIGHTS)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--increments", type=int, default=200)
+    args = ap.parse_args()
+    t0 = time.perf_counter()
+    X, T = generate(n_inc=args.increments)
+    print(json.dumps({"samples": int(X.shape[0]), "seconds": round(time.perf_counter() - t0, 1)}), flush=True)
+    log = []
+    net = train(X, T, steps=args.steps, log=log)
+    net.save(args.out)
+    print(json.dumps({"loss": log, "out": args.out}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
