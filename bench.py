@@ -524,9 +524,12 @@ def batch_arm(args):
 def warm_arm(args):
     """ADR wall-time per load increment to a 1e-6 relative residual on the
     1M-node warm-start plate: plain start (previous solution) against the
-    learned start (network shipped in pd_gpu1_gb300/data), increments
-    1..K after the common first one."""
-    import ctypes as C
+    learned start (network shipped in pd_gpu1_gb300/data).  Increments
+    0..W-1 are solved first (untimed: increment 0 has no history); each timed
+    increment W+j is then solved twice from the same converged state (a
+    snapshot), once from each start, and the learned run's state carries on."""
+    import os
+    import tempfile
 
     import torch
 
@@ -546,64 +549,67 @@ def warm_arm(args):
     L = lib()
     p, setup, meta = presets.build_warm_start_plate(scale=args.scale)
     net = warm.Net.load()
-    K = args.increments
-    res = {}
+    K, W = args.increments, args.warm_increments
+    snap = os.path.join(tempfile.mkdtemp(), "state.snap")
     clocks = ClockSampler(torch.cuda.current_device())
-    clocks.start()
-    for mode in ("plain", "learned"):
-        with E.Engine(p) as eng:
-            setup(eng)
-            B = int(eng.get("ROWPTR")[p.N_int])
-            torch.cuda.synchronize()
-            st = warm.run_increments(eng, meta, K + 1, mode=mode, net=net)
-            res[mode] = st
-            if mode == "learned":
-                # the network's inference alone (features + 4 tcgen05 products + candidates)
-                du = torch.zeros(4 * p.N_int, dtype=torch.float64, device="cuda")
-                eng.damage()
-                U = (K + 1) * meta["delta"]
-                nnref = warm.nn_reference(eng)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                for _ in range(5):
-                    L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], nnref, du.data_ptr(), None)
-                e1.record()
-                torch.cuda.synchronize()
-                infer_ms = e0.elapsed_time(e1) / 5
-                # e2e: the same increments through the C ABI with the displacement
-                # field read back to pinned host memory after each increment
-                n = p.N
-                pin = torch.zeros(n, dtype=torch.float64).pin_memory()
-                t0 = time.perf_counter()
-                for j in range(2):
-                    warm.run_increments(eng, meta, 1, mode=mode, net=net, start=K + 1 + j)
-                    eng._c(L.pd_get_field(eng.ctx, FIELD["UY"], pin.data_ptr(), n, None), "pd_get_field")
-                res["e2e"] = ((time.perf_counter() - t0) * 1e3 / 2, None)
-    clk = clocks.stop()
-    plain_ms = np.array([s["ms"] for s in res["plain"][1:]])
-    learned_ms = np.array([s["ms"] for s in res["learned"][1:]])
+    rows = []
+    with E.Engine(p) as eng:
+        setup(eng)
+        B = int(eng.get("ROWPTR")[p.N_int])
+        pre = warm.run_increments(eng, meta, W, mode="learned", net=net)
+        clocks.start()
+        for j in range(K):
+            eng.snapshot_save(snap)
+            plain = warm.run_increments(eng, meta, 1, mode="plain", start=W + j)[0]
+            eng.snapshot_load(snap)
+            learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j)[0]
+            rows.append((plain, learned))
+        clk = clocks.stop()
+        # the network's inference alone (features, four tcgen05 products, candidates)
+        du = torch.zeros(4 * p.N_int, dtype=torch.float64, device="cuda")
+        eng.damage()
+        U = (W + K) * meta["delta"]
+        nnref = warm.nn_reference(eng)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], nnref, du.data_ptr(), None)
+        e1.record()
+        torch.cuda.synchronize()
+        infer_ms = e0.elapsed_time(e1) / 5
+        # e2e: further increments through the C ABI, the displacement field read
+        # back to pinned host memory after each one
+        n = p.N
+        pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+        t0 = time.perf_counter()
+        for j in range(2):
+            warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + K + j)
+            eng._c(L.pd_get_field(eng.ctx, FIELD["UY"], pin.data_ptr(), n, None), "pd_get_field")
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / 2
+    os.remove(snap)
+    plain_ms = np.array([r[0]["ms"] for r in rows])
+    learned_ms = np.array([r[1]["ms"] for r in rows])
     flops = 2.0 * p.N_int * (16 * 128 + 2 * 128 * 128 + 128 * 16)
     peaks, peak_kind = measured_peaks()
     line = {
         "metric": "ADR wall-time to a 1e-6 relative residual per load increment, learned start",
-        "value": float(learned_ms.mean()), "unit": "ms", "n_gpus": world, "steps": K, "warmup": 1,
+        "value": float(learned_ms.mean()), "unit": "ms", "n_gpus": world, "steps": K, "warmup": W,
         "ms_per_step": float(learned_ms.mean()), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64 (solver); bf16 x bf16 -> f32 (network)", "data": "synthetic (deterministic lattice)",
         "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "increment_m": meta["delta"],
-                   "tol": 1e-6, "increments_timed": K, "first_increment": "common plain start, not timed"},
-        "plain": {"ms_per_increment": float(plain_ms.mean()),
-                  "iters": [s["iters"] for s in res["plain"][1:]]},
-        "learned": {"ms_per_increment": float(learned_ms.mean()), "iters": [s["iters"] for s in res["learned"][1:]],
-                    "candidate_used": [s["warm_used"] for s in res["learned"][1:]],
-                    "r_start_over_r_plain": [s["r_start"] / s["r_plain"] for s in res["learned"][1:]]},
+                   "tol": 1e-6, "timed_increments": list(range(W, W + K)),
+                   "untimed_increments_first": W, "untimed_iters": [s["iters"] for s in pre]},
+        "plain": {"ms_per_increment": float(plain_ms.mean()), "iters": [r[0]["iters"] for r in rows]},
+        "learned": {"ms_per_increment": float(learned_ms.mean()), "iters": [r[1]["iters"] for r in rows],
+                    "candidate_used": [r[1]["warm_used"] for r in rows],
+                    "r_start_over_r_plain": [r[1]["r_start"] / r[1]["r_plain"] for r in rows]},
         "speedup_vs_plain": float(plain_ms.mean() / learned_ms.mean()),
         "roofline": {"bound": "tensor", "kernel": "k_gemm (network inference, all four layers)",
                      "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks.get("bf16_tflops"),
                      "unit": "TFLOP/s", "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1.0),
                      "traffic": None, "peak_source": peak_kind, "inference_ms": infer_ms,
-                     "note": "inference is <1 % of an increment; the increment is bound by the ADR force kernel"},
-        "e2e": {"value": res["e2e"][0], "unit": "ms", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": p.N * 8},
+                     "note": "inference is <1 % of an increment; an increment is bound by the ADR force kernel"},
+        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": p.N * 8},
         "gpu_launches": None, "clocks": clk, "cpu_baseline": None,
     }
     if rank == 0:
@@ -799,6 +805,8 @@ def main():
     ap.add_argument("--seq-steps", type=int, default=100, help="batch workload: steps per plate when run one "
                                                                 "after another")
     ap.add_argument("--increments", type=int, default=3, help="warm_start workload: timed load increments")
+    ap.add_argument("--warm-increments", type=int, default=10, help="warm_start workload: increments solved "
+                                                                     "before the timed ones")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

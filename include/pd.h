@@ -247,8 +247,10 @@ int pd_residual(pd_ctx* ctx, double* norm, void* stream);
 int pd_adr_solve(pd_ctx* ctx, int ct0, int max_iters, int check_every, double tol, int* iters, double* norm,
                  void* stream);
 typedef struct pd_load_step_stats {
-    int32_t iters;      /* ADR steps run                                      */
+    int32_t iters;      /* ADR steps run (probes included)                    */
     int32_t warm_used;  /* 0: plain start; k: the k-th candidate start        */
+    int32_t probes;     /* candidates probed (rule 2)                         */
+    int32_t pad_;
     double r_plain;     /* residual of the plain start (previous solution)     */
     double r_start;     /* residual of the start used                         */
     double r_final;     /* last residual seen                                 */
@@ -258,12 +260,18 @@ typedef struct pd_load_step_stats {
  * rows), the ADR state restarts (half-step velocity and old force zero, step
  * index 0), and ADR runs until the residual is <= tol_rel times the plain
  * start's.  dev_du holds ncand (0..8) candidate increments on the device,
- * each N_int x increments then N_int y increments; the start is the previous
- * solution plus the candidate with the smallest residual, or the previous
- * solution itself (the plain start) when no candidate's residual is smaller:
- * the converged answer is the plain method's either way. */
-int pd_load_step(pd_ctx* ctx, double delta, const double* dev_du, int ncand, double tol_rel, int max_iters,
-                 int check_every, pd_load_step_stats* out, void* stream);
+ * each N_int x increments then N_int y increments; a candidate start is the
+ * previous solution plus the candidate.  Rule 1: a candidate whose start has
+ * a larger residual than the plain start (the previous solution) is dropped;
+ * with none left the plain start is used.  Rule 2: of several admissible
+ * candidates, the one with the smallest starting residual is used when
+ * probe_iters is 0; otherwise each runs probe_iters ADR steps and the one
+ * with the lowest residual after them continues from where its probe ended
+ * (the starting residual says little about how fast ADR converges: smooth
+ * errors have small residuals and decay slowly).  The converged answer is the
+ * plain method's in every case: all starts stop at the same residual. */
+int pd_load_step(pd_ctx* ctx, double delta, const double* dev_du, int ncand, int probe_iters, double tol_rel,
+                 int max_iters, int check_every, pd_load_step_stats* out, void* stream);
 
 /* ---- learned warm start (per-node MLP on the tensor cores) --------------- */
 /* No reference counterpart.  8 -> 128 -> 128 -> 128 -> 2, GELU on the hidden
@@ -297,11 +305,12 @@ int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int6
  * half sizes, family size / nn_ref; U is the accumulated boundary displacement. */
 int pd_warm_features(pd_ctx* ctx, double U, double delta, double nn_ref, void* dev_x, void* stream);
 /* Candidate increments for pd_load_step (ncand = 2): dev_du[0 .. 2*N_int) =
- * u * delta / U + delta * net(features) on nodes with damage > 0 (u * delta / U
- * elsewhere), dev_du[2*N_int .. 4*N_int) = u * delta / U.  The skip term is
- * the proportional (secant) increment, exact for a linear response loaded
- * proportionally from rest; the network predicts the departure from it next
- * to cracks (the damage field must be current: pd_damage). */
+ * u * delta / U + U * net(features), dev_du[2*N_int .. 4*N_int) = u * delta / U.
+ * The skip term is the proportional (secant) increment, exact for a linear
+ * response loaded proportionally from rest; the network predicts the
+ * departure from proportionality per unit of accumulated boundary
+ * displacement (the geometric nonlinearity of the bonds makes it grow with
+ * the load: u = a U + b U^2 departs by b U delta per increment). */
 int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, double nn_ref, double* dev_du, void* stream);
 
 /* ---- batches of specimens ----------------------------------------------- */

@@ -103,7 +103,8 @@ class PDLoadStepStats(C.Structure):
     """pd_load_step_stats: one quasi-static load increment."""
 
     _fields_ = [
-        ("iters", C.c_int32), ("warm_used", C.c_int32), ("r_plain", C.c_double), ("r_start", C.c_double),
+        ("iters", C.c_int32), ("warm_used", C.c_int32), ("probes", C.c_int32), ("pad_", C.c_int32),
+        ("r_plain", C.c_double), ("r_start", C.c_double),
         ("r_final", C.c_double), ("ms", C.c_double),
     ]
 

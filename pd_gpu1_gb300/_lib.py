@@ -64,7 +64,7 @@ _SIGS = {
     "pd_run_explicit": (I32, [VP, I32, D, I32, VP]),
     "pd_residual": (I32, [VP, P(D), VP]),
     "pd_adr_solve": (I32, [VP, I32, I32, I32, D, P(I32), P(D), VP]),
-    "pd_load_step": (I32, [VP, D, VP, I32, D, I32, I32, P(PDLoadStepStats), VP]),
+    "pd_load_step": (I32, [VP, D, VP, I32, I32, D, I32, I32, P(PDLoadStepStats), VP]),
     "pd_mlp_create": (VP, [I64, P(I32)]),
     "pd_mlp_destroy": (I32, [VP]),
     "pd_mlp_num_params": (I32, []),

@@ -802,10 +802,10 @@ int pd_adr_solve(pd_ctx* c, int ct0, int max_iters, int check_every, double tol,
     return PD_OK;
 }
 
-int pd_load_step(pd_ctx* c, double delta, const double* dev_du, int ncand, double tol_rel, int max_iters,
-                 int check_every, pd_load_step_stats* out, void* stream) {
+int pd_load_step(pd_ctx* c, double delta, const double* dev_du, int ncand, int probe_iters, double tol_rel,
+                 int max_iters, int check_every, pd_load_step_stats* out, void* stream) {
     if (!c || !out || !(tol_rel > 0.0) || max_iters < 1 || check_every < 1 || ncand < 0 || ncand > 8 ||
-        (ncand > 0 && !dev_du))
+        (ncand > 0 && !dev_du) || probe_iters < 0 || probe_iters >= max_iters)
         return PD_ERR_ARG;
     if (c->batch.count) return set_err(c, PD_ERR_UNSUPPORTED, "load stepping of a batch: not provided");
     if (c->p.mass == 0.0) return set_err(c, PD_ERR_ARG, "ADR needs the fictitious mass (bond-based parameters)");
@@ -818,46 +818,89 @@ int pd_load_step(pd_ctx* c, double delta, const double* dev_du, int ncand, doubl
     pd_load_step_stats st{};
     int rc = ensure_ready(c, s);
     const int64_t ni = c->p.N_int;
-    double* saved = nullptr;
+    double* saved = nullptr;  // [0, 2 ni): previous solution; [2 ni, 8 ni): best probed state
     // the increment: boundary rows move by +-delta (kernel_quick_load), ADR restarts
     if (!rc) rc = launch_quick_load(c, delta / c->p.dt, s);
     const int zero[] = {PD_F_VHX, PD_F_VHY, PD_F_VHZ, PD_F_FOX, PD_F_FOY, PD_F_FOZ};
-    for (int k = 0; k < 6 && !rc; k++)
-        rc = cuda_err(c, cudaMemsetAsync(c->nf[zero[k]], 0, c->p.N * sizeof(double), s), "ADR restart");
+    auto restart = [&]() -> int {
+        for (int k = 0; k < 6; k++) {
+            cudaError_t e = cudaMemsetAsync(c->nf[zero[k]], 0, c->p.N * sizeof(double), s);
+            if (e != cudaSuccess) return cuda_err(c, e, "ADR restart");
+        }
+        return PD_OK;
+    };
+    if (!rc) rc = restart();
     c->pos_valid = false;
     if (!rc) rc = residual_now(c, s, &st.r_plain);
     st.r_start = st.r_plain;
+    int ct0 = 0;
     if (!rc && ncand > 0) {
-        // candidate starts: previous solution plus each predicted increment;
-        // the one with the smallest residual is kept, the plain start unless
-        // a candidate's residual is smaller
-        cudaError_t e = cudaMallocAsync(&saved, 2 * ni * sizeof(double), s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(saved, c->nf[PD_F_UX], ni * 8, cudaMemcpyDeviceToDevice, s);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(saved + ni, c->nf[PD_F_UY], ni * 8, cudaMemcpyDeviceToDevice, s);
-        rc = cuda_err(c, e, "warm start save");
-        auto restore = [&]() -> int {
-            cudaError_t r = cudaMemcpyAsync(c->nf[PD_F_UX], saved, ni * 8, cudaMemcpyDeviceToDevice, s);
-            if (r == cudaSuccess) r = cudaMemcpyAsync(c->nf[PD_F_UY], saved + ni, ni * 8, cudaMemcpyDeviceToDevice, s);
-            c->pos_valid = false;
-            return cuda_err(c, r, "warm start restore");
-        };
-        for (int k = 0; k < ncand && !rc; k++) {
-            if (k > 0) rc = restore();
-            if (!rc) rc = add_increment(c, dev_du + (int64_t)k * 2 * ni, s);
-            double rw = 0.0;
-            if (!rc) rc = residual_now(c, s, &rw);
-            if (!rc && rw < st.r_start) {
-                st.warm_used = k + 1;
-                st.r_start = rw;
+        cudaError_t e = cudaMallocAsync(&saved, 8 * ni * sizeof(double), s);
+        rc = cuda_err(c, e, "warm start scratch");
+        const int state[] = {PD_F_UX, PD_F_UY, PD_F_VHX, PD_F_VHY, PD_F_FOX, PD_F_FOY};
+        auto copy_state = [&](int nfields, double* dst, bool to_ctx) -> int {
+            for (int k = 0; k < nfields; k++) {
+                double* f = c->nf[state[k]];
+                cudaError_t r = to_ctx ? cudaMemcpyAsync(f, dst + k * ni, ni * 8, cudaMemcpyDeviceToDevice, s)
+                                       : cudaMemcpyAsync(dst + k * ni, f, ni * 8, cudaMemcpyDeviceToDevice, s);
+                if (r != cudaSuccess) return cuda_err(c, r, "warm start state copy");
             }
+            c->pos_valid = false;
+            return PD_OK;
+        };
+        if (!rc) rc = copy_state(2, saved, false);
+        // rule 1: a candidate is admissible when its start's residual is not
+        // larger than the plain start's
+        std::vector<int> ok;
+        std::vector<double> rw(ncand, HUGE_VAL);
+        for (int k = 0; k < ncand && !rc; k++) {
+            if (k > 0) rc = copy_state(2, saved, true);
+            if (!rc) rc = add_increment(c, dev_du + (int64_t)k * 2 * ni, s);
+            if (!rc) rc = residual_now(c, s, &rw[k]);
+            if (!rc && rw[k] <= st.r_plain) ok.push_back(k);
         }
-        if (!rc && st.warm_used != ncand) {  // bring back the chosen start
-            rc = restore();
+        if (!rc && ok.size() == 1) {
+            st.warm_used = ok[0] + 1;
+        } else if (!rc && ok.size() > 1 && probe_iters == 0) {
+            int best = ok[0];
+            for (int k : ok)
+                if (rw[k] < rw[best]) best = k;
+            st.warm_used = best + 1;
+        } else if (!rc && ok.size() > 1) {
+            // rule 2: among several admissible starts, the one whose residual is
+            // lowest after probe_iters ADR steps; its state after the probe is kept
+            double best_r = HUGE_VAL;
+            for (int k : ok) {
+                if ((rc = copy_state(2, saved, true)) || (rc = add_increment(c, dev_du + (int64_t)k * 2 * ni, s)) ||
+                    (rc = restart()))
+                    break;
+                int it = 0;
+                double r = 0.0;
+                if ((rc = pd_adr_solve(c, 0, probe_iters, probe_iters, 0.0, &it, &r, s))) break;
+                st.iters += it;
+                st.probes++;
+                if (r < best_r) {
+                    best_r = r;
+                    st.warm_used = k + 1;
+                    if ((rc = copy_state(6, saved + 2 * ni, false))) break;
+                }
+            }
+            if (!rc) rc = copy_state(6, saved + 2 * ni, true);
+            ct0 = probe_iters;
+        }
+        if (!rc && st.warm_used > 0) st.r_start = rw[st.warm_used - 1];
+        if (!rc && st.probes == 0) {  // bring back the chosen start (or the plain one)
+            rc = copy_state(2, saved, true);
             if (!rc && st.warm_used > 0) rc = add_increment(c, dev_du + (int64_t)(st.warm_used - 1) * 2 * ni, s);
         }
     }
     if (saved) cudaFreeAsync(saved, s);
-    if (!rc) rc = pd_adr_solve(c, 0, max_iters, check_every, tol_rel * st.r_plain, &st.iters, &st.r_final, s);
+    if (!rc) {
+        int it = 0;
+        rc = pd_adr_solve(c, ct0, std::max(1, max_iters - st.iters), check_every, tol_rel * st.r_plain, &it,
+                          &st.r_final, s);
+        st.iters += it;
+    }
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
     float ms = 0.f;

@@ -326,21 +326,18 @@ __global__ void k_features(int64_t n, const double* __restrict__ x, const double
     }
 }
 
-// du = delta * net + u_prev * (delta / U): the network's output is the
-// correction to the proportional (secant) increment, which the skip term adds
-// in FP64.  The correction applies to nodes with damage (next to a crack,
-// where large crack-face rotations make the response depart from
-// proportionality); elsewhere the skip term stands alone, so BF16-level
-// output noise never reaches the undamaged bulk.  The skip term alone is
-// written as the second candidate.
-__global__ void k_scale_out(int64_t n, const float* __restrict__ y, double delta, double ratio,
-                            const double* __restrict__ ux, const double* __restrict__ uy,
-                            const double* __restrict__ dmg, double* __restrict__ du) {
+// du = u * (delta / U) + U * net: the skip term is the proportional (secant)
+// increment, added in FP64; the network predicts the departure from
+// proportionality per unit of accumulated boundary displacement (for a
+// response u = a U + b U^2 the departure of an increment is 2 b U delta - b U delta
+// = b U delta, i.e. U * (b delta): a load-independent target).  The skip term
+// alone is written as the second candidate.
+__global__ void k_scale_out(int64_t n, const float* __restrict__ y, double U, double ratio,
+                            const double* __restrict__ ux, const double* __restrict__ uy, double* __restrict__ du) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double sx = ux[i] * ratio, sy = uy[i] * ratio;
-        const bool near_crack = dmg[i] > 0.0;
-        du[i] = near_crack ? fma(delta, (double)y[i * kOut], sx) : sx;
-        du[n + i] = near_crack ? fma(delta, (double)y[i * kOut + 1], sy) : sy;
+        du[i] = fma(U, (double)y[i * kOut], sx);
+        du[n + i] = fma(U, (double)y[i * kOut + 1], sy);
         du[2 * n + i] = sx;
         du[3 * n + i] = sy;
     }
@@ -662,9 +659,9 @@ int pd_warm_features(pd_ctx* c, double U, double delta, double nn_ref, void* dev
     return cuda_err(c, cudaGetLastError(), "pd_warm_features");
 }
 
-// Predicted increment of the free nodes: features, forward pass, then
-// du = delta * output + u * delta / U (x components, then y components): the
-// network predicts the departure from proportional loading.
+// Candidate increments of the free nodes: features, forward pass, then
+// du = u * delta / U + U * output (x components, then y components), and the
+// skip term u * delta / U alone.
 int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref, double* dev_du, void* stream) {
     if (!c || !n || !dev_du) return PD_ERR_ARG;
     cudaStream_t s = st(stream);
@@ -680,7 +677,7 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
     if (!rc) rc = pd_mlp_forward(n, x, ni, y, s);
     if (!rc) {
         k_scale_out<<<(unsigned)std::min<int64_t>((ni + 255) / 256, 4096), 256, 0, s>>>(
-            ni, y, delta, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], c->nf[PD_F_DMG], dev_du);
+            ni, y, U, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], dev_du);
         c->launches++;
         rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
     } else {

@@ -243,13 +243,15 @@ class Engine:
                                        self.stream), "pd_adr_solve")
         return it.value, r.value
 
-    def load_step(self, delta, du_ptr=None, tol_rel=1e-6, max_iters=200000, check_every=100, ncand=1):
+    def load_step(self, delta, du_ptr=None, tol_rel=1e-6, max_iters=200000, check_every=100, ncand=1,
+                  probe_iters=0):
         """One load increment solved by ADR to tol_rel; du_ptr: device pointer
-        to ncand candidate increments (2*N_int doubles each) or None.
+        to ncand candidate increments (2*N_int doubles each) or None; probe_iters:
+        ADR steps of the probe that chooses among admissible candidates.
         Returns the stats."""
         st = PDLoadStepStats()
-        self._c(self._lib.pd_load_step(self.ctx, delta, du_ptr, ncand if du_ptr else 0, tol_rel, max_iters,
-                                       check_every, C.byref(st), self.stream), "pd_load_step")
+        self._c(self._lib.pd_load_step(self.ctx, delta, du_ptr, ncand if du_ptr else 0, probe_iters, tol_rel,
+                                       max_iters, check_every, C.byref(st), self.stream), "pd_load_step")
         return st.as_dict()
 
     def check_finite(self):

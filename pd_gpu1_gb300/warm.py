@@ -9,16 +9,19 @@ increment ``delta * net(features)`` and is kept only when its residual is
 not larger than the plain start's, so the converged answer is the plain
 method's.  Features (``pd_warm_features``) and targets are normalised:
 features use the accumulated boundary displacement U of the previous
-increment.  The prediction is ``u * delta / U + delta * net(features)``: a
+increment.  The prediction is ``u * delta / U + U * net(features)``: a
 skip term, the proportional (secant) increment, plus the network's output
-on the nodes with damage (next to cracks), so the target of training is the
-converged increment over delta minus ``u / U`` on those nodes — zero while
-the plate responds linearly to proportional loading, nonzero where large
-crack-face rotations make the response depart from proportionality.  Increments in which a crack advances
-(bonds break during the increment) are left out of training: no local
-predictor sees them coming.  pd_load_step receives two candidates, the
-network's prediction and the skip term alone, and keeps whichever start
-(or the plain one) has the smallest residual.
+scaled by U, so the target of training is ``(du - u * delta / U) / U`` —
+the departure from proportionality per unit of load, which the bonds'
+geometric nonlinearity keeps nearly constant along the loading
+(u = a U + b U^2 departs by b U delta per increment).  Training uses the
+increments before the first crack advance of each run; after a crack has
+grown the plate is outside what the network saw, and the residual rule
+decides: pd_load_step receives two candidates, the network's prediction and
+the skip term alone; a candidate whose starting residual exceeds the plain
+start's is dropped, and of two admissible ones the start with the smaller
+residual is used (``probe`` > 0 instead runs each for that many ADR steps
+and keeps the lower residual after them).
 
 No reference counterpart: the reference runs a fixed number of ADR steps
 (Solve_Plate_Tensile.cu:106-131).
@@ -113,7 +116,7 @@ def nn_reference(eng):
 
 
 def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1e-6, max_iters=400000,
-                   check_every=100, keep=1.0, seed=0, start=0):
+                   check_every=100, keep=0.25, seed=0, start=0, probe=0):
     """Solve n_inc load increments on a set-up engine.
 
     mode: "plain" (previous solution); "learned" (the two candidates of
@@ -121,8 +124,8 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     plain start; net required); "network" / "secant" (one of the two alone,
     for ablations); "extrapolate" (previous solution plus the previous
     increment: used to generate training states quickly).  collect: a list that receives (features, targets) device
-    tensors of a random ``keep`` fraction of the damaged free nodes per
-    increment without crack advance.
+    tensors of a random ``keep`` fraction of the free nodes per increment,
+    up to the first increment in which a crack advances.
     Returns the per-increment statistics of pd_load_step."""
     import torch
 
@@ -135,6 +138,7 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")  # two candidates
     X = torch.zeros((ni, 16), dtype=torch.bfloat16, device="cuda") if collect is not None else None
     prev = None
+    grown = False  # a crack has advanced in this run
     out = []
     for k in range(start, start + n_inc):
         U = k * delta  # accumulated boundary displacement before this increment
@@ -162,20 +166,19 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
         elif mode == "extrapolate" and prev is not None:
             du[: 2 * ni].copy_(torch.from_numpy(prev))
             ptr = du.data_ptr()
-        st = eng.load_step(delta, ptr, tol, max_iters, check_every, ncand)
+        st = eng.load_step(delta, ptr, tol, max_iters, check_every, ncand, probe if ncand > 1 else 0)
         st["wall_ms"] = (time.perf_counter() - t0) * 1e3
         st["increment"] = k
         if u0 is not None:
             u1 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
             prev = u1 - u0
             if collect is not None and U > 0.0:
-                tt = prev / delta - u0 / U  # departure from the proportional increment
+                tt = (prev - u0 * (delta / U)) / U  # departure from proportionality per unit load
                 st["max_target"] = float(np.abs(tt).max())
                 st["advanced"] = int((eng.get("FAIL") == 0).sum()) - broken0  # bonds broken in the increment
-                if st["advanced"] == 0:
-                    # nodes next to a crack (the correction applies there only)
-                    near = np.nonzero(eng.get("DMG")[:ni] > 0.0)[0]
-                    idx = np.sort(rng.choice(near, max(1, int(keep * len(near))), replace=False))
+                grown = grown or st["advanced"] > 0
+                if not grown:
+                    idx = np.sort(rng.choice(ni, max(1, int(keep * ni)), replace=False))
                     t = np.stack([tt[idx], tt[ni + idx]], axis=1).astype(np.float32)
                     ii = torch.from_numpy(idx).cuda()
                     collect.append((X.index_select(0, ii).clone(), torch.from_numpy(t).cuda()))
@@ -208,7 +211,7 @@ TRAIN_RUNS = [  # (scale, crack fraction, seed): 100k-1M-node plates of the same
 ]
 
 
-def generate(runs=TRAIN_RUNS, n_inc=200, keep=1.0, log=print):
+def generate(runs=TRAIN_RUNS, n_inc=200, keep=0.25, log=print):
     """Converged states of seeded load-stepping runs -> (X, T) device tensors."""
     import torch
 
@@ -238,7 +241,7 @@ def main():
     ap.add_argument("cmd", choices=["train"])
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--steps", type=int, default=3000)
-    ap.add_argument("--increments", type=int, default=200)
+    ap.add_argument("--increments", type=int, default=60)
     args = ap.parse_args()
     t0 = time.perf_counter()
     X, T = generate(n_inc=args.increments)
