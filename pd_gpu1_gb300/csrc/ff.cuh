@@ -96,4 +96,40 @@ __device__ __forceinline__ ff ff_rsqrt(ff x) {
     return ff_fast(y0, (0.5f * y0) * rho);
 }
 
+// a * b for a pair a and a float b.
+__device__ __forceinline__ ff ff_mul_f(ff a, float b) {
+    const float p = a.h * b;
+    float e = fmaf(a.h, b, -p);
+    e = fmaf(a.l, b, e);
+    return ff_fast(p, e);
+}
+
+// a^2 for a pair a.
+__device__ __forceinline__ ff ff_sq(ff a) {
+    const float p = a.h * a.h;
+    float e = fmaf(a.h, a.h, -p);
+    e = fmaf(2.0f * a.h, a.l, e);
+    return ff_fast(p, e);
+}
+
+__device__ __forceinline__ float rcp_approx_f32(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// 1/z of a positive pair, relative error ~2e-14: the FP32 hardware estimate
+// r0 and one Newton step r0 + r0 (1 - z r0), the residual formed as in ff_rsqrt.
+__device__ __forceinline__ ff ff_rcp(ff z) {
+    const float r0 = rcp_approx_f32(z.h);
+    const float q = z.h * r0;
+    const float qe = fmaf(z.h, r0, -q);
+    const float c = fmaf(z.l, r0, qe);
+    const float rho = (1.0f - q) - c;
+    return ff_fast(r0, r0 * rho);
+}
+
+// a > b for normalized pairs (|l| <= ulp(h) / 2), as exact values.
+__device__ __forceinline__ bool ff_gt(ff a, ff b) { return a.h > b.h || (a.h == b.h && a.l > b.l); }
+
 }  // namespace pdg

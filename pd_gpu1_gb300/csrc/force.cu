@@ -37,6 +37,7 @@
 //               Integrate.cu:7-49) reduced across the grid; the last block to
 //               finish forms the damping coefficient (cal_cn, :108-129) on the
 //               device, so ADR needs no host round trip.
+#include "exact_sub.h"
 #include "ff.cuh"
 #include "pd_internal.cuh"
 
@@ -54,6 +55,10 @@ struct ForceArgs {
     const double* ecrit;
     const double* k2;
     const float2* k2f;  // k2 * 2^-S as a float pair
+    const float* xif;   // bond reference vector rounded to float, per component (SoA)
+    const float2* c0f;  // |xif|^2 - l0^2 (pair)
+    const float2* ecf;  // break threshold on e (pair; +inf: never)
+    const float2* l0f;  // l0 (pair)
     double kscale;      // 2^S
     const double* c1;
     const double* c2;
@@ -105,6 +110,19 @@ constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
 constexpr bool kSeedFp32 = true;
 // Bond-force tail (t = k2 e h, f += t d) in pair arithmetic instead of FP64.
 constexpr bool kTailFF = true;
+// Bond kernels' per-bond recipe: 3 = the reference-rounded bond vector d and
+// its exact offset eta from a per-slot float reference vector, with the two
+// exact subtractions on the integer pipe and one FP64 subtraction per
+// component (the reference's rounding), then the extension from the
+// cancellation-free L^2 - l0^2 = c0 + 2 xif.eta + eta.eta in pairs; anything
+// else = the earlier recipe (FP64 bond vector, L^2, root residual and e: 10
+// FP64 instructions per 2-D bond).
+constexpr int kRecipe = 3;
+// P_c - x_i by integer operations (exact_sub.h) instead of an FP64 subtraction.
+// Measured slower on the 1.6M-node plate (1.01 ms against 0.85 ms per step):
+// the normalisation of the difference costs more issue slots than the FP64
+// instruction it replaces.
+constexpr bool kIntExactA = false;
 
 // float of a positive double whose exponent is within the float normal range:
 // rebias the 11-bit exponent to 8 bits and keep the top 23 mantissa bits
@@ -178,6 +196,43 @@ __device__ __forceinline__ void extension_ff(double x, double L0, double& e, ff&
     h = ff{0.5f * y.h, 0.5f * y.l};
     const double d = fma(-s, s, x);
     e = fma(d, f64_of_f32s(h.h), s - L0);
+}
+
+// diff * 2^(e - 1075) as a normalized pair; exact for |diff| < 2^48 and a
+// scale within the float range (the caller checks both).
+__device__ __forceinline__ ff ff_from_scaled(int64_t diff, int e) {
+    const float sc = __int_as_float((e - 1075 + 127) << 23);
+    const float h = __int2float_rn((int)(diff >> 24)) * (sc * 16777216.0f);
+    const float l = __int2float_rn((int)(diff & 0xffffff)) * sc;
+    return ff_two_sum(h, l);
+}
+
+__device__ __forceinline__ uint64_t dbits(double v) { return (uint64_t)__double_as_longlong(v); }
+
+// One component of a bond: d = (P_c - x_i) - u_i with the reference's
+// roundings and eta = d - xf exactly, as a pair.  The two exact subtractions
+// run on the integer pipe (exact_sub.h) and fall back to FP64 outside
+// Sterbenz's range; the rounding one is an FP64 subtraction.
+__device__ __forceinline__ ff bond_offset(double pc, double xi, double ui, float xf) {
+    double a;
+    if (kIntExactA) {
+        uint64_t ua;
+        if (sub_exact(dbits(pc), dbits(xi), ua))
+            a = __longlong_as_double((long long)ua);
+        else
+            a = pc - xi;
+    } else {
+        a = pc - xi;
+    }
+    const double d = a - ui;
+    if (xf == 0.0f) return ff_split(d);
+    const double x = f64_of_f32s(xf);
+    int64_t diff;
+    int e;
+    if (sub_exact_scaled(dbits(d), dbits(x), diff, e) && e >= 949 && e <= 1170 && diff < (1ll << 48) &&
+        diff > -(1ll << 48))
+        return ff_from_scaled(diff, e);
+    return ff_split(d - x);
 }
 
 // e > ecrit for ecrit > 0: ordered like the IEEE bit patterns read as signed
@@ -432,12 +487,46 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
+            // neighbour index of the next slot loaded one iteration ahead, so the
+            // gather of slot k starts at the top of iteration k
+            int c_next = W > 0 ? __ldg(A.col + b + lane) : 0;
             for (int k = 0; k < W; k++) {
                 const int64_t slot = b + (int64_t)k * 32 + lane;
+                const int c_cur = c_next;
+                if (kRecipe == 3 && k + 1 < W) c_next = __ldg(A.col + slot + 32);
                 const uint32_t word = wbits[k];
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
-                if (alive) {
+                if (alive && kRecipe == 3) {
+                    // d = (P_c - x_i) - u_i with the reference's roundings (FP64),
+                    // eta = d - xif exactly (Sterbenz), then everything in pairs:
+                    // L^2 - l0^2 = c0 + 2 xif.eta + eta.eta, no cancellation
+                    const int c = c_cur;
+                    const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
+                    const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
+                    ff dp[3], D{0.0f, 0.0f}, Q{0.0f, 0.0f};
+#pragma unroll
+                    for (int a = 0; a < DIM; a++) {
+                        const float xf = __ldg(A.xif + (int64_t)a * A.S + slot);
+                        const ff eta = bond_offset(pc[a], xr[a], ur[a], xf);
+                        D = ff_add(D, ff_mul_f(eta, xf));
+                        Q = ff_add(Q, ff_sq(eta));
+                        dp[a] = ff_add(ff{xf, 0.0f}, eta);
+                    }
+                    const float2 c0 = __ldg(A.c0f + slot), l0 = __ldg(A.l0f + slot);
+                    D = ff_add(ff_add(ff{c0.x, c0.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
+                    const ff L0p{l0.x, l0.y};
+                    const ff L2p = ff_add(ff_sq(L0p), D);
+                    const ff y = ff_rsqrt(L2p);                                  // 1/L
+                    const ff e2 = ff_mul(D, ff_rcp(ff_add(ff_mul(L2p, y), L0p)));  // L - l0
+                    const float2 kf = __ldg(A.k2f + slot);
+                    const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
+                    fxa = ff_add(fxa, ff_mul(t, dp[0]));
+                    fya = ff_add(fya, ff_mul(t, dp[1]));
+                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, dp[2]));
+                    const float2 ec = __ldg(A.ecf + slot);
+                    brk = ff_gt(e2, ff{ec.x, ec.y});
+                } else if (alive) {
                     const int c = A.col[slot];
                     const double dx = (A.pcx[c] - xi) - uxi;
                     const double dy = (A.pcy[c] - yi) - uyi;
@@ -470,7 +559,7 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
             }
-            if (kTailFF) {
+            if (kTailFF || kRecipe == 3) {
                 // undo the power-of-two scaling of the bond coefficient (exact)
                 fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
                 fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
@@ -688,6 +777,10 @@ static ForceArgs make_args(pd_ctx* c) {
     A.ecrit = S.ecrit;
     A.k2 = S.k2;
     A.k2f = S.k2f;
+    A.xif = S.xif;
+    A.c0f = S.c0f;
+    A.ecf = S.ecf;
+    A.l0f = S.l0f;
     A.kscale = S.kscale;
     A.c1 = S.c1;
     A.c2 = S.c2;

@@ -266,6 +266,10 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             if (S.k2) {
                 S.k2[slot] = 0.0;
                 S.k2f[slot] = make_float2(0.0f, 0.0f);
+                for (int a = 0; a < P.dim; a++) S.xif[a * S.S + slot] = 0.0f;
+                S.c0f[slot] = make_float2(0.0f, 0.0f);
+                S.ecf[slot] = make_float2(__int_as_float(0x7f800000), 0.0f);
+                S.l0f[slot] = make_float2(1.0f, 0.0f);
             }
             if (S.c1) {
                 S.c1[slot] = 0.0;
@@ -293,6 +297,33 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             S.k2[slot] = k2;
             const ff kf = ff_split(k2 * S.kscale_inv);
             S.k2f[slot] = make_float2(kf.h, kf.l);
+            // reference vector rounded to float per component, and the exact
+            // constant |xif|^2 - l0^2 (products of floats are exact doubles;
+            // the sums carried as double pairs, TwoSum / FMA TwoProduct)
+            const double xa[3] = {x[c] - x[r], y[c] - y[r], P.dim == 3 ? z[c] - z[r] : 0.0};
+            double sh = 0.0, sl = 0.0;
+            for (int a = 0; a < P.dim; a++) {
+                const float f = __double2float_rn(xa[a]);
+                S.xif[a * S.S + slot] = f;
+                const double sq = (double)f * (double)f;  // exact: 24-bit x 24-bit mantissas
+                const double t = sh + sq;
+                const double bb = t - sh;
+                sl += (sh - (t - bb)) + (sq - bb);
+                sh = t;
+            }
+            const double ph = L0 * L0;
+            const double pl = fma(L0, L0, -ph);
+            const double c0 = (sh - ph) + (sl - pl);  // sh - ph exact: both within a factor 2 of l0^2
+            const ff cf = ff_split(c0);
+            S.c0f[slot] = make_float2(cf.h, cf.l);
+            const ff lf = ff_split(L0);
+            S.l0f[slot] = make_float2(lf.h, lf.l);
+            if (breakable) {
+                const ff ef = ff_split(S.ecrit[slot]);
+                S.ecf[slot] = make_float2(ef.h, ef.l);
+            } else {
+                S.ecf[slot] = make_float2(__int_as_float(0x7f800000), 0.0f);
+            }
         }
         if (S.c1) {
             const double pr = P.pratio;
@@ -468,6 +499,10 @@ static void free_sell(Sell& S) {
     free_ptr(S.ecrit);
     free_ptr(S.k2);
     free_ptr(S.k2f);
+    free_ptr(S.xif);
+    free_ptr(S.c0f);
+    free_ptr(S.ecf);
+    free_ptr(S.l0f);
     free_ptr(S.c1);
     free_ptr(S.c2);
     free_ptr(S.cth);
@@ -522,7 +557,9 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
     bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.l0, n8) &&
               !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
-    if (ok && !state) ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.k2f, n8);
+    if (ok && !state)
+        ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.k2f, n8) && !cudaMalloc(&S.xif, n4 * P.dim) &&
+             !cudaMalloc(&S.c0f, n8) && !cudaMalloc(&S.ecf, n8) && !cudaMalloc(&S.l0f, n8);
     // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,
     // so that the pair arithmetic of the force kernels stays in float range
     {
