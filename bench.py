@@ -500,13 +500,13 @@ def batch_arm(args):
             "data": f"synthetic (seeded specimen table, seed {meta['seed']})",
             "config": {"workload": meta["workload"], "specimens": len(specs), "nodes": p.N, "interior": p.N_int,
                        "bonds": B, "dx": p.dx, "dt": p.dt, "parallelism": "replicas" if world > 1 else "single",
-                       "launch": {"block": tuned[0], "chunked": tuned[1], "waves": tuned[2]},
+                       "launch": {"block": tuned[0], "chunked": tuned[1], "waves": tuned[2], "split": tuned[3]},
                        "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 28 / 1e9),
                        "setup_s": setup_s, "broken_bond_fraction": broken},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_bond_force<2, ADR>", "kernel_ms": kern_ms,
-                         "kernel_share_of_step": kern_ms / step_ms, "autotune_ms": tuned[3],
+                         "kernel_share_of_step": kern_ms / step_ms, "autotune_ms": tuned[4],
                          "alg_bytes_per_launch": alg_bytes,
                          "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
                                   "frac": alg_flops / (kern_ms * 1e-3) / 1e12 / fp64_peak,
@@ -779,7 +779,7 @@ def gb300_arm(args):
                        "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 44 / 1e9),
                        "setup_s": setup_s,
                        "launch": None if tuned is None else {"block": tuned[0], "chunked": tuned[1],
-                                                             "waves": tuned[2]}},
+                                                             "waves": tuned[2], "split": tuned[3]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
                          "kernel": "k_bond_force" if p.model == 1 else "k_theta + k_state_force",

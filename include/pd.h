@@ -350,17 +350,24 @@ int pd_batch_get_cn(pd_ctx* ctx, double* cn, void* stream);
 
 /* ---- launch shape of the bond-force kernels ------------------------------ */
 /* Threads per block (128, 256, 512), warp-to-slice order (0: grid-strided,
- * 1: one contiguous run of slices per warp) and grid size in waves of
- * resident blocks (1..8).  The per-node force sums do not depend on the
- * shape; sums over the whole grid (the single-specimen ADR damping
- * coefficient, the impactor reaction) follow the block order and may differ
- * in the last bits.  Default 256 / 0 / 1. */
-int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves);
-int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves);
+ * 1: one contiguous run of slices per warp), grid size in waves of resident
+ * blocks (1..8) and warps per slice (split: 1, 2, 4, 8; 2-D bond kernel,
+ * strided order only): with split > 1 the slots of a slice are shared by
+ * that many warps and summed in slot order by the first, which multiplies
+ * the bonds in flight on small problems.  The per-node force sums do not
+ * depend on the shape; sums over the whole grid (the single-specimen ADR
+ * damping coefficient, the impactor reaction) follow the block order and may
+ * differ in the last bits.  Default 256 / 0 / 1 / 1.  The reference's two
+ * mappings, thread per node (kernel_particle_force_2D, Force_Bond.cu:52-85)
+ * and warp per node (kernel_bond_force_2D, :6-50), correspond to split 1 and
+ * to the widest split. */
+int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves, int split);
+int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves, int* split);
 /* Times the bond-force kernel (reps launches per shape, at the current
- * displacements) over the 18 shapes above and keeps the fastest; *best_ms
- * receives its time per launch.  Intact flags and forces are restored, so a
- * run continues exactly as without the call.  Bond-based contexts only. */
+ * displacements) over the shapes above (18 with split 1, 12 more with split
+ * 2 and 4 in 2-D) and keeps the fastest; *best_ms receives its time per
+ * launch.  Intact flags and forces are restored, so a run continues exactly
+ * as without the call.  Bond-based contexts only. */
 int pd_autotune(pd_ctx* ctx, int reps, double* best_ms, void* stream);
 
 /* ---- step profile --------------------------------------------------------- */

@@ -1014,24 +1014,28 @@ int pd_profile_steps(pd_ctx* c, int kind, int ct0, int nsteps, double load, doub
     return PD_OK;
 }
 
-int pd_set_launch(pd_ctx* c, int block, int chunked, int waves) {
+int pd_set_launch(pd_ctx* c, int block, int chunked, int waves, int split) {
     if (!c || (block != 128 && block != 256 && block != 512) || (chunked != 0 && chunked != 1) || waves < 1 ||
-        waves > 8)
+        waves > 8 || (split != 1 && split != 2 && split != 4 && split != 8))
         return PD_ERR_ARG;
-    if (block != c->tune_block || chunked != c->tune_chunked || waves != c->tune_waves) {
+    if (split > 1 && (chunked || block / 32 < split || c->p.dim != 2 || c->p.model != PD_MODEL_BOND))
+        return set_err(c, PD_ERR_ARG, "a split slice needs the 2-D bond kernel, strided order and block >= 32 split");
+    if (block != c->tune_block || chunked != c->tune_chunked || waves != c->tune_waves || split != c->tune_split) {
         drop_graphs(c);  // captured launches carry the old shape
         c->tune_block = block;
         c->tune_chunked = chunked;
         c->tune_waves = waves;
+        c->tune_split = split;
     }
     return PD_OK;
 }
 
-int pd_get_launch(const pd_ctx* c, int* block, int* chunked, int* waves) {
-    if (!c || !block || !chunked || !waves) return PD_ERR_ARG;
+int pd_get_launch(const pd_ctx* c, int* block, int* chunked, int* waves, int* split) {
+    if (!c || !block || !chunked || !waves || !split) return PD_ERR_ARG;
     *block = c->tune_block;
     *chunked = c->tune_chunked;
     *waves = c->tune_waves;
+    *split = c->tune_split;
     return PD_OK;
 }
 
@@ -1061,7 +1065,7 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     cudaMemcpyAsync(saved_f, c->nf[PD_F_FX], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
     cudaMemcpyAsync(saved_f + N, c->nf[PD_F_FY], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
     const bool csr_current = c->csr_fail_current, pos_valid = c->pos_valid;
-    const int b0 = c->tune_block, k0 = c->tune_chunked, w0 = c->tune_waves;
+    const int b0 = c->tune_block, k0 = c->tune_chunked, w0 = c->tune_waves, p0 = c->tune_split;
     StepFlags f;
     f.epi = c->batch.count ? EPI_ADR : EPI_NONE;  // a batch's ADR epilogue writes only per-slice scratch
     // between timed launches a 256 MB write evicts the node arrays from L2, as
@@ -1076,14 +1080,25 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     double best = 1e300;
-    int bb = b0, bk = k0, bw = w0;
-    const int blocks[3] = {128, 256, 512}, waves[3] = {1, 2, 4};
-    for (int ib = 0; ib < 3 && !rc; ib++)
-        for (int ck = 0; ck < 2 && !rc; ck++)
-            for (int iw = 0; iw < 3 && !rc; iw++) {
-                c->tune_block = blocks[ib];
-                c->tune_chunked = ck;
-                c->tune_waves = waves[iw];
+    int bb = b0, bk = k0, bw = w0, bp = p0;
+    // shapes: block x order x waves with one warp per slice, and for the 2-D
+    // kernel block x {2, 4} warps per slice x waves {1, 2}
+    struct Shape {
+        int block, chunked, waves, split;
+    };
+    std::vector<Shape> shapes;
+    for (int blk : {128, 256, 512})
+        for (int ck : {0, 1})
+            for (int wv : {1, 2, 4}) shapes.push_back({blk, ck, wv, 1});
+    if (c->p.dim == 2)
+        for (int blk : {128, 256, 512})
+            for (int sp : {2, 4})
+                for (int wv : {1, 2}) shapes.push_back({blk, 0, wv, sp});
+    for (size_t ish = 0; ish < shapes.size() && !rc; ish++) {
+                c->tune_block = shapes[ish].block;
+                c->tune_chunked = shapes[ish].chunked;
+                c->tune_waves = shapes[ish].waves;
+                c->tune_split = shapes[ish].split;
                 if ((rc = launch_force(c, f, s))) break;  // warm-up
                 double tot = 0.0;
                 for (int r = 0; r < reps && !rc; r++) {
@@ -1102,7 +1117,7 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
                 if (rc) break;
                 if (tot / reps < best) {
                     best = tot / reps;
-                    bb = blocks[ib], bk = ck, bw = waves[iw];
+                    bb = shapes[ish].block, bk = shapes[ish].chunked, bw = shapes[ish].waves, bp = shapes[ish].split;
                 }
             }
     cudaMemcpyAsync(S.bits, saved_bits, nbits, cudaMemcpyDeviceToDevice, s);
@@ -1116,11 +1131,11 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     cudaEventDestroy(e1);
     c->csr_fail_current = csr_current;
     c->pos_valid = pos_valid;
-    c->tune_block = b0, c->tune_chunked = k0, c->tune_waves = w0;
+    c->tune_block = b0, c->tune_chunked = k0, c->tune_waves = w0, c->tune_split = p0;
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_err(c, e, "pd_autotune");
     if (best_ms) *best_ms = best;
-    return pd_set_launch(c, bb, bk, bw);
+    return pd_set_launch(c, bb, bk, bw, bp);
 }
 
 // ---- drivers ----------------------------------------------------------------

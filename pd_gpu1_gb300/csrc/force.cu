@@ -90,6 +90,8 @@ struct ForceArgs {
     unsigned int* ticket;
     double* cn_out;
     int chunked;              // contiguous slice runs per warp instead of a grid stride
+    int split;                // warps sharing one slice (k_bond_split)
+    int wmax;                 // widest slice
     int nobreak;              // evaluate forces without updating the intact flags
     double* res_out;          // ADR: sum over force rows of |F + b|^2 (device scalar)
     // batch of specimens (null for a single one)
@@ -458,6 +460,40 @@ __device__ void finish_reduction(const ForceArgs& A, double red[3], int nred) {
     }
 }
 
+// One bond of the pair-arithmetic recipe (kRecipe 3): its force contribution
+// t (xif + eta) per component as pairs (cf) and whether it breaks.
+//   d = (P_c - x_i) - u_i with the reference's roundings (FP64),
+//   eta = d - xif exactly (integer pipe), then everything in pairs:
+//   L^2 - l0^2 = c0 + 2 xif.eta + eta.eta, no cancellation.
+template <int DIM>
+__device__ __forceinline__ bool bond3(const ForceArgs& A, int64_t slot, unsigned craw, double xi, double yi,
+                                      double zi, double uxi, double uyi, double uzi, ff cf[3]) {
+    const int c = (int)craw;
+    const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
+    const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
+    ff dp[3], D{0.0f, 0.0f}, Q{0.0f, 0.0f};
+#pragma unroll
+    for (int a = 0; a < DIM; a++) {
+        const float xf = __ldg(A.xif + (int64_t)a * A.S + slot);
+        const ff eta = bond_offset(pc[a], xr[a], ur[a], xf);
+        D = ff_add(D, ff_mul_f(eta, xf));
+        Q = ff_add(Q, ff_sq(eta));
+        dp[a] = ff_add(ff{xf, 0.0f}, eta);
+    }
+    const float2 c0 = __ldg(A.c0f + slot), l0 = __ldg(A.l0f + slot);
+    D = ff_add(ff_add(ff{c0.x, c0.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
+    const ff L0p{l0.x, l0.y};
+    const ff L2p = ff_add(ff_sq(L0p), D);
+    const ff y = ff_rsqrt(L2p);                                  // 1/L
+    const ff e2 = ff_mul(D, ff_rcp(ff_add(ff_mul(L2p, y), L0p)));  // L - l0
+    const float2 kf = __ldg(A.k2f + slot);
+    const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
+#pragma unroll
+    for (int a = 0; a < DIM; a++) cf[a] = ff_mul(t, dp[a]);
+    const float2 ec = __ldg(A.ecf + slot);
+    return ff_gt(e2, ff{ec.x, ec.y});
+}
+
 template <int DIM, int EPI>
 __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
@@ -498,34 +534,11 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
                 if (alive && kRecipe == 3) {
-                    // d = (P_c - x_i) - u_i with the reference's roundings (FP64),
-                    // eta = d - xif exactly (Sterbenz), then everything in pairs:
-                    // L^2 - l0^2 = c0 + 2 xif.eta + eta.eta, no cancellation
-                    const int c = c_cur;
-                    const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
-                    const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
-                    ff dp[3], D{0.0f, 0.0f}, Q{0.0f, 0.0f};
-#pragma unroll
-                    for (int a = 0; a < DIM; a++) {
-                        const float xf = __ldg(A.xif + (int64_t)a * A.S + slot);
-                        const ff eta = bond_offset(pc[a], xr[a], ur[a], xf);
-                        D = ff_add(D, ff_mul_f(eta, xf));
-                        Q = ff_add(Q, ff_sq(eta));
-                        dp[a] = ff_add(ff{xf, 0.0f}, eta);
-                    }
-                    const float2 c0 = __ldg(A.c0f + slot), l0 = __ldg(A.l0f + slot);
-                    D = ff_add(ff_add(ff{c0.x, c0.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
-                    const ff L0p{l0.x, l0.y};
-                    const ff L2p = ff_add(ff_sq(L0p), D);
-                    const ff y = ff_rsqrt(L2p);                                  // 1/L
-                    const ff e2 = ff_mul(D, ff_rcp(ff_add(ff_mul(L2p, y), L0p)));  // L - l0
-                    const float2 kf = __ldg(A.k2f + slot);
-                    const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
-                    fxa = ff_add(fxa, ff_mul(t, dp[0]));
-                    fya = ff_add(fya, ff_mul(t, dp[1]));
-                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, dp[2]));
-                    const float2 ec = __ldg(A.ecf + slot);
-                    brk = ff_gt(e2, ff{ec.x, ec.y});
+                    ff cf[3];
+                    brk = bond3<DIM>(A, slot, (unsigned)c_cur, xi, yi, zi, uxi, uyi, uzi, cf);
+                    fxa = ff_add(fxa, cf[0]);
+                    fya = ff_add(fya, cf[1]);
+                    if (DIM == 3) fza = ff_add(fza, cf[2]);
                 } else if (alive) {
                     const int c = A.col[slot];
                     const double dx = (A.pcx[c] - xi) - uxi;
@@ -569,6 +582,76 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
+    }
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
+// 2-D bond force with several warps per slice (A.split of them): warp `sub`
+// of a slice group computes the slots k = sub, sub + split, ... and leaves
+// each contribution in shared memory; the group's first warp then adds them
+// in slot order, so every row's sums are the same, bit for bit, as with one
+// warp per slice.  For small problems (fewer slices than the GPU has warp
+// slots) the split multiplies the bonds in flight.  Shared memory per group:
+// wmax slots x 2 components x 32 lanes pairs + one alive word per slot.
+template <int EPI>
+__global__ void __launch_bounds__(kMaxBondBlock) k_bond_split(const ForceArgs A) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int split = A.split, G = (int)(blockDim.x >> 5) / split;
+    const int g = wib / split, sub = wib % split;
+    const int Wm = A.wmax;
+    float2* contrib = reinterpret_cast<float2*>(sm_raw) + (size_t)g * Wm * 64;
+    uint32_t* alive_w = reinterpret_cast<uint32_t*>(reinterpret_cast<float2*>(sm_raw) + (size_t)G * Wm * 64) + g * Wm;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    const int64_t groups = (int64_t)gridDim.x * G;
+    const int64_t rounds = (A.nslices + groups - 1) / groups;
+    for (int64_t it = 0; it < rounds; it++) {
+        const int64_t s = it * groups + (int64_t)blockIdx.x * G + g;
+        const int64_t r = s * 32 + lane;
+        const bool in = s < A.nslices;
+        const bool force_row = in && r < A.nforce;
+        const bool work = in && s * 32 < A.nforce;
+        const int64_t rr = force_row ? r : (A.nforce > 0 ? A.nforce - 1 : 0);
+        double xi = 0.0, yi = 0.0, uxi = 0.0, uyi = 0.0;
+        int W = 0;
+        if (work) {
+            xi = A.x[rr], yi = A.y[rr], uxi = A.ux[rr], uyi = A.uy[rr];
+            W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            for (int k = sub; k < W; k += split) {
+                const int64_t slot = b + (int64_t)k * 32 + lane;
+                const uint32_t word = wbits[k];
+                const bool alive = force_row && ((word >> lane) & 1u);
+                bool brk = false;
+                ff cf[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
+                if (alive) brk = bond3<2>(A, slot, (unsigned)__ldg(A.col + slot), xi, yi, 0.0, uxi, uyi, 0.0, cf);
+                contrib[(k * 2 + 0) * 32 + lane] = make_float2(cf[0].h, cf[0].l);
+                contrib[(k * 2 + 1) * 32 + lane] = make_float2(cf[1].h, cf[1].l);
+                const uint32_t am = __ballot_sync(0xffffffffu, alive);
+                if (lane == 0) alive_w[k] = am;
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+            }
+        }
+        __syncthreads();
+        if (sub == 0 && work) {
+            ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
+            for (int k = 0; k < W; k++) {
+                if (!((alive_w[k] >> lane) & 1u)) continue;
+                const float2 cx = contrib[(k * 2 + 0) * 32 + lane], cy = contrib[(k * 2 + 1) * 32 + lane];
+                fxa = ff_add(fxa, ff{cx.x, cx.y});
+                fya = ff_add(fya, ff{cy.x, cy.y});
+            }
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
+            if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
+        }
+        if (sub == 0 && EPI == EPI_VERLET && A.do_next && in && !force_row && r < P.N) boundary_row<2>(A, r);
+        __syncthreads();
     }
     if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
@@ -895,6 +978,33 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
     const int blk = bond ? c->tune_block : kForceBlock;
     const int waves = bond ? c->tune_waves : 1;
     A.chunked = bond ? c->tune_chunked : 0;
+    if (bond && !d3 && c->tune_split > 1) {
+        // several warps per slice (k_bond_split), one wave of slice groups
+        A.split = c->tune_split;
+        A.wmax = std::max(1, c->sell.wmax);
+        const int G = (blk / 32) / A.split;
+        const size_t smem = (size_t)G * A.wmax * (64 * sizeof(float2) + sizeof(uint32_t));
+        const void* kern = f.epi == EPI_VERLET ? (const void*)k_bond_split<EPI_VERLET>
+                            : f.epi == EPI_ADR ? (const void*)k_bond_split<EPI_ADR>
+                                               : (const void*)k_bond_split<EPI_NONE>;
+        if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, blk, smem) != cudaSuccess || per_sm < 1)
+            per_sm = 1;
+        const int64_t want = (A.nslices + G - 1) / G;
+        const unsigned grid = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>(std::min<int64_t>(want, (int64_t)c->num_sms * per_sm * waves), kMaxPartials));
+        if (f.epi == EPI_VERLET)
+            k_bond_split<EPI_VERLET><<<grid, blk, smem, s>>>(A);
+        else if (f.epi == EPI_ADR)
+            k_bond_split<EPI_ADR><<<grid, blk, smem, s>>>(A);
+        else
+            k_bond_split<EPI_NONE><<<grid, blk, smem, s>>>(A);
+        c->launches++;
+        if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
+        c->csr_fail_current = false;
+        return cuda_err(c, cudaGetLastError(), "bond force (split)");
+    }
 #define PD_LAUNCH(KER, D, E) \
     KER<D, E><<<resident_grid(c, (const void*)KER<D, E>, A.nslices, blk, waves), blk, 0, s>>>(A)
 #define PD_DISPATCH(KER)                                  \

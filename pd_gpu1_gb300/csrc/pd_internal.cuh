@@ -45,6 +45,7 @@ struct Sell {
     int64_t nslices = 0;     // ceil(N / 32)
     int64_t S = 0;           // total slots (sum of 32 * width)
     int64_t F = 0;           // total flag words (sum of width)
+    int wmax = 0;            // widest slice
     int* width = nullptr;    // [nslices]
     int64_t* base = nullptr; // [nslices] slot offset
     int64_t* fbase = nullptr;// [nslices] flag-word offset
@@ -142,6 +143,7 @@ struct pd_ctx {
     int tune_block = 256;   // threads per block: 128, 256 or 512
     int tune_waves = 1;     // grid = resident blocks x waves
     int tune_chunked = 0;   // 1: contiguous slice runs per warp
+    int tune_split = 1;     // warps sharing one slice's slots (2-D bond kernels)
 };
 
 namespace pdg {

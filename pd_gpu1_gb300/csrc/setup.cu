@@ -550,6 +550,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
         wmax = std::max(wmax, w[k]);
     }
     fb[S.nslices] = acc;
+    S.wmax = wmax;
     S.F = acc;
     S.S = acc * 32;
     cudaMemcpyAsync(S.fbase, fb.data(), fb.size() * 8, cudaMemcpyHostToDevice, s);

@@ -266,17 +266,18 @@ class Engine:
         return f.value, st.value
 
     # ---- launch shape of the bond-force kernel ------------------------------
-    def set_launch(self, block=256, chunked=0, waves=1):
-        self._c(self._lib.pd_set_launch(self.ctx, block, chunked, waves), "pd_set_launch")
+    def set_launch(self, block=256, chunked=0, waves=1, split=1):
+        self._c(self._lib.pd_set_launch(self.ctx, block, chunked, waves, split), "pd_set_launch")
 
     def launch(self):
-        b, k, w = C.c_int(), C.c_int(), C.c_int()
-        self._c(self._lib.pd_get_launch(self.ctx, C.byref(b), C.byref(k), C.byref(w)), "pd_get_launch")
-        return b.value, k.value, w.value
+        b, k, w, p = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        self._c(self._lib.pd_get_launch(self.ctx, C.byref(b), C.byref(k), C.byref(w), C.byref(p)),
+                "pd_get_launch")
+        return b.value, k.value, w.value, p.value
 
     def autotune(self, reps=5):
-        """Times the 18 launch shapes at the current state and keeps the
-        fastest; returns (block, chunked, waves, ms per launch)."""
+        """Times the launch shapes at the current state and keeps the fastest;
+        returns (block, chunked, waves, split, ms per launch)."""
         ms = C.c_double()
         self._c(self._lib.pd_autotune(self.ctx, reps, C.byref(ms), self.stream), "pd_autotune")
         return self.launch() + (ms.value,)

@@ -180,7 +180,8 @@ def test_batch_specimen_matches_oracle(E, base):
     bat.close()
 
 
-@pytest.mark.parametrize("shape", [(128, 1, 2), (512, 0, 4), (256, 1, 1)])
+@pytest.mark.parametrize("shape", [(128, 1, 2, 1), (512, 0, 4, 1), (256, 1, 1, 1), (128, 0, 1, 2), (256, 0, 2, 4),
+                                   (512, 0, 1, 8)])
 def test_launch_shapes_bitwise(E, base, shape):
     b, load = base
     ref = E.Batch(b, SPECS)
@@ -204,12 +205,18 @@ def test_launch_shape_explicit_bitwise(E):
     setup(a)
     setup(c)
     c.set_launch(512, 1, 2)
+    d = E.Engine(p)
+    setup(d)
+    d.set_launch(256, 0, 1, 4)  # four warps per slice
     a.run_explicit(40)
     c.run_explicit(40)
+    d.run_explicit(40)
     for f in ["UX", "UY", "VX", "VY", "FAIL"]:
         np.testing.assert_array_equal(a.get(f), c.get(f), err_msg=f)
+        np.testing.assert_array_equal(a.get(f), d.get(f), err_msg="split " + f)
     a.close()
     c.close()
+    d.close()
 
 
 def test_autotune_leaves_the_run_unchanged(E, base):
@@ -218,8 +225,9 @@ def test_autotune_leaves_the_run_unchanged(E, base):
     tun = E.Batch(b, SPECS)
     ref.run_adr(0, 40, load)
     tun.run_adr(0, 20, load)
-    block, chunked, waves, ms = tun.autotune(reps=3)
-    assert block in (128, 256, 512) and chunked in (0, 1) and waves in (1, 2, 4) and ms > 0.0
+    block, chunked, waves, split, ms = tun.autotune(reps=3)
+    assert block in (128, 256, 512) and chunked in (0, 1) and waves in (1, 2, 4) and split in (1, 2, 4)
+    assert ms > 0.0
     tun.run_adr(20, 20, load)
     for f in ["UX", "UY", "FAIL"]:
         np.testing.assert_array_equal(tun.get(f), ref.get(f), err_msg=f)
@@ -237,7 +245,8 @@ def test_batch_refuses_single_plate_loops(E, base):
     assert lib.pd_run_explicit(bat.ctx, 1, 0.0, 0, None) == PD_ERR_UNSUPPORTED
     one = standalone(E, b, SPECS[0])
     assert lib.pd_batch_run_adr(one.ctx, 0, 1, load, None) == PD_ERR_STATE
-    assert lib.pd_set_launch(one.ctx, 64, 0, 1) != 0
+    assert lib.pd_set_launch(one.ctx, 64, 0, 1, 1) != 0
+    assert lib.pd_set_launch(one.ctx, 128, 1, 1, 2) != 0  # a split slice needs the strided order
     one.close()
     bat.close()
 

@@ -227,6 +227,35 @@ def test_adr_loop_matches_oracle(E):
     eng.close()
 
 
+def test_split_slices_match(E):
+    """Four warps per slice (the small-problem mapping): forces bit for bit
+    the same as with one warp per slice; an ADR run within the chaos bar (its
+    damping coefficient is a grid-wide sum whose block order follows the
+    launch shape)."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_plate_tensile(scale=0.3)
+    a, b = E.Engine(p), E.Engine(p)
+    setup(a)
+    setup(b)
+    b.set_launch(128, 0, 2, 4)
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((2, p.N)) * 1e-7
+    for eng in (a, b):
+        eng.set("UX", u[0])
+        eng.set("UY", u[1])
+        eng.bond_force_gpu()
+    for k in ["FX", "FY", "FAIL"]:
+        np.testing.assert_array_equal(a.get(k), b.get(k), err_msg=k)
+    for eng in (a, b):
+        eng.set("UX", np.zeros(p.N))
+        eng.set("UY", np.zeros(p.N))
+        eng.run_adr(0, 40, load=meta["load"])
+    assert_close_norm(b.get("UY"), a.get("UY"), 1e-9, "uy")
+    a.close()
+    b.close()
+
+
 def test_adr_single_calls_match_fused(E):
     """pd_bond_force + pd_integrate_adr per step equals the fused pd_run_adr."""
     from pd_gpu1_gb300 import presets
