@@ -753,12 +753,41 @@ def gb300_arm(args):
                 r.run(variant, args.warmup, meta.get("dmg_every", 0))
                 ms_ref = r.run(variant, kref, meta.get("dmg_every", 0))
                 rates[name] = B * kref / (ms_ref * 1e-3)
+            # the damage field after the whole run, both implementations from the
+            # same initial state: nodes whose damage agrees, and the crack tips
+            setup(eng)
+            dref = {}
+            for name, variant in (("particle", ref_gpu.RefGPU.PARTICLE), ("warp", ref_gpu.RefGPU.WARP)):
+                r.setup(p, *r_inputs(eng, p))
+                r.run(variant, args.steps, meta.get("dmg_every", 0))
+                dref[name] = r.get()["dmg"][: p.N_int]
             r.free()
+            run_steps(eng, meta, args.steps)
+            eng.damage()
+            de, dr = eng.get("DMG")[: p.N_int], dref["particle"]
+            xs = eng.get("X")[: p.N_int]
+
+            def tip(d):
+                hot = np.nonzero(d > 0.38)[0]
+                return float(xs[hot].max()) if len(hot) else None
+
+            tip_r = tip(dr)
+            tip_e = eng.crack_tip(0.38)[0]
             best = max(rates.values())
             ref_cuda = {"unit": "bond-updates/s", "steps": kref, **rates, "best": best,
                         "engine_over_best": value / best,
                         "what": "the reference's kernels (compiled from its sources, FP64) in its step loop: "
-                                "integrate_2D_1, force, integrate_2D_2, damage every 100 steps"}
+                                "integrate_2D_1, force, integrate_2D_2, damage every 100 steps",
+                        "damage_after_steps": args.steps,
+                        "damage_nodes_equal": float(np.mean(np.abs(de - dr) <= 1e-12)),
+                        "damage_max_abs_diff": float(np.abs(de - dr).max()),
+                        "damaged_nodes": int((dr > 0).sum()),
+                        "crack_tip_x": {"engine": None if tip_e != tip_e else float(tip_e), "reference": tip_r,
+                                        "reference_warp_kernel": tip(dref["warp"]), "horizon": p.delta},
+                        "reference_kernels_between_themselves": {
+                            "damage_nodes_equal": float(np.mean(np.abs(dref["warp"] - dr) <= 1e-12)),
+                            "what": "kernel_bond_force_2D against kernel_particle_force_2D (same formulas, "
+                                    "different summation order)"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

@@ -95,10 +95,10 @@ class RefGPU:
 
     def get(self, NN=None):
         N, MN = self.N, self.MN
-        out = {k: np.zeros(N) for k in ("ux", "uy", "fx", "fy", "vy")}
+        out = {k: np.zeros(N) for k in ("ux", "uy", "fx", "fy", "vy", "dmg")}
         fail = np.zeros(N * MN, dtype=np.int32)
         self._check(self.lib.rr_get(_d(out["ux"]), _d(out["uy"]), _d(out["fx"]), _d(out["fy"]), _d(out["vy"]),
-                                    _i(fail)), "rr_get")
+                                    _i(fail), _d(out["dmg"])), "rr_get")
         if NN is not None:
             mask = (np.arange(MN)[None, :] < NN[:, None]).reshape(-1)
             out["fail"] = fail[mask]

@@ -296,8 +296,9 @@ int rr_run_adr(int ct0, int nsteps, double load, double* ms, double* cn_out) {
     return 0;
 }
 
-// Read back node fields (N doubles each; NULL skips) and the N*MN fail flags.
-int rr_get(double* ux, double* uy, double* fx, double* fy, double* vy, int* fail) {
+// Read back node fields (N doubles each; NULL skips), the N*MN fail flags and
+// the damage field (written by kernel_cal_dmg_2D at the damage steps of rr_run).
+int rr_get(double* ux, double* uy, double* fx, double* fy, double* vy, int* fail, double* dmg) {
     if (!R.ready) return -1;
     const size_t N = (size_t)R.p.N;
     RR_TRY(cuStreamSynchronize(R.stream), "sync");
@@ -307,6 +308,7 @@ int rr_get(double* ux, double* uy, double* fx, double* fy, double* vy, int* fail
     if (fy) RR_TRY(cuMemcpyDtoH(fy, R.fy, N * 8), "fy");
     if (vy) RR_TRY(cuMemcpyDtoH(vy, R.vy, N * 8), "vy");
     if (fail) RR_TRY(cuMemcpyDtoH(fail, R.fail, N * (size_t)R.p.MN * 4), "fail");
+    if (dmg) RR_TRY(cuMemcpyDtoH(dmg, R.dmg, N * 8), "dmg");
     return 0;
 }
 
