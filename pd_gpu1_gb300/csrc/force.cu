@@ -57,7 +57,6 @@ struct ForceArgs {
     const float2* k2f;  // k2 * 2^-S as a float pair
     const float* xif;   // bond reference vector rounded to float, per component (SoA)
     const float2* c0f;  // |xif|^2 - l0^2 (pair)
-    const float2* ecf;  // break threshold on e (pair; +inf: never)
     const float2* l0f;  // l0 (pair)
     double kscale;      // 2^S
     const double* c1;
@@ -490,8 +489,10 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int64_t slot, unsigned
     const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
 #pragma unroll
     for (int a = 0; a < DIM; a++) cf[a] = ff_mul(t, dp[a]);
-    const float2 ec = __ldg(A.ecf + slot);
-    return ff_gt(e2, ff{ec.x, ec.y});
+    // the break test in double against the double s0 l0: a threshold held as a
+    // pair (48 bits) moves near-threshold breaks by a step and, over a long
+    // fracture run, the crack path with them
+    return exceeds(f64_of_f32s(e2.h) + f64_of_f32s(e2.l), __ldg(A.ecrit + slot));
 }
 
 template <int DIM, int EPI>
@@ -862,7 +863,6 @@ static ForceArgs make_args(pd_ctx* c) {
     A.k2f = S.k2f;
     A.xif = S.xif;
     A.c0f = S.c0f;
-    A.ecf = S.ecf;
     A.l0f = S.l0f;
     A.kscale = S.kscale;
     A.c1 = S.c1;

@@ -57,7 +57,6 @@ struct Sell {
     float2* k2f = nullptr;   // [S] the same times 2^-kexp as a float pair (h, l)
     float* xif = nullptr;    // [S*dim] bond-based: x_c - x_i rounded to float per component (SoA blocks)
     float2* c0f = nullptr;   // [S] bond-based: |xif|^2 - l0^2 as a float pair (computed exactly)
-    float2* ecf = nullptr;   // [S] bond-based: ecrit as a float pair (h = +inf: never breaks)
     float2* l0f = nullptr;   // [S] bond-based: l0 as a float pair
     int kexp = 0;            // power-of-two scale that brings k2 near one
     double kscale = 1.0;     // 2^kexp

@@ -268,7 +268,6 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                 S.k2f[slot] = make_float2(0.0f, 0.0f);
                 for (int a = 0; a < P.dim; a++) S.xif[a * S.S + slot] = 0.0f;
                 S.c0f[slot] = make_float2(0.0f, 0.0f);
-                S.ecf[slot] = make_float2(__int_as_float(0x7f800000), 0.0f);
                 S.l0f[slot] = make_float2(1.0f, 0.0f);
             }
             if (S.c1) {
@@ -318,12 +317,7 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             S.c0f[slot] = make_float2(cf.h, cf.l);
             const ff lf = ff_split(L0);
             S.l0f[slot] = make_float2(lf.h, lf.l);
-            if (breakable) {
-                const ff ef = ff_split(S.ecrit[slot]);
-                S.ecf[slot] = make_float2(ef.h, ef.l);
-            } else {
-                S.ecf[slot] = make_float2(__int_as_float(0x7f800000), 0.0f);
-            }
+
         }
         if (S.c1) {
             const double pr = P.pratio;
@@ -501,7 +495,6 @@ static void free_sell(Sell& S) {
     free_ptr(S.k2f);
     free_ptr(S.xif);
     free_ptr(S.c0f);
-    free_ptr(S.ecf);
     free_ptr(S.l0f);
     free_ptr(S.c1);
     free_ptr(S.c2);
@@ -560,7 +553,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
               !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
     if (ok && !state)
         ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.k2f, n8) && !cudaMalloc(&S.xif, n4 * P.dim) &&
-             !cudaMalloc(&S.c0f, n8) && !cudaMalloc(&S.ecf, n8) && !cudaMalloc(&S.l0f, n8);
+             !cudaMalloc(&S.c0f, n8) && !cudaMalloc(&S.l0f, n8);
     // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,
     // so that the pair arithmetic of the force kernels stays in float range
     {
