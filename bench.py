@@ -8,7 +8,8 @@ of the force-computed nodes (broken bonds still count: both implementations
 visit them).  Setup (neighbour build, surface correction) is timed separately.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload crack_branching|plate_tensile|kalthoff_winkler|crack_grow|batch]
+                  [--workload crack_branching|plate_tensile|kalthoff_winkler|kalthoff_winkler_bond|
+                              crack_grow|batch|warm_start]
 
 --workload batch: 256 seeded uneven plates (6.25M interior nodes) solved
 together by ADR (1000 steps), against the same plates run one after another
@@ -138,9 +139,13 @@ def build_workload(name, scale, host_only=False):
         return presets.build_crack_branching(scale=scale, **kw)
     if name == "plate_tensile":
         return presets.build_plate_tensile(scale=scale, **kw)
-    if name == "kalthoff_winkler":
+    if name in ("kalthoff_winkler", "kalthoff_winkler_bond"):
+        from pd_gpu1_gb300._abi import PD_MODEL_BOND
+
         if host_only:
             kw["coord_fn"] = orc.coord_kw
+        if name == "kalthoff_winkler_bond":  # the reference's own impact driver is bond-based
+            kw["model"] = PD_MODEL_BOND
         return presets.build_kalthoff_winkler(scale=scale, **kw)
     if name == "crack_grow":
         return presets.build_crack_grow(scale=scale, **kw)
@@ -175,8 +180,11 @@ def cpu_reference(p, meta, eng_coords, max_seconds, max_steps, threads):
     elif w.startswith("plate_tensile"):
         m.surface_correct()
     elif w.startswith("kalthoff"):
-        m.vol_corr()
-        m.initial_weight()
+        if p.model == 1:
+            m.surface_correct()
+        else:
+            m.vol_corr()
+            m.initial_weight()
         m.set_crack_kw(meta["rad"])
     else:
         m.set_crack_2d(0.01 * p.length / 0.05, 0.0, 0.0, 0.0)
@@ -226,6 +234,79 @@ def reference_arm(args):
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def reference_cuda_kw(eng, p, setup, meta, args, value, B):
+    """The reference's impact-driver loop (kernel_bond_force_3D, kernel_contact,
+    the 3-D Verlet halves and the cylinder kernels, compiled from its sources)
+    on the same slab and GPU: its rate, and the intact flags and damage after
+    the whole run against the engine's, both from the same initial state (the
+    reference run twice: its contact reaction is summed by atomicAdd, so two of
+    its runs need not agree to the last bit)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+
+    if not ref_gpu.available():
+        return None
+    cyl = meta["cylinder"]
+    setup(eng)
+    r, NN = ref_gpu.from_engine(eng, p, cyl=cyl)
+    kref = min(args.steps, 300)
+    r.run_kw(args.warmup)
+    ms_ref = r.run_kw(kref)
+    rate = B * kref / (ms_ref * 1e-3)
+    runs = []
+    for _ in range(2):
+        setup(eng)
+        r.free()
+        r, NN = ref_gpu.from_engine(eng, p, cyl=cyl)
+        r.run_kw(args.steps)
+        out = r.get(NN)
+        out.update(r.get_z())
+        runs.append(out)
+    r.free()
+    # the engine twice: its tuned launch shape and one warp per slice (the
+    # impactor's reaction is then summed in another block order)
+    shape = eng.launch()
+    eng.set_launch(256, 0, 1, 1)
+    setup(eng)
+    run_steps(eng, meta, args.steps)
+    fe1, uy1 = eng.get("FAIL"), eng.get("UY")
+    eng.set_launch(*shape)
+    setup(eng)
+    cut = int((eng.get("FAIL") == 0).sum())  # the notch cuts
+    run_steps(eng, meta, args.steps)
+    fac = eng.get("FAC")
+    fe = eng.get("FAIL")
+    de = ref_gpu.damage_from_flags(NN, fe, fac, p.vol)[: p.N_int]
+    de1 = ref_gpu.damage_from_flags(NN, fe1, fac, p.vol)[: p.N_int]
+    dr = [ref_gpu.damage_from_flags(NN, o["fail"], fac, p.vol)[: p.N_int] for o in runs]
+    uy = eng.get("UY")
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    return {"unit": "bond-updates/s", "steps": kref, "kernel_bond_force_3D_loop": rate, "best": rate,
+            "engine_over_best": value / rate,
+            "what": "the reference's impact-driver loop (integrate_3D_1, cy_integrate_1, bond_force_3D, contact, "
+                    "integrate_3D_2, cy_integrate_2; compiled from its sources, FP64), kernel_integrate_3D_1 "
+                    "given its arrays by declared name",
+            "damage_after_steps": args.steps,
+            "damage_nodes_equal": float(np.mean(np.abs(de - dr[0]) <= 1e-12)),
+            "damage_max_abs_diff": float(np.abs(de - dr[0]).max()),
+            "bonds_broken": {"engine": int((fe == 0).sum()), "reference": int((runs[0]["fail"] == 0).sum()),
+                             "notch_cuts": cut},
+            "intact_flags_equal": float(np.mean(fe == runs[0]["fail"])),
+            "damaged_nodes": int((dr[0] > 0).sum()),
+            "uy_rel_diff": rel(uy, runs[0]["uy"]),
+            "impactor_vel_y": {"engine": float(eng.cylinder().vel[1]), "reference": float(runs[0]["cyl_vel"][1])},
+            "reference_runs_between_themselves": {
+                "damage_nodes_equal": float(np.mean(np.abs(dr[1] - dr[0]) <= 1e-12)),
+                "uy_rel_diff": rel(runs[1]["uy"], runs[0]["uy"])},
+            "engine_runs_between_launch_shapes": {
+                "shapes": [list(shape), [256, 0, 1, 1]],
+                "damage_nodes_equal": float(np.mean(np.abs(de1 - de) <= 1e-12)),
+                "uy_rel_diff": rel(uy1, uy)}}
 
 
 def r_inputs(eng, p):
@@ -789,6 +870,9 @@ def gb300_arm(args):
                             "what": "kernel_bond_force_2D against kernel_particle_force_2D (same formulas, "
                                     "different summation order)"}}
 
+    if rank == 0 and not args.no_ref_cuda and p.dim == 3 and p.model == 1 and meta["workload"].startswith("kalthoff"):
+        ref_cuda = reference_cuda_kw(eng, p, setup, meta, args, value, B)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         rate, steps, secs, bonds = cpu_reference(p, meta, host_coords(p, meta), max_seconds=args.cpu_seconds,
@@ -849,6 +933,7 @@ def main():
         args.warmup = 3
     if args.steps is None:
         args.steps = {"crack_branching": 1800, "plate_tensile": 1000, "kalthoff_winkler": 1350,
+                      "kalthoff_winkler_bond": 1350,
                       "crack_grow": 1250, "batch": 1000, "warm_start": 3}.get(args.workload, 1800)
     if args.workload == "batch":
         return batch_arm(args)

@@ -351,10 +351,12 @@ int pd_batch_get_cn(pd_ctx* ctx, double* cn, void* stream);
 /* ---- launch shape of the bond-force kernels ------------------------------ */
 /* Threads per block (128, 256, 512), warp-to-slice order (0: grid-strided,
  * 1: one contiguous run of slices per warp), grid size in waves of resident
- * blocks (1..8) and warps per slice (split: 1, 2, 4, 8; 2-D bond kernel,
+ * blocks (1..8) and warps per slice (split: 1, 2, 4, 8; bond kernels,
  * strided order only): with split > 1 the slots of a slice are shared by
- * that many warps and summed in slot order by the first, which multiplies
- * the bonds in flight on small problems.  The per-node force sums do not
+ * that many warps and summed by the first in the one-warp order (2-D: slot
+ * order; 3-D: blocks of 32 slots, each summed in slot order, then the block
+ * sums in order), which multiplies the bonds in flight on small problems and
+ * evens out the last wave on large 3-D ones.  The per-node force sums do not
  * depend on the shape; sums over the whole grid (the single-specimen ADR
  * damping coefficient, the impactor reaction) follow the block order and may
  * differ in the last bits.  Default 256 / 0 / 1 / 1.  The reference's two
@@ -365,7 +367,7 @@ int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves, int split);
 int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves, int* split);
 /* Times the bond-force kernel (reps launches per shape, at the current
  * displacements) over the shapes above (18 with split 1, 12 more with split
- * 2 and 4 in 2-D) and keeps the fastest; *best_ms receives its time per
+ * 2 and 4) and keeps the fastest; *best_ms receives its time per
  * launch.  Intact flags and forces are restored, so a run continues exactly
  * as without the call.  Bond-based contexts only. */
 int pd_autotune(pd_ctx* ctx, int reps, double* best_ms, void* stream);

@@ -43,6 +43,7 @@ class RefGPU:
         self.lib.rr_error.restype = C.c_char_p
         self.lib.rr_run.argtypes = [C.c_int, C.c_int, C.c_int, D]
         self.lib.rr_run_adr.argtypes = [C.c_int, C.c_int, C.c_double, D, D]
+        self.lib.rr_run_kw.argtypes = [C.c_int, D]
         self._check(self.lib.rr_init(CUBIN.encode()), "rr_init")
         self.N = self.MN = 0
 
@@ -72,6 +73,35 @@ class RefGPU:
         self._check(self.lib.rr_setup(_d(dv), _i(iv), _d(self.keep[0]), _d(self.keep[1]), _i(self.NNc), _i(a["NL"]),
                                       _d(a["idist"]), _d(a["scr"]), _d(a["fac"]), _i(a["fail"]), _d(self.keep[2]),
                                       _d(self.keep[3])), "rr_setup")
+
+    def setup_z(self, z, bz, cyl):
+        """Third component and impactor (cyl: rad mass height v x y z) of a 3-D
+        problem set up by :meth:`setup`; starts the cylinder as the impact
+        driver does."""
+        self.keep_z = [np.ascontiguousarray(v, dtype=np.float64) for v in (z, bz)]
+        c = np.ascontiguousarray(cyl, dtype=np.float64)
+        self._check(self.lib.rr_setup_z(_d(self.keep_z[0]), _d(self.keep_z[1]), _d(c)), "rr_setup_z")
+
+    def set_disp_z(self, uz):
+        uz = np.ascontiguousarray(uz, dtype=np.float64)
+        self._check(self.lib.rr_set_disp_z(_d(uz)), "rr_set_disp_z")
+
+    def force3(self):
+        self._check(self.lib.rr_force3(), "rr_force3")
+
+    def run_kw(self, nsteps):
+        """nsteps of the impact driver's loop; returns the elapsed ms."""
+        ms = C.c_double()
+        self._check(self.lib.rr_run_kw(nsteps, C.byref(ms)), "rr_run_kw")
+        return ms.value
+
+    def get_z(self):
+        """uz, vz, fz and the impactor state (acc, disp, vel, force)."""
+        out = {k: np.zeros(self.N) for k in ("uz", "vz", "fz")}
+        cyl = np.zeros(12)
+        self._check(self.lib.rr_get_z(_d(out["uz"]), _d(out["vz"]), _d(out["fz"]), _d(cyl)), "rr_get_z")
+        out.update(cyl_acc=cyl[0:3], cyl_disp=cyl[3:6], cyl_vel=cyl[6:9], cyl_force=cyl[9:12])
+        return out
 
     def set_disp(self, ux, uy):
         ux = np.ascontiguousarray(ux, dtype=np.float64)
@@ -108,11 +138,29 @@ class RefGPU:
         self.lib.rr_free()
 
 
-def from_engine(eng, p):
+def from_engine(eng, p, cyl=None):
     """A RefGPU loaded with the engine context's current problem (family,
-    coefficients, fail flags, body forces)."""
+    coefficients, fail flags, body forces; in 3-D also z and the impactor
+    ``cyl``, an object with rad, mass, height, v, x, y, z)."""
     r = RefGPU()
     NN = eng.get("NN")
     r.setup(p, eng.get("X"), eng.get("Y"), NN, eng.get("ROWPTR"), eng.get("NL"), eng.get("IDIST"), eng.get("SCR"),
             eng.get("FAC"), eng.get("FAIL"), eng.get("BX"), eng.get("BY"))
+    if p.dim == 3:
+        c = [0.0] * 7 if cyl is None else [cyl.rad, cyl.mass, cyl.height, cyl.v, cyl.x, cyl.y, cyl.z]
+        r.setup_z(eng.get("Z"), eng.get("BZ"), c)
     return r, NN
+
+
+def damage_from_flags(NN, fail, fac, vol=1.0):
+    """Node damage 1 - sum(fail vol fac) / sum(vol fac) over each row's bonds
+    (kernel_cal_dmg_2D/3D, Base_Function.cu:149-217), from CSR-ordered flags
+    and volume-correction factors; rows without bonds get 0."""
+    NN = np.asarray(NN, dtype=np.int64)
+    row = np.repeat(np.arange(len(NN)), NN)
+    fac = np.asarray(fac, dtype=np.float64)
+    num = np.bincount(row, weights=np.asarray(fail, dtype=np.float64) * vol * fac, minlength=len(NN))
+    den = np.bincount(row, weights=vol * fac, minlength=len(NN))
+    den[NN == 0] = 1.0
+    num[NN == 0] = 1.0
+    return 1.0 - num / den

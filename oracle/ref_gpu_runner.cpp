@@ -10,7 +10,26 @@
 // N threads (Solve_Plate_Tensile.cu:109), kernel_bond_force_2D over N*MN
 // threads (Force_Bond.cu:143-147), the Verlet halves over N_int threads
 // (Integrate.cu:204-209, :251-256), kernel_cal_dmg_2D over N_int*MN threads
-// (Solve_Plate_Crack_Grow.cu:301).
+// (Solve_Plate_Crack_Grow.cu:301); the impact driver's loop as written at
+// Solve_Kalthoff_Winkler.cu:406-430 (kernel_bond_force_3D over N*MN threads
+// with 3*256 doubles of shared memory, kernel_contact over N threads, the
+// cylinder kernels on one warp).
+//
+// Two deviations from the reference's own calls, both for defined behaviour:
+//  * kernel_integrate_3D_1 declares its z parameters as (disp_z, vel_z, acc_z)
+//    (Integrate.cu:188-191, Integrate.cuh:35-36) while the impact driver passes
+//    (vel_z, acc_z, disp_z) (Solve_Kalthoff_Winkler.cu:408-410), which would
+//    add dt/2 * disp_z to acc_z and never advance disp_z.  The runner passes
+//    the arrays by the declared names: the update of the reference's host twin
+//    integrate_1 (Integrate.cu:447-462).
+//  * kernel_cal_dmg_3D holds __syncthreads inside "if (i < N_int)"
+//    (Base_Function.cu:185-207), a divergent barrier in the last block when
+//    N_int*MN is not a multiple of the block; it is not launched.  The damage
+//    of a 3-D run is computed by the caller from the intact flags.
+// kernel_bond_force_3D stores the node sums of thread j == 0 without a bound
+// test (Force_Bond.cu:133-139), so the tail of the last block writes element
+// N of the force arrays; node arrays are allocated with kNodePad spare
+// elements to keep that store inside the allocation.
 #include <cuda.h>
 
 #include <cmath>
@@ -29,11 +48,20 @@ struct device_parameter {
     double mass, K, G;
 };
 
+constexpr size_t kNodePad = 256;
+
+// Cylinder_Parameter (Base.cuh:227-236) with real = double.
+struct cylinder_parameter {
+    double rad, mass, height, v, x, y, z;
+};
+
 struct Runner {
     CUcontext ctx = nullptr;
     CUmodule mod = nullptr;
     CUfunction f_particle = nullptr, f_bond = nullptr, f_int1 = nullptr, f_int2 = nullptr, f_dmg = nullptr;
     CUfunction f_cnn = nullptr, f_adr = nullptr, f_reduce = nullptr, f_qload = nullptr;
+    CUfunction f_bond3 = nullptr, f_int31 = nullptr, f_int32 = nullptr, f_contact = nullptr, f_cy1 = nullptr,
+               f_cy2 = nullptr, f_cyinit = nullptr;
     CUdeviceptr static_y = 0;  // Reduce.cu's block partial array
     CUstream stream = nullptr;
     device_parameter p{};
@@ -42,7 +70,9 @@ struct Runner {
                 dmg = 0, NN = 0, NL = 0, idist = 0, scr = 0, fac = 0, fail = 0;
     // ADR arrays (velhalf, velhalfold, pforceold per axis; kernel_cnn's outputs)
     CUdeviceptr vhx = 0, vhy = 0, vhox = 0, vhoy = 0, fox = 0, foy = 0, cn_xy = 0, disp_xy = 0;
-    bool ready = false;
+    // third component and the impactor (Cylinder: acc, disp, vel, force, 3 doubles each)
+    CUdeviceptr z = 0, uz = 0, vz = 0, az = 0, fz = 0, bz = 0, cacc = 0, cdisp = 0, cvel = 0, cforce = 0;
+    bool ready = false, has_z = false;
 };
 
 Runner R;
@@ -65,7 +95,8 @@ void free_all() {
     CUdeviceptr* all[] = {&R.x,     &R.y,   &R.ux,   &R.uy,   &R.vx,   &R.vy,    &R.ax,   &R.ay,
                           &R.fx,    &R.fy,  &R.bx,   &R.by,   &R.dmg,  &R.NN,    &R.NL,   &R.idist,
                           &R.scr,   &R.fac, &R.fail, &R.vhx,  &R.vhy,  &R.vhox,  &R.vhoy, &R.fox,
-                          &R.foy,   &R.cn_xy, &R.disp_xy};
+                          &R.foy,   &R.cn_xy, &R.disp_xy, &R.z,   &R.uz,    &R.vz,   &R.az,
+                          &R.fz,    &R.bz,  &R.cacc, &R.cdisp, &R.cvel, &R.cforce};
     for (CUdeviceptr* d : all)
         if (*d) {
             cuMemFree(*d);
@@ -73,8 +104,8 @@ void free_all() {
         }
 }
 
-int launch(CUfunction f, unsigned grid, void** args) {
-    RR_TRY(cuLaunchKernel(f, grid, 1, 1, 256, 1, 1, 0, R.stream, args, nullptr), "launch");
+int launch(CUfunction f, unsigned grid, void** args, unsigned block = 256, unsigned smem = 0) {
+    RR_TRY(cuLaunchKernel(f, grid, 1, 1, block, 1, 1, smem, R.stream, args, nullptr), "launch");
     return 0;
 }
 
@@ -106,6 +137,18 @@ int rr_init(const char* cubin) {
            "kernel_integrate");
     RR_TRY(cuModuleGetFunction(&R.f_reduce, R.mod, "_Z9reduce_cpPKdPdi"), "reduce_cp");
     RR_TRY(cuModuleGetFunction(&R.f_qload, R.mod, "harness_quick_load"), "harness_quick_load");
+    RR_TRY(cuModuleGetFunction(&R.f_bond3, R.mod, "_Z20kernel_bond_force_3DPdS_S_S_S_S_S_S_S_PiS0_S_S_S0_S_"),
+           "kernel_bond_force_3D");
+    RR_TRY(cuModuleGetFunction(&R.f_int31, R.mod, "_Z21kernel_integrate_3D_1PdS_S_S_S_S_S_S_S_"),
+           "kernel_integrate_3D_1");
+    RR_TRY(cuModuleGetFunction(&R.f_int32, R.mod, "_Z21kernel_integrate_3D_2PdS_S_S_S_S_S_S_S_S_S_S_"),
+           "kernel_integrate_3D_2");
+    RR_TRY(cuModuleGetFunction(&R.f_contact, R.mod, "_Z14kernel_contactiPdS_S_S_S_S_S_S_S_S_S_S_"),
+           "kernel_contact");
+    RR_TRY(cuModuleGetFunction(&R.f_cy1, R.mod, "_Z21kernel_cy_integrate_1PdS_S_"), "kernel_cy_integrate_1");
+    RR_TRY(cuModuleGetFunction(&R.f_cy2, R.mod, "_Z21kernel_cy_integrate_2PdS_S_"), "kernel_cy_integrate_2");
+    RR_TRY(cuModuleGetFunction(&R.f_cyinit, R.mod, "_Z23kernel_initial_cylinderPdS_S_S_"),
+           "kernel_initial_cylinder");
     size_t ys = 0;
     RR_TRY(cuModuleGetGlobal(&R.static_y, &ys, R.mod, "static_y"), "static_y");
     if (ys != 256 * sizeof(double)) return fail_with(CUDA_ERROR_INVALID_VALUE, "static_y size");
@@ -153,8 +196,8 @@ int rr_setup(const double* dparams, const int* iparams, const double* x, const d
                             &R.fy,  &R.bx,   &R.by,   &R.dmg, &R.vhx, &R.vhy,   &R.vhox,    &R.vhoy, &R.fox,
                             &R.foy, &R.cn_xy, &R.disp_xy};
     for (CUdeviceptr* d : nodes) {
-        RR_TRY(cuMemAlloc(d, N * 8), "node alloc");
-        RR_TRY(cuMemsetD8(*d, 0, N * 8), "node zero");
+        RR_TRY(cuMemAlloc(d, (N + kNodePad) * 8), "node alloc");
+        RR_TRY(cuMemsetD8(*d, 0, (N + kNodePad) * 8), "node zero");
     }
     RR_TRY(cuMemAlloc(&R.NN, N * 4), "NN");
     RR_TRY(cuMemAlloc(&R.NL, S * 4), "NL");
@@ -173,6 +216,39 @@ int rr_setup(const double* dparams, const int* iparams, const double* x, const d
     RR_TRY(cuMemcpyHtoD(R.fac, fac, S * 8), "fac");
     RR_TRY(cuMemcpyHtoD(R.fail, fail, S * 4), "fail");
     R.ready = true;
+    R.has_z = false;
+    return 0;
+}
+
+// Third component and impactor of a 3-D problem set up by rr_setup: z, bz (N
+// doubles each); cyl: rad mass height v x y z (Cylinder_Parameter), copied to
+// the reference's dcyp, then kernel_initial_cylinder as the impact driver
+// launches it (Solve_Kalthoff_Winkler.cu:403).
+int rr_setup_z(const double* z, const double* bz, const double* cyl) {
+    if (!R.ready) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup first");
+    const size_t N = (size_t)R.p.N;
+    CUdeviceptr* nodes[] = {&R.z, &R.uz, &R.vz, &R.az, &R.fz, &R.bz};
+    for (CUdeviceptr* d : nodes) {
+        RR_TRY(cuMemAlloc(d, (N + kNodePad) * 8), "node alloc");
+        RR_TRY(cuMemsetD8(*d, 0, (N + kNodePad) * 8), "node zero");
+    }
+    RR_TRY(cuMemcpyHtoD(R.z, z, N * 8), "z");
+    RR_TRY(cuMemcpyHtoD(R.bz, bz, N * 8), "bz");
+    CUdeviceptr* cy[] = {&R.cacc, &R.cdisp, &R.cvel, &R.cforce};
+    for (CUdeviceptr* d : cy) {
+        RR_TRY(cuMemAlloc(d, 4 * 8), "cylinder alloc");
+        RR_TRY(cuMemsetD8(*d, 0, 4 * 8), "cylinder zero");
+    }
+    cylinder_parameter c{cyl[0], cyl[1], cyl[2], cyl[3], cyl[4], cyl[5], cyl[6]};
+    CUdeviceptr cpp;
+    size_t cps;
+    RR_TRY(cuModuleGetGlobal(&cpp, &cps, R.mod, "dcyp"), "dcyp symbol");
+    if (cps != sizeof(cylinder_parameter)) return fail_with(CUDA_ERROR_INVALID_VALUE, "dcyp size");
+    RR_TRY(cuMemcpyHtoD(cpp, &c, sizeof(c)), "dcyp copy");
+    void* a[] = {&R.cvel, &R.cdisp, &R.cacc, &R.cforce};
+    if (launch(R.f_cyinit, 1, a, 32)) return -1;
+    RR_TRY(cuStreamSynchronize(R.stream), "cylinder init");
+    R.has_z = true;
     return 0;
 }
 
@@ -296,6 +372,81 @@ int rr_run_adr(int ct0, int nsteps, double load, double* ms, double* cn_out) {
     return 0;
 }
 
+// Set the third displacement component (N doubles).
+int rr_set_disp_z(const double* uz) {
+    if (!R.ready || !R.has_z) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_z first");
+    RR_TRY(cuMemcpyHtoD(R.uz, uz, (size_t)R.p.N * 8), "uz");
+    return 0;
+}
+
+// One kernel_bond_force_3D evaluation (rr_setup_z first).
+int rr_force3(void) {
+    if (!R.ready || !R.has_z) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_z first");
+    void* a[] = {&R.x, &R.ux, &R.fx, &R.y, &R.uy, &R.fy, &R.z, &R.uz, &R.fz, &R.NN, &R.NL, &R.idist, &R.scr,
+                 &R.fail, &R.fac};
+    const unsigned gS = (unsigned)(((int64_t)R.p.N * R.p.MN - 1) / 256 + 1);
+    if (launch(R.f_bond3, gS, a, 256, 3 * 256 * sizeof(double))) return -1;
+    RR_TRY(cuStreamSynchronize(R.stream), "force3");
+    return 0;
+}
+
+// nsteps of the impact driver's loop (Solve_Kalthoff_Winkler.cu:406-430):
+// integrate_3D_1, cy_integrate_1, bond_force_3D, contact, integrate_3D_2,
+// cy_integrate_2.  Elapsed time of the loop (CUDA events) in *ms.
+int rr_run_kw(int nsteps, double* ms) {
+    if (!R.ready || !R.has_z) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_z first");
+    int loc_begin = R.p.N_int - R.p.nx * R.p.ny;  // unused by kernel_contact (its use is commented out)
+    void* a1[] = {&R.vx, &R.ax, &R.ux, &R.vy, &R.ay, &R.uy, &R.uz, &R.vz, &R.az};  // declared order, see above
+    void* ac1[] = {&R.cvel, &R.cdisp, &R.cacc};
+    void* af[] = {&R.x, &R.ux, &R.fx, &R.y, &R.uy, &R.fy, &R.z, &R.uz, &R.fz, &R.NN, &R.NL, &R.idist, &R.scr,
+                  &R.fail, &R.fac};
+    void* ak[] = {&loc_begin, &R.dmg, &R.x, &R.ux, &R.vx, &R.y, &R.uy, &R.vy, &R.z, &R.uz, &R.vz, &R.cforce,
+                  &R.cdisp};
+    void* a2[] = {&R.vx, &R.ax, &R.fx, &R.bx, &R.vy, &R.ay, &R.fy, &R.by, &R.vz, &R.az, &R.fz, &R.bz};
+    void* ac2[] = {&R.cvel, &R.cacc, &R.cforce};
+    const unsigned g1 = (unsigned)((R.p.N - 1) / 256 + 1);
+    const unsigned g2 = (unsigned)(((int64_t)R.p.N * R.p.MN - 1) / 256 + 1);
+    const unsigned g3 = (unsigned)((R.p.N_int - 1) / 256 + 1);
+    CUevent e0, e1;
+    RR_TRY(cuEventCreate(&e0, CU_EVENT_DEFAULT), "event");
+    RR_TRY(cuEventCreate(&e1, CU_EVENT_DEFAULT), "event");
+    RR_TRY(cuEventRecord(e0, R.stream), "record");
+    for (int s = 0; s < nsteps; s++) {
+        if (launch(R.f_int31, g3, a1)) return -1;
+        if (launch(R.f_cy1, 1, ac1, 32)) return -1;
+        if (launch(R.f_bond3, g2, af, 256, 3 * 256 * sizeof(double))) return -1;
+        if (launch(R.f_contact, g1, ak)) return -1;
+        if (launch(R.f_int32, g3, a2)) return -1;
+        if (launch(R.f_cy2, 1, ac2, 32)) return -1;
+    }
+    RR_TRY(cuEventRecord(e1, R.stream), "record");
+    RR_TRY(cuEventSynchronize(e1), "sync");
+    float t = 0.f;
+    RR_TRY(cuEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+    cuEventDestroy(e0);
+    cuEventDestroy(e1);
+    return 0;
+}
+
+// Third-component node fields (N doubles each; NULL skips) and the impactor
+// state cyl[12] = acc, disp, vel, force (3 each; NULL skips).
+int rr_get_z(double* uz, double* vz, double* fz, double* cyl) {
+    if (!R.ready || !R.has_z) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_z first");
+    const size_t N = (size_t)R.p.N;
+    RR_TRY(cuStreamSynchronize(R.stream), "sync");
+    if (uz) RR_TRY(cuMemcpyDtoH(uz, R.uz, N * 8), "uz");
+    if (vz) RR_TRY(cuMemcpyDtoH(vz, R.vz, N * 8), "vz");
+    if (fz) RR_TRY(cuMemcpyDtoH(fz, R.fz, N * 8), "fz");
+    if (cyl) {
+        RR_TRY(cuMemcpyDtoH(cyl, R.cacc, 24), "cylinder acc");
+        RR_TRY(cuMemcpyDtoH(cyl + 3, R.cdisp, 24), "cylinder disp");
+        RR_TRY(cuMemcpyDtoH(cyl + 6, R.cvel, 24), "cylinder vel");
+        RR_TRY(cuMemcpyDtoH(cyl + 9, R.cforce, 24), "cylinder force");
+    }
+    return 0;
+}
+
 // Read back node fields (N doubles each; NULL skips), the N*MN fail flags and
 // the damage field (written by kernel_cal_dmg_2D at the damage steps of rr_run).
 int rr_get(double* ux, double* uy, double* fx, double* fy, double* vy, int* fail, double* dmg) {
@@ -315,6 +466,7 @@ int rr_get(double* ux, double* uy, double* fx, double* fy, double* vy, int* fail
 int rr_free(void) {
     free_all();
     R.ready = false;
+    R.has_z = false;
     return 0;
 }
 

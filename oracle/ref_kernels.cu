@@ -5,7 +5,9 @@
 // on the GPU machine by oracle/ref_gpu_runner.cpp through the CUDA driver API and
 // timed beside the engine.  The kernels are the reference's, unmodified; this
 // file only defines the constant-memory parameter blocks that main.cu defines
-// (main.cu:6-7) and one harness kernel (below).
+// (main.cu:6-7) and one harness kernel (below).  Solve_Kalthoff_Winkler.cu is
+// included for the impact driver's own kernels (cylinder start and halves,
+// contact); its host function is parsed but not part of the cubin.
 #include "Base.cuh"
 #include "Neighbor.cu"
 #include "Force_Bond.cu"
@@ -13,6 +15,7 @@
 #include "Integrate.cu"
 #include "Base_Function.cu"
 #include "Reduce.cu"
+#include "Solve_Kalthoff_Winkler.cu"
 
 __constant__ device_parameter dp;
 __constant__ Cylinder_Parameter dcyp;

@@ -1018,8 +1018,8 @@ int pd_set_launch(pd_ctx* c, int block, int chunked, int waves, int split) {
     if (!c || (block != 128 && block != 256 && block != 512) || (chunked != 0 && chunked != 1) || waves < 1 ||
         waves > 8 || (split != 1 && split != 2 && split != 4 && split != 8))
         return PD_ERR_ARG;
-    if (split > 1 && (chunked || block / 32 < split || c->p.dim != 2 || c->p.model != PD_MODEL_BOND))
-        return set_err(c, PD_ERR_ARG, "a split slice needs the 2-D bond kernel, strided order and block >= 32 split");
+    if (split > 1 && (chunked || block / 32 < split || c->p.model != PD_MODEL_BOND))
+        return set_err(c, PD_ERR_ARG, "a split slice needs the bond kernel, strided order and block >= 32 split");
     if (block != c->tune_block || chunked != c->tune_chunked || waves != c->tune_waves || split != c->tune_split) {
         drop_graphs(c);  // captured launches carry the old shape
         c->tune_block = block;
@@ -1041,7 +1041,7 @@ int pd_get_launch(const pd_ctx* c, int* block, int* chunked, int* waves, int* sp
 
 // Times the bond-force kernel at the current displacements for every launch
 // shape (block 128/256/512 x strided/chunked slice order x 1/2/4 waves of
-// resident blocks) and keeps the fastest.  The intact flags and forces are
+// resident blocks, and 2 or 4 warps per slice) and keeps the fastest.  The intact flags and forces are
 // restored afterwards, so a run continues exactly as it would have.
 int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     if (!c || reps < 1) return PD_ERR_ARG;
@@ -1057,13 +1057,15 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     double* saved_f = nullptr;
     cudaError_t e;
     if ((e = cudaMallocAsync(&saved_bits, nbits, s)) != cudaSuccess) return cuda_err(c, e, "autotune scratch");
-    if ((e = cudaMallocAsync(&saved_f, 2 * N * sizeof(double), s)) != cudaSuccess) {
+    const int nf = c->p.dim;  // force components saved and restored
+    const int fid[3] = {PD_F_FX, PD_F_FY, PD_F_FZ};
+    if ((e = cudaMallocAsync(&saved_f, nf * N * sizeof(double), s)) != cudaSuccess) {
         cudaFreeAsync(saved_bits, s);
         return cuda_err(c, e, "autotune scratch");
     }
     cudaMemcpyAsync(saved_bits, S.bits, nbits, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(saved_f, c->nf[PD_F_FX], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(saved_f + N, c->nf[PD_F_FY], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    for (int a = 0; a < nf; a++)
+        cudaMemcpyAsync(saved_f + a * N, c->nf[fid[a]], N * sizeof(double), cudaMemcpyDeviceToDevice, s);
     const bool csr_current = c->csr_fail_current, pos_valid = c->pos_valid;
     const int b0 = c->tune_block, k0 = c->tune_chunked, w0 = c->tune_waves, p0 = c->tune_split;
     StepFlags f;
@@ -1081,8 +1083,8 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     cudaEventCreate(&e1);
     double best = 1e300;
     int bb = b0, bk = k0, bw = w0, bp = p0;
-    // shapes: block x order x waves with one warp per slice, and for the 2-D
-    // kernel block x {2, 4} warps per slice x waves {1, 2}
+    // shapes: block x order x waves with one warp per slice, and block x
+    // {2, 4} warps per slice x waves {1, 2}
     struct Shape {
         int block, chunked, waves, split;
     };
@@ -1090,10 +1092,9 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     for (int blk : {128, 256, 512})
         for (int ck : {0, 1})
             for (int wv : {1, 2, 4}) shapes.push_back({blk, ck, wv, 1});
-    if (c->p.dim == 2)
-        for (int blk : {128, 256, 512})
-            for (int sp : {2, 4})
-                for (int wv : {1, 2}) shapes.push_back({blk, 0, wv, sp});
+    for (int blk : {128, 256, 512})
+        for (int sp : {2, 4})
+            for (int wv : {1, 2}) shapes.push_back({blk, 0, wv, sp});
     for (size_t ish = 0; ish < shapes.size() && !rc; ish++) {
                 c->tune_block = shapes[ish].block;
                 c->tune_chunked = shapes[ish].chunked;
@@ -1121,8 +1122,8 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
                 }
             }
     cudaMemcpyAsync(S.bits, saved_bits, nbits, cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(c->nf[PD_F_FX], saved_f, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
-    cudaMemcpyAsync(c->nf[PD_F_FY], saved_f + N, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    for (int a = 0; a < nf; a++)
+        cudaMemcpyAsync(c->nf[fid[a]], saved_f + a * N, N * sizeof(double), cudaMemcpyDeviceToDevice, s);
     cudaFreeAsync(saved_bits, s);
     cudaFreeAsync(saved_f, s);
     if (flush) cudaFreeAsync(flush, s);

@@ -102,6 +102,13 @@ namespace {
 
 constexpr int kWarpsPerBlock = kForceBlock / 32;
 constexpr int kMaxBondBlock = 512;  // the bond kernels take any block size up to this
+// The bond kernels are compiled for two resident 512-thread blocks per SM (64
+// registers a thread, 32 warps an SM).  Left alone the compiler takes 111
+// registers for the fused 3-D Verlet + contact epilogue and the SM holds 18
+// warps, too few to cover the neighbour gathers (measured on the 180,873-node
+// impact slab: 0.90 ms per step uncapped, 0.70 ms capped, a few spilled bytes
+// outside the slot loop); the 2-D kernels fit 64 without spilling.
+constexpr int kBondMinBlocks = 2;
 constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
 // Seed of the square-root iteration: the FP32 reciprocal square root (about
 // 23 correct bits, one Newton step to ~3e-14) or the FP64 one (about 20 bits,
@@ -496,7 +503,7 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int64_t slot, unsigned
 }
 
 template <int DIM, int EPI>
-__global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A) {
+__global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const KParams& P = A.P;
@@ -521,6 +528,7 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
             const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
             ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
+            ff bxa{0.0f, 0.0f}, bya{0.0f, 0.0f}, bza{0.0f, 0.0f};  // 3-D: sums of the current 32-slot block
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
@@ -537,9 +545,14 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
                 if (alive && kRecipe == 3) {
                     ff cf[3];
                     brk = bond3<DIM>(A, slot, (unsigned)c_cur, xi, yi, zi, uxi, uyi, uzi, cf);
-                    fxa = ff_add(fxa, cf[0]);
-                    fya = ff_add(fya, cf[1]);
-                    if (DIM == 3) fza = ff_add(fza, cf[2]);
+                    if (DIM == 3) {
+                        bxa = ff_add(bxa, cf[0]);
+                        bya = ff_add(bya, cf[1]);
+                        bza = ff_add(bza, cf[2]);
+                    } else {
+                        fxa = ff_add(fxa, cf[0]);
+                        fya = ff_add(fya, cf[1]);
+                    }
                 } else if (alive) {
                     const int c = A.col[slot];
                     const double dx = (A.pcx[c] - xi) - uxi;
@@ -572,6 +585,14 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_force(const ForceArgs A)
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+                if (DIM == 3 && kRecipe == 3 && ((k & 31) == 31 || k + 1 == W)) {
+                    // a 3-D row is summed in blocks of 32 slots, each from zero, the
+                    // block sums in block order: the order k_bond_split3 keeps
+                    fxa = ff_add(fxa, bxa);
+                    fya = ff_add(fya, bya);
+                    fza = ff_add(fza, bza);
+                    bxa = bya = bza = ff{0.0f, 0.0f};
+                }
             }
             if (kTailFF || kRecipe == 3) {
                 // undo the power-of-two scaling of the bond coefficient (exact)
@@ -658,6 +679,93 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_split(const ForceArgs A)
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
+// 3-D bond force with several warps per slice (A.split of them).  A 3-D row
+// (about 120 slots at a horizon of three spacings) is summed in blocks of 32
+// slots, each block from zero in slot order and the block sums in block order
+// (as k_bond_force<3> does), so warp `sub` of a slice group takes the blocks
+// sub, sub + split, ... and leaves their sums in shared memory for the
+// group's first warp: bit for bit the one-warp result.  It turns the 5,652
+// slices of the impact slab into four times as many shorter tasks, which
+// fill the SMs evenly where one slice per warp leaves a partial second wave.
+// Shared memory per group: ceil(wmax / 32) blocks x 3 components x 32 lanes
+// pairs.
+template <int EPI>
+__global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split3(const ForceArgs A) {
+    extern __shared__ __align__(16) unsigned char sm_raw[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int split = A.split, G = (int)(blockDim.x >> 5) / split;
+    const int g = wib / split, sub = wib % split;
+    const int nbm = (A.wmax + 31) / 32;
+    float2* bsum = reinterpret_cast<float2*>(sm_raw) + (size_t)g * nbm * 96;  // [block][component][lane]
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    const int64_t groups = (int64_t)gridDim.x * G;
+    const int64_t rounds = (A.nslices + groups - 1) / groups;
+    for (int64_t it = 0; it < rounds; it++) {
+        const int64_t s = it * groups + (int64_t)blockIdx.x * G + g;
+        const int64_t r = s * 32 + lane;
+        const bool in = s < A.nslices;
+        const bool force_row = in && r < A.nforce;
+        const bool work = in && s * 32 < A.nforce;
+        const int64_t rr = force_row ? r : (A.nforce > 0 ? A.nforce - 1 : 0);
+        double xi = 0.0, yi = 0.0, zi = 0.0, uxi = 0.0, uyi = 0.0, uzi = 0.0;
+        int W = 0;
+        if (work) {
+            xi = A.x[rr], yi = A.y[rr], zi = A.z[rr];
+            uxi = A.ux[rr], uyi = A.uy[rr], uzi = A.uz[rr];
+            W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            for (int kb = sub * 32; kb < W; kb += split * 32) {
+                const int ke = kb + 32 < W ? kb + 32 : W;
+                ff bx{0.0f, 0.0f}, by{0.0f, 0.0f}, bz{0.0f, 0.0f};
+                int c_next = __ldg(A.col + b + (int64_t)kb * 32 + lane);
+                for (int k = kb; k < ke; k++) {
+                    const int64_t slot = b + (int64_t)k * 32 + lane;
+                    const int c_cur = c_next;
+                    if (k + 1 < ke) c_next = __ldg(A.col + slot + 32);
+                    const uint32_t word = wbits[k];
+                    const bool alive = force_row && ((word >> lane) & 1u);
+                    bool brk = false;
+                    if (alive) {
+                        ff cf[3];
+                        brk = bond3<3>(A, slot, (unsigned)c_cur, xi, yi, zi, uxi, uyi, uzi, cf);
+                        bx = ff_add(bx, cf[0]);
+                        by = ff_add(by, cf[1]);
+                        bz = ff_add(bz, cf[2]);
+                    }
+                    const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                    if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+                }
+                float2* o = bsum + (size_t)(kb >> 5) * 96;
+                o[lane] = make_float2(bx.h, bx.l);
+                o[32 + lane] = make_float2(by.h, by.l);
+                o[64 + lane] = make_float2(bz.h, bz.l);
+            }
+        }
+        __syncthreads();
+        if (sub == 0 && work) {
+            ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
+            for (int kb = 0; kb < W; kb += 32) {
+                const float2* o = bsum + (size_t)(kb >> 5) * 96;
+                const float2 cx = o[lane], cy = o[32 + lane], cz = o[64 + lane];
+                fxa = ff_add(fxa, ff{cx.x, cx.y});
+                fya = ff_add(fya, ff{cy.x, cy.y});
+                fza = ff_add(fza, ff{cz.x, cz.y});
+            }
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
+            if (force_row) row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+            if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
+        }
+        if (sub == 0 && EPI == EPI_VERLET && A.do_next && in && !force_row && r < P.N) boundary_row<3>(A, r);
+        __syncthreads();
+    }
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
 // Dilatation pass (kernel_cal_theta_2D/3D): every row of [0, N).  Stores the
 // extension e per bond with the reference's operand order for this pass,
 // ((x_c - x_i) + u_c) - u_i, and theta/m per node.  The 2-D pass counts every
@@ -728,6 +836,7 @@ __global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) 
             const double nai = A.na[rr], nbi = A.nb[rr];
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
             ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
+            ff bxa{0.0f, 0.0f}, bya{0.0f, 0.0f}, bza{0.0f, 0.0f};  // 3-D: sums of the current 32-slot block
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
@@ -978,15 +1087,19 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
     const int blk = bond ? c->tune_block : kForceBlock;
     const int waves = bond ? c->tune_waves : 1;
     A.chunked = bond ? c->tune_chunked : 0;
-    if (bond && !d3 && c->tune_split > 1) {
-        // several warps per slice (k_bond_split), one wave of slice groups
+    if (bond && c->tune_split > 1) {
+        // several warps per slice (k_bond_split / k_bond_split3), one wave of slice groups
         A.split = c->tune_split;
         A.wmax = std::max(1, c->sell.wmax);
         const int G = (blk / 32) / A.split;
-        const size_t smem = (size_t)G * A.wmax * (64 * sizeof(float2) + sizeof(uint32_t));
-        const void* kern = f.epi == EPI_VERLET ? (const void*)k_bond_split<EPI_VERLET>
-                            : f.epi == EPI_ADR ? (const void*)k_bond_split<EPI_ADR>
-                                               : (const void*)k_bond_split<EPI_NONE>;
+        const size_t smem = d3 ? (size_t)G * ((A.wmax + 31) / 32) * 96 * sizeof(float2)
+                               : (size_t)G * A.wmax * (64 * sizeof(float2) + sizeof(uint32_t));
+        const void* kern = d3 ? (f.epi == EPI_VERLET ? (const void*)k_bond_split3<EPI_VERLET>
+                                 : f.epi == EPI_ADR  ? (const void*)k_bond_split3<EPI_ADR>
+                                                     : (const void*)k_bond_split3<EPI_NONE>)
+                              : (f.epi == EPI_VERLET ? (const void*)k_bond_split<EPI_VERLET>
+                                 : f.epi == EPI_ADR  ? (const void*)k_bond_split<EPI_ADR>
+                                                     : (const void*)k_bond_split<EPI_NONE>);
         if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int per_sm = 0;
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, blk, smem) != cudaSuccess || per_sm < 1)
@@ -994,14 +1107,23 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         const int64_t want = (A.nslices + G - 1) / G;
         const unsigned grid = (unsigned)std::max<int64_t>(
             1, std::min<int64_t>(std::min<int64_t>(want, (int64_t)c->num_sms * per_sm * waves), kMaxPartials));
-        if (f.epi == EPI_VERLET)
+        if (d3) {
+            if (f.epi == EPI_VERLET)
+                k_bond_split3<EPI_VERLET><<<grid, blk, smem, s>>>(A);
+            else if (f.epi == EPI_ADR)
+                k_bond_split3<EPI_ADR><<<grid, blk, smem, s>>>(A);
+            else
+                k_bond_split3<EPI_NONE><<<grid, blk, smem, s>>>(A);
+        } else if (f.epi == EPI_VERLET) {
             k_bond_split<EPI_VERLET><<<grid, blk, smem, s>>>(A);
-        else if (f.epi == EPI_ADR)
+        } else if (f.epi == EPI_ADR) {
             k_bond_split<EPI_ADR><<<grid, blk, smem, s>>>(A);
-        else
+        } else {
             k_bond_split<EPI_NONE><<<grid, blk, smem, s>>>(A);
+        }
         c->launches++;
         if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
+        if (f.epi == EPI_VERLET && f.contact && !f.do_next) c->pos_valid = false;  // contact moved u, not P
         c->csr_fail_current = false;
         return cuda_err(c, cudaGetLastError(), "bond force (split)");
     }

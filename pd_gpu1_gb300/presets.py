@@ -152,8 +152,8 @@ def build_kalthoff_winkler(scale=1.0, dx=1e-3, nt=1350, model=PD_MODEL_STATE, de
         eng.cylinder_init(cyl)
         eng.prepare()
 
-    return p, setup, dict(load=0.0, nt=nt, workload="kalthoff_winkler_3d_state_verlet", cylinder=cyl, s0=s0, rad=rad,
-                          coords=(x, y, z))
+    name = "kalthoff_winkler_3d_pmb_verlet" if model == PD_MODEL_BOND else "kalthoff_winkler_3d_state_verlet"
+    return p, setup, dict(load=0.0, nt=nt, workload=name, cylinder=cyl, s0=s0, rad=rad, coords=(x, y, z))
 
 
 # ---- crack growth, 2-D state-based, Verlet (the reference crack-grow driver) ---------

@@ -256,6 +256,47 @@ def test_split_slices_match(E):
     b.close()
 
 
+def test_split_slices_match_3d(E):
+    """The 3-D bond kernel with 2 and 4 warps per slice (k_bond_split3, blocks
+    of 32 slots per warp) against one warp per slice: forces and intact flags
+    bit for bit at strains that break bonds; an impact run within the chaos
+    bar (the impactor's reaction is a grid-wide sum in block order)."""
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=30, model=PD_MODEL_BOND)
+    engs = [E.Engine(p) for _ in range(4)]
+    for eng in engs:
+        setup(eng)
+    assert engs[0].get("NN").max() > 64  # rows span three 32-slot blocks
+    engs[1].set_launch(128, 0, 1, 2)
+    engs[2].set_launch(256, 0, 2, 4)
+    engs[3].set_launch(512, 1, 1, 1)  # one warp per slice, chunked order
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal((3, p.N)) * 8e-6  # strains of a few 1e-3, around s0 (4e-3 at dx = 2e-3)
+    for eng in engs:
+        for a, k in enumerate(["UX", "UY", "UZ"]):
+            eng.set(k, u[a])
+        for _ in range(2):  # the second pass sees the bonds the first one broke
+            eng.bond_force_gpu()
+    assert (engs[0].get("FAIL") == 0).sum() > (engs[0].get("FAIL").size // 100)
+    for eng in engs[1:]:
+        for k in ["FX", "FY", "FZ", "FAIL"]:
+            np.testing.assert_array_equal(eng.get(k), engs[0].get(k), err_msg=f"{eng.launch()} {k}")
+    for eng in engs:
+        eng.close()
+    a, b = E.Engine(p), E.Engine(p)
+    setup(a)
+    setup(b)
+    b.set_launch(256, 0, 1, 4)
+    a.run_explicit(30)
+    b.run_explicit(30)
+    for k in ["UX", "UY", "UZ"]:
+        assert_close_norm(b.get(k), a.get(k), 1e-9, k)
+    a.close()
+    b.close()
+
+
 def test_adr_single_calls_match_fused(E):
     """pd_bond_force + pd_integrate_adr per step equals the fused pd_run_adr."""
     from pd_gpu1_gb300 import presets

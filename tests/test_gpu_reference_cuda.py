@@ -78,3 +78,65 @@ def test_explicit_crack_branching_matches_reference_kernels(E):
         fail_e, fail_r = eng.get("FAIL"), out["fail"]
         assert (fail_e != fail_r).sum() <= 0.001 * len(fail_r)
         r.free()
+
+
+def test_bond_force_3d_matches_reference_kernel(E, golden):
+    """kernel_bond_force_3D (4 warps per node, the KW y >= -0.04 breaking guard)
+    against the engine's 3-D bond kernel: forces 1e-12, intact flags exact."""
+    g = golden("kalthoff_winkler_bond")
+    p = params_from_golden(g)
+    p.critical_s = float(g["f_s0"])  # low enough that bonds break
+    with E.Engine(p) as eng:
+        eng.set_coords(g["x"], g["y"], g["z"])
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
+        eng.set_crack_kw(float(g["rad"]))
+        cut = int((eng.get("FAIL") == 0).sum())  # the notch cuts
+        r, NN = ref_gpu.from_engine(eng, p)
+        u = {k: g["f_" + k] for k in ("ux", "uy", "uz")}
+        for k, v in u.items():
+            eng.set(k.upper(), v)
+        r.set_disp(u["ux"], u["uy"])
+        r.set_disp_z(u["uz"])
+        for _ in range(2):  # the second pass sees the bonds the first one broke
+            eng.bond_force_gpu()
+            r.force3()
+        out, oz = r.get(NN), r.get_z()
+        for k, ref in (("FX", out["fx"]), ("FY", out["fy"]), ("FZ", oz["fz"])):
+            assert_close_norm(eng.get(k), ref, 1e-12, k)
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+        assert (out["fail"] == 0).sum() > cut  # bonds broke beyond the notch cuts
+        r.free()
+
+
+def test_kalthoff_winkler_bond_matches_reference_loop(E):
+    """The impact driver's loop (Solve_Kalthoff_Winkler.cu:406-430) on the
+    reference's kernels against the engine's fused steps: 100 steps with the
+    impactor in contact from the start.  Displacements 1e-9 and the
+    impactor's velocity 1e-9; node velocities 1e-7, because contact sets a
+    projected node's velocity to (u_new - u_old) / dt (:159-161), which turns
+    a displacement difference at the 1e-12 m level into 1e-5 m/s at dt = 1e-7
+    s (measured: 1.1e-8 of the largest velocity after 100 steps)."""
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=100, model=PD_MODEL_BOND)
+    c = meta["cylinder"]
+    c.y -= 0.3 * p.dx  # start 0.3 dx into the slab: contact from the first step
+    with E.Engine(p) as eng:
+        setup(eng)  # starts the impactor of meta["cylinder"]
+        r, NN = ref_gpu.from_engine(eng, p, cyl=c)
+        eng.run_explicit(100)
+        r.run_kw(100)
+        out, oz = r.get(NN), r.get_z()
+        assert_close_norm(eng.get("UX"), out["ux"], 1e-9, "ux")
+        assert_close_norm(eng.get("UY"), out["uy"], 1e-9, "uy")
+        assert_close_norm(eng.get("UZ"), oz["uz"], 1e-9, "uz")
+        assert_close_norm(eng.get("VY"), out["vy"], 1e-7, "vy")
+        assert_close_norm(eng.get("VZ"), oz["vz"], 1e-7, "vz")
+        assert np.abs(out["uy"]).max() > 0.0
+        assert eng.cylinder().vel[1] == pytest.approx(oz["cyl_vel"][1], rel=1e-9)
+        assert oz["cyl_vel"][1] != -32.0  # the slab pushed back
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+        r.free()
