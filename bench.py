@@ -725,7 +725,10 @@ def gb300_arm(args):
     B = int(eng.get("ROWPTR")[p.N_int])
     is3d = p.dim == 3
     tuned = None
-    if p.model == 1 and not args.no_tune:
+    if p.model == 1 and args.launch:
+        tuned = tuple(int(v) for v in args.launch.split(","))
+        eng.set_launch(*tuned)
+    elif p.model == 1 and not args.no_tune:
         # launch shape of the bond kernel: the library's autotuner at the initial state
         with torch.cuda.stream(stream):
             tuned = eng.autotune(reps=5)
@@ -921,6 +924,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-ref-cuda", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default launch shape of the bond kernel")
+    ap.add_argument("--launch", default=None, help="fixed launch shape of the bond kernel, block,chunked,waves,split "
+                                                    "(instead of the autotuner)")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--count", type=int, default=256, help="batch workload: number of specimens")
     ap.add_argument("--seq-steps", type=int, default=100, help="batch workload: steps per plate when run one "

@@ -109,6 +109,10 @@ constexpr int kMaxBondBlock = 512;  // the bond kernels take any block size up t
 // impact slab: 0.90 ms per step uncapped, 0.70 ms capped, a few spilled bytes
 // outside the slot loop); the 2-D kernels fit 64 without spilling.
 constexpr int kBondMinBlocks = 2;
+// The state-force kernel likewise at four resident 256-thread blocks (64
+// registers): the 3-D instance drops from 70 registers, +6 % on the
+// Kalthoff-Winkler slab (1.52 -> 1.44 ms per step); the 2-D one is unchanged.
+constexpr int kStateMinBlocks = 4;
 constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
 // Seed of the square-root iteration: the FP32 reciprocal square root (about
 // 23 correct bits, one Newton step to ~3e-14) or the FP64 one (about 20 bits,
@@ -820,7 +824,7 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
 // State-based force pass (kernel_state_force_2D/3D) on rows [0, N_int):
 // t_i + t_j = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j) per bond.
 template <int DIM, int EPI>
-__global__ void __launch_bounds__(kForceBlock) k_state_force(const ForceArgs A) {
+__global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const KParams& P = A.P;
