@@ -5,25 +5,26 @@
 // (Force_State.cu:56-306).
 //
 // Mapping: one warp per SELL slice (32 consecutive node rows), lane l owns row
-// 32s+l and walks its bond slots k = 0..width-1.  Slot loads (neighbour id and
-// per-bond coefficients) are 32-wide coalesced; on the regular lattices of the
-// reference's drivers slot k of every interior row points at the same lattice
-// offset, so the neighbour gathers are coalesced as well.  The intact flags of
-// a slot are one 32-bit word, read once per warp and rewritten with a ballot
-// when bonds break.  Forces are summed per lane in registers (no shuffles).
+// 32s+l and walks its bond slots k = 0..width-1 (k_bond_force, k_state_force);
+// for small or 3-D problems several warps share a slice (k_bond_split,
+// k_bond_split3) and the first adds their parts in the one-warp order.  Slot
+// loads are 32-wide coalesced: a bond-based slot is one 48-byte BondRec
+// (three 128-bit loads), and the 32 records of a slot row are contiguous.  On
+// the regular lattices of the reference's drivers slot k of every interior
+// row points at the same lattice offset, so the neighbour gathers are
+// coalesced as well.  The intact flags of a slot are one 32-bit word, read
+// once per warp and rewritten with a ballot when bonds break.  Forces are
+// summed per lane in registers (no shuffles).
 //
-// GB300's FP64 pipe issues about 1/64 of the FP32 rate, so these kernels are
-// FP64-issue-bound, not HBM-bound.  Each bond therefore costs as few FP64
-// instructions as parity allows:
-//   d = (P_c - x_i) - u_i     P = x + u kept per node, so d rounds exactly as
-//                             the reference's x_c + u_c - x_i - u_i
-//   L^2 = d.d                 one product, one FMA
-//   L, 1/(2L)                 coupled Newton iteration from the hardware
-//                             reciprocal-square-root seed, then one residual
-//                             correction of L (no divide, no IEEE sqrt call)
-//   e = L - L0, t = k2 e h    k2 = 2 vol fac bc scr / L0 precomputed per bond
-//   f += t d                  one FMA per component
-// and breakage compares e with s0 L0 (precomputed) instead of dividing.
+// GB300's FP64 pipe issues about 1/64 of the FP32 rate, so each bond costs as
+// few FP64 instructions as parity allows.  Bond-based (bond3): the bond vector
+// d = (P_c - x_i) - u_i with the reference's roundings (P = x + u kept per
+// node, so d rounds exactly as x_c + u_c - x_i - u_i), 2 FP64 instructions
+// per component; its offset eta = d - xf from the per-slot float reference
+// vector exactly on the integer pipe; L^2 - l0^2 = c0 + 2 xf.eta + eta.eta,
+// 1/L, e = L - l0 and the force t (xf + eta) in pair-of-floats arithmetic
+// (ff.cuh); the break test e > s0 l0 in double.  State-based: FP64 bond
+// vector and L^2, the root and e by extension_ff.
 //
 // Epilogues fused into the same launch (one launch per explicit step):
 //   EPI_VERLET  a = (F+b)/rho; v += dt/2 a (kernel_integrate_2D_2, Integrate.cu:218-249),
@@ -53,11 +54,7 @@ struct ForceArgs {
     const int* col;
     const double* l0;
     const double* ecrit;
-    const double* k2;
-    const float2* k2f;  // k2 * 2^-S as a float pair
-    const float* xif;   // bond reference vector rounded to float, per component (SoA)
-    const float2* c0f;  // |xif|^2 - l0^2 (pair)
-    const float2* l0f;  // l0 (pair)
+    const BondRec* rec;  // bond-based: per-slot record (column, float reference vector, c0, l0, k2, ecrit)
     double kscale;      // 2^S
     const double* c1;
     const double* c2;
@@ -114,92 +111,18 @@ constexpr int kBondMinBlocks = 2;
 // Kalthoff-Winkler slab (1.52 -> 1.44 ms per step); the 2-D one is unchanged.
 constexpr int kStateMinBlocks = 4;
 constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
-// Seed of the square-root iteration: the FP32 reciprocal square root (about
-// 23 correct bits, one Newton step to ~3e-14) or the FP64 one (about 20 bits,
-// two steps).  On this GPU f64<->f32 conversion instructions issue on the FP64
-// pipe, so the FP32 seed moves between the formats with integer operations on
-// the IEEE-754 fields instead; it then costs 7 FP64 instructions against 11.
-constexpr bool kSeedFp32 = true;
-// Bond-force tail (t = k2 e h, f += t d) in pair arithmetic instead of FP64.
-constexpr bool kTailFF = true;
-// Bond kernels' per-bond recipe: 3 = the reference-rounded bond vector d and
-// its exact offset eta from a per-slot float reference vector, with the two
-// exact subtractions on the integer pipe and one FP64 subtraction per
-// component (the reference's rounding), then the extension from the
-// cancellation-free L^2 - l0^2 = c0 + 2 xif.eta + eta.eta in pairs; anything
-// else = the earlier recipe (FP64 bond vector, L^2, root residual and e: 10
-// FP64 instructions per 2-D bond).
-constexpr int kRecipe = 3;
 // P_c - x_i by integer operations (exact_sub.h) instead of an FP64 subtraction.
 // Measured slower on the 1.6M-node plate (1.01 ms against 0.85 ms per step):
 // the normalisation of the difference costs more issue slots than the FP64
 // instruction it replaces.
 constexpr bool kIntExactA = false;
 
-// float of a positive double whose exponent is within the float normal range:
-// rebias the 11-bit exponent to 8 bits and keep the top 23 mantissa bits
-// (truncation, relative error below 2^-23).  Integer pipe only.
-__device__ __forceinline__ float f32_of_f64(double x) {
-    const unsigned hi = (unsigned)__double2hiint(x);
-    const unsigned lo = (unsigned)__double2loint(x);
-    return __uint_as_float(((hi - (896u << 20)) << 3) | (lo >> 29));
-}
-
-// Exact double of a positive normal float (the inverse rebias); the second
-// result is the same value halved (exponent minus one).  Integer pipe only.
-__device__ __forceinline__ void f64_of_f32(float f, double& v, double& half) {
-    const unsigned b = __float_as_uint(f);
-    const unsigned hi = (b >> 3) + (896u << 20);
-    const int lo = (int)(b << 29);
-    v = __hiloint2double((int)hi, lo);
-    half = __hiloint2double((int)(hi - (1u << 20)), lo);
-}
-
-__device__ __forceinline__ double rsqrt_seed64(double x) {
-    double y;
-    asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
-    return y;
-}
-
-__device__ __forceinline__ float rsqrt_seed32(float x) {
-    float y;
-    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-// e = sqrt(x) - L0 and h = 1/(2 sqrt(x)) without a divide or a library sqrt:
-// the coupled Newton iteration for the square root and its reciprocal
-// (r = 1/2 - s h; s += s r; h += h r), then one residual correction of the
-// root folded into the subtraction, e = (s - L0) + (x - s^2) h, so that e
-// keeps the accuracy of an IEEE square root through the cancellation.
-__device__ __forceinline__ void extension(double x, double L0, double& e, double& h) {
-    double s;
-    if (kSeedFp32) {
-        double y;
-        f64_of_f32(rsqrt_seed32(f32_of_f64(x)), y, h);
-        s = x * y;
-        const double r = fma(-s, h, 0.5);
-        s = fma(s, r, s);
-        h = fma(h, r, h);
-    } else {
-        const double y = rsqrt_seed64(x);
-        s = x * y;
-        h = 0.5 * y;
-#pragma unroll
-        for (int it = 0; it < 2; it++) {
-            const double r = fma(-s, h, 0.5);
-            s = fma(s, r, s);
-            h = fma(h, r, h);
-        }
-    }
-    const double d = fma(-s, s, x);
-    e = fma(d, h, s - L0);
-}
-
-// The same quantities with the iteration in pair arithmetic: only the
-// residual correction and the cancelling subtraction stay in FP64 (s, its
-// square's residual and e), four FP64 instructions instead of eleven.  h is
-// returned as a pair, relative error ~2e-14.
+// e = sqrt(x) - L0 and h = 1/(2 sqrt(x)) (the state-based kernels' recipe):
+// the reciprocal square root in pair arithmetic (FP32 hardware seed, one
+// Newton step), then one residual correction of the root folded into the
+// cancelling subtraction in FP64, e = (s - L0) + (x - s^2) h: four FP64
+// instructions, no divide and no library sqrt.  h is returned as a pair,
+// relative error ~2e-14.
 __device__ __forceinline__ void extension_ff(double x, double L0, double& e, ff& h) {
     const ff xs = ff_split(x);
     const ff y = ff_rsqrt(xs);
@@ -470,40 +393,53 @@ __device__ void finish_reduction(const ForceArgs& A, double red[3], int nred) {
     }
 }
 
-// One bond of the pair-arithmetic recipe (kRecipe 3): its force contribution
-// t (xif + eta) per component as pairs (cf) and whether it breaks.
+// The three 16-byte words of a slot's BondRec: q0 = {col, xf[0..2]},
+// q1 = {c0, l0}, q2 = {k2, ecrit}.
+__device__ __forceinline__ int4 rec_q0(const BondRec* r, int64_t slot) {
+    return __ldg(reinterpret_cast<const int4*>(r + slot));
+}
+__device__ __forceinline__ float4 rec_q1(const BondRec* r, int64_t slot) {
+    return __ldg(reinterpret_cast<const float4*>(r + slot) + 1);
+}
+__device__ __forceinline__ float4 rec_q2(const BondRec* r, int64_t slot) {
+    return __ldg(reinterpret_cast<const float4*>(r + slot) + 2);
+}
+
+// One bond: its force contribution t (xf + eta) per component as pairs (cf)
+// and whether it breaks.
 //   d = (P_c - x_i) - u_i with the reference's roundings (FP64),
-//   eta = d - xif exactly (integer pipe), then everything in pairs:
-//   L^2 - l0^2 = c0 + 2 xif.eta + eta.eta, no cancellation.
+//   eta = d - xf exactly (integer pipe), then everything in pairs:
+//   L^2 - l0^2 = c0 + 2 xf.eta + eta.eta, no cancellation.
+// q0..q2: the slot's record words (the neighbour id is q0.x).
 template <int DIM>
-__device__ __forceinline__ bool bond3(const ForceArgs& A, int64_t slot, unsigned craw, double xi, double yi,
+__device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, float4 q2, double xi, double yi,
                                       double zi, double uxi, double uyi, double uzi, ff cf[3]) {
-    const int c = (int)craw;
+    const int c = q0.x;
     const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
     const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
+    const float xfs[3] = {__int_as_float(q0.y), __int_as_float(q0.z), __int_as_float(q0.w)};
     ff dp[3], D{0.0f, 0.0f}, Q{0.0f, 0.0f};
 #pragma unroll
     for (int a = 0; a < DIM; a++) {
-        const float xf = __ldg(A.xif + (int64_t)a * A.S + slot);
+        const float xf = xfs[a];
         const ff eta = bond_offset(pc[a], xr[a], ur[a], xf);
         D = ff_add(D, ff_mul_f(eta, xf));
         Q = ff_add(Q, ff_sq(eta));
         dp[a] = ff_add(ff{xf, 0.0f}, eta);
     }
-    const float2 c0 = __ldg(A.c0f + slot), l0 = __ldg(A.l0f + slot);
-    D = ff_add(ff_add(ff{c0.x, c0.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
-    const ff L0p{l0.x, l0.y};
+    D = ff_add(ff_add(ff{q1.x, q1.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
+    const ff L0p{q1.z, q1.w};
     const ff L2p = ff_add(ff_sq(L0p), D);
     const ff y = ff_rsqrt(L2p);                                  // 1/L
     const ff e2 = ff_mul(D, ff_rcp(ff_add(ff_mul(L2p, y), L0p)));  // L - l0
-    const float2 kf = __ldg(A.k2f + slot);
-    const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
+    const ff t = ff_mul(ff_mul(ff{q2.x, q2.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
 #pragma unroll
     for (int a = 0; a < DIM; a++) cf[a] = ff_mul(t, dp[a]);
     // the break test in double against the double s0 l0: a threshold held as a
     // pair (48 bits) moves near-threshold breaks by a step and, over a long
     // fracture run, the crack path with them
-    return exceeds(f64_of_f32s(e2.h) + f64_of_f32s(e2.l), __ldg(A.ecrit + slot));
+    const double ecrit = __hiloint2double(__float_as_int(q2.w), __float_as_int(q2.z));
+    return exceeds(f64_of_f32s(e2.h) + f64_of_f32s(e2.l), ecrit);
 }
 
 template <int DIM, int EPI>
@@ -536,19 +472,20 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
-            // neighbour index of the next slot loaded one iteration ahead, so the
-            // gather of slot k starts at the top of iteration k
-            int c_next = W > 0 ? __ldg(A.col + b + lane) : 0;
+            // the first record word of the next slot (neighbour id and float
+            // reference vector) loaded one iteration ahead, so the gather of
+            // slot k starts at the top of iteration k
+            int4 q0_next = W > 0 ? rec_q0(A.rec, b + lane) : make_int4(0, 0, 0, 0);
             for (int k = 0; k < W; k++) {
                 const int64_t slot = b + (int64_t)k * 32 + lane;
-                const int c_cur = c_next;
-                if (kRecipe == 3 && k + 1 < W) c_next = __ldg(A.col + slot + 32);
+                const int4 q0 = q0_next;
+                if (k + 1 < W) q0_next = rec_q0(A.rec, slot + 32);
                 const uint32_t word = wbits[k];
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
-                if (alive && kRecipe == 3) {
+                if (alive) {
                     ff cf[3];
-                    brk = bond3<DIM>(A, slot, (unsigned)c_cur, xi, yi, zi, uxi, uyi, uzi, cf);
+                    brk = bond3<DIM>(A, q0, rec_q1(A.rec, slot), rec_q2(A.rec, slot), xi, yi, zi, uxi, uyi, uzi, cf);
                     if (DIM == 3) {
                         bxa = ff_add(bxa, cf[0]);
                         bya = ff_add(bya, cf[1]);
@@ -557,39 +494,10 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
                         fxa = ff_add(fxa, cf[0]);
                         fya = ff_add(fya, cf[1]);
                     }
-                } else if (alive) {
-                    const int c = A.col[slot];
-                    const double dx = (A.pcx[c] - xi) - uxi;
-                    const double dy = (A.pcy[c] - yi) - uyi;
-                    double L2 = dx * dx;
-                    L2 = fma(dy, dy, L2);
-                    double dz = 0.0;
-                    if (DIM == 3) {
-                        dz = (A.pcz[c] - zi) - uzi;
-                        L2 = fma(dz, dz, L2);
-                    }
-                    double e;
-                    if (kTailFF) {
-                        ff hp;
-                        extension_ff(L2, A.l0[slot], e, hp);
-                        const float2 kf = A.k2f[slot];
-                        const ff t = ff_mul(ff_mul(ff{kf.x, kf.y}, ff_split(e)), hp);
-                        fxa = ff_add(fxa, ff_mul(t, ff_split(dx)));
-                        fya = ff_add(fya, ff_mul(t, ff_split(dy)));
-                        if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_split(dz)));
-                    } else {
-                        double h;
-                        extension(L2, A.l0[slot], e, h);
-                        const double t = (A.k2[slot] * e) * h;
-                        fxr = fma(t, dx, fxr);
-                        fyr = fma(t, dy, fyr);
-                        if (DIM == 3) fzr = fma(t, dz, fzr);
-                    }
-                    brk = exceeds(e, A.ecrit[slot]);
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
-                if (DIM == 3 && kRecipe == 3 && ((k & 31) == 31 || k + 1 == W)) {
+                if (DIM == 3 && ((k & 31) == 31 || k + 1 == W)) {
                     // a 3-D row is summed in blocks of 32 slots, each from zero, the
                     // block sums in block order: the order k_bond_split3 keeps
                     fxa = ff_add(fxa, bxa);
@@ -598,12 +506,10 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
                     bxa = bya = bza = ff{0.0f, 0.0f};
                 }
             }
-            if (kTailFF || kRecipe == 3) {
-                // undo the power-of-two scaling of the bond coefficient (exact)
-                fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-                fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
-                if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
-            }
+            // undo the power-of-two scaling of the bond coefficient (exact)
+            fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+            fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
@@ -621,7 +527,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
 // slots) the split multiplies the bonds in flight.  Shared memory per group:
 // wmax slots x 2 components x 32 lanes pairs + one alive word per slot.
 template <int EPI>
-__global__ void __launch_bounds__(kMaxBondBlock) k_bond_split(const ForceArgs A) {
+__global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split(const ForceArgs A) {
     extern __shared__ __align__(16) unsigned char sm_raw[];
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
     const int split = A.split, G = (int)(blockDim.x >> 5) / split;
@@ -653,7 +559,9 @@ __global__ void __launch_bounds__(kMaxBondBlock) k_bond_split(const ForceArgs A)
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
                 ff cf[3] = {{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}};
-                if (alive) brk = bond3<2>(A, slot, (unsigned)__ldg(A.col + slot), xi, yi, 0.0, uxi, uyi, 0.0, cf);
+                if (alive)
+                    brk = bond3<2>(A, rec_q0(A.rec, slot), rec_q1(A.rec, slot), rec_q2(A.rec, slot), xi, yi, 0.0, uxi,
+                                   uyi, 0.0, cf);
                 contrib[(k * 2 + 0) * 32 + lane] = make_float2(cf[0].h, cf[0].l);
                 contrib[(k * 2 + 1) * 32 + lane] = make_float2(cf[1].h, cf[1].l);
                 const uint32_t am = __ballot_sync(0xffffffffu, alive);
@@ -723,17 +631,18 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split3(c
             for (int kb = sub * 32; kb < W; kb += split * 32) {
                 const int ke = kb + 32 < W ? kb + 32 : W;
                 ff bx{0.0f, 0.0f}, by{0.0f, 0.0f}, bz{0.0f, 0.0f};
-                int c_next = __ldg(A.col + b + (int64_t)kb * 32 + lane);
+                int4 q0_next = rec_q0(A.rec, b + (int64_t)kb * 32 + lane);
                 for (int k = kb; k < ke; k++) {
                     const int64_t slot = b + (int64_t)k * 32 + lane;
-                    const int c_cur = c_next;
-                    if (k + 1 < ke) c_next = __ldg(A.col + slot + 32);
+                    const int4 q0 = q0_next;
+                    if (k + 1 < ke) q0_next = rec_q0(A.rec, slot + 32);
                     const uint32_t word = wbits[k];
                     const bool alive = force_row && ((word >> lane) & 1u);
                     bool brk = false;
                     if (alive) {
                         ff cf[3];
-                        brk = bond3<3>(A, slot, (unsigned)c_cur, xi, yi, zi, uxi, uyi, uzi, cf);
+                        brk = bond3<3>(A, q0, rec_q1(A.rec, slot), rec_q2(A.rec, slot), xi, yi, zi, uxi, uyi, uzi,
+                                       cf);
                         bx = ff_add(bx, cf[0]);
                         by = ff_add(by, cf[1]);
                         bz = ff_add(bz, cf[2]);
@@ -972,11 +881,7 @@ static ForceArgs make_args(pd_ctx* c) {
     A.col = S.col;
     A.l0 = S.l0;
     A.ecrit = S.ecrit;
-    A.k2 = S.k2;
-    A.k2f = S.k2f;
-    A.xif = S.xif;
-    A.c0f = S.c0f;
-    A.l0f = S.l0f;
+    A.rec = S.rec;
     A.kscale = S.kscale;
     A.c1 = S.c1;
     A.c2 = S.c2;

@@ -41,6 +41,19 @@ struct CylDev {
 };
 
 // Per-bond coefficient arrays of the SELL layout.
+// Per-slot data of the bond-based kernels, one 48-byte record per slot (three
+// 16-byte words, read with three 128-bit loads; the 32 records of a slot row
+// are one contiguous 1,536-byte run).
+struct alignas(16) BondRec {
+    int col;       // neighbour id (self for padding)
+    float xf[3];   // reference vector x_c - x_i rounded to float per component (z = 0 in 2-D)
+    float2 c0;     // |xf|^2 - l0^2 as a float pair (computed exactly)
+    float2 l0;     // l0 as a float pair
+    float2 k2;     // 2 vol fac bc scr / l0 times 2^-kexp as a float pair
+    double ecrit;  // break threshold on e = L - l0 (s0 l0; +inf: never)
+};
+static_assert(sizeof(BondRec) == 48, "BondRec is three 16-byte words");
+
 struct Sell {
     int64_t nslices = 0;     // ceil(N / 32)
     int64_t S = 0;           // total slots (sum of 32 * width)
@@ -54,10 +67,7 @@ struct Sell {
     double* l0 = nullptr;    // [S] reference length |xi|
     double* ecrit = nullptr; // [S] break threshold on e = L - l0 (s0 * l0; +inf: never)
     double* k2 = nullptr;    // [S] bond-based: 2 * vol*fac*bc*scr / l0
-    float2* k2f = nullptr;   // [S] the same times 2^-kexp as a float pair (h, l)
-    float* xif = nullptr;    // [S*dim] bond-based: x_c - x_i rounded to float per component (SoA blocks)
-    float2* c0f = nullptr;   // [S] bond-based: |xif|^2 - l0^2 as a float pair (computed exactly)
-    float2* l0f = nullptr;   // [S] bond-based: l0 as a float pair
+    BondRec* rec = nullptr;  // [S] bond-based: the force kernels' per-slot record
     int kexp = 0;            // power-of-two scale that brings k2 near one
     double kscale = 1.0;     // 2^kexp
     double kscale_inv = 1.0; // 2^-kexp

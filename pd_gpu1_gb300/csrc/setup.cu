@@ -265,10 +265,14 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             S.ecrit[slot] = HUGE_VAL;
             if (S.k2) {
                 S.k2[slot] = 0.0;
-                S.k2f[slot] = make_float2(0.0f, 0.0f);
-                for (int a = 0; a < P.dim; a++) S.xif[a * S.S + slot] = 0.0f;
-                S.c0f[slot] = make_float2(0.0f, 0.0f);
-                S.l0f[slot] = make_float2(1.0f, 0.0f);
+                BondRec R;
+                R.col = (int)(r < P.N ? r : 0);
+                R.xf[0] = R.xf[1] = R.xf[2] = 0.0f;
+                R.c0 = make_float2(0.0f, 0.0f);
+                R.l0 = make_float2(1.0f, 0.0f);
+                R.k2 = make_float2(0.0f, 0.0f);
+                R.ecrit = HUGE_VAL;
+                S.rec[slot] = R;
             }
             if (S.c1) {
                 S.c1[slot] = 0.0;
@@ -290,20 +294,25 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         // a batch of specimens carries bc and s0 per node (the row's specimen)
         const double s0 = node_s0 ? node_s0[r] : P.critical_s;
         const double bc = node_bc ? node_bc[r] : P.bc;
-        S.ecrit[slot] = breakable ? s0 * L0 : HUGE_VAL;
+        const double ecrit = breakable ? s0 * L0 : HUGE_VAL;
+        S.ecrit[slot] = ecrit;
         if (S.k2) {
             const double k2 = 2.0 * (P.vol * fac[q] * bc * scr[q]) / L0;
             S.k2[slot] = k2;
+            BondRec R;
+            R.col = (int)c;
+            R.ecrit = ecrit;
             const ff kf = ff_split(k2 * S.kscale_inv);
-            S.k2f[slot] = make_float2(kf.h, kf.l);
+            R.k2 = make_float2(kf.h, kf.l);
             // reference vector rounded to float per component, and the exact
-            // constant |xif|^2 - l0^2 (products of floats are exact doubles;
+            // constant |xf|^2 - l0^2 (products of floats are exact doubles;
             // the sums carried as double pairs, TwoSum / FMA TwoProduct)
             const double xa[3] = {x[c] - x[r], y[c] - y[r], P.dim == 3 ? z[c] - z[r] : 0.0};
             double sh = 0.0, sl = 0.0;
+            R.xf[2] = 0.0f;
             for (int a = 0; a < P.dim; a++) {
                 const float f = __double2float_rn(xa[a]);
-                S.xif[a * S.S + slot] = f;
+                R.xf[a] = f;
                 const double sq = (double)f * (double)f;  // exact: 24-bit x 24-bit mantissas
                 const double t = sh + sq;
                 const double bb = t - sh;
@@ -314,10 +323,10 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             const double pl = fma(L0, L0, -ph);
             const double c0 = (sh - ph) + (sl - pl);  // sh - ph exact: both within a factor 2 of l0^2
             const ff cf = ff_split(c0);
-            S.c0f[slot] = make_float2(cf.h, cf.l);
+            R.c0 = make_float2(cf.h, cf.l);
             const ff lf = ff_split(L0);
-            S.l0f[slot] = make_float2(lf.h, lf.l);
-
+            R.l0 = make_float2(lf.h, lf.l);
+            S.rec[slot] = R;
         }
         if (S.c1) {
             const double pr = P.pratio;
@@ -492,10 +501,7 @@ static void free_sell(Sell& S) {
     free_ptr(S.l0);
     free_ptr(S.ecrit);
     free_ptr(S.k2);
-    free_ptr(S.k2f);
-    free_ptr(S.xif);
-    free_ptr(S.c0f);
-    free_ptr(S.l0f);
+    free_ptr(S.rec);
     free_ptr(S.c1);
     free_ptr(S.c2);
     free_ptr(S.cth);
@@ -552,8 +558,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.l0, n8) &&
               !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
     if (ok && !state)
-        ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.k2f, n8) && !cudaMalloc(&S.xif, n4 * P.dim) &&
-             !cudaMalloc(&S.c0f, n8) && !cudaMalloc(&S.l0f, n8);
+        ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.rec, n8 * 6);
     // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,
     // so that the pair arithmetic of the force kernels stays in float range
     {
