@@ -162,6 +162,19 @@ __device__ __forceinline__ ff bond_offset(double pc, double xi, double ui, float
     const double d = a - ui;
     if (xf == 0.0f) return ff_split(d);
     const double x = f64_of_f32s(xf);
+    // usual case: d and x of the same sign and binade (eta is the small
+    // displacement-induced offset), where the difference of the bit patterns is
+    // the difference of the mantissas -- the value sub_exact_scaled forms, with
+    // two integer instructions instead of the exponent alignment
+    {
+        const long long bd = __double_as_longlong(d), bx = __double_as_longlong(x);
+        const int hd = (int)(bd >> 32), hx = (int)(bx >> 32);
+        const int eb = (hd >> 20) & 0x7ff;
+        long long df = bd - bx;
+        if (hd < 0) df = -df;
+        if (((hd ^ hx) & (int)0xfff00000) == 0 && eb >= 949 && eb <= 1170 && df < (1ll << 48) && df > -(1ll << 48))
+            return ff_from_scaled(df, eb);
+    }
     int64_t diff;
     int e;
     if (sub_exact_scaled(dbits(d), dbits(x), diff, e) && e >= 949 && e <= 1170 && diff < (1ll << 48) &&
@@ -175,6 +188,26 @@ __device__ __forceinline__ ff bond_offset(double pc, double xi, double ui, float
 // compare keeps the test off the FP64 pipe.
 __device__ __forceinline__ bool exceeds(double e, double ecrit) {
     return __double_as_longlong(e) > __double_as_longlong(ecrit);
+}
+
+// fl(h + l) > ecrit for a pair e = h + l (h = fl(h + l)) and a double ecrit >
+// 0, without the FP64 addition where the float h alone decides: with t =
+// ecrit truncated to float (t <= ecrit < next(t)), h at or above the second
+// float after t gives h + l >= next(t) > ecrit, and h below t gives
+// h + l <= t <= ecrit (|l| <= ulp(h) / 2; positive floats order like their
+// bit patterns, negative ones lie below).  Otherwise, and for thresholds
+// outside the float range, the double test decides as before.
+__device__ __forceinline__ bool pair_exceeds(ff e, double ecrit) {
+    const unsigned hi = (unsigned)__double2hiint(ecrit), lo = (unsigned)__double2loint(ecrit);
+    const unsigned E = hi >> 20;  // biased exponent (ecrit > 0)
+    if (E >= 1151u) return false;  // ecrit >= 2^128 (+inf: never breaks) exceeds every pair
+    if (E >= 897u) {
+        const int tb = (int)((((hi - (896u << 20)) << 3) | (lo >> 29)));
+        const int hb = __float_as_int(e.h);
+        if (hb >= tb + 2) return true;
+        if (hb < tb) return false;
+    }
+    return exceeds(f64_of_f32s(e.h) + f64_of_f32s(e.l), ecrit);
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sm) {
@@ -418,13 +451,15 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, fl
     const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
     const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
     const float xfs[3] = {__int_as_float(q0.y), __int_as_float(q0.z), __int_as_float(q0.w)};
-    ff dp[3], D{0.0f, 0.0f}, Q{0.0f, 0.0f};
+    ff dp[3], D, Q;
 #pragma unroll
     for (int a = 0; a < DIM; a++) {
         const float xf = xfs[a];
         const ff eta = bond_offset(pc[a], xr[a], ur[a], xf);
-        D = ff_add(D, ff_mul_f(eta, xf));
-        Q = ff_add(Q, ff_sq(eta));
+        // the first terms are taken as they are: ff_add of a zero pair and a
+        // pair that ff_fast produced returns that pair unchanged
+        D = a == 0 ? ff_mul_f(eta, xf) : ff_add(D, ff_mul_f(eta, xf));
+        Q = a == 0 ? ff_sq(eta) : ff_add(Q, ff_sq(eta));
         dp[a] = ff_add(ff{xf, 0.0f}, eta);
     }
     D = ff_add(ff_add(ff{q1.x, q1.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
@@ -438,8 +473,7 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, fl
     // the break test in double against the double s0 l0: a threshold held as a
     // pair (48 bits) moves near-threshold breaks by a step and, over a long
     // fracture run, the crack path with them
-    const double ecrit = __hiloint2double(__float_as_int(q2.w), __float_as_int(q2.z));
-    return exceeds(f64_of_f32s(e2.h) + f64_of_f32s(e2.l), ecrit);
+    return pair_exceeds(e2, __hiloint2double(__float_as_int(q2.w), __float_as_int(q2.z)));
 }
 
 template <int DIM, int EPI>
@@ -475,17 +509,20 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
             // the first record word of the next slot (neighbour id and float
             // reference vector) loaded one iteration ahead, so the gather of
             // slot k starts at the top of iteration k
+            // (prefetching the whole next record as well was measured slower: the
+            // twelve registers spill under the 64-register cap)
             int4 q0_next = W > 0 ? rec_q0(A.rec, b + lane) : make_int4(0, 0, 0, 0);
             for (int k = 0; k < W; k++) {
                 const int64_t slot = b + (int64_t)k * 32 + lane;
                 const int4 q0 = q0_next;
                 if (k + 1 < W) q0_next = rec_q0(A.rec, slot + 32);
+                const float4 q1 = rec_q1(A.rec, slot), q2 = rec_q2(A.rec, slot);
                 const uint32_t word = wbits[k];
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
                 if (alive) {
                     ff cf[3];
-                    brk = bond3<DIM>(A, q0, rec_q1(A.rec, slot), rec_q2(A.rec, slot), xi, yi, zi, uxi, uyi, uzi, cf);
+                    brk = bond3<DIM>(A, q0, q1, q2, xi, yi, zi, uxi, uyi, uzi, cf);
                     if (DIM == 3) {
                         bxa = ff_add(bxa, cf[0]);
                         bya = ff_add(bya, cf[1]);
