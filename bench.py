@@ -41,7 +41,7 @@ ALG_FP64_PER_BOND_2D = 23       # 10 add/sub, 8 mul, 3 div, 1 sqrt, 1 compare (s
 ALG_FP64_PER_BOND_3D = 31
 # measured DRAM bytes per bond and per node of the step kernel (ncu dram__bytes_read.sum +
 # dram__bytes_write.sum, one capture per workload)
-TRAFFIC = {"crack_branching_2d_pmb_verlet": (44.5, 139.8), "batch_plate_adr_2d_pmb": (49.5, 0.0)}
+TRAFFIC = {"crack_branching_2d_pmb_verlet": (48.9, 139.8)}
 
 
 def rank_info():
@@ -265,10 +265,11 @@ def reference_cuda_kw(eng, p, setup, meta, args, value, B):
         out.update(r.get_z())
         runs.append(out)
     r.free()
-    # the engine twice: its tuned launch shape and one warp per slice (the
-    # impactor's reaction is then summed in another block order)
+    # the engine twice: its tuned launch shape and another one (the impactor's
+    # reaction is then summed in another block order)
     shape = eng.launch()
-    eng.set_launch(256, 0, 1, 1)
+    alt = (256, 0, 1, 1) if tuple(shape) != (256, 0, 1, 1) else (128, 0, 1, 4)
+    eng.set_launch(*alt)
     setup(eng)
     run_steps(eng, meta, args.steps)
     fe1, uy1 = eng.get("FAIL"), eng.get("UY")
@@ -304,7 +305,7 @@ def reference_cuda_kw(eng, p, setup, meta, args, value, B):
                 "damage_nodes_equal": float(np.mean(np.abs(dr[1] - dr[0]) <= 1e-12)),
                 "uy_rel_diff": rel(runs[1]["uy"], runs[0]["uy"])},
             "engine_runs_between_launch_shapes": {
-                "shapes": [list(shape), [256, 0, 1, 1]],
+                "shapes": [list(shape), list(alt)],
                 "damage_nodes_equal": float(np.mean(np.abs(de1 - de) <= 1e-12)),
                 "uy_rel_diff": rel(uy1, uy)}}
 
@@ -634,6 +635,7 @@ def warm_arm(args):
     snap = os.path.join(tempfile.mkdtemp(), "state.snap")
     clocks = ClockSampler(torch.cuda.current_device())
     rows = []
+    learned_launches = 0  # kernels of the timed (learned-start) increments
     with E.Engine(p) as eng:
         setup(eng)
         B = int(eng.get("ROWPTR")[p.N_int])
@@ -643,7 +645,9 @@ def warm_arm(args):
             eng.snapshot_save(snap)
             plain = warm.run_increments(eng, meta, 1, mode="plain", start=W + j)[0]
             eng.snapshot_load(snap)
+            l0 = eng.kernel_launches
             learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j)[0]
+            learned_launches += eng.kernel_launches - l0
             rows.append((plain, learned))
         clk = clocks.stop()
         # the network's inference alone (features, four tcgen05 products, candidates)
@@ -691,7 +695,9 @@ def warm_arm(args):
                      "traffic": None, "peak_source": peak_kind, "inference_ms": infer_ms,
                      "note": "inference is <1 % of an increment; an increment is bound by the ADR force kernel"},
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": p.N * 8},
-        "gpu_launches": None, "clocks": clk, "cpu_baseline": None,
+        "gpu_launches": learned_launches // K, "gpu_launches_what": "per timed increment (ADR steps in CUDA graphs, "
+                                                                   "features, network, candidates)",
+        "clocks": clk, "cpu_baseline": None,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

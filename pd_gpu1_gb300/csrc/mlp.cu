@@ -421,6 +421,7 @@ struct pd_mlp {
     float* part = nullptr;  // split-K partials / column-sum partials
     int64_t part_floats = 0;
     int64_t step = 0;
+    int64_t launches = 0;  // kernels launched on this handle
     std::string errmsg;
 };
 
@@ -437,6 +438,7 @@ int launch_gemm(pd_mlp* n, const GemmArgs& a0, int nt, cudaStream_t s, int split
         k_gemm<16><<<grid, kThreads, 0, s>>>(a);
     else
         k_gemm<128><<<grid, kThreads, 0, s>>>(a);
+    n->launches++;
     return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
 }
 
@@ -475,6 +477,7 @@ int weight_grad(pd_mlp* n, const __nv_bfloat16* dZ, int64_t ldz, int64_t nout, c
     if (rc) return rc;
     const int64_t cnt = nout * nin;
     k_reduce_splits<<<(unsigned)((cnt + 255) / 256), 256, 0, s>>>(n->part, splits, cnt, out);
+    n->launches++;
     return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
 }
 
@@ -483,6 +486,7 @@ int bias_grad(pd_mlp* n, const __nv_bfloat16* dZ, int64_t M, int cols, float* ou
     const int blocks = (int)((M + rpb - 1) / rpb);
     k_colsum<<<blocks, 128, 0, s>>>(dZ, M, cols, rpb, n->part);
     k_reduce_splits<<<1, 128, 0, s>>>(n->part, blocks, cols, out);
+    n->launches += 2;
     return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
 }
 
@@ -493,6 +497,7 @@ int grad(pd_mlp* n, const __nv_bfloat16* X, const float* T, int64_t M, float* lo
     if (rc) return rc;
     const int lb = (int)std::min<int64_t>((M + kThreads - 1) / kThreads, 1024);
     k_loss<<<lb, kThreads, 0, s>>>(n->Y, T, M, n->dY, n->part);
+    n->launches++;
     // layer 4: dW4 = dY^T H3, db4 = colsum dY, dH3 = dY W4 -> dZ3
     std::vector<float> lp(lb);
     cudaMemcpyAsync(lp.data(), n->part, lb * sizeof(float), cudaMemcpyDeviceToHost, s);
@@ -517,6 +522,7 @@ int grad(pd_mlp* n, const __nv_bfloat16* X, const float* T, int64_t M, float* lo
     if ((rc = weight_grad(n, n->dZ, kHid, kHid, X, kInPad, kInPad, M, n->gW1, s))) return rc;
     if ((rc = bias_grad(n, n->dZ, M, kHid, n->gb1, s))) return rc;
     k_unpack_grad<<<64, 256, 0, s>>>(n->gW1, n->gb1, n->gW2, n->gb2, n->gW3, n->gb3, n->gW4, n->gb4, n->g);
+    n->launches++;
     int herr = 0;
     cudaMemcpyAsync(&herr, n->err, sizeof(int), cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
@@ -589,6 +595,7 @@ int pd_mlp_set_params(pd_mlp* n, const float* host, int64_t count) {
     cudaMemset(n->m2, 0, kParams * sizeof(float));
     n->step = 0;
     k_pack<<<64, 256>>>(n->p, n->W1, n->W2, n->W3, n->W4, n->b1, n->b2, n->b3, n->b4);
+    n->launches++;
     return cudaDeviceSynchronize() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
 }
 
@@ -637,6 +644,7 @@ int pd_mlp_train_step(pd_mlp* n, const void* dev_x, const float* dev_t, int64_t 
     const float c1 = 1.0f - std::pow(b1, (float)n->step), c2 = 1.0f - std::pow(b2, (float)n->step);
     k_adam<<<64, 256, 0, s>>>(n->p, n->g, n->m1, n->m2, lr, b1, b2, 1e-8f, c1, c2);
     k_pack<<<64, 256, 0, s>>>(n->p, n->W1, n->W2, n->W3, n->W4, n->b1, n->b2, n->b3, n->b4);
+    n->launches += 2;
     return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
 }
 
@@ -674,7 +682,9 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
         return set_err(c, PD_ERR_NOMEM, "warm outputs");
     }
     int rc = pd_warm_features(c, U, delta, nn_ref, x, s);
+    const int64_t l0 = n->launches;
     if (!rc) rc = pd_mlp_forward(n, x, ni, y, s);
+    c->launches += n->launches - l0;  // the network's kernels count as the context's
     if (!rc) {
         k_scale_out<<<(unsigned)std::min<int64_t>((ni + 255) / 256, 4096), 256, 0, s>>>(
             ni, y, U, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], dev_du);
