@@ -40,8 +40,10 @@ ALG_BYTES_PER_NODE_3D = 72.0
 ALG_FP64_PER_BOND_2D = 23       # 10 add/sub, 8 mul, 3 div, 1 sqrt, 1 compare (sqrt/div counted once)
 ALG_FP64_PER_BOND_3D = 31
 # measured DRAM bytes per bond and per node of the step kernel (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum, one capture per workload)
-TRAFFIC = {"crack_branching_2d_pmb_verlet": (48.9, 139.8)}
+# dram__bytes_write.sum, one capture per workload, summarised under profiles/; a zero per-node
+# figure means the node traffic is folded into the per-bond one)
+TRAFFIC = {"crack_branching_2d_pmb_verlet": (48.9, 139.8), "batch_plate_adr_2d_pmb": (55.0, 0.0),
+           "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0)}
 
 
 def rank_info():
@@ -310,6 +312,52 @@ def reference_cuda_kw(eng, p, setup, meta, args, value, B):
                 "uy_rel_diff": rel(uy1, uy)}}
 
 
+def reference_cuda_state(eng, p, setup, meta, args, value, B):
+    """The reference's crack-grow loop (kernel_cal_theta_2D, kernel_state_force_2D,
+    the Verlet halves and the boundary motion, compiled from its sources) on
+    the same plate and GPU: its rate, and the damage field after the whole
+    run against the engine's, both from the same initial state."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import ref_gpu
+
+    if not ref_gpu.available():
+        return None
+    setup(eng)
+    r, NN = ref_gpu.from_engine(eng, p)
+    kref = min(args.steps, 300)
+    r.run_state(args.warmup, meta["load"])
+    ms_ref = r.run_state(kref, meta["load"])
+    rate = B * kref / (ms_ref * 1e-3)
+    r.free()
+    setup(eng)
+    r, NN = ref_gpu.from_engine(eng, p)
+    r.run_state(args.steps, meta["load"], dmg_every=args.steps)  # kernel_cal_dmg_2D after the last step
+    out = r.get(NN)
+    r.free()
+    setup(eng)
+    run_steps(eng, meta, args.steps)
+    eng.damage()
+    de, dr = eng.get("DMG")[: p.N_int], out["dmg"][: p.N_int]
+    xs = eng.get("X")[: p.N_int]
+
+    def tip(d):
+        hot = np.nonzero(d > 0.38)[0]
+        return float(xs[hot].max()) if len(hot) else None
+
+    tip_e = eng.crack_tip(0.38)[0]
+    return {"unit": "bond-updates/s", "steps": kref, "kernel_state_force_2D_loop": rate, "best": rate,
+            "engine_over_best": value / rate,
+            "what": "the reference's crack-grow loop (quick_load, integrate_2D_1, cal_theta_2D, state_force_2D, "
+                    "integrate_2D_2; compiled from its sources, FP64)",
+            "damage_after_steps": args.steps,
+            "damage_nodes_equal": float(np.mean(np.abs(de - dr) <= 1e-12)),
+            "damage_max_abs_diff": float(np.abs(de - dr).max()),
+            "damaged_nodes": int((dr > 0).sum()),
+            "intact_flags_equal": float(np.mean(eng.get("FAIL") == out["fail"])),
+            "crack_tip_x": {"engine": None if tip_e != tip_e else float(tip_e), "reference": tip(dr),
+                            "horizon": p.delta}}
+
+
 def r_inputs(eng, p):
     """The engine context's problem in the argument order of RefGPU.setup."""
     return (eng.get("X"), eng.get("Y"), eng.get("NN"), eng.get("ROWPTR"), eng.get("NL"), eng.get("IDIST"),
@@ -455,8 +503,13 @@ def batch_arm(args):
             dist.barrier()
 
     # launch shape: the autotuner times the ADR force kernel at the initial state
-    with torch.cuda.stream(stream):
-        tuned = bat.autotune(reps=5)
+    # (or the fixed shape of --launch)
+    if args.launch:
+        bat.set_launch(*(int(v) for v in args.launch.split(",")))
+        tuned = bat.launch() + (None,)
+    else:
+        with torch.cuda.stream(stream):
+            tuned = bat.autotune(reps=5)
     # warm-up, then the timed steps
     with torch.cuda.stream(stream):
         bat.run_adr(0, args.warmup, load)
@@ -881,6 +934,8 @@ def gb300_arm(args):
 
     if rank == 0 and not args.no_ref_cuda and p.dim == 3 and p.model == 1 and meta["workload"].startswith("kalthoff"):
         ref_cuda = reference_cuda_kw(eng, p, setup, meta, args, value, B)
+    if rank == 0 and not args.no_ref_cuda and p.dim == 2 and p.model == 2 and meta["workload"].startswith("plate_crack"):
+        ref_cuda = reference_cuda_state(eng, p, setup, meta, args, value, B)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:

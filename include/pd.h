@@ -114,7 +114,8 @@ pd_ctx* pd_create(const pd_params* p, int* status);
 /* Base_Free (Memory.cu:276-284, which re-allocates instead of freeing). */
 int pd_destroy(pd_ctx* ctx);
 int pd_get_params(const pd_ctx* ctx, pd_params* out);
-/* Replace the parameters (same N/dim); cudaMemcpyToSymbol(dp, ...) of the drivers. */
+/* Replace the parameters (same N/dim/model; a batch keeps its dt);
+ * cudaMemcpyToSymbol(dp, ...) of the drivers. */
 int pd_set_params(pd_ctx* ctx, const pd_params* p);
 const char* pd_last_error(const pd_ctx* ctx);
 const char* pd_status_string(int status);

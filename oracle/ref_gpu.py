@@ -44,6 +44,7 @@ class RefGPU:
         self.lib.rr_run.argtypes = [C.c_int, C.c_int, C.c_int, D]
         self.lib.rr_run_adr.argtypes = [C.c_int, C.c_int, C.c_double, D, D]
         self.lib.rr_run_kw.argtypes = [C.c_int, D]
+        self.lib.rr_run_state.argtypes = [C.c_int, C.c_double, C.c_int, D]
         self._check(self.lib.rr_init(CUBIN.encode()), "rr_init")
         self.N = self.MN = 0
 
@@ -62,6 +63,7 @@ class RefGPU:
             out[mask] = v
             return out
 
+        self.ell = ell
         self.arrays = dict(NL=ell(NL, np.int32, 0), idist=ell(idist, np.float64, 1.0), scr=ell(scr, np.float64, 0.0),
                            fac=ell(fac, np.float64, 0.0), fail=ell(fail, np.int32, 1))
         dv = np.array([p.pi, p.dx, p.emod, p.dens, p.pratio, p.bc, p.delta, p.critical_s, p.vol, p.dt, p.mass, p.K,
@@ -85,6 +87,22 @@ class RefGPU:
     def set_disp_z(self, uz):
         uz = np.ascontiguousarray(uz, dtype=np.float64)
         self._check(self.lib.rr_set_disp_z(_d(uz)), "rr_set_disp_z")
+
+    def setup_state(self, m, w):
+        """Weighted volume m (N) and influence weights w (CSR order) of a 2-D
+        state-based problem set up by :meth:`setup`."""
+        self.m = np.ascontiguousarray(m, dtype=np.float64)
+        self.w = self.ell(w, np.float64, 0.0)
+        self._check(self.lib.rr_setup_state(_d(self.m), _d(self.w)), "rr_setup_state")
+
+    def force_state(self):
+        self._check(self.lib.rr_force_state(), "rr_force_state")
+
+    def run_state(self, nsteps, load, dmg_every=0):
+        """nsteps of the crack-grow driver's loop; returns the elapsed ms."""
+        ms = C.c_double()
+        self._check(self.lib.rr_run_state(nsteps, load, dmg_every, C.byref(ms)), "rr_run_state")
+        return ms.value
 
     def force3(self):
         self._check(self.lib.rr_force3(), "rr_force3")
@@ -149,6 +167,8 @@ def from_engine(eng, p, cyl=None):
     if p.dim == 3:
         c = [0.0] * 7 if cyl is None else [cyl.rad, cyl.mass, cyl.height, cyl.v, cyl.x, cyl.y, cyl.z]
         r.setup_z(eng.get("Z"), eng.get("BZ"), c)
+    if p.model == 2 and p.dim == 2:
+        r.setup_state(eng.get("M"), eng.get("W"))
     return r, NN
 
 

@@ -13,7 +13,9 @@
 // (Solve_Plate_Crack_Grow.cu:301); the impact driver's loop as written at
 // Solve_Kalthoff_Winkler.cu:406-430 (kernel_bond_force_3D over N*MN threads
 // with 3*256 doubles of shared memory, kernel_contact over N threads, the
-// cylinder kernels on one warp).
+// cylinder kernels on one warp); the crack-grow driver's state-based loop as
+// written at Solve_Plate_Crack_Grow.cu:126-149 (kernel_cal_theta_2D over N*MN
+// threads, kernel_state_force_2D over N_int*MN threads).
 //
 // Two deviations from the reference's own calls, both for defined behaviour:
 //  * kernel_integrate_3D_1 declares its z parameters as (disp_z, vel_z, acc_z)
@@ -61,7 +63,7 @@ struct Runner {
     CUfunction f_particle = nullptr, f_bond = nullptr, f_int1 = nullptr, f_int2 = nullptr, f_dmg = nullptr;
     CUfunction f_cnn = nullptr, f_adr = nullptr, f_reduce = nullptr, f_qload = nullptr;
     CUfunction f_bond3 = nullptr, f_int31 = nullptr, f_int32 = nullptr, f_contact = nullptr, f_cy1 = nullptr,
-               f_cy2 = nullptr, f_cyinit = nullptr;
+               f_cy2 = nullptr, f_cyinit = nullptr, f_theta2 = nullptr, f_state2 = nullptr;
     CUdeviceptr static_y = 0;  // Reduce.cu's block partial array
     CUstream stream = nullptr;
     device_parameter p{};
@@ -72,7 +74,9 @@ struct Runner {
     CUdeviceptr vhx = 0, vhy = 0, vhox = 0, vhoy = 0, fox = 0, foy = 0, cn_xy = 0, disp_xy = 0;
     // third component and the impactor (Cylinder: acc, disp, vel, force, 3 doubles each)
     CUdeviceptr z = 0, uz = 0, vz = 0, az = 0, fz = 0, bz = 0, cacc = 0, cdisp = 0, cvel = 0, cforce = 0;
-    bool ready = false, has_z = false;
+    // state-based: weighted volume m and dilatation theta per node, influence w and extension e per bond
+    CUdeviceptr m = 0, theta = 0, w = 0, e = 0;
+    bool ready = false, has_z = false, has_state = false;
 };
 
 Runner R;
@@ -96,7 +100,8 @@ void free_all() {
                           &R.fx,    &R.fy,  &R.bx,   &R.by,   &R.dmg,  &R.NN,    &R.NL,   &R.idist,
                           &R.scr,   &R.fac, &R.fail, &R.vhx,  &R.vhy,  &R.vhox,  &R.vhoy, &R.fox,
                           &R.foy,   &R.cn_xy, &R.disp_xy, &R.z,   &R.uz,    &R.vz,   &R.az,
-                          &R.fz,    &R.bz,  &R.cacc, &R.cdisp, &R.cvel, &R.cforce};
+                          &R.fz,    &R.bz,  &R.cacc, &R.cdisp, &R.cvel, &R.cforce, &R.m, &R.theta,
+                          &R.w,     &R.e};
     for (CUdeviceptr* d : all)
         if (*d) {
             cuMemFree(*d);
@@ -149,6 +154,10 @@ int rr_init(const char* cubin) {
     RR_TRY(cuModuleGetFunction(&R.f_cy2, R.mod, "_Z21kernel_cy_integrate_2PdS_S_"), "kernel_cy_integrate_2");
     RR_TRY(cuModuleGetFunction(&R.f_cyinit, R.mod, "_Z23kernel_initial_cylinderPdS_S_S_"),
            "kernel_initial_cylinder");
+    RR_TRY(cuModuleGetFunction(&R.f_theta2, R.mod, "_Z19kernel_cal_theta_2DPiPdS0_S_S0_S_S0_S0_S0_S0_S0_S0_S0_"),
+           "kernel_cal_theta_2D");
+    RR_TRY(cuModuleGetFunction(&R.f_state2, R.mod, "_Z21kernel_state_force_2DPiPdS0_S_S_S0_S0_S0_S0_S0_S0_S0_S0_S0_S0_"),
+           "kernel_state_force_2D");
     size_t ys = 0;
     RR_TRY(cuModuleGetGlobal(&R.static_y, &ys, R.mod, "static_y"), "static_y");
     if (ys != 256 * sizeof(double)) return fail_with(CUDA_ERROR_INVALID_VALUE, "static_y size");
@@ -217,6 +226,24 @@ int rr_setup(const double* dparams, const int* iparams, const double* x, const d
     RR_TRY(cuMemcpyHtoD(R.fail, fail, S * 4), "fail");
     R.ready = true;
     R.has_z = false;
+    R.has_state = false;
+    return 0;
+}
+
+// State-based arrays of a 2-D problem set up by rr_setup: m (N doubles, the
+// weighted volume) and w (N*MN padded ELL influence weights).
+int rr_setup_state(const double* m, const double* w) {
+    if (!R.ready) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup first");
+    const size_t N = (size_t)R.p.N, S = (size_t)R.p.N * R.p.MN;
+    RR_TRY(cuMemAlloc(&R.m, (N + kNodePad) * 8), "m");
+    RR_TRY(cuMemAlloc(&R.theta, (N + kNodePad) * 8), "theta");
+    RR_TRY(cuMemsetD8(R.theta, 0, (N + kNodePad) * 8), "theta zero");
+    RR_TRY(cuMemAlloc(&R.w, S * 8), "w");
+    RR_TRY(cuMemAlloc(&R.e, S * 8), "e");
+    RR_TRY(cuMemsetD8(R.e, 0, S * 8), "e zero");
+    RR_TRY(cuMemcpyHtoD(R.m, m, N * 8), "m copy");
+    RR_TRY(cuMemcpyHtoD(R.w, w, S * 8), "w copy");
+    R.has_state = true;
     return 0;
 }
 
@@ -372,6 +399,61 @@ int rr_run_adr(int ct0, int nsteps, double load, double* ms, double* cn_out) {
     return 0;
 }
 
+namespace {
+
+int launch_state2(void) {
+    void* at[] = {&R.NN, &R.m, &R.theta, &R.NL, &R.w, &R.fail, &R.e, &R.idist, &R.fac, &R.x, &R.ux, &R.y, &R.uy};
+    void* as[] = {&R.NN, &R.m, &R.theta, &R.fail, &R.NL, &R.e,  &R.w, &R.idist,
+                  &R.fac, &R.x, &R.ux, &R.fx, &R.y, &R.uy, &R.fy};
+    const unsigned g2 = (unsigned)(((int64_t)R.p.N * R.p.MN - 1) / 256 + 1);
+    const unsigned g4 = (unsigned)(((int64_t)R.p.N_int * R.p.MN - 1) / 256 + 1);
+    if (launch(R.f_theta2, g2, at)) return -1;
+    return launch(R.f_state2, g4, as);
+}
+
+}  // namespace
+
+// One state-based force evaluation: kernel_cal_theta_2D, kernel_state_force_2D.
+int rr_force_state(void) {
+    if (!R.ready || !R.has_state) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_state first");
+    if (launch_state2()) return -1;
+    RR_TRY(cuStreamSynchronize(R.stream), "force state");
+    return 0;
+}
+
+// nsteps of the crack-grow driver's loop (Solve_Plate_Crack_Grow.cu:126-149):
+// boundary motion, integrate_2D_1, cal_theta_2D, state_force_2D,
+// integrate_2D_2; kernel_cal_dmg_2D every dmg_every steps (0: never).
+int rr_run_state(int nsteps, double load, int dmg_every, double* ms) {
+    if (!R.ready || !R.has_state) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_state first");
+    void* aq[] = {&load, &R.uy};
+    void* a1[] = {&R.vx, &R.ax, &R.ux, &R.vy, &R.ay, &R.uy};
+    void* a2[] = {&R.vx, &R.ax, &R.fx, &R.bx, &R.vy, &R.ay, &R.fy, &R.by};
+    void* ad[] = {&R.NN, &R.dmg, &R.fail, &R.fac};
+    const unsigned gQ = (unsigned)((6 * R.p.nx - 1) / 256 + 1);
+    const unsigned g3 = (unsigned)((R.p.N_int - 1) / 256 + 1);
+    const unsigned g4 = (unsigned)(((int64_t)R.p.N_int * R.p.MN - 1) / 256 + 1);
+    CUevent e0, e1;
+    RR_TRY(cuEventCreate(&e0, CU_EVENT_DEFAULT), "event");
+    RR_TRY(cuEventCreate(&e1, CU_EVENT_DEFAULT), "event");
+    RR_TRY(cuEventRecord(e0, R.stream), "record");
+    for (int s = 0; s < nsteps; s++) {
+        if (load != 0.0 && launch(R.f_qload, gQ, aq)) return -1;
+        if (launch(R.f_int1, g3, a1)) return -1;
+        if (launch_state2()) return -1;
+        if (launch(R.f_int2, g3, a2)) return -1;
+        if (dmg_every > 0 && (s + 1) % dmg_every == 0 && launch(R.f_dmg, g4, ad)) return -1;
+    }
+    RR_TRY(cuEventRecord(e1, R.stream), "record");
+    RR_TRY(cuEventSynchronize(e1), "sync");
+    float t = 0.f;
+    RR_TRY(cuEventElapsedTime(&t, e0, e1), "elapsed");
+    *ms = t;
+    cuEventDestroy(e0);
+    cuEventDestroy(e1);
+    return 0;
+}
+
 // Set the third displacement component (N doubles).
 int rr_set_disp_z(const double* uz) {
     if (!R.ready || !R.has_z) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_z first");
@@ -467,6 +549,7 @@ int rr_free(void) {
     free_all();
     R.ready = false;
     R.has_z = false;
+    R.has_state = false;
     return 0;
 }
 

@@ -363,6 +363,8 @@ int pd_set_params(pd_ctx* c, const pd_params* p) {
     if (!c || !p) return PD_ERR_ARG;
     if (p->N != c->p.N || p->dim != c->p.dim || p->model != c->p.model || p->N_int > p->N || p->critical_s < 0.0)
         return set_err(c, PD_ERR_ARG, "pd_set_params cannot change N, dim or model");
+    if (c->batch.count && p->dt != c->p.dt)  // the per-node ADR coefficients were formed at pd_batch_create
+        return set_err(c, PD_ERR_ARG, "pd_set_params cannot change dt of a batch");
     c->p = *p;
     c->prepared = false;  // coefficients depend on the parameters
     drop_graphs(c);

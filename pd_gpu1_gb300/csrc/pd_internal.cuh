@@ -89,6 +89,7 @@ struct BatchInfo {
     double* node_sed = nullptr;        // [N] surface-correction energy density of the node's specimen
     double* node_s0 = nullptr;         // [N] critical stretch of the node's specimen
     double* node_mass = nullptr;       // [N] ADR fictitious mass per node
+    double* node_c1 = nullptr;         // [N] 2 dt / mass per node (the update's coefficient, host-computed)
     double* load_sign = nullptr;       // [N] signed load factor of moving boundary rows, 0 elsewhere
     int* slice_inst = nullptr;         // [nslices] specimen of each slice (-1: none)
     int64_t* inst_slices = nullptr;    // [count + 1] first slice of each specimen's interior

@@ -236,7 +236,9 @@ def test_autotune_leaves_the_run_unchanged(E, base):
 
 
 def test_batch_refuses_single_plate_loops(E, base):
-    from pd_gpu1_gb300._abi import PD_ERR_STATE, PD_ERR_UNSUPPORTED
+    import ctypes as C
+
+    from pd_gpu1_gb300._abi import PD_ERR_ARG, PD_ERR_STATE, PD_ERR_UNSUPPORTED
 
     b, load = base
     bat = E.Batch(b, SPECS[:2])
@@ -247,6 +249,9 @@ def test_batch_refuses_single_plate_loops(E, base):
     assert lib.pd_batch_run_adr(one.ctx, 0, 1, load, None) == PD_ERR_STATE
     assert lib.pd_set_launch(one.ctx, 64, 0, 1, 1) != 0
     assert lib.pd_set_launch(one.ctx, 128, 1, 1, 2) != 0  # a split slice needs the strided order
+    q = bat.params()
+    q.dt = 2.0 * q.dt
+    assert lib.pd_set_params(bat.ctx, C.byref(q)) == PD_ERR_ARG  # per-node coefficients hold the batch's dt
     one.close()
     bat.close()
 

@@ -140,3 +140,51 @@ def test_kalthoff_winkler_bond_matches_reference_loop(E):
         assert oz["cyl_vel"][1] != -32.0  # the slab pushed back
         np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
         r.free()
+
+
+def test_state_force_2d_matches_reference_kernels(E):
+    """kernel_cal_theta_2D + kernel_state_force_2D against the engine's
+    state-based passes on a cracked plate with boundary rows: forces 1e-12,
+    intact flags exact, at strains around s0 (0.04472)."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_grow(scale=0.2, nt=10)
+    with E.Engine(p) as eng:
+        setup(eng)
+        cut = int((eng.get("FAIL") == 0).sum())
+        r, NN = ref_gpu.from_engine(eng, p)
+        rng = np.random.default_rng(11)
+        u = rng.standard_normal((2, p.N)) * 2.5e-6  # dx = 1e-4: bond strains of a few percent
+        for eng_k, k in (("UX", 0), ("UY", 1)):
+            eng.set(eng_k, u[k])
+        r.set_disp(u[0], u[1])
+        for _ in range(2):  # the second pass sees the bonds the first one broke
+            eng.state_force_gpu()
+            r.force_state()
+        out = r.get(NN)
+        assert_close_norm(eng.get("FX")[: p.N_int], out["fx"][: p.N_int], 1e-12, "fx")
+        assert_close_norm(eng.get("FY")[: p.N_int], out["fy"][: p.N_int], 1e-12, "fy")
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+        assert (out["fail"] == 0).sum() > cut  # bonds broke beyond the pre-crack
+        r.free()
+
+
+def test_crack_grow_matches_reference_loop(E):
+    """The crack-grow driver's state-based loop (Solve_Plate_Crack_Grow.cu:126-149)
+    on the reference's kernels against the engine's steps: 40 steps with the
+    boundary rows moving; displacements and velocities 1e-9, flags equal."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_grow(scale=0.2, nt=40)
+    with E.Engine(p) as eng:
+        setup(eng)
+        r, NN = ref_gpu.from_engine(eng, p)
+        eng.run_explicit(40, load=meta["load"])
+        r.run_state(40, meta["load"])
+        out = r.get(NN)
+        assert_close_norm(eng.get("UY"), out["uy"], 1e-9, "uy")
+        assert_close_norm(eng.get("UX"), out["ux"], 1e-9, "ux")
+        assert_close_norm(eng.get("VY"), out["vy"], 1e-9, "vy")
+        assert np.abs(out["uy"][: p.N_int]).max() > 0.0
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+        r.free()
