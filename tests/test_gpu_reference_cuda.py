@@ -188,3 +188,28 @@ def test_crack_grow_matches_reference_loop(E):
         assert np.abs(out["uy"][: p.N_int]).max() > 0.0
         np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
         r.free()
+
+
+def test_explicit_1000_steps_before_breakage_match_reference_kernels(E):
+    """Before any bond breaks: 1,000 explicit Verlet steps of the traction-loaded
+    crack-branching plate (critical stretch raised so that no bond breaks)
+    on the engine and on the reference's particle-force loop; displacements
+    and velocities 1e-9 norm-relative, intact flags identical (the pre-crack
+    only)."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_branching(scale=0.05, nt=1000)
+    p.critical_s = 1.0  # no bond stretches by 100 %
+    with E.Engine(p) as eng:
+        setup(eng)
+        cut = eng.get("FAIL").copy()
+        r, NN = ref_gpu.from_engine(eng, p)
+        eng.run_explicit(1000)
+        r.run(ref_gpu.RefGPU.PARTICLE, 1000)
+        out = r.get(NN)
+        for k, ref in (("UX", out["ux"]), ("UY", out["uy"]), ("VY", out["vy"])):
+            assert_close_norm(eng.get(k), ref, 1e-9, k)
+        assert np.abs(out["uy"]).max() > 0.0
+        np.testing.assert_array_equal(eng.get("FAIL"), cut)
+        np.testing.assert_array_equal(out["fail"], cut)
+        r.free()
