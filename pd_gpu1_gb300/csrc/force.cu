@@ -23,8 +23,12 @@
 // per component; its offset eta = d - xf from the per-slot float reference
 // vector exactly on the integer pipe; L^2 - l0^2 = c0 + 2 xf.eta + eta.eta,
 // 1/L, e = L - l0 and the force t (xf + eta) in pair-of-floats arithmetic
-// (ff.cuh); the break test e > s0 l0 in double.  State-based: FP64 bond
-// vector and L^2, the root and e by extension_ff.
+// (ff.cuh); the break test e > s0 l0 decided on the pair, the double sum only
+// near the threshold.  State-based (k_theta, k_state_force): the same
+// stretch arithmetic on a 96-byte StateRec per slot, with the bond vector in
+// the dilatation pass's operand order ((x_c - x_i) + u_c) - u_i for theta and
+// the force pass's (P_c - x_i) - u_i for the force, as the reference rounds
+// them; e in double for theta and the stored extension.
 //
 // Epilogues fused into the same launch (one launch per explicit step):
 //   EPI_VERLET  a = (F+b)/rho; v += dt/2 a (kernel_integrate_2D_2, Integrate.cu:218-249),
@@ -52,14 +56,10 @@ struct ForceArgs {
     const int64_t* base;
     const int64_t* fbase;
     const int* col;
-    const double* l0;
     const double* ecrit;
     const BondRec* rec;  // bond-based: per-slot record (column, float reference vector, c0, l0, k2, ecrit)
     double kscale;      // 2^S
-    const double* c1;
-    const double* c2;
-    const double* cth;
-    const double* xi;
+    const StateRec* srec;  // state-based: per-slot record (column, reference vectors, c0, l0, coefficients)
     double* e;
     uint32_t* bits;
     int64_t S;
@@ -117,22 +117,6 @@ constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
 // instruction it replaces.
 constexpr bool kIntExactA = false;
 
-// e = sqrt(x) - L0 and h = 1/(2 sqrt(x)) (the state-based kernels' recipe):
-// the reciprocal square root in pair arithmetic (FP32 hardware seed, one
-// Newton step), then one residual correction of the root folded into the
-// cancelling subtraction in FP64, e = (s - L0) + (x - s^2) h: four FP64
-// instructions, no divide and no library sqrt.  h is returned as a pair,
-// relative error ~2e-14.
-__device__ __forceinline__ void extension_ff(double x, double L0, double& e, ff& h) {
-    const ff xs = ff_split(x);
-    const ff y = ff_rsqrt(xs);
-    const ff sp = ff_mul(xs, y);
-    const double s = f64_of_f32s(sp.h) + f64_of_f32s(sp.l);
-    h = ff{0.5f * y.h, 0.5f * y.l};
-    const double d = fma(-s, s, x);
-    e = fma(d, f64_of_f32s(h.h), s - L0);
-}
-
 // diff * 2^(e - 1075) as a normalized pair; exact for |diff| < 2^48 and a
 // scale within the float range (the caller checks both).
 __device__ __forceinline__ ff ff_from_scaled(int64_t diff, int e) {
@@ -144,22 +128,12 @@ __device__ __forceinline__ ff ff_from_scaled(int64_t diff, int e) {
 
 __device__ __forceinline__ uint64_t dbits(double v) { return (uint64_t)__double_as_longlong(v); }
 
-// One component of a bond: d = (P_c - x_i) - u_i with the reference's
-// roundings and eta = d - xf exactly, as a pair.  The two exact subtractions
-// run on the integer pipe (exact_sub.h) and fall back to FP64 outside
-// Sterbenz's range; the rounding one is an FP64 subtraction.
-__device__ __forceinline__ ff bond_offset(double pc, double xi, double ui, float xf) {
-    double a;
-    if (kIntExactA) {
-        uint64_t ua;
-        if (sub_exact(dbits(pc), dbits(xi), ua))
-            a = __longlong_as_double((long long)ua);
-        else
-            a = pc - xi;
-    } else {
-        a = pc - xi;
-    }
-    const double d = a - ui;
+// eta = d - xf exactly, as a pair, for a rounded bond-vector component d and
+// its per-slot float reference xf (d - xf is exact by Sterbenz's lemma; it is
+// formed on the integer pipe and falls back to FP64 outside the usual range).
+// bond_offset (below) forms d = (P_c - x_i) - u_i with the reference's
+// roundings first, the rounding subtraction in FP64.
+__device__ __forceinline__ ff exact_offset(double d, float xf) {
     if (xf == 0.0f) return ff_split(d);
     const double x = f64_of_f32s(xf);
     // usual case: d and x of the same sign and binade (eta is the small
@@ -181,6 +155,20 @@ __device__ __forceinline__ ff bond_offset(double pc, double xi, double ui, float
         diff > -(1ll << 48))
         return ff_from_scaled(diff, e);
     return ff_split(d - x);
+}
+
+__device__ __forceinline__ ff bond_offset(double pc, double xi, double ui, float xf) {
+    double a;
+    if (kIntExactA) {
+        uint64_t ua;
+        if (sub_exact(dbits(pc), dbits(xi), ua))
+            a = __longlong_as_double((long long)ua);
+        else
+            a = pc - xi;
+    } else {
+        a = pc - xi;
+    }
+    return exact_offset(a - ui, xf);
 }
 
 // e > ecrit for ecrit > 0: ordered like the IEEE bit patterns read as signed
@@ -438,11 +426,34 @@ __device__ __forceinline__ float4 rec_q2(const BondRec* r, int64_t slot) {
     return __ldg(reinterpret_cast<const float4*>(r + slot) + 2);
 }
 
+// From the exact offsets eta of a bond vector from its float reference xf
+// (per component) and the slot's c0 = |xf|^2 - l0^2 and l0 (pairs): the bond
+// vector xf + eta (dp), 1/L (y) and e = L - l0 (e2), all as pairs.
+//   L^2 - l0^2 = c0 + 2 xf.eta + eta.eta has no cancellation;
+//   e = (L^2 - l0^2) / (L + l0).
+template <int DIM>
+__device__ __forceinline__ void pair_stretch(const ff eta[3], const float xf[3], float2 c0, float2 l0, ff dp[3],
+                                             ff& y, ff& e2) {
+    ff D, Q;
+#pragma unroll
+    for (int a = 0; a < DIM; a++) {
+        // the first terms are taken as they are: ff_add of a zero pair and a
+        // pair that ff_fast produced returns that pair unchanged
+        D = a == 0 ? ff_mul_f(eta[a], xf[a]) : ff_add(D, ff_mul_f(eta[a], xf[a]));
+        Q = a == 0 ? ff_sq(eta[a]) : ff_add(Q, ff_sq(eta[a]));
+        dp[a] = ff_add(ff{xf[a], 0.0f}, eta[a]);
+    }
+    D = ff_add(ff_add(ff{c0.x, c0.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
+    const ff L0p{l0.x, l0.y};
+    const ff L2p = ff_add(ff_sq(L0p), D);
+    y = ff_rsqrt(L2p);                                     // 1/L
+    e2 = ff_mul(D, ff_rcp(ff_add(ff_mul(L2p, y), L0p)));  // L - l0
+}
+
 // One bond: its force contribution t (xf + eta) per component as pairs (cf)
 // and whether it breaks.
 //   d = (P_c - x_i) - u_i with the reference's roundings (FP64),
-//   eta = d - xf exactly (integer pipe), then everything in pairs:
-//   L^2 - l0^2 = c0 + 2 xf.eta + eta.eta, no cancellation.
+//   eta = d - xf exactly (integer pipe), then everything in pairs.
 // q0..q2: the slot's record words (the neighbour id is q0.x).
 template <int DIM>
 __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, float4 q2, double xi, double yi,
@@ -451,22 +462,10 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, fl
     const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
     const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
     const float xfs[3] = {__int_as_float(q0.y), __int_as_float(q0.z), __int_as_float(q0.w)};
-    ff dp[3], D, Q;
+    ff eta[3], dp[3], y, e2;
 #pragma unroll
-    for (int a = 0; a < DIM; a++) {
-        const float xf = xfs[a];
-        const ff eta = bond_offset(pc[a], xr[a], ur[a], xf);
-        // the first terms are taken as they are: ff_add of a zero pair and a
-        // pair that ff_fast produced returns that pair unchanged
-        D = a == 0 ? ff_mul_f(eta, xf) : ff_add(D, ff_mul_f(eta, xf));
-        Q = a == 0 ? ff_sq(eta) : ff_add(Q, ff_sq(eta));
-        dp[a] = ff_add(ff{xf, 0.0f}, eta);
-    }
-    D = ff_add(ff_add(ff{q1.x, q1.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
-    const ff L0p{q1.z, q1.w};
-    const ff L2p = ff_add(ff_sq(L0p), D);
-    const ff y = ff_rsqrt(L2p);                                  // 1/L
-    const ff e2 = ff_mul(D, ff_rcp(ff_add(ff_mul(L2p, y), L0p)));  // L - l0
+    for (int a = 0; a < DIM; a++) eta[a] = bond_offset(pc[a], xr[a], ur[a], xfs[a]);
+    pair_stretch<DIM>(eta, xfs, make_float2(q1.x, q1.y), make_float2(q1.z, q1.w), dp, y, e2);
     const ff t = ff_mul(ff_mul(ff{q2.x, q2.y}, e2), ff{0.5f * y.h, 0.5f * y.l});
 #pragma unroll
     for (int a = 0; a < DIM; a++) cf[a] = ff_mul(t, dp[a]);
@@ -475,6 +474,13 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, fl
     // fracture run, the crack path with them
     return pair_exceeds(e2, __hiloint2double(__float_as_int(q2.w), __float_as_int(q2.z)));
 }
+
+// Record words of a StateRec (16 bytes each).
+__device__ __forceinline__ float4 srec_w(const StateRec* r, int64_t slot, int w) {
+    return __ldg(reinterpret_cast<const float4*>(r + slot) + w);
+}
+__device__ __forceinline__ double lo_f64(float4 v) { return __hiloint2double(__float_as_int(v.y), __float_as_int(v.x)); }
+__device__ __forceinline__ double hi_f64(float4 v) { return __hiloint2double(__float_as_int(v.w), __float_as_int(v.z)); }
 
 template <int DIM, int EPI>
 __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(const ForceArgs A) {
@@ -743,20 +749,20 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
             bool use = k < nn;
             if (check_bits) use = use && ((wbits[k] >> lane) & 1u);
             if (use) {
-                const int c = A.col[slot];
-                const double dx = (A.xi[slot] + A.ux[c]) - uxi;
-                const double dy = (A.xi[A.S + slot] + A.uy[c]) - uyi;
-                double L2 = dx * dx;
-                L2 = fma(dy, dy, L2);
-                if (DIM == 3) {
-                    const double dz = (A.xi[2 * A.S + slot] + A.uz[c]) - uzi;
-                    L2 = fma(dz, dz, L2);
-                }
-                double e;
-                ff h;
-                extension_ff(L2, A.l0[slot], e, h);
+                const float4 w0 = srec_w(A.srec, slot, 0), w1 = srec_w(A.srec, slot, 1);
+                const float4 w2 = srec_w(A.srec, slot, 2), w3 = srec_w(A.srec, slot, 3);
+                const int c = __float_as_int(w0.x);
+                const float xf[3] = {w0.y, w0.z, w0.w};
+                // d = (xi + u_c) - u_i, the dilatation pass's operand order, then
+                // its exact offset from xf and the extension in pairs
+                ff eta[3], dp[3], y, e2;
+                eta[0] = exact_offset((lo_f64(w2) + A.ux[c]) - uxi, xf[0]);
+                eta[1] = exact_offset((hi_f64(w2) + A.uy[c]) - uyi, xf[1]);
+                if (DIM == 3) eta[2] = exact_offset((lo_f64(w3) + A.uz[c]) - uzi, xf[2]);
+                pair_stretch<DIM>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
+                const double e = f64_of_f32s(e2.h) + f64_of_f32s(e2.l);
                 A.e[slot] = e;
-                acc = fma(A.cth[slot], e, acc);
+                acc = fma(hi_f64(w3), e, acc);
             }
         }
         if (row) {
@@ -796,29 +802,29 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
                 if (alive) {
-                    const int c = A.col[slot];
-                    const double dx = (A.pcx[c] - xi) - uxi;
-                    const double dy = (A.pcy[c] - yi) - uyi;
-                    double L2 = dx * dx;
-                    L2 = fma(dy, dy, L2);
-                    double dz = 0.0;
+                    const float4 w0 = srec_w(A.srec, slot, 0), w1 = srec_w(A.srec, slot, 1);
+                    const float4 w4 = srec_w(A.srec, slot, 4), w5 = srec_w(A.srec, slot, 5);
+                    const int c = __float_as_int(w0.x);
+                    const float xf[3] = {w0.y, w0.z, w0.w};
+                    // d = (P_c - x_i) - u_i, the force pass's operand order, then its
+                    // exact offsets from xf and the stretch in pairs
+                    ff eta[3], dp[3], y, e2, etaz{0.0f, 0.0f};
+                    eta[0] = bond_offset(A.pcx[c], xi, uxi, xf[0]);
+                    eta[1] = bond_offset(A.pcy[c], yi, uyi, xf[1]);
                     if (DIM == 3) {
                         // the reference's 3-D force kernel takes the z term of the
                         // length in the dilatation pass's operand order (Force_State.cu:272)
-                        const double dzl = (A.xi[2 * A.S + slot] + A.uz[c]) - uzi;
-                        dz = (A.pcz[c] - zi) - uzi;
-                        L2 = fma(dzl, dzl, L2);
+                        eta[2] = exact_offset((lo_f64(srec_w(A.srec, slot, 3)) + A.uz[c]) - uzi, xf[2]);
+                        etaz = bond_offset(A.pcz[c], zi, uzi, xf[2]);
                     }
-                    double ef;
-                    ff h;
-                    extension_ff(L2, A.l0[slot], ef, h);
-                    const double T = fma(A.c2[slot] * A.e[slot], nbi + A.nb[c], A.c1[slot] * (nai + A.na[c]));
-                    // t = T h and f += t d in pair arithmetic (as in the bond-based kernel)
-                    const ff t = ff_mul(ff_split(T), h);
-                    fxa = ff_add(fxa, ff_mul(t, ff_split(dx)));
-                    fya = ff_add(fya, ff_mul(t, ff_split(dy)));
-                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_split(dz)));
-                    brk = exceeds(ef, A.ecrit[slot]);
+                    pair_stretch<DIM>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
+                    const double T = fma(hi_f64(w4) * A.e[slot], nbi + A.nb[c], lo_f64(w4) * (nai + A.na[c]));
+                    // t = T / (2 L) and f += t d in pair arithmetic (as in the bond-based kernel)
+                    const ff t = ff_mul(ff_split(T), ff{0.5f * y.h, 0.5f * y.l});
+                    fxa = ff_add(fxa, ff_mul(t, dp[0]));
+                    fya = ff_add(fya, ff_mul(t, dp[1]));
+                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_add(ff{xf[2], 0.0f}, etaz)));
+                    brk = pair_exceeds(e2, lo_f64(w5));
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
@@ -916,14 +922,10 @@ static ForceArgs make_args(pd_ctx* c) {
     A.base = S.base;
     A.fbase = S.fbase;
     A.col = S.col;
-    A.l0 = S.l0;
     A.ecrit = S.ecrit;
     A.rec = S.rec;
     A.kscale = S.kscale;
-    A.c1 = S.c1;
-    A.c2 = S.c2;
-    A.cth = S.cth;
-    A.xi = S.xi;
+    A.srec = S.srec;
     A.e = S.e;
     A.bits = S.bits;
     A.S = S.S;

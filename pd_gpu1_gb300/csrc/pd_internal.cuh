@@ -54,6 +54,24 @@ struct alignas(16) BondRec {
 };
 static_assert(sizeof(BondRec) == 48, "BondRec is three 16-byte words");
 
+// Per-slot data of the state-based kernels, one 96-byte record per slot (six
+// 16-byte words): w0 {col, xf[3]}, w1 {c0, l0}, w2 {xi[0], xi[1]},
+// w3 {xi[2], cth}, w4 {c1, c2}, w5 {ecrit, unused}.  The dilatation pass
+// reads w0-w3, the force pass w0, w1, w4, w5 (and w3 in 3-D).
+struct alignas(16) StateRec {
+    int col;       // neighbour id (self for padding)
+    float xf[3];   // xi rounded to float per component (z = 0 in 2-D)
+    float2 c0;     // |xf|^2 - l0^2 as a float pair (computed exactly)
+    float2 l0;     // l0 as a float pair
+    double xi[3];  // reference vector x_c - x_i (FP64, the dilatation pass's operand)
+    double cth;    // dilatation weight of e
+    double c1;     // dilatation coefficient of t
+    double c2;     // extension coefficient of t
+    double ecrit;  // break threshold on e = L - l0 (s0 l0; +inf: never)
+    double unused;
+};
+static_assert(sizeof(StateRec) == 96, "StateRec is six 16-byte words");
+
 struct Sell {
     int64_t nslices = 0;     // ceil(N / 32)
     int64_t S = 0;           // total slots (sum of 32 * width)
@@ -64,17 +82,13 @@ struct Sell {
     int64_t* fbase = nullptr;// [nslices] flag-word offset
     int* col = nullptr;      // [S] neighbour id (self for padding)
     int* csr = nullptr;      // [S] CSR index of the slot (-1 for padding)
-    double* l0 = nullptr;    // [S] reference length |xi|
     double* ecrit = nullptr; // [S] break threshold on e = L - l0 (s0 * l0; +inf: never)
     double* k2 = nullptr;    // [S] bond-based: 2 * vol*fac*bc*scr / l0
     BondRec* rec = nullptr;  // [S] bond-based: the force kernels' per-slot record
     int kexp = 0;            // power-of-two scale that brings k2 near one
     double kscale = 1.0;     // 2^kexp
     double kscale_inv = 1.0; // 2^-kexp
-    double* c1 = nullptr;    // [S] state-based: dilatation coefficient of t
-    double* c2 = nullptr;    // [S] state-based: extension coefficient of t
-    double* cth = nullptr;   // [S] state-based: dilatation weight of e
-    double* xi = nullptr;    // [S*dim] state-based: x_c - x_i per component (SoA blocks)
+    StateRec* srec = nullptr; // [S] state-based: the force kernels' per-slot record
     double* e = nullptr;     // [S] state-based: extension (dilatation-pass operand order)
     uint32_t* bits = nullptr;// [F] intact flags
 };

@@ -239,6 +239,31 @@ __global__ void k_slice_width(int64_t N, int64_t nslices, const int* __restrict_
     if (lane == 0) width[s] = v;
 }
 
+// The reference vector xa rounded to float per component (xf, z = 0 in 2-D)
+// and the exact constant |xf|^2 - l0^2 as a float pair (c0): products of
+// floats are exact doubles, and the sums are carried as double pairs
+// (TwoSum / FMA TwoProduct); sh - ph is exact, both within a factor 2 of
+// l0^2.  l0 itself as a float pair (lf).
+__device__ void float_reference(const double xa[3], int dim, double L0, float xf[3], float2& c0, float2& lf) {
+    double sh = 0.0, sl = 0.0;
+    xf[2] = 0.0f;
+    for (int a = 0; a < dim; a++) {
+        const float f = __double2float_rn(xa[a]);
+        xf[a] = f;
+        const double sq = (double)f * (double)f;  // exact: 24-bit x 24-bit mantissas
+        const double t = sh + sq;
+        const double bb = t - sh;
+        sl += (sh - (t - bb)) + (sq - bb);
+        sh = t;
+    }
+    const double ph = L0 * L0;
+    const double pl = fma(L0, L0, -ph);
+    const ff cf = ff_split((sh - ph) + (sl - pl));
+    c0 = make_float2(cf.h, cf.l);
+    const ff l = ff_split(L0);
+    lf = make_float2(l.h, l.l);
+}
+
 // One thread per slot.  Padding slots point at their own row, carry zero
 // coefficients and a cleared intact bit, so they contribute nothing.
 __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ width,
@@ -261,7 +286,6 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         S.csr[slot] = (int)(used ? q : -1);
         if (!used) {
             S.col[slot] = (int)(r < P.N ? r : 0);
-            S.l0[slot] = 1.0;
             S.ecrit[slot] = HUGE_VAL;
             if (S.k2) {
                 S.k2[slot] = 0.0;
@@ -274,11 +298,12 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                 R.ecrit = HUGE_VAL;
                 S.rec[slot] = R;
             }
-            if (S.c1) {
-                S.c1[slot] = 0.0;
-                S.c2[slot] = 0.0;
-                S.cth[slot] = 0.0;
-                for (int a = 0; a < P.dim; a++) S.xi[a * S.S + slot] = 0.0;
+            if (S.srec) {
+                StateRec R{};
+                R.col = (int)(r < P.N ? r : 0);
+                R.l0 = make_float2(1.0f, 0.0f);
+                R.ecrit = HUGE_VAL;
+                S.srec[slot] = R;
                 S.e[slot] = 0.0;
             }
             continue;
@@ -286,7 +311,6 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         const int64_t c = NL[q];
         S.col[slot] = (int)c;
         const double L0 = idist[q];
-        S.l0[slot] = L0;
         // break when s = (L - L0)/L0 > s0, i.e. e = L - L0 > s0 L0; the 3-D
         // kernels break only bonds whose ends both have y >= -0.04 (Force_Bond.cu:117)
         bool breakable = true;
@@ -304,31 +328,11 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             R.ecrit = ecrit;
             const ff kf = ff_split(k2 * S.kscale_inv);
             R.k2 = make_float2(kf.h, kf.l);
-            // reference vector rounded to float per component, and the exact
-            // constant |xf|^2 - l0^2 (products of floats are exact doubles;
-            // the sums carried as double pairs, TwoSum / FMA TwoProduct)
             const double xa[3] = {x[c] - x[r], y[c] - y[r], P.dim == 3 ? z[c] - z[r] : 0.0};
-            double sh = 0.0, sl = 0.0;
-            R.xf[2] = 0.0f;
-            for (int a = 0; a < P.dim; a++) {
-                const float f = __double2float_rn(xa[a]);
-                R.xf[a] = f;
-                const double sq = (double)f * (double)f;  // exact: 24-bit x 24-bit mantissas
-                const double t = sh + sq;
-                const double bb = t - sh;
-                sl += (sh - (t - bb)) + (sq - bb);
-                sh = t;
-            }
-            const double ph = L0 * L0;
-            const double pl = fma(L0, L0, -ph);
-            const double c0 = (sh - ph) + (sl - pl);  // sh - ph exact: both within a factor 2 of l0^2
-            const ff cf = ff_split(c0);
-            R.c0 = make_float2(cf.h, cf.l);
-            const ff lf = ff_split(L0);
-            R.l0 = make_float2(lf.h, lf.l);
+            float_reference(xa, P.dim, L0, R.xf, R.c0, R.l0);
             S.rec[slot] = R;
         }
-        if (S.c1) {
+        if (S.srec) {
             const double pr = P.pratio;
             double a_coef, b_coef, th_coef;
             if (P.dim == 2) {
@@ -341,12 +345,17 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                 th_coef = 3.0;
             }
             const double wf = w[q] * fac[q] * P.vol;
-            S.c1[slot] = 2.0 * a_coef * wf * L0;
-            S.c2[slot] = 2.0 * b_coef * wf;
-            S.cth[slot] = th_coef * w[q] * L0 * fac[q] * P.vol;
-            S.xi[slot] = x[c] - x[r];
-            S.xi[S.S + slot] = y[c] - y[r];
-            if (P.dim == 3) S.xi[2 * S.S + slot] = z[c] - z[r];
+            StateRec R{};
+            R.col = (int)c;
+            R.c1 = 2.0 * a_coef * wf * L0;
+            R.c2 = 2.0 * b_coef * wf;
+            R.cth = th_coef * w[q] * L0 * fac[q] * P.vol;
+            R.xi[0] = x[c] - x[r];
+            R.xi[1] = y[c] - y[r];
+            R.xi[2] = P.dim == 3 ? z[c] - z[r] : 0.0;
+            R.ecrit = ecrit;
+            float_reference(R.xi, P.dim, L0, R.xf, R.c0, R.l0);
+            S.srec[slot] = R;
             S.e[slot] = 0.0;
         }
     }
@@ -498,14 +507,10 @@ static void free_sell(Sell& S) {
     free_ptr(S.fbase);
     free_ptr(S.col);
     free_ptr(S.csr);
-    free_ptr(S.l0);
     free_ptr(S.ecrit);
     free_ptr(S.k2);
     free_ptr(S.rec);
-    free_ptr(S.c1);
-    free_ptr(S.c2);
-    free_ptr(S.cth);
-    free_ptr(S.xi);
+    free_ptr(S.srec);
     free_ptr(S.e);
     free_ptr(S.bits);
     S.nslices = S.S = S.F = 0;
@@ -555,7 +560,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.fbase, fb.data(), fb.size() * 8, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
-    bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.l0, n8) &&
+    bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) &&
               !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
     if (ok && !state)
         ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.rec, n8 * 6);
@@ -568,8 +573,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
         S.kscale_inv = std::ldexp(1.0, -S.kexp);
     }
     if (ok && state)
-        ok = !cudaMalloc(&S.c1, n8) && !cudaMalloc(&S.c2, n8) && !cudaMalloc(&S.cth, n8) &&
-             !cudaMalloc(&S.xi, n8 * P.dim) && !cudaMalloc(&S.e, n8);
+        ok = !cudaMalloc(&S.srec, n8 * 12) && !cudaMalloc(&S.e, n8);
     if (!ok) {
         free_sell(S);
         return set_err(c, PD_ERR_NOMEM, "SELL bond arrays");
