@@ -25,7 +25,7 @@
 // 1/L, e = L - l0 and the force t (xf + eta) in pair-of-floats arithmetic
 // (ff.cuh); the break test e > s0 l0 decided on the pair, the double sum only
 // near the threshold.  State-based (k_theta, k_state_force): the same
-// stretch arithmetic on a 96-byte StateRec per slot, with the bond vector in
+// stretch arithmetic on three 32-byte records per slot, with the bond vector in
 // the dilatation pass's operand order ((x_c - x_i) + u_c) - u_i for theta and
 // the force pass's (P_c - x_i) - u_i for the force, as the reference rounds
 // them; e in double for theta and the stored extension.
@@ -59,7 +59,9 @@ struct ForceArgs {
     const double* ecrit;
     const BondRec* rec;  // bond-based: per-slot record (column, float reference vector, c0, l0, k2, ecrit)
     double kscale;      // 2^S
-    const StateRec* srec;  // state-based: per-slot record (column, reference vectors, c0, l0, coefficients)
+    const StateGeo* sgeo;    // state-based: per-slot geometry (column, float reference vector, c0, l0)
+    const StateTheta* sth;   // state-based: dilatation-pass record (xi, cth)
+    const StateForce* sfo;   // state-based: force-pass record (c1, c2, ecrit, xi_z)
     double* e;
     uint32_t* bits;
     int64_t S;
@@ -475,8 +477,9 @@ __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, fl
     return pair_exceeds(e2, __hiloint2double(__float_as_int(q2.w), __float_as_int(q2.z)));
 }
 
-// Record words of a StateRec (16 bytes each).
-__device__ __forceinline__ float4 srec_w(const StateRec* r, int64_t slot, int w) {
+// Record words of the 32-byte state records (16 bytes each).
+template <typename R>
+__device__ __forceinline__ float4 srec_w(const R* r, int64_t slot, int w) {
     return __ldg(reinterpret_cast<const float4*>(r + slot) + w);
 }
 __device__ __forceinline__ double lo_f64(float4 v) { return __hiloint2double(__float_as_int(v.y), __float_as_int(v.x)); }
@@ -749,8 +752,8 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
             bool use = k < nn;
             if (check_bits) use = use && ((wbits[k] >> lane) & 1u);
             if (use) {
-                const float4 w0 = srec_w(A.srec, slot, 0), w1 = srec_w(A.srec, slot, 1);
-                const float4 w2 = srec_w(A.srec, slot, 2), w3 = srec_w(A.srec, slot, 3);
+                const float4 w0 = srec_w(A.sgeo, slot, 0), w1 = srec_w(A.sgeo, slot, 1);
+                const float4 w2 = srec_w(A.sth, slot, 0), w3 = srec_w(A.sth, slot, 1);
                 const int c = __float_as_int(w0.x);
                 const float xf[3] = {w0.y, w0.z, w0.w};
                 // d = (xi + u_c) - u_i, the dilatation pass's operand order, then
@@ -802,8 +805,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
                 if (alive) {
-                    const float4 w0 = srec_w(A.srec, slot, 0), w1 = srec_w(A.srec, slot, 1);
-                    const float4 w4 = srec_w(A.srec, slot, 4), w5 = srec_w(A.srec, slot, 5);
+                    const float4 w0 = srec_w(A.sgeo, slot, 0), w1 = srec_w(A.sgeo, slot, 1);
+                    const float4 w4 = srec_w(A.sfo, slot, 0), w5 = srec_w(A.sfo, slot, 1);
                     const int c = __float_as_int(w0.x);
                     const float xf[3] = {w0.y, w0.z, w0.w};
                     // d = (P_c - x_i) - u_i, the force pass's operand order, then its
@@ -814,7 +817,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                     if (DIM == 3) {
                         // the reference's 3-D force kernel takes the z term of the
                         // length in the dilatation pass's operand order (Force_State.cu:272)
-                        eta[2] = exact_offset((lo_f64(srec_w(A.srec, slot, 3)) + A.uz[c]) - uzi, xf[2]);
+                        eta[2] = exact_offset((hi_f64(w5) + A.uz[c]) - uzi, xf[2]);
                         etaz = bond_offset(A.pcz[c], zi, uzi, xf[2]);
                     }
                     pair_stretch<DIM>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
@@ -925,7 +928,9 @@ static ForceArgs make_args(pd_ctx* c) {
     A.ecrit = S.ecrit;
     A.rec = S.rec;
     A.kscale = S.kscale;
-    A.srec = S.srec;
+    A.sgeo = S.sgeo;
+    A.sth = S.sth;
+    A.sfo = S.sfo;
     A.e = S.e;
     A.bits = S.bits;
     A.S = S.S;

@@ -54,23 +54,29 @@ struct alignas(16) BondRec {
 };
 static_assert(sizeof(BondRec) == 48, "BondRec is three 16-byte words");
 
-// Per-slot data of the state-based kernels, one 96-byte record per slot (six
-// 16-byte words): w0 {col, xf[3]}, w1 {c0, l0}, w2 {xi[0], xi[1]},
-// w3 {xi[2], cth}, w4 {c1, c2}, w5 {ecrit, unused}.  The dilatation pass
-// reads w0-w3, the force pass w0, w1, w4, w5 (and w3 in 3-D).
-struct alignas(16) StateRec {
-    int col;       // neighbour id (self for padding)
-    float xf[3];   // xi rounded to float per component (z = 0 in 2-D)
-    float2 c0;     // |xf|^2 - l0^2 as a float pair (computed exactly)
-    float2 l0;     // l0 as a float pair
-    double xi[3];  // reference vector x_c - x_i (FP64, the dilatation pass's operand)
+// Per-slot data of the state-based kernels: three 32-byte records per slot in
+// three arrays, so that each pass streams only what it reads (the dilatation
+// pass StateGeo + StateTheta, the force pass StateGeo + StateForce; one
+// 96-byte record read in part was measured to pull whole lines, ~99 B per
+// bond for the 64 the pass used).
+struct alignas(16) StateGeo {
+    int col;      // neighbour id (self for padding)
+    float xf[3];  // xi rounded to float per component (z = 0 in 2-D)
+    float2 c0;    // |xf|^2 - l0^2 as a float pair (computed exactly)
+    float2 l0;    // l0 as a float pair
+};
+struct alignas(16) StateTheta {
+    double xi[3];  // reference vector x_c - x_i (FP64, the dilatation pass's operand; z = 0 in 2-D)
     double cth;    // dilatation weight of e
+};
+struct alignas(16) StateForce {
     double c1;     // dilatation coefficient of t
     double c2;     // extension coefficient of t
     double ecrit;  // break threshold on e = L - l0 (s0 l0; +inf: never)
-    double unused;
+    double xiz;    // xi[2] again (the 3-D length's z term in the dilatation order)
 };
-static_assert(sizeof(StateRec) == 96, "StateRec is six 16-byte words");
+static_assert(sizeof(StateGeo) == 32 && sizeof(StateTheta) == 32 && sizeof(StateForce) == 32,
+              "state records are two 16-byte words each");
 
 struct Sell {
     int64_t nslices = 0;     // ceil(N / 32)
@@ -88,7 +94,9 @@ struct Sell {
     int kexp = 0;            // power-of-two scale that brings k2 near one
     double kscale = 1.0;     // 2^kexp
     double kscale_inv = 1.0; // 2^-kexp
-    StateRec* srec = nullptr; // [S] state-based: the force kernels' per-slot record
+    StateGeo* sgeo = nullptr;     // [S] state-based: geometry record (both passes)
+    StateTheta* sth = nullptr;    // [S] state-based: dilatation-pass record
+    StateForce* sfo = nullptr;    // [S] state-based: force-pass record
     double* e = nullptr;     // [S] state-based: extension (dilatation-pass operand order)
     uint32_t* bits = nullptr;// [F] intact flags
 };

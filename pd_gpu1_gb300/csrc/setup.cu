@@ -298,12 +298,15 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                 R.ecrit = HUGE_VAL;
                 S.rec[slot] = R;
             }
-            if (S.srec) {
-                StateRec R{};
-                R.col = (int)(r < P.N ? r : 0);
-                R.l0 = make_float2(1.0f, 0.0f);
-                R.ecrit = HUGE_VAL;
-                S.srec[slot] = R;
+            if (S.sgeo) {
+                StateGeo G{};
+                G.col = (int)(r < P.N ? r : 0);
+                G.l0 = make_float2(1.0f, 0.0f);
+                S.sgeo[slot] = G;
+                S.sth[slot] = StateTheta{};
+                StateForce F{};
+                F.ecrit = HUGE_VAL;
+                S.sfo[slot] = F;
                 S.e[slot] = 0.0;
             }
             continue;
@@ -332,7 +335,7 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             float_reference(xa, P.dim, L0, R.xf, R.c0, R.l0);
             S.rec[slot] = R;
         }
-        if (S.srec) {
+        if (S.sgeo) {
             const double pr = P.pratio;
             double a_coef, b_coef, th_coef;
             if (P.dim == 2) {
@@ -345,17 +348,22 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                 th_coef = 3.0;
             }
             const double wf = w[q] * fac[q] * P.vol;
-            StateRec R{};
-            R.col = (int)c;
-            R.c1 = 2.0 * a_coef * wf * L0;
-            R.c2 = 2.0 * b_coef * wf;
-            R.cth = th_coef * w[q] * L0 * fac[q] * P.vol;
-            R.xi[0] = x[c] - x[r];
-            R.xi[1] = y[c] - y[r];
-            R.xi[2] = P.dim == 3 ? z[c] - z[r] : 0.0;
-            R.ecrit = ecrit;
-            float_reference(R.xi, P.dim, L0, R.xf, R.c0, R.l0);
-            S.srec[slot] = R;
+            StateTheta T;
+            T.xi[0] = x[c] - x[r];
+            T.xi[1] = y[c] - y[r];
+            T.xi[2] = P.dim == 3 ? z[c] - z[r] : 0.0;
+            T.cth = th_coef * w[q] * L0 * fac[q] * P.vol;
+            StateGeo G;
+            G.col = (int)c;
+            float_reference(T.xi, P.dim, L0, G.xf, G.c0, G.l0);
+            StateForce F;
+            F.c1 = 2.0 * a_coef * wf * L0;
+            F.c2 = 2.0 * b_coef * wf;
+            F.ecrit = ecrit;
+            F.xiz = T.xi[2];
+            S.sgeo[slot] = G;
+            S.sth[slot] = T;
+            S.sfo[slot] = F;
             S.e[slot] = 0.0;
         }
     }
@@ -510,7 +518,9 @@ static void free_sell(Sell& S) {
     free_ptr(S.ecrit);
     free_ptr(S.k2);
     free_ptr(S.rec);
-    free_ptr(S.srec);
+    free_ptr(S.sgeo);
+    free_ptr(S.sth);
+    free_ptr(S.sfo);
     free_ptr(S.e);
     free_ptr(S.bits);
     S.nslices = S.S = S.F = 0;
@@ -573,7 +583,8 @@ int prepare(pd_ctx* c, cudaStream_t s) {
         S.kscale_inv = std::ldexp(1.0, -S.kexp);
     }
     if (ok && state)
-        ok = !cudaMalloc(&S.srec, n8 * 12) && !cudaMalloc(&S.e, n8);
+        ok = !cudaMalloc(&S.sgeo, n8 * 4) && !cudaMalloc(&S.sth, n8 * 4) && !cudaMalloc(&S.sfo, n8 * 4) &&
+             !cudaMalloc(&S.e, n8);
     if (!ok) {
         free_sell(S);
         return set_err(c, PD_ERR_NOMEM, "SELL bond arrays");
