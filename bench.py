@@ -784,7 +784,7 @@ def gb300_arm(args):
     B = int(eng.get("ROWPTR")[p.N_int])
     is3d = p.dim == 3
     tuned = None
-    if p.model == 1 and args.launch:
+    if args.launch:
         tuned = tuple(int(v) for v in args.launch.split(","))
         eng.set_launch(*tuned)
     elif p.model == 1 and not args.no_tune:
