@@ -43,7 +43,8 @@ ALG_FP64_PER_BOND_3D = 31
 # dram__bytes_write.sum, one capture per workload, summarised under profiles/; a zero per-node
 # figure means the node traffic is folded into the per-bond one)
 TRAFFIC = {"crack_branching_2d_pmb_verlet": (48.9, 139.8), "batch_plate_adr_2d_pmb": (55.0, 0.0),
-           "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0)}
+           "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0), "plate_crack_grow_2d_state_verlet": (153.3, 0.0),
+           "kalthoff_winkler_3d_state_verlet": (148.9, 0.0)}
 
 
 def rank_info():
