@@ -55,8 +55,6 @@ struct ForceArgs {
     const int* width;
     const int64_t* base;
     const int64_t* fbase;
-    const int* col;
-    const double* ecrit;
     const BondRec* rec;  // bond-based: per-slot record (column, float reference vector, c0, l0, k2, ecrit)
     double kscale;      // 2^S
     const StateGeo* sgeo;    // state-based: per-slot geometry (column, float reference vector, c0, l0)
@@ -924,8 +922,6 @@ static ForceArgs make_args(pd_ctx* c) {
     A.width = S.width;
     A.base = S.base;
     A.fbase = S.fbase;
-    A.col = S.col;
-    A.ecrit = S.ecrit;
     A.rec = S.rec;
     A.kscale = S.kscale;
     A.sgeo = S.sgeo;

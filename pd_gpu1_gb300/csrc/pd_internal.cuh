@@ -86,10 +86,7 @@ struct Sell {
     int* width = nullptr;    // [nslices]
     int64_t* base = nullptr; // [nslices] slot offset
     int64_t* fbase = nullptr;// [nslices] flag-word offset
-    int* col = nullptr;      // [S] neighbour id (self for padding)
     int* csr = nullptr;      // [S] CSR index of the slot (-1 for padding)
-    double* ecrit = nullptr; // [S] break threshold on e = L - l0 (s0 * l0; +inf: never)
-    double* k2 = nullptr;    // [S] bond-based: 2 * vol*fac*bc*scr / l0
     BondRec* rec = nullptr;  // [S] bond-based: the force kernels' per-slot record
     int kexp = 0;            // power-of-two scale that brings k2 near one
     double kscale = 1.0;     // 2^kexp

@@ -285,10 +285,7 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         const int64_t q = used ? rowptr[r] + k : -1;
         S.csr[slot] = (int)(used ? q : -1);
         if (!used) {
-            S.col[slot] = (int)(r < P.N ? r : 0);
-            S.ecrit[slot] = HUGE_VAL;
-            if (S.k2) {
-                S.k2[slot] = 0.0;
+            if (S.rec) {
                 BondRec R;
                 R.col = (int)(r < P.N ? r : 0);
                 R.xf[0] = R.xf[1] = R.xf[2] = 0.0f;
@@ -312,7 +309,6 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             continue;
         }
         const int64_t c = NL[q];
-        S.col[slot] = (int)c;
         const double L0 = idist[q];
         // break when s = (L - L0)/L0 > s0, i.e. e = L - L0 > s0 L0; the 3-D
         // kernels break only bonds whose ends both have y >= -0.04 (Force_Bond.cu:117)
@@ -322,10 +318,8 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
         const double s0 = node_s0 ? node_s0[r] : P.critical_s;
         const double bc = node_bc ? node_bc[r] : P.bc;
         const double ecrit = breakable ? s0 * L0 : HUGE_VAL;
-        S.ecrit[slot] = ecrit;
-        if (S.k2) {
+        if (S.rec) {
             const double k2 = 2.0 * (P.vol * fac[q] * bc * scr[q]) / L0;
-            S.k2[slot] = k2;
             BondRec R;
             R.col = (int)c;
             R.ecrit = ecrit;
@@ -513,10 +507,7 @@ static void free_sell(Sell& S) {
     free_ptr(S.width);
     free_ptr(S.base);
     free_ptr(S.fbase);
-    free_ptr(S.col);
     free_ptr(S.csr);
-    free_ptr(S.ecrit);
-    free_ptr(S.k2);
     free_ptr(S.rec);
     free_ptr(S.sgeo);
     free_ptr(S.sth);
@@ -570,10 +561,9 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.fbase, fb.data(), fb.size() * 8, cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
-    bool ok = !cudaMalloc(&S.col, n4) && !cudaMalloc(&S.csr, n4) &&
-              !cudaMalloc(&S.ecrit, n8) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
+    bool ok = !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
     if (ok && !state)
-        ok = !cudaMalloc(&S.k2, n8) && !cudaMalloc(&S.rec, n8 * 6);
+        ok = !cudaMalloc(&S.rec, n8 * 6);
     // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,
     // so that the pair arithmetic of the force kernels stays in float range
     {
