@@ -693,14 +693,14 @@ def warm_arm(args):
     with E.Engine(p) as eng:
         setup(eng)
         B = int(eng.get("ROWPTR")[p.N_int])
-        pre = warm.run_increments(eng, meta, W, mode="learned", net=net)
+        pre = warm.run_increments(eng, meta, W, mode="learned", net=net, smooth=args.smooth)
         clocks.start()
         for j in range(K):
             eng.snapshot_save(snap)
             plain = warm.run_increments(eng, meta, 1, mode="plain", start=W + j)[0]
             eng.snapshot_load(snap)
             l0 = eng.kernel_launches
-            learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j)[0]
+            learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=args.smooth)[0]
             learned_launches += eng.kernel_launches - l0
             rows.append((plain, learned))
         clk = clocks.stop()
@@ -712,7 +712,7 @@ def warm_arm(args):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(5):
-            L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], nnref, du.data_ptr(), None)
+            L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], nnref, args.smooth, du.data_ptr(), None)
         e1.record()
         torch.cuda.synchronize()
         infer_ms = e0.elapsed_time(e1) / 5
@@ -722,7 +722,7 @@ def warm_arm(args):
         pin = torch.zeros(n, dtype=torch.float64).pin_memory()
         t0 = time.perf_counter()
         for j in range(2):
-            warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + K + j)
+            warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + K + j, smooth=args.smooth)
             eng._c(L.pd_get_field(eng.ctx, FIELD["UY"], pin.data_ptr(), n, None), "pd_get_field")
         e2e_ms = (time.perf_counter() - t0) * 1e3 / 2
     os.remove(snap)
@@ -993,6 +993,8 @@ def main():
     ap.add_argument("--seq-steps", type=int, default=100, help="batch workload: steps per plate when run one "
                                                                 "after another")
     ap.add_argument("--increments", type=int, default=3, help="warm_start workload: timed load increments")
+    ap.add_argument("--smooth", type=int, default=0, help="warm_start workload: family-averaging passes of the "
+                                                           "network's correction")
     ap.add_argument("--warm-increments", type=int, default=10, help="warm_start workload: increments solved "
                                                                      "before the timed ones")
     args = ap.parse_args()

@@ -311,8 +311,13 @@ int pd_warm_features(pd_ctx* ctx, double U, double delta, double nn_ref, void* d
  * response loaded proportionally from rest; the network predicts the
  * departure from proportionality per unit of accumulated boundary
  * displacement (the geometric nonlinearity of the bonds makes it grow with
- * the load: u = a U + b U^2 departs by b U delta per increment). */
-int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, double nn_ref, double* dev_du, void* stream);
+ * the load: u = a U + b U^2 departs by b U delta per increment).
+ * smooth_passes > 0 (bond-based contexts): the correction U * net is first
+ * averaged that many times over each free node's intact family (prescribed
+ * rows count as zero), which removes the node-to-node rounding noise of the
+ * BF16 network that the residual amplifies. */
+int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, double nn_ref, int smooth_passes,
+                    double* dev_du, void* stream);
 
 /* ---- batches of specimens ----------------------------------------------- */
 /* No counterpart in the reference, which solves one plate per process.  A

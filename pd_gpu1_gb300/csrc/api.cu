@@ -161,6 +161,8 @@ struct StreamScope {
 
 }  // namespace
 
+int make_ready(pd_ctx* c, cudaStream_t s) { return ensure_ready(c, s); }
+
 // Look-up helper shared by the run loops: finds a cached graph whose low flag
 // bits match, or captures one.
 template <typename F>

@@ -343,6 +343,62 @@ __global__ void k_scale_out(int64_t n, const float* __restrict__ y, double U, do
     }
 }
 
+// The network's correction U * net of the free nodes (x components, then y).
+__global__ void k_correction(int64_t n, const float* __restrict__ y, double U, double* __restrict__ corr) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        corr[i] = U * (double)y[i * kOut];
+        corr[n + i] = U * (double)y[i * kOut + 1];
+    }
+}
+
+// One smoothing pass of the correction over the bond family: each free node
+// takes the mean of its own value and those of its intact neighbours (the
+// prescribed boundary rows count with a zero correction).  One warp per SELL
+// slice, lane per row, as the force kernels walk it.
+__global__ void k_smooth(int64_t nslices, int64_t n, const int* __restrict__ width, const int64_t* __restrict__ base,
+                         const int64_t* __restrict__ fbase, const BondRec* __restrict__ rec,
+                         const uint32_t* __restrict__ bits, const double* __restrict__ in, double* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < nslices;
+         s += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        const int64_t r = s * 32 + lane;
+        if (s * 32 >= n) continue;
+        const bool row = r < n;
+        double sx = row ? in[r] : 0.0, sy = row ? in[n + r] : 0.0;
+        int cnt = 1;
+        const int W = width[s];
+        const int64_t b = base[s];
+        for (int k = 0; k < W; k++) {
+            const bool alive = row && ((bits[fbase[s] + k] >> lane) & 1u);
+            if (alive) {
+                const int c = rec[b + (int64_t)k * 32 + lane].col;
+                if (c < n) {
+                    sx += in[c];
+                    sy += in[n + c];
+                }
+                cnt++;
+            }
+        }
+        if (row) {
+            out[r] = sx / cnt;
+            out[n + r] = sy / cnt;
+        }
+    }
+}
+
+// Candidates from a smoothed correction: the skip term u * delta / U plus
+// the correction, and the skip term alone.
+__global__ void k_combine(int64_t n, const double* __restrict__ corr, double ratio, const double* __restrict__ ux,
+                          const double* __restrict__ uy, double* __restrict__ du) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double sx = ux[i] * ratio, sy = uy[i] * ratio;
+        du[i] = sx + corr[i];
+        du[n + i] = sy + corr[n + i];
+        du[2 * n + i] = sx;
+        du[3 * n + i] = sy;
+    }
+}
+
 }  // namespace mlp
 }  // namespace pdg
 
@@ -670,8 +726,11 @@ int pd_warm_features(pd_ctx* c, double U, double delta, double nn_ref, void* dev
 // Candidate increments of the free nodes: features, forward pass, then
 // du = u * delta / U + U * output (x components, then y components), and the
 // skip term u * delta / U alone.
-int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref, double* dev_du, void* stream) {
-    if (!c || !n || !dev_du) return PD_ERR_ARG;
+int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref, int smooth_passes, double* dev_du,
+                    void* stream) {
+    if (!c || !n || !dev_du || smooth_passes < 0) return PD_ERR_ARG;
+    if (smooth_passes > 0 && (c->p.model != PD_MODEL_BOND || !c->family))
+        return set_err(c, PD_ERR_STATE, "smoothing the correction needs a bond-based family");
     cudaStream_t s = st(stream);
     const int64_t ni = c->p.N_int;
     void* x = nullptr;
@@ -685,11 +744,33 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
     const int64_t l0 = n->launches;
     if (!rc) rc = pd_mlp_forward(n, x, ni, y, s);
     c->launches += n->launches - l0;  // the network's kernels count as the context's
-    if (!rc) {
-        k_scale_out<<<(unsigned)std::min<int64_t>((ni + 255) / 256, 4096), 256, 0, s>>>(
-            ni, y, U, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], dev_du);
+    const unsigned g = (unsigned)std::min<int64_t>((ni + 255) / 256, 4096);
+    if (!rc && smooth_passes == 0) {
+        k_scale_out<<<g, 256, 0, s>>>(ni, y, U, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], dev_du);
         c->launches++;
         rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
+    } else if (!rc) {
+        // the correction, smoothed over the family, then the candidates
+        double* cb = nullptr;
+        if ((rc = make_ready(c, s)) == PD_OK &&
+            (rc = cuda_err(c, cudaMallocAsync(&cb, 4 * ni * sizeof(double), s), "warm correction")) == PD_OK) {
+            k_correction<<<g, 256, 0, s>>>(ni, y, U, cb);
+            c->launches++;
+            const Sell& S = c->sell;
+            const int64_t ns = (ni + 31) / 32;
+            const unsigned gs = (unsigned)std::min<int64_t>((ns * 32 + 255) / 256, 65535);
+            for (int k = 0; k < smooth_passes; k++) {
+                const double* in = cb + (k & 1) * 2 * ni;
+                double* out = cb + ((k + 1) & 1) * 2 * ni;
+                k_smooth<<<gs, 256, 0, s>>>(ns, ni, S.width, S.base, S.fbase, S.rec, S.bits, in, out);
+                c->launches++;
+            }
+            k_combine<<<g, 256, 0, s>>>(ni, cb + (smooth_passes & 1) * 2 * ni, delta / U, c->nf[PD_F_UX],
+                                        c->nf[PD_F_UY], dev_du);
+            c->launches++;
+            rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
+            cudaFreeAsync(cb, s);
+        }
     } else {
         set_err(c, rc, rc == PD_ERR_TIMEOUT ? "tensor-core wait gave up" : "MLP forward failed");
     }

@@ -253,6 +253,8 @@ int check_finite(pd_ctx* c, cudaStream_t s, int* bad_host);
 int residual_sq(pd_ctx* c, double* out_dev, cudaStream_t s);
 // u += du on the free nodes (du on the device: N_int x components, then N_int y)
 int add_increment(pd_ctx* c, const double* du, cudaStream_t s);
+// Bond coefficients, intact bits and positions current (the run loops' entry check).
+int make_ready(pd_ctx* c, cudaStream_t s);
 int fp64_probe(double* gfma_per_s);
 // batch.cu
 void release_batch(pd_ctx* c);

@@ -58,3 +58,41 @@ def test_bad_prediction_falls_back_to_plain(W):
     st, _ = _run(W, "network", 3, bad)
     for s in st[1:]:
         assert s["warm_used"] == 0 and s["r_start"] == s["r_plain"]
+
+
+def test_smoothing_lowers_the_network_start_residual(W):
+    """pd_warm_predict's family averaging of the network's correction removes
+    the node-to-node rounding noise that the residual amplifies: the
+    network's starting residual falls several-fold; the skip-term candidate
+    is unchanged."""
+    from pd_gpu1_gb300 import presets
+    from pd_gpu1_gb300.engine import Engine
+
+    net = W.Net.load()
+    p, setup, meta = presets.build_warm_start_plate(scale=0.2)
+    ratios = {}
+    for sm in (0, 64):
+        with Engine(p) as eng:
+            setup(eng)
+            st = W.run_increments(eng, meta, 4, mode="network", net=net, smooth=sm)
+            assert all(s["warm_used"] == 1 for s in st[1:])  # admissible: used
+            ratios[sm] = [s["r_start"] / s["r_plain"] for s in st[1:]]
+    for a, b in zip(ratios[0], ratios[64]):
+        assert b < 0.2 * a, (ratios[0], ratios[64])
+    import torch
+
+    L = W.lib()
+    with Engine(p) as eng:
+        setup(eng)
+        W.run_increments(eng, meta, 2, mode="plain")
+        eng.damage()
+        ni = p.N_int
+        U, nnref = 2 * meta["delta"], W.nn_reference(eng)
+        outs = []
+        for sm in (0, 16):
+            du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")
+            W.check(L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], nnref, sm, du.data_ptr(), eng.stream),
+                    eng.ctx, "pd_warm_predict")
+            outs.append(du.cpu().numpy())
+        np.testing.assert_array_equal(outs[0][2 * ni:], outs[1][2 * ni:])  # the skip term
+        assert not np.array_equal(outs[0][: 2 * ni], outs[1][: 2 * ni])
