@@ -221,8 +221,9 @@ TRAIN_RUNS = [  # (scale, crack fraction, seed): 100k-1M-node plates of the same
 ]
 
 
-def generate(runs=TRAIN_RUNS, n_inc=200, keep=0.25, log=print):
-    """Converged states of seeded load-stepping runs -> (X, T) device tensors."""
+def generate(runs=TRAIN_RUNS, n_inc=200, keep=0.25, tol=1e-6, log=print):
+    """Converged states of seeded load-stepping runs (ADR to tol) -> (X, T)
+    device tensors."""
     import torch
 
     data = []
@@ -231,7 +232,7 @@ def generate(runs=TRAIN_RUNS, n_inc=200, keep=0.25, log=print):
         with Engine(p) as eng:
             setup(eng)
             t0 = time.perf_counter()
-            st = run_increments(eng, meta, n_inc, mode="extrapolate", collect=data, keep=keep, seed=seed)
+            st = run_increments(eng, meta, n_inc, mode="extrapolate", collect=data, keep=keep, seed=seed, tol=tol)
             broken = int((eng.get("FAIL") == 0).sum())
         jumps = [(s["increment"], s["iters"], s.get("advanced", 0), round(s.get("max_target", 0.0), 2))
                  for s in st if s.get("advanced", 0) > 0]
@@ -252,9 +253,10 @@ def main():
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--increments", type=int, default=60)
+    ap.add_argument("--tol", type=float, default=1e-6, help="ADR tolerance of the training runs")
     args = ap.parse_args()
     t0 = time.perf_counter()
-    X, T = generate(n_inc=args.increments)
+    X, T = generate(n_inc=args.increments, tol=args.tol)
     print(json.dumps({"samples": int(X.shape[0]), "seconds": round(time.perf_counter() - t0, 1)}), flush=True)
     log = []
     net = train(X, T, steps=args.steps, log=log)
