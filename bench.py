@@ -14,6 +14,16 @@ visit them).  Setup (neighbour build, surface correction) is timed separately.
 --workload batch: 256 seeded uneven plates (6.25M interior nodes) solved
 together by ADR (1000 steps), against the same plates run one after another
 (the engine's single-plate loop, and the reference's own kernels).
+--workload warm_start: ADR wall-time to a 1e-6 relative residual per load
+increment of the 1M-node plate, learned start against the plain start.
+--workload kalthoff_winkler_bond: the reference's own impact driver (3-D
+bond-based with the rigid impactor); kalthoff_winkler is the state-based
+version of the same slab.
+
+Where the reference's kernels were compiled here (oracle/_ref/ref_kernels.cubin)
+the line also carries a `reference_cuda` key: the reference's own step loop
+for the workload timed on the same GPU, and the damage field after the whole
+run compared node by node with the engine's.
 
 --impl reference times the oracle's OpenMP host loop (the reference's
 formulas, its padded-ELL layout) on all host cores, on a bounded sample of the
