@@ -466,3 +466,37 @@ def test_rebuild_after_run_recaptures_graphs(E):
     np.testing.assert_array_equal(a.get("FAIL"), b.get("FAIL"))
     a.close()
     b.close()
+
+
+def test_autotune_3d_restores_state_and_keeps_forces(E):
+    """pd_autotune on a 3-D bond context (one-warp and split shapes): the
+    forces (all three components) and intact flags are restored afterwards,
+    and the forces under the chosen shape equal the default shape's bit for
+    bit."""
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=10, model=PD_MODEL_BOND)
+    with E.Engine(p) as eng:
+        setup(eng)
+        rng = np.random.default_rng(9)
+        u = rng.standard_normal((3, p.N)) * 8e-6
+        for a, k in enumerate(["UX", "UY", "UZ"]):
+            eng.set(k, u[a])
+        eng.bond_force_gpu()
+        ref = {k: eng.get(k) for k in ["FX", "FY", "FZ", "FAIL"]}
+        block, chunked, waves, split, ms = eng.autotune(reps=2)
+        assert ms > 0.0
+        for k, v in ref.items():
+            np.testing.assert_array_equal(eng.get(k), v, err_msg=f"restored {k}")
+        eng.bond_force_gpu()  # same displacements and flags, the tuned shape
+        eng.set_launch(256, 0, 1, 1)
+        tuned = {k: eng.get(k) for k in ["FX", "FY", "FZ", "FAIL"]}
+    with E.Engine(p) as one:
+        setup(one)
+        for a, k in enumerate(["UX", "UY", "UZ"]):
+            one.set(k, u[a])
+        one.set("FAIL", ref["FAIL"])
+        one.bond_force_gpu()
+        for k in ["FX", "FY", "FZ", "FAIL"]:
+            np.testing.assert_array_equal(tuned[k], one.get(k), err_msg=f"shape {block, chunked, waves, split} {k}")
