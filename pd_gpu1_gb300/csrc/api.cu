@@ -35,12 +35,6 @@ void drop_graphs(pd_ctx* c) {
 
 namespace {
 
-__global__ void k_init_state(KParams P, double* const* fields, int nfields, double* cn) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x)
-        for (int f = 0; f < nfields; f++) fields[f][i] = 0.0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) *cn = 0.0;
-}
-
 __global__ void k_fill_int(int* a, int64_t n, int v) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         a[i] = v;

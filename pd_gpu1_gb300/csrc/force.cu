@@ -793,7 +793,6 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
             const double nai = A.na[rr], nbi = A.nb[rr];
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
             ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
-            ff bxa{0.0f, 0.0f}, bya{0.0f, 0.0f}, bza{0.0f, 0.0f};  // 3-D: sums of the current 32-slot block
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
