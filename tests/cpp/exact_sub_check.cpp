@@ -13,12 +13,6 @@ static uint64_t bits(double v) {
     std::memcpy(&u, &v, 8);
     return u;
 }
-static double val(uint64_t u) {
-    double v;
-    std::memcpy(&v, &u, 8);
-    return v;
-}
-
 int main() {
     std::mt19937_64 rng(12345);
     std::uniform_real_distribution<double> U(0.5, 2.0);
