@@ -372,8 +372,8 @@ int pd_batch_get_cn(pd_ctx* ctx, double* cn, void* stream);
 int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves, int split);
 int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves, int* split);
 /* Times the bond-force kernel (reps launches per shape, at the current
- * displacements) over the shapes above (18 with split 1, 12 more with split
- * 2 and 4) and keeps the fastest; *best_ms receives its time per
+ * displacements) over the shapes above (24 with split 1: 1, 2, 4 or 8 waves;
+ * 12 more with split 2 and 4) and keeps the fastest; *best_ms receives its time per
  * launch.  Intact flags and forces are restored, so a run continues exactly
  * as without the call.  Bond-based contexts only. */
 int pd_autotune(pd_ctx* ctx, int reps, double* best_ms, void* stream);

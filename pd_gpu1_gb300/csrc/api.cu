@@ -1038,7 +1038,7 @@ int pd_get_launch(const pd_ctx* c, int* block, int* chunked, int* waves, int* sp
 }
 
 // Times the bond-force kernel at the current displacements for every launch
-// shape (block 128/256/512 x strided/chunked slice order x 1/2/4 waves of
+// shape (block 128/256/512 x strided/chunked slice order x 1/2/4/8 waves of
 // resident blocks, and 2 or 4 warps per slice) and keeps the fastest.  The intact flags and forces are
 // restored afterwards, so a run continues exactly as it would have.
 int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
@@ -1089,7 +1089,7 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     std::vector<Shape> shapes;
     for (int blk : {128, 256, 512})
         for (int ck : {0, 1})
-            for (int wv : {1, 2, 4}) shapes.push_back({blk, ck, wv, 1});
+            for (int wv : {1, 2, 4, 8}) shapes.push_back({blk, ck, wv, 1});
     for (int blk : {128, 256, 512})
         for (int sp : {2, 4})
             for (int wv : {1, 2}) shapes.push_back({blk, 0, wv, sp});
