@@ -837,7 +837,7 @@ def gb300_arm(args):
         kern_ms, step_ms = eng.profile_steps(kind, args.warmup + args.steps, kern_steps, meta["load"])
     torch.cuda.synchronize()
     state = p.model == 2
-    if state:  # dilatation + force passes (SURVEY's 3-D state-based model; 2-D by the same count)
+    if state:  # dilatation + force passes (the 3-D state-based byte model; 2-D by the same count)
         alg_bytes = (88.0 if is3d else 64.0) * p.N_int + 16.125 * B
     else:
         alg_bytes = (ALG_BYTES_PER_NODE_3D if is3d else ALG_BYTES_PER_NODE_2D) * p.N_int + \
