@@ -964,7 +964,8 @@ def gb300_arm(args):
             "data": "synthetic (deterministic lattice, seeded nothing: the geometry fixes every input)",
             "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "dt": p.dt,
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 44 / 1e9),
+                       "l2": "inputs larger than L2: per-slot records %.2f GB read per step"
+                             % (B * (48 if p.model == 1 else 2 * 64 + 16) / 1e9),
                        "setup_s": setup_s,
                        "launch": None if tuned is None else {"block": tuned[0], "chunked": tuned[1],
                                                              "waves": tuned[2], "split": tuned[3]}},

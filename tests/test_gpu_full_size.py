@@ -1,0 +1,135 @@
+"""Parity at the full sizes of the benchmark workloads, against the
+reference's own CUDA kernels on the same GPU (oracle/_ref/ref_kernels.cubin,
+compiled from the reference sources; oracle/ref_gpu.py runs them through the
+CUDA driver API on the engine's inputs).
+
+* Crack-branching plate, 2000 x 800 = 1,600,000 nodes, 44,699,236 bonds:
+  forces of a smooth compressive displacement field (bond strains about
+  -4e-4) 1e-12 norm-relative with identical intact flags.  The strain is
+  not smaller on purpose: the reference forms the stretch as
+  (|xi + eta| - |xi|) / |xi| in FP64, which cancels log10(1/s) of its 16
+  digits, so at strains of 1e-4 its own rounding already reaches ~1e-12 of
+  the force scale (measured 1.2e-12 against the engine's cancellation-free
+  extension).  After the whole 1,800-step run (damage every 100 steps) the
+  damage field agrees on at least 99.9 % of the nodes, the intact flags on
+  at least 99.9 % of the bonds, and the crack tips lie within one horizon.
+* Kalthoff-Winkler slab, 180,873 nodes, 18,809,054 bonds (3-D bond-based,
+  the reference's impact driver): 100 steps with the impactor in contact
+  from the first step; displacements and the impactor's velocity 1e-9,
+  intact flags identical.
+* Plate tensile, 10,600 nodes (ADR): the first 40 steps of the reference's
+  ADR loop; damping coefficient and displacements 1e-9.  Longer ADR runs are
+  not compared bit for bit: the damping rule amplifies last-bit differences
+  of its two sums (test_oracle_behaviour.py::test_adr_damping_is_chaotic).
+"""
+import numpy as np
+import pytest
+
+import ref_gpu
+from helpers import assert_close_norm
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(not ref_gpu.available(), reason="reference cubin not built (make -C oracle ref)")]
+
+
+@pytest.fixture(scope="module")
+def E():
+    from pd_gpu1_gb300 import engine
+
+    engine.lib()
+    return engine
+
+
+def test_crack_branching_full_plate_matches_reference_kernels(E):
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_branching()
+    assert p.N == 1_600_000
+    with E.Engine(p) as eng:
+        setup(eng)
+        assert eng.num_bonds == 44_699_236
+        # forces of one smooth, non-uniform compressive field: every bond
+        # strain lies in [-4.7e-4, -3.3e-4], so none can break
+        x, y = eng.get("X"), eng.get("Y")
+        ux = -4.0e-4 * x + 1.0e-3 * x * y
+        uy = -4.0e-4 * y + 5.0e-4 * x * x
+        eng.set("UX", ux)
+        eng.set("UY", uy)
+        eng.bond_force_gpu()
+        r, NN = ref_gpu.from_engine(eng, p)
+        try:
+            r.set_disp(ux, uy)
+            r.force(ref_gpu.RefGPU.PARTICLE)
+            out = r.get(NN)
+        finally:
+            r.free()
+        assert_close_norm(eng.get("FX"), out["fx"], 1e-12, "fx")
+        assert_close_norm(eng.get("FY"), out["fy"], 1e-12, "fy")
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+
+        # the whole run from the same initial state
+        setup(eng)
+        r, NN = ref_gpu.from_engine(eng, p)
+        try:
+            r.run(ref_gpu.RefGPU.PARTICLE, meta["nt"], meta["dmg_every"])
+            out = r.get(NN)
+        finally:
+            r.free()
+        eng.run_explicit(meta["nt"], load=meta["load"], dmg_every=meta["dmg_every"])
+        eng.damage()
+        de, dr = eng.get("DMG")[: p.N_int], out["dmg"][: p.N_int]
+        assert (dr > 0.0).sum() > 10_000  # the crack ran
+        assert np.mean(np.abs(de - dr) <= 1e-12) >= 0.999
+        assert np.mean(eng.get("FAIL") == out["fail"]) >= 0.999
+        hot = np.nonzero(dr > 0.38)[0]
+        tip_ref = float(x[hot].max())
+        tip_eng = eng.crack_tip(0.38)[0]
+        assert abs(tip_eng - tip_ref) <= p.delta, (tip_eng, tip_ref)
+
+
+def test_kalthoff_winkler_full_slab_matches_reference_loop(E):
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(nt=100, model=PD_MODEL_BOND)
+    assert p.N == 180_873
+    c = meta["cylinder"]
+    c.y -= 0.3 * p.dx  # start 0.3 dx into the slab: contact from the first step
+    with E.Engine(p) as eng:
+        setup(eng)
+        assert eng.num_bonds == 18_809_054
+        r, NN = ref_gpu.from_engine(eng, p, cyl=c)
+        try:
+            eng.run_explicit(100)
+            r.run_kw(100)
+            out, oz = r.get(NN), r.get_z()
+        finally:
+            r.free()
+        assert_close_norm(eng.get("UX"), out["ux"], 1e-9, "ux")
+        assert_close_norm(eng.get("UY"), out["uy"], 1e-9, "uy")
+        assert_close_norm(eng.get("UZ"), oz["uz"], 1e-9, "uz")
+        assert np.abs(out["uy"]).max() > 0.0
+        assert eng.cylinder().vel[1] == pytest.approx(oz["cyl_vel"][1], rel=1e-9)
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+
+
+def test_plate_tensile_full_plate_adr_matches_reference_loop(E):
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_plate_tensile()
+    assert p.N == 10_600
+    steps = 40
+    with E.Engine(p) as eng:
+        setup(eng)
+        r, NN = ref_gpu.from_engine(eng, p)
+        try:
+            _, cn_ref = r.run_adr(0, steps, meta["load"])
+            out = r.get(NN)
+        finally:
+            r.free()
+        eng.run_adr(0, steps, load=meta["load"])
+        assert eng.adr_cn() == pytest.approx(cn_ref, rel=1e-9)
+        assert_close_norm(eng.get("UX")[: p.N_int], out["ux"][: p.N_int], 1e-9, "ux")
+        assert_close_norm(eng.get("UY")[: p.N_int], out["uy"][: p.N_int], 1e-9, "uy")
+        assert np.abs(out["uy"][: p.N_int]).max() > 0.0
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
