@@ -458,6 +458,16 @@ int pd_reduce_sum_static(const double* dev_x, int64_t n, double* dev_result, voi
  * microbenchmark, best of 3): the denominator of the FP64 roofline. */
 int pd_probe_fp64(double* gfma_per_s);
 
+/* Self-check of the division recipe the update kernels use for a divisor
+ * with a known reciprocal (density, ADR mass, the ADR update's 2 + cn dt, the
+ * state-based 1/m): n / d formed from y = 1 / d by two FMA corrections
+ * (Markstein's correctly rounded division) against the IEEE division, on
+ * count device pairs dev_n[i] / dev_d[i].  Writes the number of quotients
+ * whose bit patterns differ to *dev_mismatches (a device counter).  No
+ * counterpart in the reference, whose kernels divide directly. */
+int pd_check_division(const double* dev_n, const double* dev_d, int64_t count, unsigned long long* dev_mismatches,
+                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif

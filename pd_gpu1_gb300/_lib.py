@@ -97,6 +97,7 @@ _SIGS = {
     "pd_check_finite": (I32, [VP, VP]),
     "pd_kernel_launches": (I64, [VP]),
     "pd_probe_fp64": (I32, [P(D)]),
+    "pd_check_division": (I32, [VP, VP, I64, VP, VP]),
     "pd_reduce_sum_static": (I32, [VP, I64, VP, VP]),
 }
 

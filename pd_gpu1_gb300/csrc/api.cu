@@ -1296,4 +1296,9 @@ int64_t pd_kernel_launches(const pd_ctx* c) { return c ? c->launches : -1; }
 
 int pd_probe_fp64(double* gfma_per_s) { return gfma_per_s ? fp64_probe(gfma_per_s) : PD_ERR_ARG; }
 
+int pd_check_division(const double* dev_n, const double* dev_d, int64_t count, unsigned long long* dev_mismatches,
+                      void* stream) {
+    return div_check(dev_n, dev_d, count, dev_mismatches, st(stream));
+}
+
 }  // extern "C"

@@ -34,9 +34,11 @@ namespace {
 constexpr int T = 256;
 
 // cal_cn (Integrate.cu:108-129) per specimen: one warp sums the specimen's
-// per-slice damping sums in a fixed order.
+// per-slice damping sums in a fixed order.  It also forms the update's
+// 2 - cn dt and 2 + cn dt (kernel_integrate's expressions) and the IEEE
+// reciprocal of the latter, once per specimen.
 __global__ void k_batch_cn(int count, const int64_t* __restrict__ inst_slices, const double* __restrict__ part,
-                           double* __restrict__ inst_cn) {
+                           double dt, double* __restrict__ inst_cn, double* __restrict__ inst_nd) {
     const int k = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (k >= count) return;
@@ -56,6 +58,10 @@ __global__ void k_batch_cn(int count, const int64_t* __restrict__ inst_slices, c
         }
         if (cn > 2.0) cn = 1.9;
         inst_cn[k] = cn;
+        const double num = 2.0 - cn * dt, den = 2.0 + cn * dt;
+        inst_nd[3 * k] = num;
+        inst_nd[3 * k + 1] = den;
+        inst_nd[3 * k + 2] = 1.0 / den;
     }
 }
 
@@ -67,6 +73,7 @@ struct BatchArgs {
     const double* sign;
     const int* slice_inst;
     const double* inst_cn;
+    const double* inst_nd;  // per specimen: 2 - cn dt, 2 + cn dt, 1 / (2 + cn dt)
 };
 
 // kernel_quick_load with the row's signed speed factor: +1 / -1 times the
@@ -84,13 +91,16 @@ __global__ void k_batch_update(BatchArgs A, int ct, int do_next, double load) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < P.N_int) {
             const int k = A.slice_inst[i >> 5];
-            const double cn = k >= 0 ? A.inst_cn[k] : 0.0;
             // 2 dt / mass comes precomputed (the same IEEE operations, on the
             // host): two FP64 divides per node fewer on a pipe this GPU runs
-            // at 1/64 rate; dt / mass is formed only for the first step
+            // at 1/64 rate; dt / mass is formed only for the first step.  The
+            // division by 2 + cn dt goes through the specimen's reciprocal
+            // (div_recip: bit for bit the quotient).  A padding row (k < 0)
+            // takes cn = 0, the values k_batch_cn forms for cn = 0.
             const double c1 = A.c1[i];
             const double c0 = ct == 0 ? 1.0 * P.dt / A.mass[i] : 0.0;
-            const double num = 2.0 - cn * P.dt, den = 2.0 + cn * P.dt;
+            const double num = k >= 0 ? A.inst_nd[3 * k] : 2.0, den = k >= 0 ? A.inst_nd[3 * k + 1] : 2.0;
+            const double rden = k >= 0 ? A.inst_nd[3 * k + 2] : 0.5;
             double* vh[2] = {A.vhx, A.vhy};
             double* v[2] = {A.vx, A.vy};
             double* u[2] = {A.ux, A.uy};
@@ -104,7 +114,7 @@ __global__ void k_batch_update(BatchArgs A, int ct, int do_next, double load) {
                 if (ct == 0)
                     vhn = c0 * fb / 2.0;
                 else
-                    vhn = (num * vho + c1 * fb) / den;
+                    vhn = div_recip(num * vho + c1 * fb, den, rden);
                 v[a][i] = 0.5 * (vho + vhn);
                 u[a][i] = fma(vhn, P.dt, u[a][i]);
                 vh[a][i] = vhn;
@@ -141,6 +151,7 @@ BatchArgs batch_args(pd_ctx* c) {
     a.sign = c->batch.load_sign;
     a.slice_inst = c->batch.slice_inst;
     a.inst_cn = c->batch.inst_cn;
+    a.inst_nd = c->batch.inst_nd;
     return a;
 }
 
@@ -160,8 +171,9 @@ cudaError_t upload(V*& dst, const std::vector<V>& src) {
 
 void release_batch(pd_ctx* c) {
     BatchInfo& b = c->batch;
-    void* ptrs[] = {b.node_group, b.node_bc,     b.node_sed,    b.node_s0,    b.node_mass, b.node_c1,
-                    b.load_sign,  b.slice_inst,  b.inst_slices, b.slice_part, b.inst_cn};
+    void* ptrs[] = {b.node_group, b.node_bc,    b.node_sed,    b.node_s0,    b.node_mass, b.node_c1,
+                    b.node_rmass, b.load_sign,  b.slice_inst,  b.inst_slices, b.slice_part, b.inst_cn,
+                    b.inst_nd};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     b = BatchInfo{};
@@ -184,7 +196,7 @@ int batch_force(pd_ctx* c, cudaStream_t s) {
 int batch_finish(pd_ctx* c, int ct, int last, double load, cudaStream_t s) {
     const BatchInfo& B = c->batch;
     k_batch_cn<<<(unsigned)(((int64_t)B.count * 32 + T - 1) / T), T, 0, s>>>(B.count, B.inst_slices, B.slice_part,
-                                                                              B.inst_cn);
+                                                                              c->p.dt, B.inst_cn, B.inst_nd);
     BatchArgs A = batch_args(c);
     k_batch_update<<<node_grid(c, A.P.N), T, 0, s>>>(A, ct, last ? 0 : 1, load);
     c->launches += 2;
@@ -310,12 +322,15 @@ pd_ctx* pd_batch_create(const pd_params* base, const pd_specimen* spec, int coun
         std::vector<double> c1((size_t)N);
         for (int64_t r = 0; r < N; r++) c1[r] = 2.0 * p.dt / mass[r];  // kernel_integrate's 2 dt / mass
         up(B.node_c1, c1);
+        for (int64_t r = 0; r < N; r++) c1[r] = 1.0 / mass[r];  // the ADR epilogue's divisor reciprocal
+        up(B.node_rmass, c1);
     }
     up(B.load_sign, sign);
     up(B.slice_inst, slice_inst);
     up(B.inst_slices, inst_slices);
     up(B.slice_part, std::vector<double>(2 * (size_t)nslices, 0.0));
     up(B.inst_cn, std::vector<double>((size_t)count, 0.0));
+    up(B.inst_nd, std::vector<double>(3 * (size_t)count, 0.0));
     if (e != cudaSuccess) {
         pd_destroy(c);
         return fail(e == cudaErrorMemoryAllocation ? PD_ERR_NOMEM : PD_ERR_CUDA);

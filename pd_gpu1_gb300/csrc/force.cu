@@ -92,6 +92,7 @@ struct ForceArgs {
     double* res_out;          // ADR: sum over force rows of |F + b|^2 (device scalar)
     // batch of specimens (null for a single one)
     const double* node_mass;  // ADR fictitious mass per node
+    const double* node_rmass; // 1 / node_mass (IEEE-rounded)
     double* slice_part;       // per-slice damping sums (2 per slice) instead of a grid reduction
 };
 
@@ -258,17 +259,24 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
     if (DIM == 3) A.fz[r] = fzr;
     if (EPI == EPI_ADR) {
         // kernel_cnn (Integrate.cu:17-33), same operand order; a batch of
-        // specimens carries its fictitious mass per node
+        // specimens carries its fictitious mass per node.  The divisions by
+        // the mass go through its reciprocal (div_recip: bit for bit the
+        // quotient); the one by dt * vh is a plain division.
         const double mass = A.node_mass ? A.node_mass[r] : P.mass;
+        const double rmass = A.node_mass ? A.node_rmass[r] : P.rmass;
         const double vhx = A.vhx[r], vhy = A.vhy[r];
         double cn = 0.0, disp;
-        if (vhx != 0.0) cn = -1.0 * uxi * uxi * (fxr / mass - A.fox[r] / mass) / (P.dt * vhx);
+        if (vhx != 0.0)
+            cn = -1.0 * uxi * uxi * (div_recip(fxr, mass, rmass) - div_recip(A.fox[r], mass, rmass)) / (P.dt * vhx);
         disp = uxi * uxi;
-        if (vhy != 0.0) cn -= 1.0 * uyi * uyi * (fyr / mass - A.foy[r] / mass) / (P.dt * vhy);
+        if (vhy != 0.0)
+            cn -= 1.0 * uyi * uyi * (div_recip(fyr, mass, rmass) - div_recip(A.foy[r], mass, rmass)) / (P.dt * vhy);
         disp += uyi * uyi;
         if (DIM == 3) {
             const double vhz = A.vhz[r];
-            if (vhz != 0.0) cn -= 1.0 * uzi * uzi * (fzr / mass - A.foz[r] / mass) / (P.dt * vhz);
+            if (vhz != 0.0)
+                cn -= 1.0 * uzi * uzi * (div_recip(fzr, mass, rmass) - div_recip(A.foz[r], mass, rmass)) /
+                      (P.dt * vhz);
             disp += uzi * uzi;
         }
         red[0] += cn;
@@ -288,15 +296,16 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
         double ux = uxi, uy = uyi, uz = uzi;
         if (DIM == 3 && A.contact && A.dmg[r] < 1.0) contact_node(P, *A.cyl, xi, yi, zi, ux, uy, uz, vx, vy, vz, red);
         const double hdt = P.dt / 2.0;
-        const double ax = (fxr + A.bx[r]) / P.dens;
-        const double ay = (fyr + A.by[r]) / P.dens;
+        // a = (F + b) / rho through rho's reciprocal (div_recip: bit for bit the quotient)
+        const double ax = div_recip(fxr + A.bx[r], P.dens, P.rdens);
+        const double ay = div_recip(fyr + A.by[r], P.dens, P.rdens);
         vx = fma(hdt, ax, vx);
         vy = fma(hdt, ay, vy);
         A.ax[r] = ax;
         A.ay[r] = ay;
         double az = 0.0;
         if (DIM == 3) {
-            az = (fzr + A.bz[r]) / P.dens;
+            az = div_recip(fzr + A.bz[r], P.dens, P.rdens);
             vz = fma(hdt, az, vz);
             A.az[r] = az;
         }
@@ -767,9 +776,11 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
             }
         }
         if (row) {
-            const double th = acc / A.m[r];
+            // theta = acc / m and theta / m through 1/m (nb, IEEE-rounded at set-up)
+            const double m = A.m[r], rm = A.nb[r];
+            const double th = div_recip(acc, m, rm);
             A.theta[r] = th;
-            A.na[r] = th / A.m[r];
+            A.na[r] = div_recip(th, m, rm);
         }
     }
 }
@@ -970,6 +981,7 @@ static ForceArgs make_args(pd_ctx* c) {
     A.ticket = c->ticket;
     A.cn_out = c->cn;
     A.node_mass = c->batch.node_mass;
+    A.node_rmass = c->batch.node_rmass;
     A.slice_part = c->batch.slice_part;
     A.res_out = c->res;
     return A;

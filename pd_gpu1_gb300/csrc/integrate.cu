@@ -103,6 +103,7 @@ __global__ void k_adr_update(NodeArgs A, int ct, int do_next, double load) {
     const double c0 = 1.0 * P.dt / P.mass;       // ct == 0
     const double c1 = 2.0 * P.dt / P.mass;
     const double num = 2.0 - cn * P.dt, den = 2.0 + cn * P.dt;
+    const double rden = 1.0 / den;  // one IEEE division per thread; per node div_recip (bit for bit the quotient)
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < P.N_int) {
             double* vh[3] = {A.vhx, A.vhy, A.vhz};
@@ -118,7 +119,7 @@ __global__ void k_adr_update(NodeArgs A, int ct, int do_next, double load) {
                 if (ct == 0)
                     vhn = c0 * fb / 2.0;
                 else
-                    vhn = (num * vho + c1 * fb) / den;
+                    vhn = div_recip(num * vho + c1 * fb, den, rden);
                 v[a][i] = 0.5 * (vho + vhn);
                 u[a][i] = fma(vhn, P.dt, u[a][i]);
                 vh[a][i] = vhn;
@@ -152,12 +153,12 @@ __global__ void k_verlet2(NodeArgs A) {
     const double hdt = P.dt / 2.0;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N_int;
          i += (int64_t)gridDim.x * blockDim.x) {
-        A.ax[i] = (A.fx[i] + A.bx[i]) / P.dens;
-        A.ay[i] = (A.fy[i] + A.by[i]) / P.dens;
+        A.ax[i] = div_recip(A.fx[i] + A.bx[i], P.dens, P.rdens);
+        A.ay[i] = div_recip(A.fy[i] + A.by[i], P.dens, P.rdens);
         A.vx[i] = fma(hdt, A.ax[i], A.vx[i]);
         A.vy[i] = fma(hdt, A.ay[i], A.vy[i]);
         if (P.dim == 3) {
-            A.az[i] = (A.fz[i] + A.bz[i]) / P.dens;
+            A.az[i] = div_recip(A.fz[i] + A.bz[i], P.dens, P.rdens);
             A.vz[i] = fma(hdt, A.az[i], A.vz[i]);
         }
     }
@@ -280,7 +281,38 @@ __global__ void k_fp64_probe(double* out, double a, double b, int iters) {
     out[blockIdx.x * (int64_t)blockDim.x + threadIdx.x] = x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
 }
 
+// div_recip against the IEEE division on the same operands: counts the
+// pairs whose bit patterns differ (y formed here as the update kernels form
+// it, 1.0 / d).
+__global__ void k_div_check(const double* __restrict__ n, const double* __restrict__ d, int64_t count,
+                            unsigned long long* __restrict__ mismatches) {
+    unsigned long long bad = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ni = n[i], di = d[i];
+        const double q = div_recip(ni, di, 1.0 / di);
+        const double r = ni / di;
+        // bit patterns equal, or both NaN (a NaN's payload is not compared)
+        if (__double_as_longlong(q) != __double_as_longlong(r) && !(q != q && r != r)) bad++;
+    }
+    for (int off = 16; off > 0; off >>= 1) bad += __shfl_down_sync(0xffffffffu, bad, off);
+    if ((threadIdx.x & 31) == 0 && bad) atomicAdd(mismatches, bad);
+}
+
 }  // namespace
+
+int div_check(const double* n, const double* d, int64_t count, unsigned long long* mismatches, cudaStream_t s) {
+    if (!n || !d || !mismatches || count < 0) return PD_ERR_ARG;
+    cudaMemsetAsync(mismatches, 0, sizeof(unsigned long long), s);
+    if (count > 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        const int64_t want = (count + T - 1) / T;
+        const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(want, (int64_t)sms * 8));
+        k_div_check<<<grid, T, 0, s>>>(n, d, count, mismatches);
+    }
+    return cudaGetLastError() == cudaSuccess ? PD_OK : PD_ERR_CUDA;
+}
 
 int fp64_probe(double* gfma_per_s) {
     int dev = 0, sms = 0;

@@ -32,7 +32,30 @@ struct KParams {
     int64_t N, N_int;
     int nx, ny, nz, dim, model;
     double dx, emod, dens, pratio, bc, delta, critical_s, vol, dt, mass, K, G, pi, break_ymin;
+    double rdens, rmass;  // 1 / dens and 1 / mass, IEEE-rounded (the divisors' reciprocals for div_recip)
 };
+
+// n / d rounded to nearest, given y = RN(1/d) (an IEEE division done once per
+// divisor).  q1 = RN(n y) corrected once by its residual is a faithful
+// quotient; one more correction, q2 = RN(q1 + (n - d q1) y) with the
+// residual exact under FMA, is RN(n / d) by Markstein's theorem (P. Markstein,
+// IBM J. Res. Develop. 34(1), 1990; Muller et al., Handbook of Floating-Point
+// Arithmetic, Newton-Raphson-based division with an FMA): a faithful q and a
+// y within 2^-53 relative of 1/d give the correctly rounded quotient.  Five
+// FP64 instructions against a full division's sequence, on GB300's slow FP64
+// pipe.  Outside the range where the theorem's no-underflow conditions hold
+// for certain (|n|, |y| or |q| outside [2^-900, 2^900], zeros, infinities,
+// NaNs, or y = 0 for "no reciprocal") the IEEE division is taken, so the
+// result is always bit for bit n / d.
+__device__ __forceinline__ double div_recip(double n, double d, double y) {
+    const double q0 = n * y;
+    const unsigned en = ((unsigned)__double2hiint(n) >> 20) & 0x7ffu;
+    const unsigned ey = ((unsigned)__double2hiint(y) >> 20) & 0x7ffu;
+    const unsigned eq = ((unsigned)__double2hiint(q0) >> 20) & 0x7ffu;
+    if ((en - 123u > 1800u) | (ey - 123u > 1800u) | (eq - 123u > 1800u)) return n / d;  // biased 123..1923
+    const double q1 = fma(fma(-q0, d, n), y, q0);
+    return fma(fma(-q1, d, n), y, q1);
+}
 
 // Rigid impactor state kept in device memory (Cylinder, Base.cuh:237-242).
 struct CylDev {
@@ -109,11 +132,13 @@ struct BatchInfo {
     double* node_s0 = nullptr;         // [N] critical stretch of the node's specimen
     double* node_mass = nullptr;       // [N] ADR fictitious mass per node
     double* node_c1 = nullptr;         // [N] 2 dt / mass per node (the update's coefficient, host-computed)
+    double* node_rmass = nullptr;      // [N] 1 / mass per node (host-computed, IEEE-rounded)
     double* load_sign = nullptr;       // [N] signed load factor of moving boundary rows, 0 elsewhere
     int* slice_inst = nullptr;         // [nslices] specimen of each slice (-1: none)
     int64_t* inst_slices = nullptr;    // [count + 1] first slice of each specimen's interior
     double* slice_part = nullptr;      // [2 * nslices] per-slice damping sums
     double* inst_cn = nullptr;         // [count] damping coefficient per specimen
+    double* inst_nd = nullptr;         // [3 count] 2 - cn dt, 2 + cn dt and 1 / (2 + cn dt) per specimen
     std::vector<int64_t> h_inst_nodes; // host: interior node offset of each specimen (+ total)
     std::vector<int64_t> h_inst_bnd;   // host: boundary node offset of each specimen (+ total)
 };
@@ -200,6 +225,8 @@ inline KParams kparams(const pd_params& p) {
     k.G = p.G;
     k.pi = p.pi;
     k.break_ymin = p.break_ymin;
+    k.rdens = 1.0 / p.dens;
+    k.rmass = 1.0 / p.mass;
     return k;
 }
 
@@ -256,6 +283,7 @@ int add_increment(pd_ctx* c, const double* du, cudaStream_t s);
 // Bond coefficients, intact bits and positions current (the run loops' entry check).
 int make_ready(pd_ctx* c, cudaStream_t s);
 int fp64_probe(double* gfma_per_s);
+int div_check(const double* n, const double* d, int64_t count, unsigned long long* mismatches, cudaStream_t s);
 // batch.cu
 void release_batch(pd_ctx* c);
 int batch_prologue(pd_ctx* c, double load, cudaStream_t s);
