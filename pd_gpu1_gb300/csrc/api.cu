@@ -40,11 +40,12 @@ __global__ void k_fill_int(int* a, int64_t n, int v) {
         a[i] = v;
 }
 
-__global__ void k_sell_to_csr(int64_t S, const int* __restrict__ csr, const double* __restrict__ src,
+// The extension of each slot (a float pair) into the CSR-ordered double array.
+__global__ void k_sell_to_csr(int64_t S, const int* __restrict__ csr, const float2* __restrict__ src,
                               double* __restrict__ dst) {
     for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < S; t += (int64_t)gridDim.x * blockDim.x) {
         const int q = csr[t];
-        if (q >= 0) dst[q] = src[t];
+        if (q >= 0) dst[q] = (double)src[t].x + (double)src[t].y;
     }
 }
 
@@ -300,6 +301,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     ok = ok && cudaMalloc(&c->NN, (size_t)p->N * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&c->rowptr, ((size_t)p->N + 1) * 8) == cudaSuccess;
     ok = ok && cudaMalloc(&c->node_a, nb) == cudaSuccess && cudaMalloc(&c->node_b, nb) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->node_c, nb) == cudaSuccess;
     ok = ok && cudaMalloc(&c->partials, (size_t)kMaxPartials * 4 * 8) == cudaSuccess;
     ok = ok && cudaMalloc(&c->ticket, 4 * sizeof(unsigned)) == cudaSuccess;
     ok = ok && cudaMalloc(&c->cn, 8) == cudaSuccess && cudaMalloc(&c->red_out, 8) == cudaSuccess;
@@ -317,6 +319,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     cudaMemset(c->rowptr, 0, ((size_t)p->N + 1) * 8);
     cudaMemset(c->node_a, 0, nb);
     cudaMemset(c->node_b, 0, nb);
+    cudaMemset(c->node_c, 0, nb);
     cudaMemset(c->ticket, 0, 4 * sizeof(unsigned));
     cudaMemset(c->cn, 0, 8);
     cudaMemset(c->res, 0, 8);
@@ -338,9 +341,8 @@ int pd_destroy(pd_ctx* c) {
     for (int b = 0; b < 2; b++)
         for (int a = 0; a < 3; a++)
             if (c->pos[b][a]) cudaFree(c->pos[b][a]);
-    void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->partials, c->ticket, c->cn, c->red_out,
-                    c->res, c->cyl,    c->NL,     c->idist,  c->fac,      c->scr,    c->w,  c->e,
-                    c->fail};
+    void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->node_c, c->partials, c->ticket, c->cn,
+                    c->red_out, c->res, c->cyl, c->NL, c->idist, c->fac, c->scr, c->w, c->e, c->fail};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     release_sell(c);

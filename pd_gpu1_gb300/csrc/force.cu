@@ -28,7 +28,8 @@
 // stretch arithmetic on three 32-byte records per slot, with the bond vector in
 // the dilatation pass's operand order ((x_c - x_i) + u_c) - u_i for theta and
 // the force pass's (P_c - x_i) - u_i for the force, as the reference rounds
-// them; e in double for theta and the stored extension.
+// them; e, the theta sum and t_i + t_j in pairs (the node quantities theta/m
+// and 1/m as power-of-two-scaled pairs).
 //
 // Epilogues fused into the same launch (one launch per explicit step):
 //   EPI_VERLET  a = (F+b)/rho; v += dt/2 a (kernel_integrate_2D_2, Integrate.cu:218-249),
@@ -60,7 +61,10 @@ struct ForceArgs {
     const StateGeo* sgeo;    // state-based: per-slot geometry (column, float reference vector, c0, l0)
     const StateTheta* sth;   // state-based: dilatation-pass record (xi, cth)
     const StateForce* sfo;   // state-based: force-pass record (c1, c2, ecrit, xi_z)
-    double* e;
+    float2* e;                // state: extension per slot as a float pair
+    double sn_scale;          // state: 2^-sn_exp (theta/m and 1/m pairs)
+    double sth_inv;           // state: 2^-sth_exp (undoes the dilatation weights' scale)
+    double st_scale;          // state: 2^st_exp (undoes the force pairs' scale)
     uint32_t* bits;
     int64_t S;
     const int* NN;
@@ -74,8 +78,9 @@ struct ForceArgs {
     const double *bx, *by, *bz;
     const double *fox, *foy, *foz;
     const double *vhx, *vhy, *vhz;
-    double* na;        // state: theta/m
-    const double* nb;  // state: 1/m
+    float2* na;         // state: theta/m times 2^-sn_exp as a float pair
+    const double* nb;   // state: 1/m (IEEE-rounded)
+    const float2* nb2;  // state: 1/m times 2^-sn_exp as a float pair
     const double* m;
     double* theta;
     const double* dmg;
@@ -753,7 +758,7 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
         const int W = A.width[s];
         const int64_t b = A.base[s];
         const uint32_t* wbits = A.bits + A.fbase[s];
-        double acc = 0.0;
+        ff acc{0.0f, 0.0f};  // sum of the weighted extensions, times 2^sth_exp
         for (int k = 0; k < W; k++) {
             const int64_t slot = b + (int64_t)k * 32 + lane;
             bool use = k < nn;
@@ -770,17 +775,20 @@ __global__ void __launch_bounds__(kForceBlock) k_theta(const ForceArgs A) {
                 eta[1] = exact_offset((hi_f64(w2) + A.uy[c]) - uyi, xf[1]);
                 if (DIM == 3) eta[2] = exact_offset((lo_f64(w3) + A.uz[c]) - uzi, xf[2]);
                 pair_stretch<DIM>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
-                const double e = f64_of_f32s(e2.h) + f64_of_f32s(e2.l);
-                A.e[slot] = e;
-                acc = fma(hi_f64(w3), e, acc);
+                // e stays a pair for the force pass; the weighted sum is formed in
+                // pairs too (no FP64 instruction per bond beyond the bond vector)
+                A.e[slot] = make_float2(e2.h, e2.l);
+                acc = ff_add(acc, ff_mul(ff{w3.z, w3.w}, e2));
             }
         }
         if (row) {
             // theta = acc / m and theta / m through 1/m (nb, IEEE-rounded at set-up)
             const double m = A.m[r], rm = A.nb[r];
-            const double th = div_recip(acc, m, rm);
+            const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
+            const double th = div_recip(a, m, rm);
             A.theta[r] = th;
-            A.na[r] = div_recip(th, m, rm);
+            const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
+            A.na[r] = make_float2(na.h, na.l);
         }
     }
 }
@@ -801,7 +809,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
             const int64_t rr = force_row ? r : A.nforce - 1;
             const double xi = A.x[rr], yi = A.y[rr], zi = DIM == 3 ? A.z[rr] : 0.0;
             const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
-            const double nai = A.na[rr], nbi = A.nb[rr];
+            const float2 na_i = A.na[rr], nb_i = A.nb2[rr];
+            const ff nai{na_i.x, na_i.y}, nbi{nb_i.x, nb_i.y};
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
             ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
             const int W = A.width[s];
@@ -829,9 +838,13 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                         etaz = bond_offset(A.pcz[c], zi, uzi, xf[2]);
                     }
                     pair_stretch<DIM>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
-                    const double T = fma(hi_f64(w4) * A.e[slot], nbi + A.nb[c], lo_f64(w4) * (nai + A.na[c]));
+                    // T = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j), times 2^-st_exp,
+                    // in pair arithmetic on the scaled pairs (no FP64 instruction)
+                    const float2 ec = A.e[slot], nac = A.na[c], nbc = A.nb2[c];
+                    const ff T = ff_add(ff_mul(ff{w4.x, w4.y}, ff_add(nai, ff{nac.x, nac.y})),
+                                        ff_mul(ff_mul(ff{w4.z, w4.w}, ff{ec.x, ec.y}), ff_add(nbi, ff{nbc.x, nbc.y})));
                     // t = T / (2 L) and f += t d in pair arithmetic (as in the bond-based kernel)
-                    const ff t = ff_mul(ff_split(T), ff{0.5f * y.h, 0.5f * y.l});
+                    const ff t = ff_mul(T, ff{0.5f * y.h, 0.5f * y.l});
                     fxa = ff_add(fxa, ff_mul(t, dp[0]));
                     fya = ff_add(fya, ff_mul(t, dp[1]));
                     if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_add(ff{xf[2], 0.0f}, etaz)));
@@ -840,9 +853,10 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
                 if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
             }
-            fxr = f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l);
-            fyr = f64_of_f32s(fya.h) + f64_of_f32s(fya.l);
-            if (DIM == 3) fzr = f64_of_f32s(fza.h) + f64_of_f32s(fza.l);
+            // undo the power-of-two scale of T (exact)
+            fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
+            fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
+            if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.st_scale;
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
@@ -938,6 +952,9 @@ static ForceArgs make_args(pd_ctx* c) {
     A.sth = S.sth;
     A.sfo = S.sfo;
     A.e = S.e;
+    A.sn_scale = std::ldexp(1.0, -S.sn_exp);
+    A.sth_inv = std::ldexp(1.0, -S.sth_exp);
+    A.st_scale = std::ldexp(1.0, S.st_exp);
     A.bits = S.bits;
     A.S = S.S;
     A.NN = c->NN;
@@ -973,6 +990,7 @@ static ForceArgs make_args(pd_ctx* c) {
     A.vhz = c->nf[PD_F_VHZ];
     A.na = c->node_a;
     A.nb = c->node_b;
+    A.nb2 = c->node_c;
     A.m = c->nf[PD_F_M];
     A.theta = c->nf[PD_F_THETA];
     A.dmg = c->nf[PD_F_DMG];

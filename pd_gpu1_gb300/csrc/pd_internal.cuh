@@ -90,11 +90,11 @@ struct alignas(16) StateGeo {
 };
 struct alignas(16) StateTheta {
     double xi[3];  // reference vector x_c - x_i (FP64, the dilatation pass's operand; z = 0 in 2-D)
-    double cth;    // dilatation weight of e
+    float2 cth;    // dilatation weight of e times 2^sth_exp, as a float pair
 };
 struct alignas(16) StateForce {
-    double c1;     // dilatation coefficient of t
-    double c2;     // extension coefficient of t
+    float2 c1;     // dilatation coefficient of t times 2^(sn_exp - st_exp), as a float pair
+    float2 c2;     // extension coefficient of t times 2^(sn_exp - st_exp), as a float pair
     double ecrit;  // break threshold on e = L - l0 (s0 l0; +inf: never)
     double xiz;    // xi[2] again (the 3-D length's z term in the dilatation order)
 };
@@ -117,7 +117,12 @@ struct Sell {
     StateGeo* sgeo = nullptr;     // [S] state-based: geometry record (both passes)
     StateTheta* sth = nullptr;    // [S] state-based: dilatation-pass record
     StateForce* sfo = nullptr;    // [S] state-based: force-pass record
-    double* e = nullptr;     // [S] state-based: extension (dilatation-pass operand order)
+    float2* e = nullptr;     // [S] state-based: extension (dilatation-pass operand order) as a float pair
+    // state-based power-of-two scales that keep the pair arithmetic of the two
+    // passes in float range whatever the lattice spacing: theta/m and 1/m are
+    // carried times 2^-sn_exp, the dilatation weights times 2^sth_exp, the force
+    // pair sums times 2^-st_exp (exact scalings, undone in FP64 per node)
+    int sn_exp = 0, sth_exp = 0, st_exp = 0;
     uint32_t* bits = nullptr;// [F] intact flags
 };
 
@@ -164,8 +169,9 @@ struct pd_ctx {
     int parity = 0;          // pos[parity] is current
     bool pos_valid = false;  // pos[parity] == x + u
     int* NN = nullptr;
-    double* node_a = nullptr;  // state-based: theta/m
-    double* node_b = nullptr;  // state-based: 1/m
+    float2* node_a = nullptr;  // state-based: theta/m times 2^-sn_exp, as a float pair
+    double* node_b = nullptr;  // state-based: 1/m (IEEE-rounded)
+    float2* node_c = nullptr;  // state-based: 1/m times 2^-sn_exp, as a float pair
 
     // CSR bond family
     int64_t B = 0;

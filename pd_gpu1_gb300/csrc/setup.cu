@@ -304,7 +304,7 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
                 StateForce F{};
                 F.ecrit = HUGE_VAL;
                 S.sfo[slot] = F;
-                S.e[slot] = 0.0;
+                S.e[slot] = make_float2(0.0f, 0.0f);
             }
             continue;
         }
@@ -346,19 +346,23 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
             T.xi[0] = x[c] - x[r];
             T.xi[1] = y[c] - y[r];
             T.xi[2] = P.dim == 3 ? z[c] - z[r] : 0.0;
-            T.cth = th_coef * w[q] * L0 * fac[q] * P.vol;
+            // the coefficients as float pairs, scaled by powers of two (exact)
+            const ff cth = ff_split(th_coef * w[q] * L0 * fac[q] * P.vol * ldexp(1.0, S.sth_exp));
+            T.cth = make_float2(cth.h, cth.l);
             StateGeo G;
             G.col = (int)c;
             float_reference(T.xi, P.dim, L0, G.xf, G.c0, G.l0);
             StateForce F;
-            F.c1 = 2.0 * a_coef * wf * L0;
-            F.c2 = 2.0 * b_coef * wf;
+            const double cs = ldexp(1.0, S.sn_exp - S.st_exp);
+            const ff c1 = ff_split(2.0 * a_coef * wf * L0 * cs), c2 = ff_split(2.0 * b_coef * wf * cs);
+            F.c1 = make_float2(c1.h, c1.l);
+            F.c2 = make_float2(c2.h, c2.l);
             F.ecrit = ecrit;
             F.xiz = T.xi[2];
             S.sgeo[slot] = G;
             S.sth[slot] = T;
             S.sfo[slot] = F;
-            S.e[slot] = 0.0;
+            S.e[slot] = make_float2(0.0f, 0.0f);
         }
     }
 }
@@ -396,9 +400,17 @@ __global__ void k_csr_from_bits(int64_t nslices, const int* __restrict__ width, 
     }
 }
 
-__global__ void k_inv_m(int64_t N, const double* __restrict__ m, double* __restrict__ inv) {
+// 1/m per node (IEEE-rounded, the dilatation pass's divisor reciprocal) and
+// the same times 2^-sn as a float pair (the force pass's operand).
+__global__ void k_inv_m(int64_t N, const double* __restrict__ m, double sn_scale, double* __restrict__ inv,
+                        float2* __restrict__ inv_pair) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < N) inv[i] = 1.0 / m[i];
+    if (i < N) {
+        const double v = 1.0 / m[i];
+        inv[i] = v;
+        const ff p = ff_split(v * sn_scale);
+        inv_pair[i] = make_float2(p.h, p.l);
+    }
 }
 
 unsigned warps_grid(int64_t nwarps) { return (unsigned)((nwarps * 32 + 255) / 256); }
@@ -572,6 +584,22 @@ int prepare(pd_ctx* c, cudaStream_t s) {
         S.kscale = std::ldexp(1.0, S.kexp);
         S.kscale_inv = std::ldexp(1.0, -S.kexp);
     }
+    // state-based: powers of two near 1/m, the dilatation weight and the force
+    // coefficient c2/m, from the lattice (m ~ half of delta^2 vol over a family
+    // of pi (delta/dx)^2 or 4/3 pi (delta/dx)^3 members); any estimate within a
+    // few binades keeps the pairs in float range, and the scalings are exact
+    if (state) {
+        const double r = P.delta / P.dx;
+        const double nfam = P.dim == 2 ? M_PI * r * r : 4.0 / 3.0 * M_PI * r * r * r;
+        const double m_est = 0.25 * P.delta * P.delta * P.vol * nfam;
+        const double pr = P.pratio;
+        const double th_coef = P.dim == 2 ? 2.0 * (2.0 * pr - 1.0) / (pr - 1.0) : 3.0;
+        const double b_coef = P.dim == 2 ? 8.0 * P.G : 15.0 * P.G;
+        auto lg = [](double v) { return (v > 0.0 && std::isfinite(v)) ? (int)std::lround(std::log2(v)) : 0; };
+        S.sn_exp = lg(1.0 / m_est);
+        S.sth_exp = -lg(std::fabs(th_coef) * P.delta * P.vol);
+        S.st_exp = S.sn_exp + lg(std::fabs(2.0 * b_coef) * P.vol);
+    }
     if (ok && state)
         ok = !cudaMalloc(&S.sgeo, n8 * 4) && !cudaMalloc(&S.sth, n8 * 4) && !cudaMalloc(&S.sfo, n8 * 4) &&
              !cudaMalloc(&S.e, n8);
@@ -586,7 +614,8 @@ int prepare(pd_ctx* c, cudaStream_t s) {
                                               c->nf[PD_F_M], c->batch.node_bc, c->batch.node_s0, S);
     c->launches++;
     if (state) {
-        k_inv_m<<<(unsigned)((P.N + 255) / 256), 256, 0, s>>>(P.N, c->nf[PD_F_M], c->node_b);
+        k_inv_m<<<(unsigned)((P.N + 255) / 256), 256, 0, s>>>(P.N, c->nf[PD_F_M], std::ldexp(1.0, -S.sn_exp),
+                                                             c->node_b, c->node_c);
         c->launches++;
     }
     c->bits_current = false;
