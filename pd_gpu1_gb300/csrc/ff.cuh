@@ -49,6 +49,12 @@ __device__ __forceinline__ ff ff_add(ff a, ff b) {
     return ff_fast(s.h, s.l + (a.l + b.l));
 }
 
+// A float plus a pair (ff_add with a zero low part, one addition fewer).
+__device__ __forceinline__ ff ff_add_f(float a, ff b) {
+    ff s = ff_two_sum(a, b.h);
+    return ff_fast(s.h, s.l + b.l);
+}
+
 // Double to pair with integer operations: h = v truncated to 24 significant
 // bits, l = the remaining 29 mantissa bits rounded to a float.
 __device__ __forceinline__ ff ff_split(double v) {

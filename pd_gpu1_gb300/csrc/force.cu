@@ -124,12 +124,14 @@ constexpr int kMaxWarpsPerBlock = kMaxBondBlock / 32;
 constexpr bool kIntExactA = false;
 
 // diff * 2^(e - 1075) as a normalized pair; exact for |diff| < 2^48 and a
-// scale within the float range (the caller checks both).
+// scale within the float range (the caller checks both).  h is zero or a
+// multiple of 2^24 sc and 0 <= l < 2^24 sc, so |h| >= |l| whenever h != 0 and
+// the fast two-sum gives the exact pair (the same one as the full two-sum).
 __device__ __forceinline__ ff ff_from_scaled(int64_t diff, int e) {
     const float sc = __int_as_float((e - 1075 + 127) << 23);
     const float h = __int2float_rn((int)(diff >> 24)) * (sc * 16777216.0f);
     const float l = __int2float_rn((int)(diff & 0xffffff)) * sc;
-    return ff_two_sum(h, l);
+    return ff_fast(h, l);
 }
 
 __device__ __forceinline__ uint64_t dbits(double v) { return (uint64_t)__double_as_longlong(v); }
@@ -455,7 +457,7 @@ __device__ __forceinline__ void pair_stretch(const ff eta[3], const float xf[3],
         // pair that ff_fast produced returns that pair unchanged
         D = a == 0 ? ff_mul_f(eta[a], xf[a]) : ff_add(D, ff_mul_f(eta[a], xf[a]));
         Q = a == 0 ? ff_sq(eta[a]) : ff_add(Q, ff_sq(eta[a]));
-        dp[a] = ff_add(ff{xf[a], 0.0f}, eta[a]);
+        dp[a] = ff_add_f(xf[a], eta[a]);
     }
     D = ff_add(ff_add(ff{c0.x, c0.y}, ff{2.0f * D.h, 2.0f * D.l}), Q);  // L^2 - l0^2
     const ff L0p{l0.x, l0.y};
@@ -847,7 +849,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                     const ff t = ff_mul(T, ff{0.5f * y.h, 0.5f * y.l});
                     fxa = ff_add(fxa, ff_mul(t, dp[0]));
                     fya = ff_add(fya, ff_mul(t, dp[1]));
-                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_add(ff{xf[2], 0.0f}, etaz)));
+                    if (DIM == 3) fza = ff_add(fza, ff_mul(t, ff_add_f(xf[2], etaz)));
                     brk = pair_exceeds(e2, lo_f64(w5));
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
