@@ -125,3 +125,39 @@ def test_batch_specimen_table_is_seeded():
         assert 70e9 <= s["emod"] <= 210e9 and 2400 <= s["dens"] <= 8000
         assert s["critical_s"] == presets.s0_2d(s["G0"], s["emod"], 3.015 * 5e-4)
         assert 0.0 <= s["crack_len"] <= 0.3 * s["nx"] * 5e-4 and 0.0 <= s["crack_theta"] < math.pi / 2
+
+
+def test_header_serves_a_plain_c_caller(tmp_path):
+    """include/pd.h compiles as pedantic C99 (a foreign-function caller binds
+    it as C), links against libpd_gb300.so, and its host-only entry points
+    run without a GPU: the parameter derivation of the crack-branching plate
+    at 5 % scale agrees with the oracle's."""
+    import shutil
+    import subprocess
+
+    from pd_gpu1_gb300._lib import LIB_PATH
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        import pytest
+
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include "pd.h"\n#include <stdio.h>\n'
+        "int main(void) {\n"
+        "    pd_params p;\n"
+        "    int st = pd_params_derive(&p, 2, PD_MODEL_BOND, PD_MODE_DYNAMIC, 1e-8, 10, 5e-5, 0.0, 5e-5,\n"
+        "                              0.005, 0.002, 0.0, 72e9, 1.0 / 3.0, 2440.0, 7e-4, 0);\n"
+        '    printf("%s %lld %.17g %.17g\\n", pd_status_string(st), (long long)p.N, p.bc, p.mass);\n'
+        "    return st;\n"
+        "}\n")
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(LIB_PATH)
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.join(ROOT, "include"), str(src), "-L", libdir, "-lpd_gb300",
+                    "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    q = orc.derive_params(2, 1, 2, 1e-8, 10, 5e-5, 0.0, 5e-5, 0.005, 0.002, 0.0, 72e9, 1 / 3, 2440.0, 7e-4)
+    assert out[0] == "PD_OK" and int(out[1]) == q.N
+    assert float(out[2]) == q.bc and float(out[3]) == q.mass
