@@ -13,6 +13,8 @@ inputs; these hold on any input.
   forces.
 * Small strains: the force is linear in the displacement to first order in
   the strain.
+The ordinary state-based force keeps the first two as well (a state-based
+plate without boundary rows).
 """
 import numpy as np
 import pytest
@@ -107,3 +109,43 @@ def test_force_is_linear_at_small_strains(plate):
     # geometric nonlinearity: relative size ~ strain (1e-6)
     assert np.abs(fx2 - 2.0 * fx1).max() < 1e-4 * scale
     assert np.abs(fy2 - 2.0 * fy1).max() < 1e-4 * scale
+
+
+@pytest.fixture(scope="module")
+def state_plate():
+    """An ordinary state-based plate (80 x 60 nodes, dx = 1e-4, the crack-grow
+    material) whose nodes all carry forces: no boundary rows."""
+    p = orc.derive_params(2, 2, 2, 1.3367e-8, 10, 1e-4, 1.0, 1e-4, 0.008, 0.006, 0.0, 192e9, 0.3, 7850.0, 0.04472)
+    x, y = orc.plate_coords(p)
+    m = orc.Model(p, x, y)
+    m.find_neighbor()
+    m.vol_corr()
+    m.initial_weight()
+    return p, x, y, m
+
+
+def _state_forces(m, ux, uy):
+    m.ux[:] = ux
+    m.uy[:] = uy
+    m.state_force()
+    return m.fx.copy(), m.fy.copy()
+
+
+def test_state_based_rigid_translation_gives_no_force(state_plate):
+    p, x, y, m = state_plate
+    fx0, fy0 = _state_forces(m, *_strain_field(x, y))
+    scale = max(np.abs(fx0).max(), np.abs(fy0).max())
+    fx, fy = _state_forces(m, np.full(p.N, 3.7e-6), np.full(p.N, -1.9e-6))
+    assert max(np.abs(fx).max(), np.abs(fy).max()) < 1e-9 * scale
+    assert np.abs(m.theta).max() < 1e-9  # no dilatation either
+
+
+def test_state_based_pair_forces_conserve_momentum(state_plate):
+    """t_i + t_j is symmetric in the two ends and the bond direction is not,
+    so the state-based pair forces balance as the bond-based ones do."""
+    p, x, y, m = state_plate
+    assert p.N == p.N_int
+    fx, fy = _state_forces(m, *_strain_field(x, y))
+    tot = np.abs(fx).sum() + np.abs(fy).sum()
+    assert abs(fx.sum()) < 1e-10 * tot
+    assert abs(fy.sum()) < 1e-10 * tot
