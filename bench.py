@@ -47,14 +47,43 @@ ALG_BYTES_PER_BOND_2D = 12.125  # int32 neighbour + one FP64 coefficient + one f
 ALG_BYTES_PER_NODE_2D = 48.0    # read x, y, ux, uy; write fx, fy
 ALG_BYTES_PER_BOND_3D = 12.125
 ALG_BYTES_PER_NODE_3D = 72.0
-ALG_FP64_PER_BOND_2D = 23       # 10 add/sub, 8 mul, 3 div, 1 sqrt, 1 compare (sqrt/div counted once)
-ALG_FP64_PER_BOND_3D = 31
-# measured DRAM bytes per bond and per node of the step kernel (ncu dram__bytes_read.sum +
-# dram__bytes_write.sum, one capture per workload, summarised under profiles/; a zero per-node
-# figure means the node traffic is folded into the per-bond one)
-TRAFFIC = {"crack_branching_2d_pmb_verlet": (48.6, 139.8), "batch_plate_adr_2d_pmb": (54.5, 0.0),
-           "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0), "plate_crack_grow_2d_state_verlet": (153.3, 0.0),
-           "kalthoff_winkler_3d_state_verlet": (148.9, 0.0)}
+# FP64 instructions the force kernels execute per bond in their bond loops,
+# counted in the kernel source (csrc/force.cu): the bond vector's FP64
+# subtractions with the reference's roundings, two per component (bond_offset),
+# plus in the state-based passes the dilatation-order vector of the theta pass
+# (and, in 3-D, its z term in the force pass).  Bonds within two float ulps of
+# their break threshold add one; per-node epilogue instructions are not counted.
+FP64_EXEC_PER_BOND = {(1, 2): 4, (1, 3): 6, (2, 2): 8, (2, 3): 14}  # (model, dim)
+# DRAM bytes per bond and per node of the step kernel: ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one capture per workload (kernel, case, date below),
+# scaled to the timed launch's bonds and nodes; a zero per-node figure means the
+# node traffic is folded into the per-bond one
+TRAFFIC = {
+    "crack_branching_2d_pmb_verlet": (48.6, 139.8, "k_bond_force<2,1>, 800k-node half plate, 2026-12-03"),
+    "batch_plate_adr_2d_pmb": (54.5, 0.0, "k_bond_force<2,2>, 64-plate batch, 2026-12-03"),
+    "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0, "k_bond_split3, full slab, 2026-12-03"),
+    "plate_crack_grow_2d_state_verlet": (153.3, 0.0, "k_theta<2> + k_state_force<2,1>, full plate, 2026-12-03"),
+    "kalthoff_winkler_3d_state_verlet": (148.9, 0.0, "k_theta<3> + k_state_force<3,0>, full slab, 2026-12-03")}
+
+
+def traffic_of(workload, bonds, nodes):
+    """(bytes per launch, description of the capture) from TRAFFIC, or (None, None)."""
+    tr = TRAFFIC.get(workload)
+    if not tr:
+        return None, None
+    return tr[0] * bonds + tr[1] * nodes, (f"ncu DRAM bytes of {tr[2]}: {tr[0]} B per bond + {tr[1]} B per node, "
+                                           f"scaled to this launch")
+
+
+def fp64_block(model, dim, bonds, kern_ms, gfma):
+    """FP64 pipe use of the force kernel's bond loop: executed FP64
+    instructions per second against the measured FP64 instruction rate
+    (pd_probe_fp64, dependent DFMA chains)."""
+    n = FP64_EXEC_PER_BOND[(model, dim)]
+    rate = n * bonds / (kern_ms * 1e-3) / 1e9
+    return {"executed_per_bond": n, "achieved_ginst_s": rate, "peak_ginst_s": gfma, "frac": rate / gfma,
+            "counted": "FP64 instructions of the bond loop, from the kernel source; epilogue not counted",
+            "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}
 
 
 def rank_info():
@@ -350,23 +379,34 @@ def reference_cuda_state(eng, p, setup, meta, args, value, B):
     eng.damage()
     de, dr = eng.get("DMG")[: p.N_int], out["dmg"][: p.N_int]
     xs = eng.get("X")[: p.N_int]
-
-    def tip(d):
-        hot = np.nonzero(d > 0.38)[0]
-        return float(xs[hot].max()) if len(hot) else None
-
     tip_e = eng.crack_tip(0.38)[0]
     return {"unit": "bond-updates/s", "steps": kref, "kernel_state_force_2D_loop": rate, "best": rate,
             "engine_over_best": value / rate,
             "what": "the reference's crack-grow loop (quick_load, integrate_2D_1, cal_theta_2D, state_force_2D, "
                     "integrate_2D_2; compiled from its sources, FP64)",
-            "damage_after_steps": args.steps,
+            **damage_parity(de, dr, xs, tip_e, p.delta, args.steps),
+            "intact_flags_equal": float(np.mean(eng.get("FAIL") == out["fail"]))}
+
+
+def crack_tip_x(d, xs, threshold=0.38):
+    """x of the rightmost node whose damage exceeds the threshold (None: none
+    does), the row scan the reference's crack-grow driver carries in a comment
+    (Solve_Plate_Crack_Grow.cu:150-162)."""
+    hot = np.nonzero(d > threshold)[0]
+    return float(xs[hot].max()) if len(hot) else None
+
+
+def damage_parity(de, dr, xs, tip_e, horizon, steps):
+    """Damage fields of two runs from the same initial state compared node by
+    node: the fraction of nodes equal to 1e-12, the largest difference, the
+    damaged nodes on each side and the crack tips (tip_e: the engine's own
+    pd_crack_tip, else taken from de)."""
+    tip_a = crack_tip_x(de, xs) if tip_e is None or tip_e != tip_e else float(tip_e)
+    return {"damage_after_steps": steps,
             "damage_nodes_equal": float(np.mean(np.abs(de - dr) <= 1e-12)),
-            "damage_max_abs_diff": float(np.abs(de - dr).max()),
-            "damaged_nodes": int((dr > 0).sum()),
-            "intact_flags_equal": float(np.mean(eng.get("FAIL") == out["fail"])),
-            "crack_tip_x": {"engine": None if tip_e != tip_e else float(tip_e), "reference": tip(dr),
-                            "horizon": p.delta}}
+            "damage_max_abs_diff": float(np.abs(de - dr).max()) if len(de) else 0.0,
+            "damaged_nodes": int((dr > 0).sum()), "damaged_nodes_engine": int((de > 0).sum()),
+            "crack_tip_x": {"engine": tip_a, "reference": crack_tip_x(dr, xs), "horizon": horizon}}
 
 
 def r_inputs(eng, p):
@@ -552,10 +592,7 @@ def batch_arm(args):
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
     gfma = C.c_double()
     L.pd_probe_fp64(C.byref(gfma))
-    fp64_peak = 2.0 * gfma.value / 1e3
-    alg_flops = ALG_FP64_PER_BOND_2D * B
-    tr = TRAFFIC.get(meta["workload"])
-    traffic = tr[0] * B + tr[1] * p.N_int if tr else None
+    traffic, traffic_src = traffic_of(meta["workload"], B, p.N_int)
 
     # end to end through the C ABI with host buffers: the initial state goes up
     # from pinned host memory, the displacement field comes back every 100 steps
@@ -650,13 +687,12 @@ def batch_arm(args):
                        "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 28 / 1e9),
                        "setup_s": setup_s, "broken_bond_fraction": broken},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
+                         "peak_source": peak_kind,
                          "kernel": "k_bond_force<2, ADR>", "kernel_ms": kern_ms,
                          "kernel_share_of_step": kern_ms / step_ms, "autotune_ms": tuned[4],
                          "alg_bytes_per_launch": alg_bytes,
-                         "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
-                                  "frac": alg_flops / (kern_ms * 1e-3) / 1e12 / fp64_peak,
-                                  "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},
+                         "fp64": fp64_block(1, 2, B, kern_ms, gfma.value)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk, "sequential": sequential,
             "reference_cuda": ref_cuda,
         }
@@ -852,14 +888,9 @@ def gb300_arm(args):
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
     gfma = C.c_double()
     lib().pd_probe_fp64(C.byref(gfma))
-    fp64_peak_tflops = 2.0 * gfma.value / 1e3
-    alg_flops = (ALG_FP64_PER_BOND_3D if is3d else ALG_FP64_PER_BOND_2D) * B * (2 if state else 1)
-    # DRAM bytes per launch from the ncu capture summarised in
-    # profiles/k_bond_force_crack_branching.md (half-size plate, scaled by bonds and nodes)
-    traffic = None
-    tr = TRAFFIC.get(meta["workload"])
-    if tr:
-        traffic = tr[0] * B + tr[1] * p.N_int
+    # DRAM bytes per launch from one ncu capture of the same kernel (the case
+    # and date are carried in the line), scaled by bonds and nodes
+    traffic, traffic_src = traffic_of(meta["workload"], B, p.N_int)
 
     # end to end through the C ABI with host buffers: the initial state and the
     # loading go up from pinned host memory, the damage field comes back at
@@ -914,38 +945,31 @@ def gb300_arm(args):
                 ms_ref = r.run(variant, kref, meta.get("dmg_every", 0))
                 rates[name] = B * kref / (ms_ref * 1e-3)
             # the damage field after the whole run, both implementations from the
-            # same initial state: nodes whose damage agrees, and the crack tips
+            # same initial state: nodes whose damage agrees, and the crack tips.
+            # The reference's kernel_cal_dmg_2D runs once after its last step
+            # (the damage field does not feed back into these steps), whatever
+            # the step count: a run shorter than the dump interval still compares
+            # two computed fields
             setup(eng)
             dref = {}
             for name, variant in (("particle", ref_gpu.RefGPU.PARTICLE), ("warp", ref_gpu.RefGPU.WARP)):
                 r.setup(p, *r_inputs(eng, p))
-                r.run(variant, args.steps, meta.get("dmg_every", 0))
+                r.run(variant, args.steps, args.steps)
                 dref[name] = r.get()["dmg"][: p.N_int]
             r.free()
             run_steps(eng, meta, args.steps)
             eng.damage()
             de, dr = eng.get("DMG")[: p.N_int], dref["particle"]
             xs = eng.get("X")[: p.N_int]
-
-            def tip(d):
-                hot = np.nonzero(d > 0.38)[0]
-                return float(xs[hot].max()) if len(hot) else None
-
-            tip_r = tip(dr)
             tip_e = eng.crack_tip(0.38)[0]
             best = max(rates.values())
             ref_cuda = {"unit": "bond-updates/s", "steps": kref, **rates, "best": best,
                         "engine_over_best": value / best,
                         "what": "the reference's kernels (compiled from its sources, FP64) in its step loop: "
                                 "integrate_2D_1, force, integrate_2D_2, damage every 100 steps",
-                        "damage_after_steps": args.steps,
-                        "damage_nodes_equal": float(np.mean(np.abs(de - dr) <= 1e-12)),
-                        "damage_max_abs_diff": float(np.abs(de - dr).max()),
-                        "damaged_nodes": int((dr > 0).sum()),
-                        "crack_tip_x": {"engine": None if tip_e != tip_e else float(tip_e), "reference": tip_r,
-                                        "reference_warp_kernel": tip(dref["warp"]), "horizon": p.delta},
+                        **damage_parity(de, dr, xs, tip_e, p.delta, args.steps),
                         "reference_kernels_between_themselves": {
-                            "damage_nodes_equal": float(np.mean(np.abs(dref["warp"] - dr) <= 1e-12)),
+                            **damage_parity(dref["warp"], dr, xs, None, p.delta, args.steps),
                             "what": "kernel_bond_force_2D against kernel_particle_force_2D (same formulas, "
                                     "different summation order)"}}
 
@@ -976,13 +1000,12 @@ def gb300_arm(args):
                        "launch": None if tuned is None else {"block": tuned[0], "chunked": tuned[1],
                                                              "waves": tuned[2], "split": tuned[3]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
-                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "peak_source": peak_kind,
+                         "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
+                         "peak_source": peak_kind,
                          "kernel": "k_bond_force" if p.model == 1 else "k_theta + k_state_force",
                          "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / step_ms,
                          "alg_bytes_per_launch": alg_bytes,
-                         "fp64": {"achieved_tflops": alg_flops / (kern_ms * 1e-3) / 1e12,
-                                  "peak_tflops": fp64_peak_tflops, "frac": alg_flops / (kern_ms * 1e-3) / 1e12 /
-                                  fp64_peak_tflops, "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}},
+                         "fp64": fp64_block(p.model, p.dim, B, kern_ms, gfma.value)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk, "reference_cuda": ref_cuda,
         }
         print(json.dumps(line), flush=True)

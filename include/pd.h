@@ -301,6 +301,15 @@ int pd_mlp_train_step(pd_mlp* net, const void* dev_x, const float* dev_t, int64_
  * FP32 out; a stored [K][M] when transpose_a); N = 16 or a multiple of 128. */
 int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d, int transpose_a,
                 void* stream);
+/* Self-check of the bounded device-side wait: the same product with the
+ * iteration limit of the kernel's mbarrier wait set to spin_limit (<= 0: the
+ * library's limit, ~0.3 s) and, with issue = 0, neither the products nor
+ * their commit issued, so that the wait never completes.  The kernel then
+ * gives up after spin_limit iterations, releases its tensor memory and
+ * returns; the call reports PD_ERR_TIMEOUT and the CUDA context stays
+ * usable.  No counterpart in the reference (no tensor-core code). */
+int pd_mlp_gemm_wait_check(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d,
+                           int transpose_a, long long spin_limit, int issue, void* stream);
 /* Features of the free nodes for a load increment (BF16 [N_int][16]): previous
  * displacement / U, increment / U, damage, loaded-edge flag, x and y over the
  * half sizes, family size / nn_ref; U is the accumulated boundary displacement. */
@@ -447,7 +456,9 @@ int64_t pd_kernel_launches(const pd_ctx* ctx);
  * block partial sums use a 64 KiB array in the library's own device memory,
  * which every GPU that loads the library keeps until exit.  n is at most
  * 33,554,432 (8,192 blocks of 4,096 elements); larger n returns PD_ERR_ARG.
- * The first call on each device looks the array's address up
+ * The first call in each CUDA context (one per device for runtime-API
+ * callers; a context rebuilt by cudaDeviceReset or a driver-API caller's own
+ * context counts as a new one) looks the array's address up
  * (cudaGetSymbolAddress) and must come before any stream capture that
  * contains this call.  All calls share the array: calls that overlap on the
  * GPU (different streams, no ordering between them) race and may return

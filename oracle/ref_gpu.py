@@ -107,6 +107,41 @@ class RefGPU:
     def force3(self):
         self._check(self.lib.rr_force3(), "rr_force3")
 
+    def setup_state3(self, m, w):
+        """Weighted volume m (N) and influence weights w (CSR order) of a 3-D
+        state-based problem set up by :meth:`setup` and :meth:`setup_z`."""
+        self.m = np.ascontiguousarray(m, dtype=np.float64)
+        self.w = self.ell(w, np.float64, 0.0)
+        self._check(self.lib.rr_setup_state3(_d(self.m), _d(self.w)), "rr_setup_state3")
+
+    def initial_weight3(self):
+        """kernel_initial_weight_3D (N must be even)."""
+        self._check(self.lib.rr_initial_weight3(), "rr_initial_weight3")
+
+    def get_state3(self):
+        """(m, w) of the 3-D state-based arrays; w in the padded N*MN layout."""
+        m = np.zeros(self.N)
+        w = np.zeros(self.N * self.MN)
+        self._check(self.lib.rr_get_state3(_d(m), _d(w)), "rr_get_state3")
+        return m, w
+
+    def set_theta_e(self, theta, e):
+        """Dilatation (N) and per-bond extension (padded N*MN layout) for
+        kernel_state_force_3D."""
+        self.theta_h = np.ascontiguousarray(theta, dtype=np.float64)
+        self.e_h = np.ascontiguousarray(e, dtype=np.float64)
+        self._check(self.lib.rr_set_theta_e(_d(self.theta_h), _d(self.e_h)), "rr_set_theta_e")
+
+    def force_state3(self):
+        """One kernel_state_force_3D evaluation (N_int must be even)."""
+        self._check(self.lib.rr_force_state3(), "rr_force_state3")
+
+    def get_fail(self):
+        """The N*MN intact flags in the padded layout."""
+        fail = np.zeros(self.N * self.MN, dtype=np.int32)
+        self._check(self.lib.rr_get(None, None, None, None, None, _i(fail), None), "rr_get")
+        return fail
+
     def run_kw(self, nsteps):
         """nsteps of the impact driver's loop; returns the elapsed ms."""
         ms = C.c_double()

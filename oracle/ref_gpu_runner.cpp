@@ -28,6 +28,15 @@
 //    (Base_Function.cu:185-207), a divergent barrier in the last block when
 //    N_int*MN is not a multiple of the block; it is not launched.  The damage
 //    of a 3-D run is computed by the caller from the intact flags.
+// The 3-D state-based kernels (Force_State.cu:29-54, :242-306) put two nodes in
+// each 256-thread block (MN = 128) and hold __syncthreads inside "if (i < N)"
+// (kernel_initial_weight_3D) and "if (i < N_int)" (kernel_state_force_3D):
+// the runner launches them only when N (resp. N_int) is even, so that no block
+// straddles the bound and every barrier is reached by the whole block.
+// kernel_cal_theta_3D is never launched: it reads fail[idx] before its bounds
+// test and holds its barrier inside "if (fail[idx] == 1)", a divergent branch
+// once any bond of a block is broken (Force_State.cu:214-234); the caller
+// supplies theta and e instead (rr_set_theta_e).
 // kernel_bond_force_3D stores the node sums of thread j == 0 without a bound
 // test (Force_Bond.cu:133-139), so the tail of the last block writes element
 // N of the force arrays; node arrays are allocated with kNodePad spare
@@ -63,7 +72,8 @@ struct Runner {
     CUfunction f_particle = nullptr, f_bond = nullptr, f_int1 = nullptr, f_int2 = nullptr, f_dmg = nullptr;
     CUfunction f_cnn = nullptr, f_adr = nullptr, f_reduce = nullptr, f_qload = nullptr;
     CUfunction f_bond3 = nullptr, f_int31 = nullptr, f_int32 = nullptr, f_contact = nullptr, f_cy1 = nullptr,
-               f_cy2 = nullptr, f_cyinit = nullptr, f_theta2 = nullptr, f_state2 = nullptr;
+               f_cy2 = nullptr, f_cyinit = nullptr, f_theta2 = nullptr, f_state2 = nullptr, f_weight3 = nullptr,
+               f_state3 = nullptr;
     CUdeviceptr static_y = 0;  // Reduce.cu's block partial array
     CUstream stream = nullptr;
     device_parameter p{};
@@ -76,7 +86,7 @@ struct Runner {
     CUdeviceptr z = 0, uz = 0, vz = 0, az = 0, fz = 0, bz = 0, cacc = 0, cdisp = 0, cvel = 0, cforce = 0;
     // state-based: weighted volume m and dilatation theta per node, influence w and extension e per bond
     CUdeviceptr m = 0, theta = 0, w = 0, e = 0;
-    bool ready = false, has_z = false, has_state = false;
+    bool ready = false, has_z = false, has_state = false, has_state3 = false;
 };
 
 Runner R;
@@ -158,6 +168,11 @@ int rr_init(const char* cubin) {
            "kernel_cal_theta_2D");
     RR_TRY(cuModuleGetFunction(&R.f_state2, R.mod, "_Z21kernel_state_force_2DPiPdS0_S_S_S0_S0_S0_S0_S0_S0_S0_S0_S0_S0_"),
            "kernel_state_force_2D");
+    RR_TRY(cuModuleGetFunction(&R.f_weight3, R.mod, "_Z24kernel_initial_weight_3DPdPiS_S_S_"),
+           "kernel_initial_weight_3D");
+    RR_TRY(cuModuleGetFunction(&R.f_state3, R.mod,
+                               "_Z21kernel_state_force_3DPiPdS0_S_S_S0_S0_S0_S0_S0_S0_S0_S0_S0_S0_S0_S0_S0_"),
+           "kernel_state_force_3D");
     size_t ys = 0;
     RR_TRY(cuModuleGetGlobal(&R.static_y, &ys, R.mod, "static_y"), "static_y");
     if (ys != 256 * sizeof(double)) return fail_with(CUDA_ERROR_INVALID_VALUE, "static_y size");
@@ -227,6 +242,7 @@ int rr_setup(const double* dparams, const int* iparams, const double* x, const d
     R.ready = true;
     R.has_z = false;
     R.has_state = false;
+    R.has_state3 = false;
     return 0;
 }
 
@@ -529,6 +545,72 @@ int rr_get_z(double* uz, double* vz, double* fz, double* cyl) {
     return 0;
 }
 
+// State-based arrays of a 3-D problem set up by rr_setup and rr_setup_z: m (N
+// doubles) and w (N*MN padded ELL); theta (N) and e (N*MN) start at zero.
+int rr_setup_state3(const double* m, const double* w) {
+    if (!R.ready || !R.has_z) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_z first");
+    const size_t N = (size_t)R.p.N, S = (size_t)R.p.N * R.p.MN;
+    CUdeviceptr* arrs[] = {&R.m, &R.theta, &R.w, &R.e};
+    const size_t bytes[] = {(N + kNodePad) * 8, (N + kNodePad) * 8, S * 8, S * 8};
+    for (int k = 0; k < 4; k++) {
+        if (*arrs[k]) {
+            cuMemFree(*arrs[k]);
+            *arrs[k] = 0;
+        }
+        RR_TRY(cuMemAlloc(arrs[k], bytes[k]), "state3 alloc");
+        RR_TRY(cuMemsetD8(*arrs[k], 0, bytes[k]), "state3 zero");
+    }
+    RR_TRY(cuMemcpyHtoD(R.m, m, N * 8), "m copy");
+    RR_TRY(cuMemcpyHtoD(R.w, w, S * 8), "w copy");
+    R.has_state3 = true;
+    return 0;
+}
+
+// kernel_initial_weight_3D over N*MN threads with 256 doubles of shared
+// memory (the driver's commented launch, Solve_Kalthoff_Winkler.cu:400-401):
+// overwrites m and w.  Refused for odd N (see the note at the top).
+int rr_initial_weight3(void) {
+    if (!R.has_state3) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_state3 first");
+    if (R.p.N % 2 != 0 || R.p.MN != 128) return fail_with(CUDA_ERROR_INVALID_VALUE, "N odd or MN != 128");
+    void* a[] = {&R.m, &R.NN, &R.w, &R.idist, &R.fac};
+    const unsigned g = (unsigned)(((int64_t)R.p.N * R.p.MN - 1) / 256 + 1);
+    if (launch(R.f_weight3, g, a, 256, 256 * sizeof(double))) return -1;
+    RR_TRY(cuStreamSynchronize(R.stream), "initial weight 3D");
+    return 0;
+}
+
+// Dilatation theta (N doubles) and per-bond extension e (N*MN padded ELL), the
+// inputs kernel_cal_theta_3D would have written.
+int rr_set_theta_e(const double* theta, const double* e) {
+    if (!R.has_state3) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_state3 first");
+    RR_TRY(cuMemcpyHtoD(R.theta, theta, (size_t)R.p.N * 8), "theta copy");
+    RR_TRY(cuMemcpyHtoD(R.e, e, (size_t)R.p.N * R.p.MN * 8), "e copy");
+    return 0;
+}
+
+// One kernel_state_force_3D evaluation over N_int*MN threads with 3*256
+// doubles of shared memory (Solve_Kalthoff_Winkler.cu:420-422).  Refused for
+// odd N_int (see the note at the top).
+int rr_force_state3(void) {
+    if (!R.has_state3) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_state3 first");
+    if (R.p.N_int % 2 != 0 || R.p.MN != 128) return fail_with(CUDA_ERROR_INVALID_VALUE, "N_int odd or MN != 128");
+    void* a[] = {&R.NN, &R.m, &R.theta, &R.fail, &R.NL, &R.e, &R.w, &R.idist, &R.fac,
+                 &R.x,  &R.ux, &R.fx,   &R.y,    &R.uy, &R.fy, &R.z, &R.uz,    &R.fz};
+    const unsigned g = (unsigned)(((int64_t)R.p.N_int * R.p.MN - 1) / 256 + 1);
+    if (launch(R.f_state3, g, a, 256, 3 * 256 * sizeof(double))) return -1;
+    RR_TRY(cuStreamSynchronize(R.stream), "state force 3D");
+    return 0;
+}
+
+// m (N doubles) and w (N*MN) of the 3-D state-based arrays.
+int rr_get_state3(double* m, double* w) {
+    if (!R.has_state3) return fail_with(CUDA_ERROR_NOT_INITIALIZED, "rr_setup_state3 first");
+    RR_TRY(cuStreamSynchronize(R.stream), "sync");
+    if (m) RR_TRY(cuMemcpyDtoH(m, R.m, (size_t)R.p.N * 8), "m");
+    if (w) RR_TRY(cuMemcpyDtoH(w, R.w, (size_t)R.p.N * R.p.MN * 8), "w");
+    return 0;
+}
+
 // Read back node fields (N doubles each; NULL skips), the N*MN fail flags and
 // the damage field (written by kernel_cal_dmg_2D at the damage steps of rr_run).
 int rr_get(double* ux, double* uy, double* fx, double* fy, double* vy, int* fail, double* dmg) {
@@ -550,6 +632,7 @@ int rr_free(void) {
     R.ready = false;
     R.has_z = false;
     R.has_state = false;
+    R.has_state3 = false;
     return 0;
 }
 

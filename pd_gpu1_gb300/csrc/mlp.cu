@@ -52,6 +52,8 @@ struct GemmArgs {
     int64_t ldh;
     const float* Zin;    // E_BWD: pre-activation [M][ldh]
     int* err;
+    long long spin_limit;  // iterations of each bounded mbarrier wait
+    int issue;             // 0: issue neither the products nor their commit (bounded-wait self-check)
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -117,8 +119,8 @@ __device__ void load_tile(unsigned char* tile, const __nv_bfloat16* X, int64_t s
     }
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
-    for (long long it = 0; it < kSpinLimit; it++) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, long long limit) {
+    for (long long it = 0; it < limit; it++) {
         uint32_t ok;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -177,7 +179,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm(GemmArgs g) {
     int chunks = 0;
     for (int64_t k0 = kb; k0 < ke; k0 += kChunkK, chunks++) {
         if (chunks > 0) {  // the previous chunk's products have read the tiles
-            if (!mbar_wait(bar_a, phase)) failed = 1;
+            if (!mbar_wait(bar_a, phase, g.spin_limit)) failed = 1;
             phase ^= 1;
         }
         __syncthreads();
@@ -186,7 +188,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm(GemmArgs g) {
         load_tile(sb, g.B, g.sbn, g.sbk, n0, NT, g.N, k0, ke);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
-        if (threadIdx.x == 0) {
+        if (threadIdx.x == 0 && g.issue) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             const int ksteps = (int)((ke - k0 < kChunkK ? ke - k0 : kChunkK) + 15) / 16;
             for (int j = 0; j < ksteps; j++) {
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm(GemmArgs g) {
         }
     }
     if (chunks > 0 && !failed) {
-        if (!mbar_wait(bar_a, phase)) failed = 1;
+        if (!mbar_wait(bar_a, phase, g.spin_limit)) failed = 1;
     }
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -489,6 +491,7 @@ int launch_gemm(pd_mlp* n, const GemmArgs& a0, int nt, cudaStream_t s, int split
     GemmArgs a = a0;
     a.err = n->err;
     if (a.k_per_split <= 0) a.k_per_split = a.K;
+    if (a.spin_limit <= 0) a.spin_limit = kSpinLimit;
     const dim3 grid((unsigned)((a.M + kTileM - 1) / kTileM), (unsigned)((a.N + nt - 1) / nt), (unsigned)splits);
     if (nt == 16)
         k_gemm<16><<<grid, kThreads, 0, s>>>(a);
@@ -503,6 +506,8 @@ GemmArgs gemm(const __nv_bfloat16* A, int64_t sam, int64_t sak, const __nv_bfloa
     GemmArgs a{};
     a.A = A, a.sam = sam, a.sak = sak, a.B = B, a.sbn = sbn, a.sbk = sbk, a.M = M, a.N = N, a.K = K;
     a.k_per_split = K;
+    a.spin_limit = kSpinLimit;
+    a.issue = 1;
     return a;
 }
 
@@ -784,6 +789,15 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
 // row-major BF16 A and B (FP32 D), through the same kernel and loader.
 int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d, int transpose_a,
                 void* stream) {
+    return pd_mlp_gemm_wait_check(dev_a, dev_b, M, N, K, dev_d, transpose_a, 0, 1, stream);
+}
+
+// The same product with the bounded mbarrier wait's iteration limit given
+// (spin_limit <= 0: the library's limit) and, with issue = 0, no product and
+// no commit issued: the wait then never completes, gives up after spin_limit
+// iterations, and the call returns PD_ERR_TIMEOUT with the context usable.
+int pd_mlp_gemm_wait_check(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d,
+                           int transpose_a, long long spin_limit, int issue, void* stream) {
     if (!dev_a || !dev_b || !dev_d || M < 1 || N < 1 || K < 1 || (N != 16 && N % 128 != 0)) return PD_ERR_ARG;
     pd_mlp tmp;
     if (cudaMalloc(&tmp.err, sizeof(int)) != cudaSuccess) return PD_ERR_NOMEM;
@@ -794,6 +808,8 @@ int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int6
     GemmArgs a = transpose_a ? gemm(A, 1, M, reinterpret_cast<const __nv_bfloat16*>(dev_b), K, 1, M, N, K)
                              : gemm(A, K, 1, reinterpret_cast<const __nv_bfloat16*>(dev_b), K, 1, M, N, K);
     a.epi = E_F32, a.D = dev_d, a.ldd = N;
+    a.spin_limit = spin_limit > 0 ? spin_limit : kSpinLimit;
+    a.issue = issue ? 1 : 0;
     int rc = launch_gemm(&tmp, a, N == 16 ? 16 : 128, s);
     int herr = 0;
     cudaMemcpyAsync(&herr, tmp.err, sizeof(int), cudaMemcpyDeviceToHost, s);

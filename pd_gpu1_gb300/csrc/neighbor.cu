@@ -238,6 +238,11 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     double* Z = c->nf[PD_F_Z];
     const int* grp = c->batch.node_group;
     if (grp && dim != 2) return set_err(c, PD_ERR_ARG, "grouped family builds are 2-D");
+    // until this build succeeds the context holds no valid family: every
+    // failure below leaves it refused by the stages that need one
+    c->family = false;
+    c->volcorr = c->surfcorr = c->weights = false;
+    c->prepared = false;
     cudaError_t e;
 
     // bounding box
@@ -360,15 +365,15 @@ int build_family(pd_ctx* c, cudaStream_t s) {
     c->launches += 3;
     cleanup();
     if ((e = cudaGetLastError()) != cudaSuccess) return cuda_err(c, e, "family kernels");
-    c->family = true;
-    c->volcorr = c->surfcorr = c->weights = false;
-    c->prepared = false;
     c->bits_current = false;
     c->csr_fail_current = true;
     if (p.MN > 0 && maxnn > p.MN) {
+        // the arrays hold the oversized family, but it is not the reference's
+        // (whose rows stop at MN): the context stays without a family
         return set_err(c, PD_ERR_FAMILY,
                        "a node has " + std::to_string(maxnn) + " neighbours, more than MN=" + std::to_string(p.MN));
     }
+    c->family = true;
     return PD_OK;
 }
 

@@ -64,3 +64,98 @@ def assert_close_norm(actual, expected, rtol, what=""):
     err = float(np.max(np.abs(actual - expected))) if expected.size else 0.0
     assert err <= rtol * scale + 1e-300, f"{what}: max err {err:.3e} > {rtol:.1e} * {scale:.3e}"
     return err / scale if scale else 0.0
+
+
+def exact_bond_forces_2d(x, y, ux, uy, rowptr, NL, idist, fac, scr, fail, vol, bc, nodes):
+    """Node forces of the 2-D PMB kernels (Force_Bond.cu:52-85) on the given
+    nodes, evaluated in extended precision (numpy longdouble: 64 or 113
+    significant bits) from the reference's own FP64 bond vector
+    d = ((x_c + u_c) - x_i) - u_i, which both implementations form with the
+    same roundings.  Everything after d (length, stretch, force) is carried
+    beyond FP64, so the result stands for the exact value of the reference's
+    formula: the yardstick that separates an implementation's error from the
+    reference's own FP64 rounding."""
+    ld = np.longdouble
+    nodes = np.asarray(nodes, dtype=np.int64)
+    rp = np.asarray(rowptr, dtype=np.int64)
+    cnt = rp[nodes + 1] - rp[nodes]
+    own = np.repeat(np.arange(len(nodes)), cnt)
+    idx = np.concatenate([np.arange(rp[n], rp[n + 1]) for n in nodes]) if len(nodes) else np.zeros(0, np.int64)
+    i = nodes[own]
+    c = np.asarray(NL, dtype=np.int64)[idx]
+    alive = np.asarray(fail)[idx] == 1
+    dx = ((x[c] + ux[c]) - x[i]) - ux[i]
+    dy = ((y[c] + uy[c]) - y[i]) - uy[i]
+    dxl, dyl = dx.astype(ld), dy.astype(ld)
+    L = np.sqrt(dxl * dxl + dyl * dyl)
+    l0 = np.asarray(idist)[idx].astype(ld)
+    k = ld(vol) * np.asarray(fac)[idx].astype(ld) * ld(bc) * np.asarray(scr)[idx].astype(ld) * ((L - l0) / l0) / L
+    k = np.where(alive, k, ld(0))
+    fx = np.zeros(len(nodes), dtype=ld)
+    fy = np.zeros(len(nodes), dtype=ld)
+    np.add.at(fx, own, k * dxl)
+    np.add.at(fy, own, k * dyl)
+    return fx, fy
+
+
+def per_node_errors(fx, fy, fx_ref, fy_ref):
+    """Per-node relative difference |f - f_ref| / |f_ref| of 2-D force vectors."""
+    fx_ref = np.asarray(fx_ref, dtype=np.float64)
+    fy_ref = np.asarray(fy_ref, dtype=np.float64)
+    mag = np.hypot(fx_ref, fy_ref)
+    d = np.hypot(np.asarray(fx, dtype=np.float64) - fx_ref, np.asarray(fy, dtype=np.float64) - fy_ref)
+    return d / np.maximum(mag, 1e-300)
+
+
+def significant_nodes(fx, fy, frac=1e-3, cap=None, seed=0):
+    """Nodes whose force magnitude is at least frac of the largest (edge rows,
+    crack faces, the stretched field), optionally a seeded sample of cap of
+    them that always keeps the 1,000 largest."""
+    mag = np.hypot(fx, fy)
+    sel = np.nonzero(mag >= frac * mag.max())[0]
+    if cap is not None and len(sel) > cap:
+        top = sel[np.argsort(mag[sel])[-1000:]]
+        rest = np.setdiff1d(sel, top)
+        rng = np.random.default_rng(seed)
+        sel = np.union1d(top, rng.choice(rest, cap - len(top), replace=False))
+    return sel
+
+
+def check_per_node_2d(eng, fx, fy, ref_fx, ref_fy, ux, uy, fail, nodes_limit=None, frac=1e-3, rtol=1e-12, what=""):
+    """Per-node relative force check of a 2-D bond-based evaluation.
+
+    On the nodes whose force is at least ``frac`` of the largest (a seeded
+    sample of ``nodes_limit`` of them when given), the engine's forces
+    (``fx``, ``fy``, from the context ``eng`` whose family and coefficients
+    they used, with the CSR intact flags ``fail`` the pass started from) and
+    the reference's (``ref_fx``, ``ref_fy``) are each
+    compared with the extended-precision value of the reference's formula
+    (exact_bond_forces_2d).  Asserted:
+      * the engine is within ``rtol`` of that value on every such node;
+      * engine and reference differ by no more than ``rtol`` plus the
+        reference's own distance from that value, node by node (the reference
+        forms the stretch (|xi + eta| - |xi|) / |xi| in FP64, which cancels
+        and leaves its node forces up to ~1e-10 off where bond forces cancel).
+    Returns the report (worst nodes and quantiles), for printing."""
+    p = eng.params()
+    N = p.N_int
+    fx, fy = np.asarray(fx)[:N], np.asarray(fy)[:N]
+    ref_fx, ref_fy = np.asarray(ref_fx)[:N], np.asarray(ref_fy)[:N]
+    sel = significant_nodes(ref_fx, ref_fy, frac, cap=nodes_limit)
+    ex, ey = exact_bond_forces_2d(eng.get("X"), eng.get("Y"), ux, uy, eng.get("ROWPTR"), eng.get("NL"),
+                                  eng.get("IDIST"), eng.get("FAC"), eng.get("SCR"), fail, p.vol, p.bc, sel)
+    e_eng = per_node_errors(fx[sel], fy[sel], ex, ey)
+    e_ref = per_node_errors(ref_fx[sel], ref_fy[sel], ex, ey)
+    e_er = per_node_errors(fx[sel], fy[sel], ref_fx[sel], ref_fy[sel])
+    w = int(np.argmax(e_eng))
+    wr = int(np.argmax(e_er - e_ref))
+    rep = {"what": what, "nodes": int(len(sel)), "frac": frac,
+           "engine_vs_exact": {"max": float(e_eng.max()), "p99": float(np.quantile(e_eng, 0.99)),
+                               "worst_node": int(sel[w])},
+           "reference_vs_exact": {"max": float(e_ref.max()), "p99": float(np.quantile(e_ref, 0.99))},
+           "engine_vs_reference": {"max": float(e_er.max()), "p99": float(np.quantile(e_er, 0.99)),
+                                   "worst_excess_node": int(sel[wr]),
+                                   "within_rtol": float(np.mean(e_er <= rtol))}}
+    assert e_eng.max() <= rtol, (what, rep)
+    assert np.all(e_er <= rtol + e_ref * (1.0 + 1e-6)), (what, rep)
+    return rep

@@ -38,3 +38,36 @@ def test_reference_arm_line():
 def test_reference_arm_without_a_counterpart_says_so():
     d = _run("--workload", "warm_start", "--steps", "1", "--warmup", "3")
     assert d["impl"] == "reference" and d["unavailable"]
+
+
+def test_damage_parity_of_a_short_precracked_run():
+    """bench.damage_parity on a run shorter than the damage interval: the
+    pre-cracked plate (the headline workload's layout, 16,000 nodes) after 20
+    explicit steps on the oracle, its damage computed once after the last
+    step as the bench now asks of the reference's kernels.  The pre-crack
+    alone damages nodes, so both sides count damaged nodes and agree."""
+    import numpy as np
+
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "oracle")]
+    import bench
+    import oracle as orc
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_branching(scale=0.1, derive=orc.derive_params)
+    x, y = orc.plate_coords(p)
+    m = orc.Model(p, x, y)
+    m.find_neighbor()
+    m.surface_correct()
+    m.set_crack_2d(p.length / 2.0, -p.length / 4.0, 0.0, 0.0)
+    m.by[:] = presets.traction_field(p, meta["sigma"])
+    for _ in range(20):
+        m.explicit_step()
+    m.damage()
+    d = m.dmg[: p.N_int].copy()
+    rep = bench.damage_parity(d, d, x[: p.N_int], None, p.delta, 20)
+    assert rep["damaged_nodes"] > 0 and rep["damaged_nodes"] == rep["damaged_nodes_engine"]
+    assert rep["damage_nodes_equal"] == 1.0 and rep["damage_max_abs_diff"] == 0.0
+    assert rep["crack_tip_x"]["engine"] == rep["crack_tip_x"]["reference"] is not None
+    # a reference field that was never computed (all zero) is reported as a mismatch
+    bad = bench.damage_parity(d, np.zeros_like(d), x[: p.N_int], None, p.delta, 20)
+    assert bad["damaged_nodes"] == 0 and bad["damage_nodes_equal"] < 1.0

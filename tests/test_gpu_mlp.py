@@ -119,3 +119,30 @@ def test_training_lowers_loss(L):
     assert L.pd_mlp_get_params(n, q.ctypes.data, q.size) == 0
     assert np.isfinite(q).all() and not np.array_equal(q, p)
     L.pd_mlp_destroy(n)
+
+
+@pytest.mark.parametrize("K", [64, 200])
+def test_bounded_wait_gives_up_and_reports_timeout(L, K):
+    """The tensor-core kernel's mbarrier wait is bounded.  With no product and
+    no commit issued the barrier never completes: the kernel gives up after
+    the given number of iterations, frees its tensor memory and returns, and
+    the call reports PD_ERR_TIMEOUT (-7).  The same call with the products
+    issued then completes and is exact, so the GPU and the context stay
+    usable after a wait ran out (K = 200 also runs out inside the chunk loop,
+    before the last chunk)."""
+    import torch
+
+    M, N = 256, 128
+    rng = np.random.default_rng(K)
+    a = mo.bf16(rng.standard_normal((M, K)).astype(np.float32))
+    b = mo.bf16(rng.standard_normal((N, K)).astype(np.float32))
+    da, db = _dev(a, torch.bfloat16), _dev(b, torch.bfloat16)
+    dd = torch.zeros((M, N), dtype=torch.float32, device="cuda")
+    rc = L.pd_mlp_gemm_wait_check(da.data_ptr(), db.data_ptr(), M, N, K, dd.data_ptr(), 0, 2000, 0, None)
+    assert rc == -7
+    assert float(dd.abs().max().item()) == 0.0  # gave up before its epilogue
+    rc = L.pd_mlp_gemm_wait_check(da.data_ptr(), db.data_ptr(), M, N, K, dd.data_ptr(), 0, 2000000, 1, None)
+    assert rc == 0
+    want = a.astype(np.float64) @ b.astype(np.float64).T
+    got = dd.cpu().numpy().astype(np.float64)
+    assert np.abs(got - want).max() <= 1e-5 * np.abs(want).max()

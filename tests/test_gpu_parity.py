@@ -65,6 +65,12 @@ def test_family_overflow_reported(E, golden):
         with pytest.raises(E.PDError) as ei:
             eng.find_neighbor_gpu()
         assert ei.value.status == -4
+        # the failed build leaves no family behind: every stage that needs one
+        # refuses with PD_ERR_STATE (-3) instead of running on it
+        for stage in (eng.vol_corr, eng.surface_correct_gpu, eng.prepare, eng.damage):
+            with pytest.raises(E.PDError) as ei:
+                stage()
+            assert ei.value.status == -3, stage.__name__
 
 
 def test_surface_correction(E, golden):

@@ -10,7 +10,7 @@ import numpy as np
 import pytest
 
 import ref_gpu
-from helpers import assert_close_norm, params_from_golden
+from helpers import assert_close_norm, check_per_node_2d, params_from_golden
 
 pytestmark = [pytest.mark.gpu,
               pytest.mark.skipif(not ref_gpu.available(), reason="reference cubin not built (make -C oracle ref)")]
@@ -34,6 +34,7 @@ def test_forces_and_breakage_match_reference_kernels(E, golden):
         eng.initial_state()
         eng.set("UX", g["f_ux"])
         eng.set("UY", g["f_uy"])
+        fail0 = eng.get("FAIL")
         eng.bond_force_gpu()
         fx, fy = eng.get("FX"), eng.get("FY")
         for variant in (ref_gpu.RefGPU.PARTICLE, ref_gpu.RefGPU.WARP):
@@ -44,6 +45,9 @@ def test_forces_and_breakage_match_reference_kernels(E, golden):
             out = r.get(NN)
             assert_close_norm(fx, out["fx"], 1e-12, f"fx variant {variant}")
             assert_close_norm(fy, out["fy"], 1e-12, f"fy variant {variant}")
+            rep = check_per_node_2d(eng, fx, fy, out["fx"], out["fy"], g["f_ux"], g["f_uy"], fail0,
+                                    what=f"variant {variant}")
+            print("per-node forces:", rep)
             r.free()
         # breakage at a lowered critical stretch: identical intact flags
         q = eng.params()
@@ -213,3 +217,67 @@ def test_explicit_1000_steps_before_breakage_match_reference_kernels(E):
         np.testing.assert_array_equal(eng.get("FAIL"), cut)
         np.testing.assert_array_equal(out["fail"], cut)
         r.free()
+
+
+def test_state_force_3d_matches_reference_kernel(E):
+    """kernel_state_force_3D (Force_State.cu:242-306), the 3-D ordinary
+    state-based force, against the engine's 3-D state-based passes on a small
+    notched slab of the impact layout (1,750 nodes, an even count so that the
+    reference kernel's barrier, inside "if (i < N_int)" with two nodes per
+    block, is reached by whole blocks).  The reference's own
+    kernel_initial_weight_3D supplies m and w (checked against the engine's to
+    1e-13).  kernel_cal_theta_3D is not launched (its barrier sits in a branch
+    on each bond's intact flag): the dilatation theta and the per-bond
+    extension e come from the oracle's restatement of it, evaluated on the
+    reference's own intact flags.  Two evaluations at a lowered critical
+    stretch, the second seeing the bonds the first broke: forces 1e-12, intact
+    flags identical."""
+    import oracle as orc
+    from pd_gpu1_gb300 import presets
+    from pd_gpu1_gb300._abi import PD_MODEL_STATE
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10, model=PD_MODEL_STATE)
+    assert p.N == p.N_int == 1750 and p.MN == 128
+    rng = np.random.default_rng(17)
+    u = rng.standard_normal((3, p.N)) * 5e-6  # dx = 2e-3: bond strains around s0 (4.0e-3)
+    with E.Engine(p) as eng:
+        setup(eng)
+        cut = int((eng.get("FAIL") == 0).sum())  # the notch cuts
+        r, NN = ref_gpu.from_engine(eng, p)
+        try:
+            r.setup_state3(eng.get("M"), eng.get("W"))
+            r.initial_weight3()
+            m_ref, w_ref = r.get_state3()
+            mask = (np.arange(p.MN)[None, :] < NN[:, None]).reshape(-1)
+            assert_close_norm(eng.get("M"), m_ref, 1e-13, "m")
+            assert_close_norm(eng.get("W"), w_ref[mask], 1e-13, "w")
+            for k, key in enumerate(("UX", "UY", "UZ")):
+                eng.set(key, u[k])
+            r.set_disp(u[0], u[1])
+            r.set_disp_z(u[2])
+            # the oracle's view of the same problem, in the reference's layout
+            om = orc.Model(p, eng.get("X"), eng.get("Y"), eng.get("Z"))
+            om.NN[:] = NN
+            om.NL[:] = r.arrays["NL"]
+            om.idist[:] = r.arrays["idist"]
+            om.fac[:] = r.arrays["fac"]
+            om.w[:] = w_ref
+            om.m[:] = m_ref
+            om.ux[:], om.uy[:], om.uz[:] = u
+            for _ in range(2):  # the second pass sees the bonds the first one broke
+                eng.state_force_gpu()
+                om.fail[:] = r.get_fail()
+                orc.lib().or_state_theta(orc.C.byref(p), *[orc._d(a) for a in (om.x, om.y, om.z, om.ux, om.uy,
+                                                                                 om.uz)],
+                                         orc._i(om.NN), orc._i(om.NL), orc._d(om.idist), orc._d(om.fac),
+                                         orc._d(om.w), orc._d(om.m), orc._i(om.fail), orc._d(om.e),
+                                         orc._d(om.theta))
+                r.set_theta_e(om.theta, om.e)
+                r.force_state3()
+            out, oz = r.get(NN), r.get_z()
+        finally:
+            r.free()
+        for k, ref in (("FX", out["fx"]), ("FY", out["fy"]), ("FZ", oz["fz"])):
+            assert_close_norm(eng.get(k), ref, 1e-12, k)
+        np.testing.assert_array_equal(eng.get("FAIL"), out["fail"])
+        assert (out["fail"] == 0).sum() > cut + 1000  # bonds broke beyond the notch cuts
