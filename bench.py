@@ -98,8 +98,64 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
+class NvmlSampler:
+    """SM clock and clock-event reasons of the GPU, read through NVML (ctypes on
+    the driver's libnvidia-ml) every ~2 ms in a thread while the timed region
+    runs: a region of a few milliseconds still gets samples.  Reads only."""
+
+    SW_POWER_CAP, HW_SLOWDOWN, SW_THERMAL, HW_THERMAL = 0x4, 0x8, 0x20, 0x40
+
+    def __init__(self, props):
+        import ctypes as C
+
+        self.C = C
+        self.nv = C.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        uuid = str(props.uuid)
+        uuid = uuid if uuid.startswith("GPU-") else "GPU-" + uuid
+        bus = "%08x:%02x:%02x.0" % (props.pci_domain_id, props.pci_bus_id, props.pci_device_id)
+        if self.nv.nvmlDeviceGetHandleByUUID(uuid.encode(), C.byref(self.h)) != 0 and \
+                self.nv.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), C.byref(self.h)) != 0:
+            raise OSError("no NVML handle for " + uuid)
+        self.reasons_fn = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        mx = C.c_uint()
+        self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(mx))
+        self.max_mhz = float(mx.value)
+        self.samples, self.stop_flag, self.t = [], False, None
+
+    def _poll(self):
+        C = self.C
+        mhz, rs = C.c_uint(), C.c_ulonglong()
+        while not self.stop_flag:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0 and \
+                    self.reasons_fn(self.h, C.byref(rs)) == 0:
+                self.samples.append((float(mhz.value), int(rs.value)))
+            time.sleep(0.002)
+
+    def start(self):
+        self.stop_flag = False
+        self.t = threading.Thread(target=self._poll, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        self.stop_flag = True
+        if self.t is not None:
+            self.t.join(timeout=2)
+        names = {self.HW_SLOWDOWN: "hw_slowdown", self.HW_THERMAL: "hw_thermal_slowdown",
+                 self.SW_THERMAL: "sw_thermal_slowdown", self.SW_POWER_CAP: "sw_power_cap"}
+        reasons = sorted({nm for _, r in self.samples for bit, nm in names.items() if r & bit})
+        sm = [m for m, _ in self.samples]
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": self.max_mhz, "reasons": reasons,
+                "samples": len(sm), "source": "NVML, every ~2 ms during the timed region"}
+
+
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons sampled during the timed region
+    (NVML polling where the driver's library loads; nvidia-smi at 200 ms
+    otherwise)."""
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -109,8 +165,18 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.lines = []
+        self.nvml = None
+        try:
+            import torch
+
+            self.nvml = NvmlSampler(torch.cuda.get_device_properties(gpu_index))
+        except Exception:
+            self.nvml = None
 
     def start(self):
+        if self.nvml is not None:
+            self.nvml.start()
+            return
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.QUERY,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
@@ -125,6 +191,8 @@ class ClockSampler:
             self.lines.append(line.strip())
 
     def stop(self):
+        if self.nvml is not None:
+            return self.nvml.stop()
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -147,7 +215,7 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(nm)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm), "source": "nvidia-smi, every 200 ms"}
 
 
 def aggregate_replicas(elapsed_s, work, dist=None, device="cpu"):

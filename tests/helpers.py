@@ -121,41 +121,46 @@ def significant_nodes(fx, fy, frac=1e-3, cap=None, seed=0):
     return sel
 
 
-def check_per_node_2d(eng, fx, fy, ref_fx, ref_fy, ux, uy, fail, nodes_limit=None, frac=1e-3, rtol=1e-12, what=""):
+def check_per_node_2d(eng, fx, fy, ref_fx, ref_fy, ux, uy, fail, nodes_limit=None, bars=((1e-3, 1e-11), (1e-2, 1e-12)),
+                      what=""):
     """Per-node relative force check of a 2-D bond-based evaluation.
 
-    On the nodes whose force is at least ``frac`` of the largest (a seeded
-    sample of ``nodes_limit`` of them when given), the engine's forces
-    (``fx``, ``fy``, from the context ``eng`` whose family and coefficients
-    they used, with the CSR intact flags ``fail`` the pass started from) and
-    the reference's (``ref_fx``, ``ref_fy``) are each
-    compared with the extended-precision value of the reference's formula
-    (exact_bond_forces_2d).  Asserted:
-      * the engine is within ``rtol`` of that value on every such node;
-      * engine and reference differ by no more than ``rtol`` plus the
-        reference's own distance from that value, node by node (the reference
-        forms the stretch (|xi + eta| - |xi|) / |xi| in FP64, which cancels
-        and leaves its node forces up to ~1e-10 off where bond forces cancel).
-    Returns the report (worst nodes and quantiles), for printing."""
+    The engine's forces (``fx``, ``fy``, from the context ``eng`` whose family
+    and coefficients they used, with the CSR intact flags ``fail`` the pass
+    started from) and the reference's (``ref_fx``, ``ref_fy``) are each
+    compared, node by node, with the extended-precision value of the
+    reference's formula (exact_bond_forces_2d) on the nodes whose force is at
+    least a fraction of the largest (a seeded sample of ``nodes_limit`` of
+    them when given).  ``bars``: (fraction, bound) pairs; on the nodes above
+    each fraction the engine must lie within the bound of that value.  The
+    reference's own distance from it, and the engine-reference difference,
+    are reported beside (the reference forms the stretch
+    (|xi + eta| - |xi|) / |xi| in FP64, which cancels, and its node forces lie
+    up to ~1e-10 off where bond forces cancel).  Returns the report."""
     p = eng.params()
     N = p.N_int
     fx, fy = np.asarray(fx)[:N], np.asarray(fy)[:N]
     ref_fx, ref_fy = np.asarray(ref_fx)[:N], np.asarray(ref_fy)[:N]
-    sel = significant_nodes(ref_fx, ref_fy, frac, cap=nodes_limit)
+    lo = min(f for f, _ in bars)
+    sel = significant_nodes(ref_fx, ref_fy, lo, cap=nodes_limit)
     ex, ey = exact_bond_forces_2d(eng.get("X"), eng.get("Y"), ux, uy, eng.get("ROWPTR"), eng.get("NL"),
                                   eng.get("IDIST"), eng.get("FAC"), eng.get("SCR"), fail, p.vol, p.bc, sel)
     e_eng = per_node_errors(fx[sel], fy[sel], ex, ey)
     e_ref = per_node_errors(ref_fx[sel], ref_fy[sel], ex, ey)
     e_er = per_node_errors(fx[sel], fy[sel], ref_fx[sel], ref_fy[sel])
-    w = int(np.argmax(e_eng))
-    wr = int(np.argmax(e_er - e_ref))
-    rep = {"what": what, "nodes": int(len(sel)), "frac": frac,
-           "engine_vs_exact": {"max": float(e_eng.max()), "p99": float(np.quantile(e_eng, 0.99)),
-                               "worst_node": int(sel[w])},
-           "reference_vs_exact": {"max": float(e_ref.max()), "p99": float(np.quantile(e_ref, 0.99))},
-           "engine_vs_reference": {"max": float(e_er.max()), "p99": float(np.quantile(e_er, 0.99)),
-                                   "worst_excess_node": int(sel[wr]),
-                                   "within_rtol": float(np.mean(e_er <= rtol))}}
-    assert e_eng.max() <= rtol, (what, rep)
-    assert np.all(e_er <= rtol + e_ref * (1.0 + 1e-6)), (what, rep)
+    mag = np.hypot(ref_fx[sel], ref_fy[sel])
+    top = float(np.hypot(ref_fx, ref_fy).max())
+    rep = {"what": what, "nodes": int(len(sel))}
+    ok = True
+    for frac, bound in bars:
+        m = mag >= frac * top
+        w = int(np.argmax(np.where(m, e_eng, -1.0)))
+        r = {"nodes": int(m.sum()), "bound": bound,
+             "engine_vs_exact": {"max": float(e_eng[m].max()), "p99": float(np.quantile(e_eng[m], 0.99)),
+                                 "worst_node": int(sel[w]), "worst_node_force_over_max": float(mag[w] / top)},
+             "reference_vs_exact": {"max": float(e_ref[m].max()), "p99": float(np.quantile(e_ref[m], 0.99))},
+             "engine_vs_reference": {"max": float(e_er[m].max()), "p99": float(np.quantile(e_er[m], 0.99))}}
+        rep[f"force_ge_{frac:g}_of_max"] = r
+        ok = ok and e_eng[m].max() <= bound
+    assert ok, (what, rep)
     return rep
