@@ -380,6 +380,26 @@ int pd_batch_get_cn(pd_ctx* ctx, double* cn, void* stream);
  * to the widest split. */
 int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves, int split);
 int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves, int* split);
+/* Per-bond storage of the bond-based force kernels.  PD_LAYOUT_RECORDS: one
+ * 48-byte record per bond slot (column, float reference vector, c0, l0, k2,
+ * break threshold), any geometry, 2-D and 3-D.  PD_LAYOUT_COMPACT (2-D): one
+ * 16-byte record per slot (column, l0 - l0t with the offset class id, k2 / 2)
+ * plus one template per offset class (bonds whose reference vectors round to
+ * the same float vector, one class per lattice offset on the reference's
+ * regular grids), for problems with at most 255 classes whose bond lengths
+ * differ from the class's smallest by a float with a free low byte;
+ * pd_prepare returns PD_ERR_UNSUPPORTED when a problem does not fit.
+ * PD_LAYOUT_AUTO (default): compact where it fits, records otherwise.  Both
+ * layouts give the reference's intact flags and forces to the same bars; the
+ * forces of the two differ in the last bits (different pair arithmetic).  No
+ * counterpart in the reference, whose bond arrays are padded ELL
+ * (Memory.cu:38-43).  Changing the layout releases the prepared arrays. */
+#define PD_LAYOUT_AUTO 0
+#define PD_LAYOUT_RECORDS 1
+#define PD_LAYOUT_COMPACT 2
+int pd_set_force_layout(pd_ctx* ctx, int layout);
+/* The layout prepared (PD_LAYOUT_AUTO: none yet). */
+int pd_get_force_layout(const pd_ctx* ctx, int* layout);
 /* Times the bond-force kernel (reps launches per shape, at the current
  * displacements) over the shapes above (24 with split 1: 1, 2, 4 or 8 waves;
  * 12 more with split 2 and 4) and keeps the fastest; *best_ms receives its time per

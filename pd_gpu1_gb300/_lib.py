@@ -83,6 +83,8 @@ _SIGS = {
     "pd_batch_get_cn": (I32, [VP, P(D), VP]),
     "pd_set_launch": (I32, [VP, I32, I32, I32, I32]),
     "pd_get_launch": (I32, [VP, P(I32), P(I32), P(I32), P(I32)]),
+    "pd_set_force_layout": (I32, [VP, I32]),
+    "pd_get_force_layout": (I32, [VP, P(I32)]),
     "pd_autotune": (I32, [VP, I32, P(D), VP]),
     "pd_profile_steps": (I32, [VP, I32, I32, I32, D, P(D), P(D), VP]),
     "pd_solve_plate_tensile": (I32, [D, I32, P(D), P(D), P(D), P(PDResult)]),

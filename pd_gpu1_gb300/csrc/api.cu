@@ -1030,6 +1030,29 @@ int pd_set_launch(pd_ctx* c, int block, int chunked, int waves, int split) {
     return PD_OK;
 }
 
+int pd_set_force_layout(pd_ctx* c, int layout) {
+    if (!c || layout < PD_LAYOUT_AUTO || layout > PD_LAYOUT_COMPACT) return PD_ERR_ARG;
+    if (layout != c->layout_pref) {
+        c->layout_pref = layout;
+        if (c->prepared) {
+            // the intact flags back to the CSR array, then the SELL arrays go;
+            // the next prepare rebuilds them in the requested layout
+            int rc = sync_fail_to_csr(c, nullptr);
+            if (rc) return rc;
+            release_sell(c);
+            c->prepared = false;
+            c->bits_current = false;
+        }
+    }
+    return PD_OK;
+}
+
+int pd_get_force_layout(const pd_ctx* c, int* layout) {
+    if (!c || !layout) return PD_ERR_ARG;
+    *layout = c->sell.rec16 ? PD_LAYOUT_COMPACT : c->sell.rec ? PD_LAYOUT_RECORDS : PD_LAYOUT_AUTO;
+    return PD_OK;
+}
+
 int pd_get_launch(const pd_ctx* c, int* block, int* chunked, int* waves, int* split) {
     if (!c || !block || !chunked || !waves || !split) return PD_ERR_ARG;
     *block = c->tune_block;

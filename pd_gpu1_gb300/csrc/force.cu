@@ -99,6 +99,13 @@ struct ForceArgs {
     const double* node_mass;  // ADR fictitious mass per node
     const double* node_rmass; // 1 / node_mass (IEEE-rounded)
     double* slice_part;       // per-slice damping sums (2 per slice) instead of a grid reduction
+    // 2-D bond-based compact layout (null: the 48-byte records)
+    const bt::Rec* rec16;     // per-slot record: column, dl and class id, k2 / 2
+    const bt::Tpl* tpl;       // offset-class templates
+    int ntpl;
+    const int* inst_tbase;    // batch: first template of each specimen (null: one specimen)
+    const int* slice_inst;    // batch: specimen of each slice
+    const double* node_s0;    // batch: critical stretch per node (null: P.critical_s)
 };
 
 namespace {
@@ -651,6 +658,180 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split(co
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
+// ---- 2-D bond force on the compact layout ----------------------------------
+//
+// Per slot one 16-byte record (column; dl = l0 - l0t with the offset class id
+// in its low byte; k2 / 2 as a pair) and the class's template (bondtpl.h: the
+// float reference vector, |xf|^2, c0, l0t), read through the read-only cache:
+// a specimen has a few dozen classes, and on a regular lattice the 32 lanes
+// of a slot read the same one.  The bond arithmetic is bt::bond2; the break
+// test bt::exceeds decides on floats away from the threshold and on the double
+// test near it.
+
+// The templates of slice s's specimen.
+__device__ __forceinline__ const bt::Tpl* slice_templates(const ForceArgs& A, int64_t s) {
+    return A.inst_tbase ? A.tpl + A.inst_tbase[A.slice_inst[s]] : A.tpl;
+}
+
+// One bond of the compact layout: its force contribution (pairs, times
+// 2^-kexp) and whether it breaks.
+__device__ __forceinline__ bool bond_compact(const ForceArgs& A, const bt::Tpl* __restrict__ tpls, int4 rq, double xi,
+                                             double yi,
+                                             double uxi, double uyi, double s0, float s0f, bt::f2 cf[2]) {
+    const int c = rq.x;
+    const uint32_t dlb = (uint32_t)rq.y;
+    const bt::Tpl& T = tpls[dlb & 0xffu];
+    const float dl = __uint_as_float(dlb & ~0xffu);
+    const double pc[2] = {__ldg(A.pcx + c), __ldg(A.pcy + c)};
+    const double xr[2] = {xi, yi}, ur[2] = {uxi, uyi};
+    bt::f2 eta[2];
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        // d = (P_c - x_i) - u_i with the reference's roundings, then its exact
+        // offset from the class's float reference vector
+        const double d = (pc[a] - xr[a]) - ur[a];
+        const uint64_t xb = T.xd[a];
+        if (xb == 0)
+            eta[a] = bt::split_bits(d);
+        else if (!bt::offset_pair(d, xb, eta[a]))
+            eta[a] = bt::split_bits(d - bt::dfrom(xb));  // exact by Sterbenz's lemma
+    }
+    const bt::BondOut o = bt::bond2(eta, T, dl, bt::f2{__int_as_float(rq.z), __int_as_float(rq.w)});
+    cf[0] = o.f[0];
+    cf[1] = o.f[1];
+    return bt::exceeds(o.e, s0, s0f, T, dl);
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    const int64_t nwarps = (int64_t)gridDim.x * (blockDim.x >> 5);
+    const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + wib;
+    int64_t s_begin = w, s_end = A.nslices, s_step = nwarps;
+    if (A.chunked) {
+        const int64_t per = (A.nslices + nwarps - 1) / nwarps;
+        s_begin = w * per;
+        s_end = s_begin + per < A.nslices ? s_begin + per : A.nslices;
+        s_step = 1;
+    }
+    for (int64_t s = s_begin; s < s_end; s += s_step) {
+        const int64_t r = s * 32 + lane;
+        const bool force_row = r < A.nforce;
+        if (s * 32 < A.nforce) {
+            const int64_t rr = force_row ? r : A.nforce - 1;
+            const double xi = A.x[rr], yi = A.y[rr];
+            const double uxi = A.ux[rr], uyi = A.uy[rr];
+            const double s0 = A.node_s0 ? A.node_s0[rr] : P.critical_s;
+            const float s0f = __double2float_rn(s0);
+            const bt::Tpl* tpls = slice_templates(A, s);
+            bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
+            const int W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            for (int k = 0; k < W; k++) {
+                const int64_t slot = b + (int64_t)k * 32 + lane;
+                const int4 rq = __ldg(reinterpret_cast<const int4*>(A.rec16 + slot));
+                const uint32_t word = wbits[k];
+                const bool alive = force_row && ((word >> lane) & 1u);
+                bool brk = false;
+                if (alive) {
+                    bt::f2 cf[2];
+                    brk = bond_compact(A, tpls, rq, xi, yi, uxi, uyi, s0, s0f, cf);
+                    bt::acc_add(fxa, cf[0]);
+                    bt::acc_add(fya, cf[1]);
+                }
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+            }
+            // undo the power-of-two scaling of the bond coefficient (exact)
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
+            if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
+        }
+        if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<2>(A, r);
+    }
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
+// The compact layout with several warps per slice (as k_bond_split): warp
+// `sub` computes the slots sub, sub + split, ... into shared memory and the
+// group's first warp adds them in slot order (bit for bit the one-warp sums).
+// Shared memory per group: wmax slots x 2 components x 32 lanes pairs and one
+// alive word per slot.
+template <int EPI>
+__global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact_split(const ForceArgs A) {
+    extern __shared__ __align__(16) unsigned char sm_groups[];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    const int split = A.split, G = (int)(blockDim.x >> 5) / split;
+    const int g = wib / split, sub = wib % split;
+    const int Wm = A.wmax;
+    float2* contrib = reinterpret_cast<float2*>(sm_groups) + (size_t)g * Wm * 64;
+    uint32_t* alive_w =
+        reinterpret_cast<uint32_t*>(reinterpret_cast<float2*>(sm_groups) + (size_t)G * Wm * 64) + g * Wm;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    const int64_t groups = (int64_t)gridDim.x * G;
+    const int64_t rounds = (A.nslices + groups - 1) / groups;
+    for (int64_t it = 0; it < rounds; it++) {
+        const int64_t s = it * groups + (int64_t)blockIdx.x * G + g;
+        const int64_t r = s * 32 + lane;
+        const bool in = s < A.nslices;
+        const bool force_row = in && r < A.nforce;
+        const bool work = in && s * 32 < A.nforce;
+        const int64_t rr = force_row ? r : (A.nforce > 0 ? A.nforce - 1 : 0);
+        double xi = 0.0, yi = 0.0, uxi = 0.0, uyi = 0.0;
+        int W = 0;
+        if (work) {
+            xi = A.x[rr], yi = A.y[rr], uxi = A.ux[rr], uyi = A.uy[rr];
+            const double s0 = A.node_s0 ? A.node_s0[rr] : P.critical_s;
+            const float s0f = __double2float_rn(s0);
+            const bt::Tpl* tpls = slice_templates(A, s);
+            W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            for (int k = sub; k < W; k += split) {
+                const int64_t slot = b + (int64_t)k * 32 + lane;
+                const uint32_t word = wbits[k];
+                const bool alive = force_row && ((word >> lane) & 1u);
+                bool brk = false;
+                bt::f2 cf[2] = {{0.0f, 0.0f}, {0.0f, 0.0f}};
+                if (alive)
+                    brk = bond_compact(A, tpls, __ldg(reinterpret_cast<const int4*>(A.rec16 + slot)), xi, yi, uxi, uyi,
+                                       s0, s0f, cf);
+                contrib[(k * 2 + 0) * 32 + lane] = make_float2(cf[0].h, cf[0].l);
+                contrib[(k * 2 + 1) * 32 + lane] = make_float2(cf[1].h, cf[1].l);
+                const uint32_t am = __ballot_sync(0xffffffffu, alive);
+                if (lane == 0) alive_w[k] = am;
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+            }
+        }
+        __syncthreads();
+        if (sub == 0 && work) {
+            bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
+            for (int k = 0; k < W; k++) {
+                if (!((alive_w[k] >> lane) & 1u)) continue;
+                const float2 cx = contrib[(k * 2 + 0) * 32 + lane], cy = contrib[(k * 2 + 1) * 32 + lane];
+                bt::acc_add(fxa, bt::f2{cx.x, cx.y});
+                bt::acc_add(fya, bt::f2{cy.x, cy.y});
+            }
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
+            if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
+        }
+        if (sub == 0 && EPI == EPI_VERLET && A.do_next && in && !force_row && r < P.N) boundary_row<2>(A, r);
+        __syncthreads();
+    }
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
 // 3-D bond force with several warps per slice (A.split of them).  A 3-D row
 // (about 120 slots at a horizon of three spacings) is summed in blocks of 32
 // slots, each block from zero in slot order and the block sums in block order
@@ -1018,6 +1199,12 @@ static ForceArgs make_args(pd_ctx* c) {
     A.node_rmass = c->batch.node_rmass;
     A.slice_part = c->batch.slice_part;
     A.res_out = c->res;
+    A.rec16 = S.rec16;
+    A.tpl = S.tpl;
+    A.ntpl = S.ntpl;
+    A.inst_tbase = S.inst_tbase;
+    A.slice_inst = c->batch.slice_inst;
+    A.node_s0 = c->batch.node_s0;
     return A;
 }
 
@@ -1043,6 +1230,54 @@ int launch_theta(pd_ctx* c, cudaStream_t s) {
         k_theta<3><<<resident_grid(c, (const void*)k_theta<3>, A.nslices), kForceBlock, 0, s>>>(A);
     c->launches++;
     return cuda_err(c, cudaGetLastError(), "theta");
+}
+
+// The 2-D bond kernels on the compact layout (one warp or A.split warps per
+// slice; the templates sit in dynamic shared memory before the split groups).
+static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, int waves, cudaStream_t s) {
+    const void* kern;
+    size_t smem = 0;
+    int64_t units = A.nslices;  // slices (one warp each) or slice groups
+    int per_block = blk / 32;
+    if (c->tune_split > 1) {
+        A.split = c->tune_split;
+        A.wmax = std::max(1, c->sell.wmax);
+        const int G = (blk / 32) / A.split;
+        smem += (size_t)G * A.wmax * (64 * sizeof(float2) + sizeof(uint32_t));
+        per_block = G;
+        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact_split<EPI_VERLET>
+               : f.epi == EPI_ADR  ? (const void*)k_bond_compact_split<EPI_ADR>
+                                   : (const void*)k_bond_compact_split<EPI_NONE>;
+    } else {
+        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET>
+               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR>
+                                   : (const void*)k_bond_compact<EPI_NONE>;
+    }
+    if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, blk, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const int64_t want = (units + per_block - 1) / per_block;
+    const unsigned grid = (unsigned)std::max<int64_t>(
+        1, std::min<int64_t>(std::min<int64_t>(want, (int64_t)c->num_sms * per_sm * waves), kMaxPartials));
+    if (c->tune_split > 1) {
+        if (f.epi == EPI_VERLET)
+            k_bond_compact_split<EPI_VERLET><<<grid, blk, smem, s>>>(A);
+        else if (f.epi == EPI_ADR)
+            k_bond_compact_split<EPI_ADR><<<grid, blk, smem, s>>>(A);
+        else
+            k_bond_compact_split<EPI_NONE><<<grid, blk, smem, s>>>(A);
+    } else if (f.epi == EPI_VERLET) {
+        k_bond_compact<EPI_VERLET><<<grid, blk, smem, s>>>(A);
+    } else if (f.epi == EPI_ADR) {
+        k_bond_compact<EPI_ADR><<<grid, blk, smem, s>>>(A);
+    } else {
+        k_bond_compact<EPI_NONE><<<grid, blk, smem, s>>>(A);
+    }
+    c->launches++;
+    if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
+    c->csr_fail_current = false;
+    return cuda_err(c, cudaGetLastError(), "bond force (compact)");
 }
 
 int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
@@ -1081,6 +1316,7 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
     const int blk = bond ? c->tune_block : kForceBlock;
     const int waves = bond ? c->tune_waves : 1;
     A.chunked = bond ? c->tune_chunked : 0;
+    if (bond && !d3 && A.rec16) return launch_compact(c, A, f, blk, waves, s);
     if (bond && c->tune_split > 1) {
         // several warps per slice (k_bond_split / k_bond_split3), one wave of slice groups
         A.split = c->tune_split;

@@ -357,8 +357,10 @@ __global__ void k_correction(int64_t n, const float* __restrict__ y, double U, d
 // takes the mean of its own value and those of its intact neighbours (the
 // prescribed boundary rows count with a zero correction).  One warp per SELL
 // slice, lane per row, as the force kernels walk it.
+// cols: the neighbour ids of the slots, cols[slot * stride] (the first word of
+// the layout's per-slot record).
 __global__ void k_smooth(int64_t nslices, int64_t n, const int* __restrict__ width, const int64_t* __restrict__ base,
-                         const int64_t* __restrict__ fbase, const BondRec* __restrict__ rec,
+                         const int64_t* __restrict__ fbase, const int* __restrict__ cols, int stride,
                          const uint32_t* __restrict__ bits, const double* __restrict__ in, double* __restrict__ out) {
     const int lane = threadIdx.x & 31;
     for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < nslices;
@@ -373,7 +375,7 @@ __global__ void k_smooth(int64_t nslices, int64_t n, const int* __restrict__ wid
         for (int k = 0; k < W; k++) {
             const bool alive = row && ((bits[fbase[s] + k] >> lane) & 1u);
             if (alive) {
-                const int c = rec[b + (int64_t)k * 32 + lane].col;
+                const int c = cols[(b + (int64_t)k * 32 + lane) * stride];
                 if (c < n) {
                     sx += in[c];
                     sy += in[n + c];
@@ -767,7 +769,9 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
             for (int k = 0; k < smooth_passes; k++) {
                 const double* in = cb + (k & 1) * 2 * ni;
                 double* out = cb + ((k + 1) & 1) * 2 * ni;
-                k_smooth<<<gs, 256, 0, s>>>(ns, ni, S.width, S.base, S.fbase, S.rec, S.bits, in, out);
+                const int* cols = S.rec16 ? reinterpret_cast<const int*>(S.rec16) : reinterpret_cast<const int*>(S.rec);
+                const int stride = S.rec16 ? (int)(sizeof(bt::Rec) / 4) : (int)(sizeof(BondRec) / 4);
+                k_smooth<<<gs, 256, 0, s>>>(ns, ni, S.width, S.base, S.fbase, cols, stride, S.bits, in, out);
                 c->launches++;
             }
             k_combine<<<g, 256, 0, s>>>(ni, cb + (smooth_passes & 1) * 2 * ni, delta / U, c->nf[PD_F_UX],

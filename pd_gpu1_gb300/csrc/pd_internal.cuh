@@ -19,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "bondtpl.h"
 #include "pd.h"
 
 namespace pdg {
@@ -124,7 +125,17 @@ struct Sell {
     // pair sums times 2^-st_exp (exact scalings, undone in FP64 per node)
     int sn_exp = 0, sth_exp = 0, st_exp = 0;
     uint32_t* bits = nullptr;// [F] intact flags
+    // 2-D bond-based compact layout: a 16-byte record per slot (column, dl and
+    // class id, k2 / 2) and one template per lattice offset class; when set,
+    // rec is not allocated
+    bt::Rec* rec16 = nullptr;  // [S]
+    bt::Tpl* tpl = nullptr;    // [ntpl] templates of all specimens
+    int ntpl = 0;
+    int* inst_tbase = nullptr; // batch: first template of each specimen (null: one specimen)
 };
+
+// Layout of the bond-based force path (pd_set_force_layout).
+enum ForceLayout { LAYOUT_AUTO = 0, LAYOUT_RECORDS = 1, LAYOUT_COMPACT = 2 };
 
 }  // namespace pdg
 
@@ -204,6 +215,7 @@ struct pd_ctx {
     int tune_waves = 1;     // grid = resident blocks x waves
     int tune_chunked = 0;   // 1: contiguous slice runs per warp
     int tune_split = 1;     // warps sharing one slice's slots (2-D bond kernels)
+    int layout_pref = pdg::LAYOUT_AUTO;  // bond-based SELL layout requested (pd_set_force_layout)
 };
 
 namespace pdg {

@@ -19,6 +19,9 @@
 #include <cmath>
 
 #include "ff.cuh"
+#include <algorithm>
+#include <cmath>
+
 #include "pd_internal.cuh"
 
 namespace pdg {
@@ -367,6 +370,114 @@ __global__ void k_sell_fill(KParams P, int64_t nslices, const int* __restrict__ 
     }
 }
 
+// ---- compact layout of the 2-D bond-based kernels ---------------------------
+//
+// Offset classes: the bonds of one specimen whose reference vectors round to
+// the same float vector xf (on a lattice, one class per lattice offset).  A
+// hash table in device memory, one region of kRegion slots per specimen (a
+// single plate is one specimen), collects the classes with the smallest bond
+// length of each (l0t); the host numbers them per specimen in key order
+// (deterministic, and the same for a plate alone and inside a batch) and
+// builds one template per class; each slot then stores dl = l0 - l0t, the
+// class id and k2 / 2 in a 16-byte record (bondtpl.h).
+
+constexpr int kRegion = 256;  // hash slots per specimen (power of two)
+constexpr unsigned long long kEmptyKey = ~0ull;
+
+__device__ __forceinline__ unsigned long long class_key(double xa, double ya) {
+    return ((unsigned long long)__float_as_uint(__double2float_rn(xa)) << 32) |
+           (unsigned long long)__float_as_uint(__double2float_rn(ya));
+}
+__device__ __forceinline__ unsigned class_hash(unsigned long long k) {
+    return (unsigned)((k * 0x9E3779B97F4A7C15ull) >> 56);  // 8 bits
+}
+
+__global__ void k_class_insert(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
+                               const int* __restrict__ csr, const int* __restrict__ NL, const int* __restrict__ grp,
+                               const double* __restrict__ x, const double* __restrict__ y,
+                               const double* __restrict__ idist, unsigned long long* __restrict__ keys,
+                               unsigned long long* __restrict__ l0min, int* __restrict__ overflow) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int q = csr[b + t];
+        if (q < 0) continue;
+        const int64_t r = s * 32 + (t & 31), c = NL[q];
+        const int64_t region = grp ? grp[r] : 0;
+        const unsigned long long key = class_key(x[c] - x[r], y[c] - y[r]);
+        const unsigned long long lb = (unsigned long long)__double_as_longlong(idist[q]);
+        unsigned h = class_hash(key);
+        bool done = false;
+        for (int probe = 0; probe < kRegion && !done; probe++, h = (h + 1) & (kRegion - 1)) {
+            const int64_t i = region * kRegion + h;
+            const unsigned long long prev = atomicCAS(keys + i, kEmptyKey, key);
+            if (prev == kEmptyKey || prev == key) {
+                atomicMin(l0min + i, lb);  // positive doubles order like their bit patterns
+                done = true;
+            }
+        }
+        if (!done) atomicExch(overflow, 1);
+    }
+}
+
+// Records of the compact layout; *bad is set where a slot cannot be
+// represented (dl not a float with a free low byte).
+__global__ void k_rec16_fill(KParams P, int64_t nslices, const int* __restrict__ width,
+                             const int64_t* __restrict__ base, const int* __restrict__ csr, const int* __restrict__ NL,
+                             const int* __restrict__ grp, const double* __restrict__ x, const double* __restrict__ y,
+                             const double* __restrict__ idist, const double* __restrict__ fac,
+                             const double* __restrict__ scr, const double* __restrict__ node_bc,
+                             const unsigned long long* __restrict__ keys, const int* __restrict__ ids,
+                             const int* __restrict__ inst_tbase, const bt::Tpl* __restrict__ tpl,
+                             double kscale_half_inv, bt::Rec* __restrict__ rec, int* __restrict__ bad) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int64_t slot = b + t;
+        const int q = csr[slot];
+        const int64_t r = s * 32 + (t & 31);
+        bt::Rec R;
+        if (q < 0) {
+            R.col = (int)(r < P.N ? r : 0);
+            R.dl = 0.0f;  // class 0, zero coefficient: a padding slot contributes nothing
+            R.k2h = R.k2l = 0.0f;
+            rec[slot] = R;
+            continue;
+        }
+        const int64_t c = NL[q];
+        const int64_t region = grp ? grp[r] : 0;
+        const unsigned long long key = class_key(x[c] - x[r], y[c] - y[r]);
+        unsigned h = class_hash(key);
+        int id = -1;
+        for (int probe = 0; probe < kRegion; probe++, h = (h + 1) & (kRegion - 1)) {
+            const int64_t i = region * kRegion + h;
+            if (keys[i] == key) {
+                id = ids[i];
+                break;
+            }
+            if (keys[i] == kEmptyKey) break;
+        }
+        const double L0 = idist[q];
+        const int64_t tb = inst_tbase ? inst_tbase[region] : 0;
+        const double dlv = id >= 0 ? L0 - tpl[tb + id].l0d : 0.0;  // exact: l0 and l0t within a factor two
+        const float dl = __double2float_rn(dlv);
+        const unsigned dlb = __float_as_uint(dl);
+        if (id < 0 || id > 255 || (double)dl != dlv || (dlb & 0xffu) != 0u) atomicExch(bad, 1);
+        R.col = (int)c;
+        R.dl = __uint_as_float((dlb & ~0xffu) | (unsigned)(id & 0xff));
+        const double bc = node_bc ? node_bc[r] : P.bc;
+        const double k2 = 2.0 * (P.vol * fac[q] * bc * scr[q]) / L0;
+        const ff kf = ff_split(k2 * kscale_half_inv);
+        R.k2h = kf.h;
+        R.k2l = kf.l;
+        rec[slot] = R;
+    }
+}
+
 // Intact flags: CSR int32 <-> SELL bit words.
 __global__ void k_bits_from_csr(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
                                 const int64_t* __restrict__ fbase, const int* __restrict__ csr,
@@ -526,12 +637,143 @@ static void free_sell(Sell& S) {
     free_ptr(S.sfo);
     free_ptr(S.e);
     free_ptr(S.bits);
+    free_ptr(S.rec16);
+    free_ptr(S.tpl);
+    free_ptr(S.inst_tbase);
+    S.ntpl = 0;
     S.nslices = S.S = S.F = 0;
 }
 
 void release_sell(pd_ctx* c) {
     drop_graphs(c);
     free_sell(c->sell);
+}
+
+// The compact layout of a 2-D bond-based problem (S.csr filled): offset
+// classes per specimen, their templates and the 16-byte slot records.
+// Returns PD_ERR_UNSUPPORTED (arrays released) where the problem does not fit
+// it: more than 255 classes in a specimen (or a region of the hash table
+// full), or a bond length that differs from its class's smallest by more
+// than a float with a free low byte can hold.
+int build_compact(pd_ctx* c, cudaStream_t s) {
+    const KParams P = kparams(c->p);
+    Sell& S = c->sell;
+    const int* grp = c->batch.node_group;
+    const int64_t regions = c->batch.count > 0 ? c->batch.count : 1;
+    const int64_t tsize = regions * kRegion;
+    unsigned long long *keys = nullptr, *l0min = nullptr;
+    int *ids = nullptr, *flags = nullptr;
+    auto cleanup = [&]() {
+        cudaFreeAsync(keys, s);
+        cudaFreeAsync(l0min, s);
+        cudaFreeAsync(ids, s);
+        cudaFreeAsync(flags, s);
+    };
+    auto release = [&]() {
+        free_ptr(S.tpl);
+        free_ptr(S.rec16);
+        free_ptr(S.inst_tbase);
+        S.ntpl = 0;
+    };
+    if (cudaMallocAsync(&keys, tsize * 8, s) || cudaMallocAsync(&l0min, tsize * 8, s) ||
+        cudaMallocAsync(&ids, tsize * 4, s) || cudaMallocAsync(&flags, 2 * 4, s)) {
+        cleanup();
+        return set_err(c, PD_ERR_NOMEM, "offset-class table");
+    }
+    cudaMemsetAsync(keys, 0xff, tsize * 8, s);
+    cudaMemsetAsync(l0min, 0xff, tsize * 8, s);
+    cudaMemsetAsync(flags, 0, 2 * 4, s);
+    const unsigned gx = (unsigned)std::min<int64_t>(S.nslices, 65535);
+    const unsigned gy = (unsigned)((S.nslices + gx - 1) / gx);
+    k_class_insert<<<dim3(gx, gy), 256, 0, s>>>(S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
+                                                 c->nf[PD_F_Y], c->idist, keys, l0min, flags);
+    c->launches++;
+    std::vector<unsigned long long> hk((size_t)tsize), hl((size_t)tsize);
+    int hflags[2] = {0, 0};
+    cudaMemcpyAsync(hk.data(), keys, tsize * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hl.data(), l0min, tsize * 8, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(hflags, flags, 2 * 4, cudaMemcpyDeviceToHost, s);
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cleanup();
+        return cuda_err(c, e, "offset classes");
+    }
+    if (hflags[0]) {
+        cleanup();
+        return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: a specimen with more offset classes than its table");
+    }
+    // templates, numbered per specimen in key order
+    std::vector<bt::Tpl> tp;
+    std::vector<int> hid((size_t)tsize, -1), tbase((size_t)regions, 0);
+    for (int64_t g = 0; g < regions; g++) {
+        std::vector<std::pair<unsigned long long, int64_t>> used;
+        for (int64_t h = 0; h < kRegion; h++)
+            if (hk[g * kRegion + h] != kEmptyKey) used.push_back({hk[g * kRegion + h], g * kRegion + h});
+        std::sort(used.begin(), used.end());
+        if (used.size() > 255) {
+            cleanup();
+            return set_err(c, PD_ERR_UNSUPPORTED,
+                           "compact layout: " + std::to_string(used.size()) + " offset classes in a specimen");
+        }
+        tbase[g] = (int)tp.size();
+        for (size_t k = 0; k < used.size(); k++) {
+            const unsigned long long key = used[k].first;
+            hid[used[k].second] = (int)k;
+            bt::Tpl T;
+            const float xf[2] = {bt::ffrom((uint32_t)(key >> 32)), bt::ffrom((uint32_t)key)};
+            double sh = 0.0, sl = 0.0;
+            for (int a = 0; a < 2; a++) {
+                T.xf[a] = xf[a];
+                T.xf2[a] = 2.0f * xf[a];
+                T.xd[a] = bt::dbits((double)xf[a]);
+                const double sq = (double)xf[a] * (double)xf[a];  // exact: 24-bit significands
+                const double t = sh + sq, bb = t - sh;
+                sl += (sh - (t - bb)) + (sq - bb);
+                sh = t;
+            }
+            const double l0t = bt::dfrom(hl[used[k].second]);
+            const double ph = l0t * l0t, pl = std::fma(l0t, l0t, -ph);
+            const bt::f2 c0 = bt::split_bits((sh - ph) + (sl - pl));  // sh - ph exact (Sterbenz)
+            const bt::f2 q0 = bt::split_bits(sh + sl);
+            const bt::f2 l0 = bt::split_bits(l0t);
+            T.c0h = c0.h, T.c0l = c0.l;
+            T.q0h = q0.h, T.q0l = q0.l;
+            T.l0h = l0.h, T.l0l = l0.l;
+            T.l0d = l0t;
+            tp.push_back(T);
+        }
+    }
+    if (tp.empty()) {
+        cleanup();
+        return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: no bonds");
+    }
+    S.ntpl = (int)tp.size();
+    if (cudaMalloc(&S.tpl, tp.size() * sizeof(bt::Tpl)) ||
+        cudaMalloc(&S.rec16, (size_t)std::max<int64_t>(S.S, 1) * sizeof(bt::Rec)) ||
+        (regions > 1 && cudaMalloc(&S.inst_tbase, regions * sizeof(int)))) {
+        cleanup();
+        release();
+        return set_err(c, PD_ERR_NOMEM, "compact records");
+    }
+    cudaMemcpyAsync(S.tpl, tp.data(), tp.size() * sizeof(bt::Tpl), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ids, hid.data(), tsize * 4, cudaMemcpyHostToDevice, s);
+    if (S.inst_tbase) cudaMemcpyAsync(S.inst_tbase, tbase.data(), regions * sizeof(int), cudaMemcpyHostToDevice, s);
+    k_rec16_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
+                                               c->nf[PD_F_Y], c->idist, c->fac, c->scr, c->batch.node_bc, keys, ids,
+                                               S.inst_tbase, S.tpl, 0.5 * S.kscale_inv, S.rec16, flags + 1);
+    c->launches++;
+    cudaMemcpyAsync(hflags + 1, flags + 1, 4, cudaMemcpyDeviceToHost, s);
+    e = cudaStreamSynchronize(s);
+    cleanup();
+    if (e != cudaSuccess) {
+        release();
+        return cuda_err(c, e, "compact records");
+    }
+    if (hflags[1]) {
+        release();
+        return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: a bond length outside its class's float range");
+    }
+    return PD_OK;
 }
 
 int prepare(pd_ctx* c, cudaStream_t s) {
@@ -574,7 +816,14 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
     bool ok = !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
-    if (ok && !state)
+    // 2-D bond-based problems try the compact layout first (16-byte records on
+    // offset-class templates); the 48-byte records are the general layout
+    const bool try_compact = !state && P.dim == 2 && c->layout_pref != LAYOUT_RECORDS;
+    if (c->layout_pref == LAYOUT_COMPACT && !try_compact) {
+        free_sell(S);
+        return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 2-D bond-based problems");
+    }
+    if (ok && !state && !try_compact)
         ok = !cudaMalloc(&S.rec, n8 * 6);
     // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,
     // so that the pair arithmetic of the force kernels stays in float range
@@ -613,6 +862,26 @@ int prepare(pd_ctx* c, cudaStream_t s) {
                                               c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac, c->scr, c->w,
                                               c->nf[PD_F_M], c->batch.node_bc, c->batch.node_s0, S);
     c->launches++;
+    if (try_compact) {
+        rc = build_compact(c, s);
+        if (rc && c->layout_pref == LAYOUT_COMPACT) {
+            free_sell(S);
+            return rc;
+        }
+        if (rc) {
+            // the general layout: 48-byte records
+            c->err.clear();
+            if (cudaMalloc(&S.rec, n8 * 6)) {
+                free_sell(S);
+                return set_err(c, PD_ERR_NOMEM, "SELL bond arrays");
+            }
+            k_sell_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, c->NN, c->rowptr, c->NL,
+                                                      c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac,
+                                                      c->scr, c->w, c->nf[PD_F_M], c->batch.node_bc,
+                                                      c->batch.node_s0, S);
+            c->launches++;
+        }
+    }
     if (state) {
         k_inv_m<<<(unsigned)((P.N + 255) / 256), 256, 0, s>>>(P.N, c->nf[PD_F_M], std::ldexp(1.0, -S.sn_exp),
                                                              c->node_b, c->node_c);

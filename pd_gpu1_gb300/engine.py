@@ -275,6 +275,19 @@ class Engine:
                 "pd_get_launch")
         return b.value, k.value, w.value, p.value
 
+    LAYOUTS = {"auto": 0, "records": 1, "compact": 2}
+
+    def set_force_layout(self, layout="auto"):
+        """Per-bond storage of the bond-based kernels: "records" (48 bytes per
+        slot), "compact" (16-byte records on offset-class templates, 2-D) or
+        "auto" (compact where it fits); takes effect at the next prepare."""
+        self._c(self._lib.pd_set_force_layout(self.ctx, self.LAYOUTS[layout]), "pd_set_force_layout")
+
+    def force_layout(self):
+        v = C.c_int()
+        self._c(self._lib.pd_get_force_layout(self.ctx, C.byref(v)), "pd_get_force_layout")
+        return {0: None, 1: "records", 2: "compact"}[v.value]
+
     def autotune(self, reps=5):
         """Times the launch shapes at the current state and keeps the fastest;
         returns (block, chunked, waves, split, ms per launch)."""

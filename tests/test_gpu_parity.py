@@ -506,3 +506,84 @@ def test_autotune_3d_restores_state_and_keeps_forces(E):
         one.bond_force_gpu()
         for k in ["FX", "FY", "FZ", "FAIL"]:
             np.testing.assert_array_equal(tuned[k], one.get(k), err_msg=f"shape {block, chunked, waves, split} {k}")
+
+
+def test_compact_layout_matches_records(E):
+    """The 2-D compact layout (16-byte slot records on offset-class templates,
+    the default where it fits) against the 48-byte records on the cracked
+    crack-branching plate: forces within 2e-13 norm-relative (the two paths
+    differ only in their pair arithmetic, ~5e-14 per bond), the same intact
+    flags after two passes at a lowered critical stretch, and the reference
+    oracle's forces within the parity bar for both."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_branching(scale=0.05)
+    rng = np.random.default_rng(3)
+    with E.Engine(p) as eng:
+        setup(eng)
+        assert eng.force_layout() == "compact"
+        x, y = eng.get("X"), eng.get("Y")
+        ux = -4.0e-4 * x + 2.0e-3 * x * y + rng.standard_normal(p.N) * 2e-9
+        uy = 3.0e-4 * y + 1.0e-3 * x * x + rng.standard_normal(p.N) * 2e-9
+        fail0 = eng.get("FAIL")
+        out = {}
+        for layout in ("compact", "records"):
+            eng.set_force_layout(layout)
+            eng.set("FAIL", fail0)
+            eng.prepare()
+            assert eng.force_layout() == layout
+            q = eng.params()
+            q.critical_s = 3.5e-4  # bonds break in the stretched corners
+            eng.set_params(q)
+            eng.set("UX", ux)
+            eng.set("UY", uy)
+            eng.bond_force_gpu()
+            first = (eng.get("FX"), eng.get("FY"))
+            eng.bond_force_gpu()
+            out[layout] = first + (eng.get("FX"), eng.get("FY"), eng.get("FAIL"))
+        for k in range(4):
+            assert_close_norm(out["compact"][k], out["records"][k], 2e-13, f"component {k}")
+        np.testing.assert_array_equal(out["compact"][4], out["records"][4])
+        assert (out["compact"][4] == 0).sum() > (fail0 == 0).sum()  # bonds broke beyond the pre-crack
+        # the oracle on the first pass
+        m = orc.Model(q, x, y)
+        m.find_neighbor(brute=False)
+        m.surface_correct()
+        m.fail[:] = helpers_ell(fail0, m.NN, q.MN)
+        m.ux[:], m.uy[:] = ux, uy
+        m.bond_force()
+        n = q.N_int
+        assert_close_norm(out["compact"][0][:n], m.fx[:n], FORCE_RTOL, "fx vs oracle")
+        assert_close_norm(out["compact"][1][:n], m.fy[:n], FORCE_RTOL, "fy vs oracle")
+
+
+def helpers_ell(values, NN, MN):
+    from helpers import ell
+
+    return ell(np.asarray(values, dtype=np.int32), NN, MN, fill=1)
+
+
+def test_compact_layout_selection(E):
+    """Where the compact layout applies: 2-D bond-based problems take it by
+    default; 3-D and state-based ones keep the records, and asking for the
+    compact layout there is refused (PD_ERR_UNSUPPORTED, -8) without
+    disturbing the context, which then runs on the records."""
+    from pd_gpu1_gb300 import presets
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10, model=PD_MODEL_BOND)
+    with E.Engine(p) as eng:
+        setup(eng)
+        assert eng.force_layout() == "records"
+        eng.set_force_layout("compact")
+        with pytest.raises(E.PDError) as ei:
+            eng.prepare()
+        assert ei.value.status == -8
+        eng.set_force_layout("auto")
+        eng.prepare()
+        assert eng.force_layout() == "records"
+        eng.bond_force_gpu()
+    p, setup, meta = presets.build_crack_grow(scale=0.1, nt=10)
+    with E.Engine(p) as eng:
+        setup(eng)
+        assert eng.force_layout() is None  # state-based: neither bond-based layout
