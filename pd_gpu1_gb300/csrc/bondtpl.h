@@ -289,12 +289,12 @@ PD_BT_HD BondOut bond2(const f2 eta[2], const Tpl& T, float dl, f2 k2half) {
     return o;
 }
 
-// Accumulate a pair into a running sum (TwoSum of the high parts, the rest
-// gathered in the low part; value acc.h + acc.l).
+// Accumulate a pair into a running sum, renormalized at every addition (the
+// low part stays within half an ulp of the high part, so the rounding of the
+// low-part sum costs 2^-48 of the running sum, not of the low part's growth).
 PD_BT_HD void acc_add(f2& acc, f2 v) {
     const f2 s = two_sum(acc.h, v.h);
-    acc.h = s.h;
-    acc.l += s.l + v.l;
+    acc = fast_sum(s.h, s.l + (acc.l + v.l));
 }
 
 // e > ecrit with ecrit = fl(s0 l0), l0 = l0t + dl, given s0 and s0f = s0
