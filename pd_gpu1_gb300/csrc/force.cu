@@ -675,14 +675,13 @@ __device__ __forceinline__ const bt::Tpl* slice_templates(const ForceArgs& A, in
 
 // One bond of the compact layout: its force contribution (pairs, times
 // 2^-kexp) and whether it breaks.
-__device__ __forceinline__ bool bond_compact(const ForceArgs& A, const bt::Tpl* __restrict__ tpls, int4 rq, double xi,
-                                             double yi,
-                                             double uxi, double uyi, double s0, float s0f, bt::f2 cf[2]) {
-    const int c = rq.x;
+__device__ __forceinline__ bool bond_compact_p(const bt::Tpl* __restrict__ tpls, int4 rq, double pcx, double pcy,
+                                               double xi, double yi, double uxi, double uyi, double s0, float s0f,
+                                               bt::f2 cf[2]) {
     const uint32_t dlb = (uint32_t)rq.y;
     const bt::Tpl& T = tpls[dlb & 0xffu];
     const float dl = __uint_as_float(dlb & ~0xffu);
-    const double pc[2] = {__ldg(A.pcx + c), __ldg(A.pcy + c)};
+    const double pc[2] = {pcx, pcy};
     const double xr[2] = {xi, yi}, ur[2] = {uxi, uyi};
     bt::f2 eta[2];
 #pragma unroll
@@ -701,9 +700,27 @@ __device__ __forceinline__ bool bond_compact(const ForceArgs& A, const bt::Tpl* 
     cf[1] = o.f[1];
     return bt::exceeds(o.e, s0, s0f, T, dl);
 }
+__device__ __forceinline__ bool bond_compact(const ForceArgs& A, const bt::Tpl* __restrict__ tpls, int4 rq, double xi,
+                                             double yi, double uxi, double uyi, double s0, float s0f, bt::f2 cf[2]) {
+    return bond_compact_p(tpls, rq, __ldg(A.pcx + rq.x), __ldg(A.pcy + rq.x), xi, yi, uxi, uyi, s0, s0f, cf);
+}
 
-template <int EPI>
+// The compact kernel's software pipeline: records two slots ahead and the
+// neighbour positions one slot ahead (true), or records one slot ahead and
+// the positions gathered in the slot's own iteration (false).
+constexpr bool kGatherAhead = false;
+
+// TSM: the templates staged in shared memory (one specimen: a few dozen
+// classes), read there instead of through the read-only cache.
+template <int EPI, bool TSM>
 __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact(const ForceArgs A) {
+    extern __shared__ __align__(16) unsigned char sm_tpl[];
+    if (TSM) {
+        float4* dst = reinterpret_cast<float4*>(sm_tpl);
+        const float4* src = reinterpret_cast<const float4*>(A.tpl);
+        for (int i = threadIdx.x; i < A.ntpl * 4; i += blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const KParams& P = A.P;
@@ -726,25 +743,56 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact(
             const double uxi = A.ux[rr], uyi = A.uy[rr];
             const double s0 = A.node_s0 ? A.node_s0[rr] : P.critical_s;
             const float s0f = __double2float_rn(s0);
-            const bt::Tpl* tpls = slice_templates(A, s);
+            const bt::Tpl* tpls = TSM ? reinterpret_cast<const bt::Tpl*>(sm_tpl) : slice_templates(A, s);
             bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
-            for (int k = 0; k < W; k++) {
-                const int64_t slot = b + (int64_t)k * 32 + lane;
-                const int4 rq = __ldg(reinterpret_cast<const int4*>(A.rec16 + slot));
-                const uint32_t word = wbits[k];
-                const bool alive = force_row && ((word >> lane) & 1u);
-                bool brk = false;
-                if (alive) {
-                    bt::f2 cf[2];
-                    brk = bond_compact(A, tpls, rq, xi, yi, uxi, uyi, s0, s0f, cf);
-                    bt::acc_add(fxa, cf[0]);
-                    bt::acc_add(fya, cf[1]);
+            // the next slot's record loaded one iteration ahead, so that its
+            // neighbour gathers can start as soon as the iteration does
+            const int4* rp = reinterpret_cast<const int4*>(A.rec16 + b) + lane;
+            if (kGatherAhead) {
+                const int4 z4 = make_int4(0, 0, 0, 0);
+                int4 rq_a = W > 0 ? __ldg(rp) : z4, rq_b = W > 1 ? __ldg(rp + 32) : z4;
+                double gx = W > 0 ? __ldg(A.pcx + rq_a.x) : 0.0, gy = W > 0 ? __ldg(A.pcy + rq_a.x) : 0.0;
+                for (int k = 0; k < W; k++) {
+                    const int4 rq = rq_a;
+                    const double pcx = gx, pcy = gy;
+                    rq_a = rq_b;
+                    if (k + 2 < W) rq_b = __ldg(rp + (int64_t)(k + 2) * 32);
+                    if (k + 1 < W) {
+                        gx = __ldg(A.pcx + rq_a.x);
+                        gy = __ldg(A.pcy + rq_a.x);
+                    }
+                    const uint32_t word = wbits[k];
+                    const bool alive = force_row && ((word >> lane) & 1u);
+                    bool brk = false;
+                    if (alive) {
+                        bt::f2 cf[2];
+                        brk = bond_compact_p(tpls, rq, pcx, pcy, xi, yi, uxi, uyi, s0, s0f, cf);
+                        bt::acc_add(fxa, cf[0]);
+                        bt::acc_add(fya, cf[1]);
+                    }
+                    const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                    if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
                 }
-                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
-                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+            } else {
+                int4 rq_next = W > 0 ? __ldg(rp) : make_int4(0, 0, 0, 0);
+                for (int k = 0; k < W; k++) {
+                    const int4 rq = rq_next;
+                    if (k + 1 < W) rq_next = __ldg(rp + (int64_t)(k + 1) * 32);
+                    const uint32_t word = wbits[k];
+                    const bool alive = force_row && ((word >> lane) & 1u);
+                    bool brk = false;
+                    if (alive) {
+                        bt::f2 cf[2];
+                        brk = bond_compact(A, tpls, rq, xi, yi, uxi, uyi, s0, s0f, cf);
+                        bt::acc_add(fxa, cf[0]);
+                        bt::acc_add(fya, cf[1]);
+                    }
+                    const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                    if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+                }
             }
             // undo the power-of-two scaling of the bond coefficient (exact)
             const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
@@ -1237,6 +1285,8 @@ int launch_theta(pd_ctx* c, cudaStream_t s) {
 static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, int waves, cudaStream_t s) {
     const void* kern;
     size_t smem = 0;
+    // one specimen: its templates fit shared memory (at most 255 x 64 bytes)
+    const bool tsm = A.inst_tbase == nullptr;
     int64_t units = A.nslices;  // slices (one warp each) or slice groups
     int per_block = blk / 32;
     if (c->tune_split > 1) {
@@ -1248,10 +1298,15 @@ static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, 
         kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact_split<EPI_VERLET>
                : f.epi == EPI_ADR  ? (const void*)k_bond_compact_split<EPI_ADR>
                                    : (const void*)k_bond_compact_split<EPI_NONE>;
+    } else if (tsm) {
+        smem = (size_t)A.ntpl * sizeof(bt::Tpl);
+        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET, true>
+               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR, true>
+                                   : (const void*)k_bond_compact<EPI_NONE, true>;
     } else {
-        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET>
-               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR>
-                                   : (const void*)k_bond_compact<EPI_NONE>;
+        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET, false>
+               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR, false>
+                                   : (const void*)k_bond_compact<EPI_NONE, false>;
     }
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
@@ -1267,12 +1322,19 @@ static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, 
             k_bond_compact_split<EPI_ADR><<<grid, blk, smem, s>>>(A);
         else
             k_bond_compact_split<EPI_NONE><<<grid, blk, smem, s>>>(A);
+    } else if (tsm) {
+        if (f.epi == EPI_VERLET)
+            k_bond_compact<EPI_VERLET, true><<<grid, blk, smem, s>>>(A);
+        else if (f.epi == EPI_ADR)
+            k_bond_compact<EPI_ADR, true><<<grid, blk, smem, s>>>(A);
+        else
+            k_bond_compact<EPI_NONE, true><<<grid, blk, smem, s>>>(A);
     } else if (f.epi == EPI_VERLET) {
-        k_bond_compact<EPI_VERLET><<<grid, blk, smem, s>>>(A);
+        k_bond_compact<EPI_VERLET, false><<<grid, blk, smem, s>>>(A);
     } else if (f.epi == EPI_ADR) {
-        k_bond_compact<EPI_ADR><<<grid, blk, smem, s>>>(A);
+        k_bond_compact<EPI_ADR, false><<<grid, blk, smem, s>>>(A);
     } else {
-        k_bond_compact<EPI_NONE><<<grid, blk, smem, s>>>(A);
+        k_bond_compact<EPI_NONE, false><<<grid, blk, smem, s>>>(A);
     }
     c->launches++;
     if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
