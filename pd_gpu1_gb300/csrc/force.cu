@@ -710,17 +710,14 @@ __device__ __forceinline__ bool bond_compact(const ForceArgs& A, const bt::Tpl* 
 // the positions gathered in the slot's own iteration (false).
 constexpr bool kGatherAhead = false;
 
-// TSM: the templates staged in shared memory (one specimen: a few dozen
-// classes), read there instead of through the read-only cache.
-template <int EPI, bool TSM>
-__global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact(const ForceArgs A) {
-    extern __shared__ __align__(16) unsigned char sm_tpl[];
-    if (TSM) {
-        float4* dst = reinterpret_cast<float4*>(sm_tpl);
-        const float4* src = reinterpret_cast<const float4*>(A.tpl);
-        for (int i = threadIdx.x; i < A.ntpl * 4; i += blockDim.x) dst[i] = __ldg(src + i);
-        __syncthreads();
-    }
+// The templates are read through the read-only cache: staged in shared memory
+// instead (one specimen, a few dozen classes) the kernel was measured twice as
+// slow on the 1.6M-node plate (1.00 against 0.49 ms per launch).
+// Resident 512-thread blocks per SM the compact kernel is compiled for (the
+// register cap: 2 -> 64 registers a thread).
+constexpr int kCompactMinBlocks = 2;
+template <int EPI>
+__global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compact(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const KParams& P = A.P;
@@ -743,7 +740,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact(
             const double uxi = A.ux[rr], uyi = A.uy[rr];
             const double s0 = A.node_s0 ? A.node_s0[rr] : P.critical_s;
             const float s0f = __double2float_rn(s0);
-            const bt::Tpl* tpls = TSM ? reinterpret_cast<const bt::Tpl*>(sm_tpl) : slice_templates(A, s);
+            const bt::Tpl* tpls = slice_templates(A, s);
             bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
             const int W = A.width[s];
             const int64_t b = A.base[s];
@@ -1285,8 +1282,6 @@ int launch_theta(pd_ctx* c, cudaStream_t s) {
 static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, int waves, cudaStream_t s) {
     const void* kern;
     size_t smem = 0;
-    // one specimen: its templates fit shared memory (at most 255 x 64 bytes)
-    const bool tsm = A.inst_tbase == nullptr;
     int64_t units = A.nslices;  // slices (one warp each) or slice groups
     int per_block = blk / 32;
     if (c->tune_split > 1) {
@@ -1298,15 +1293,10 @@ static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, 
         kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact_split<EPI_VERLET>
                : f.epi == EPI_ADR  ? (const void*)k_bond_compact_split<EPI_ADR>
                                    : (const void*)k_bond_compact_split<EPI_NONE>;
-    } else if (tsm) {
-        smem = (size_t)A.ntpl * sizeof(bt::Tpl);
-        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET, true>
-               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR, true>
-                                   : (const void*)k_bond_compact<EPI_NONE, true>;
     } else {
-        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET, false>
-               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR, false>
-                                   : (const void*)k_bond_compact<EPI_NONE, false>;
+        kern = f.epi == EPI_VERLET ? (const void*)k_bond_compact<EPI_VERLET>
+               : f.epi == EPI_ADR  ? (const void*)k_bond_compact<EPI_ADR>
+                                   : (const void*)k_bond_compact<EPI_NONE>;
     }
     if (smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
@@ -1322,19 +1312,12 @@ static int launch_compact(pd_ctx* c, ForceArgs& A, const StepFlags& f, int blk, 
             k_bond_compact_split<EPI_ADR><<<grid, blk, smem, s>>>(A);
         else
             k_bond_compact_split<EPI_NONE><<<grid, blk, smem, s>>>(A);
-    } else if (tsm) {
-        if (f.epi == EPI_VERLET)
-            k_bond_compact<EPI_VERLET, true><<<grid, blk, smem, s>>>(A);
-        else if (f.epi == EPI_ADR)
-            k_bond_compact<EPI_ADR, true><<<grid, blk, smem, s>>>(A);
-        else
-            k_bond_compact<EPI_NONE, true><<<grid, blk, smem, s>>>(A);
     } else if (f.epi == EPI_VERLET) {
-        k_bond_compact<EPI_VERLET, false><<<grid, blk, smem, s>>>(A);
+        k_bond_compact<EPI_VERLET><<<grid, blk, smem, s>>>(A);
     } else if (f.epi == EPI_ADR) {
-        k_bond_compact<EPI_ADR, false><<<grid, blk, smem, s>>>(A);
+        k_bond_compact<EPI_ADR><<<grid, blk, smem, s>>>(A);
     } else {
-        k_bond_compact<EPI_NONE, false><<<grid, blk, smem, s>>>(A);
+        k_bond_compact<EPI_NONE><<<grid, blk, smem, s>>>(A);
     }
     c->launches++;
     if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
