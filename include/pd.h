@@ -310,23 +310,37 @@ int pd_mlp_gemm(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int6
  * usable.  No counterpart in the reference (no tensor-core code). */
 int pd_mlp_gemm_wait_check(const void* dev_a, const void* dev_b, int64_t M, int64_t N, int64_t K, float* dev_d,
                            int transpose_a, long long spin_limit, int issue, void* stream);
-/* Features of the free nodes for a load increment (BF16 [N_int][16]): previous
- * displacement / U, increment / U, damage, loaded-edge flag, x and y over the
- * half sizes, family size / nn_ref; U is the accumulated boundary displacement. */
-int pd_warm_features(pd_ctx* ctx, double U, double delta, double nn_ref, void* dev_x, void* stream);
+/* Features of the free nodes for a load increment (BF16 [N_int][16], 8
+ * features, 8 zeros): previous displacement / U (x, y), increment / U,
+ * damage, loaded-edge flag, and the history of the previous increment
+ * (pd_warm_record): its departure from proportionality per unit load (x, y,
+ * times 256) and the damage it added (zeros without a history).  U is the
+ * accumulated boundary displacement before the increment. */
+int pd_warm_features(pd_ctx* ctx, double U, double delta, void* dev_x, void* stream);
+/* The increment just solved becomes the history of the next prediction:
+ * dev_u_prev (2*N_int: x then y) and dev_dmg_prev (N_int) hold the free
+ * nodes' displacement and damage before it, U_prev the accumulated boundary
+ * displacement before it.  Stored in the context: per node
+ * ((u - u_prev) - u_prev delta / U_prev) / U_prev per component (the
+ * departure of the increment from the proportional, secant, one per unit
+ * load) and dmg - dmg_prev (the damage is brought up to date first).
+ * U_prev <= 0 clears the history. */
+int pd_warm_record(pd_ctx* ctx, double U_prev, double delta, const double* dev_u_prev, const double* dev_dmg_prev,
+                   void* stream);
 /* Candidate increments for pd_load_step (ncand = 2): dev_du[0 .. 2*N_int) =
  * u * delta / U + U * net(features), dev_du[2*N_int .. 4*N_int) = u * delta / U.
  * The skip term is the proportional (secant) increment, exact for a linear
  * response loaded proportionally from rest; the network predicts the
  * departure from proportionality per unit of accumulated boundary
- * displacement (the geometric nonlinearity of the bonds makes it grow with
- * the load: u = a U + b U^2 departs by b U delta per increment).
- * smooth_passes > 0 (bond-based contexts): the correction U * net is first
- * averaged that many times over each free node's intact family (prescribed
- * rows count as zero), which removes the node-to-node rounding noise of the
- * BF16 network that the residual amplifies. */
-int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, double nn_ref, int smooth_passes,
-                    double* dev_du, void* stream);
+ * displacement, from the local state and the previous increment's departure
+ * and damage (pd_warm_record); it is trained on converged states of
+ * loadings that include crack advances.  smooth_passes > 0 (bond-based
+ * contexts): the correction U * net is first averaged that many times over
+ * each free node's intact family (prescribed rows count as zero), which
+ * removes the node-to-node rounding noise of the BF16 network that the
+ * residual amplifies. */
+int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, int smooth_passes, double* dev_du,
+                    void* stream);
 
 /* ---- batches of specimens ----------------------------------------------- */
 /* No counterpart in the reference, which solves one plate per process.  A

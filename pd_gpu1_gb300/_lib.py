@@ -75,8 +75,9 @@ _SIGS = {
     "pd_mlp_train_step": (I32, [VP, VP, VP, I64, C.c_float, P(C.c_float), VP]),
     "pd_mlp_gemm": (I32, [VP, VP, I64, I64, I64, VP, I32, VP]),
     "pd_mlp_gemm_wait_check": (I32, [VP, VP, I64, I64, I64, VP, I32, C.c_longlong, I32, VP]),
-    "pd_warm_features": (I32, [VP, D, D, D, VP, VP]),
-    "pd_warm_predict": (I32, [VP, VP, D, D, D, I32, VP, VP]),
+    "pd_warm_features": (I32, [VP, D, D, VP, VP]),
+    "pd_warm_record": (I32, [VP, D, D, VP, VP, VP]),
+    "pd_warm_predict": (I32, [VP, VP, D, D, I32, VP, VP]),
     "pd_batch_create": (VP, [P(PDParams), P(PDSpecimen), I32, P(I32)]),
     "pd_batch_info": (I32, [VP, P(I32), P(I64), P(I64)]),
     "pd_batch_run_adr": (I32, [VP, I32, I32, D, VP]),

@@ -342,7 +342,8 @@ int pd_destroy(pd_ctx* c) {
         for (int a = 0; a < 3; a++)
             if (c->pos[b][a]) cudaFree(c->pos[b][a]);
     void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->node_c, c->partials, c->ticket, c->cn,
-                    c->red_out, c->res, c->cyl, c->NL, c->idist, c->fac, c->scr, c->w, c->e, c->fail};
+                    c->red_out, c->res, c->cyl, c->NL, c->idist, c->fac, c->scr, c->w, c->e, c->fail,
+                    c->warm_hist};
     for (void* q : ptrs)
         if (q) cudaFree(q);
     release_sell(c);

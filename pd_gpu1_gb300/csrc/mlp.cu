@@ -309,10 +309,15 @@ __global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ T,
     }
 }
 
-__global__ void k_features(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
-                           const double* __restrict__ ux, const double* __restrict__ uy,
-                           const double* __restrict__ dmg, const int* __restrict__ NN, double inv_u, double inc,
-                           double inv_hx, double inv_hy, double edge, double inv_nn, __nv_bfloat16* __restrict__ X) {
+// Features of the free nodes (see pd_warm_features).  hist (may be null):
+// the previous increment's departure from proportionality per unit load, x
+// then y (2 n), and its damage increase (n); kHistScale brings the departure
+// (of the order of 1e-3 on the warm-start plates) near one.
+constexpr double kHistScale = 256.0;
+__global__ void k_features(int64_t n, const double* __restrict__ y, const double* __restrict__ ux,
+                           const double* __restrict__ uy, const double* __restrict__ dmg,
+                           const double* __restrict__ hist, double inv_u, double inc, double edge,
+                           __nv_bfloat16* __restrict__ X) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         float f[kInPad];
         f[0] = (float)(ux[i] * inv_u);
@@ -320,11 +325,24 @@ __global__ void k_features(int64_t n, const double* __restrict__ x, const double
         f[2] = (float)inc;
         f[3] = (float)dmg[i];
         f[4] = fabs(y[i]) > edge ? 1.0f : 0.0f;
-        f[5] = (float)(x[i] * inv_hx);
-        f[6] = (float)(y[i] * inv_hy);
-        f[7] = (float)(NN[i] * inv_nn);
+        f[5] = hist ? (float)(hist[i] * kHistScale) : 0.0f;
+        f[6] = hist ? (float)(hist[n + i] * kHistScale) : 0.0f;
+        f[7] = hist ? (float)hist[2 * n + i] : 0.0f;
         for (int j = kIn; j < kInPad; j++) f[j] = 0.0f;
         for (int j = 0; j < kInPad; j++) X[i * kInPad + j] = __float2bfloat16_rn(f[j]);
+    }
+}
+
+// The history of a converged increment: its departure from proportionality
+// per unit load, ((u - up) - up delta / Up) / Up per component, and the
+// damage it added.
+__global__ void k_warm_record(int64_t n, const double* __restrict__ ux, const double* __restrict__ uy,
+                              const double* __restrict__ dmg, const double* __restrict__ up,
+                              const double* __restrict__ dmgp, double ratio, double inv_up, double* __restrict__ hist) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        hist[i] = ((ux[i] - up[i]) - up[i] * ratio) * inv_up;
+        hist[n + i] = ((uy[i] - up[n + i]) - up[n + i] * ratio) * inv_up;
+        hist[2 * n + i] = dmg[i] - dmgp[i];
     }
 }
 
@@ -338,8 +356,8 @@ __global__ void k_scale_out(int64_t n, const float* __restrict__ y, double U, do
                             const double* __restrict__ ux, const double* __restrict__ uy, double* __restrict__ du) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double sx = ux[i] * ratio, sy = uy[i] * ratio;
-        du[i] = fma(U, (double)y[i * kOut], sx);
-        du[n + i] = fma(U, (double)y[i * kOut + 1], sy);
+        du[i] = fma(U, (double)y[i * kOut] * (1.0 / kHistScale), sx);
+        du[n + i] = fma(U, (double)y[i * kOut + 1] * (1.0 / kHistScale), sy);
         du[2 * n + i] = sx;
         du[3 * n + i] = sy;
     }
@@ -348,8 +366,8 @@ __global__ void k_scale_out(int64_t n, const float* __restrict__ y, double U, do
 // The network's correction U * net of the free nodes (x components, then y).
 __global__ void k_correction(int64_t n, const float* __restrict__ y, double U, double* __restrict__ corr) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        corr[i] = U * (double)y[i * kOut];
-        corr[n + i] = U * (double)y[i * kOut + 1];
+        corr[i] = U * (double)y[i * kOut] * (1.0 / kHistScale);
+        corr[n + i] = U * (double)y[i * kOut + 1] * (1.0 / kHistScale);
     }
 }
 
@@ -716,25 +734,54 @@ int pd_mlp_train_step(pd_mlp* n, const void* dev_x, const float* dev_t, int64_t 
 //   2     load increment / U
 //   3     damage
 //   4     1 within one horizon of a loaded edge
-//   5, 6  x / (half width), y / (half height)
-//   7     family size / nn_ref (1 in the bulk, below 1 near surfaces and cracks)
-int pd_warm_features(pd_ctx* c, double U, double delta, double nn_ref, void* dev_x, void* stream) {
-    if (!c || !dev_x || !(U > 0.0) || !(nn_ref > 0.0) || c->p.dim != 2) return PD_ERR_ARG;
+//   5, 6  the previous increment's departure from proportionality per unit
+//         load (pd_warm_record), times kHistScale; 0 without a history
+//   7     the damage the previous increment added; 0 without a history
+int pd_warm_features(pd_ctx* c, double U, double delta, void* dev_x, void* stream) {
+    if (!c || !dev_x || !(U > 0.0) || c->p.dim != 2) return PD_ERR_ARG;
     cudaStream_t s = st(stream);
     const int64_t n = c->p.N_int;
-    const double hx = c->p.nx * c->p.dx / 2.0, hy = c->p.ny * c->p.dx / 2.0;
+    const double hy = c->p.ny * c->p.dx / 2.0;
     k_features<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
-        n, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_UX], c->nf[PD_F_UY], c->nf[PD_F_DMG], c->NN, 1.0 / U, delta / U,
-        1.0 / hx, 1.0 / hy, hy - c->p.delta, 1.0 / nn_ref, reinterpret_cast<__nv_bfloat16*>(dev_x));
+        n, c->nf[PD_F_Y], c->nf[PD_F_UX], c->nf[PD_F_UY], c->nf[PD_F_DMG], c->warm_hist, 1.0 / U, delta / U,
+        hy - c->p.delta, reinterpret_cast<__nv_bfloat16*>(dev_x));
     c->launches++;
     return cuda_err(c, cudaGetLastError(), "pd_warm_features");
+}
+
+// Record the increment just solved as the history of the next prediction:
+// dev_u_prev (2 N_int: x then y) and dev_dmg_prev (N_int) are the free nodes'
+// displacement and damage before it, U_prev the accumulated boundary
+// displacement before it.  U_prev <= 0 (no proportional reference yet)
+// clears the history.
+int pd_warm_record(pd_ctx* c, double U_prev, double delta, const double* dev_u_prev, const double* dev_dmg_prev,
+                   void* stream) {
+    if (!c || c->p.dim != 2) return PD_ERR_ARG;
+    if (!(U_prev > 0.0)) {
+        if (c->warm_hist) cudaFree(c->warm_hist);
+        c->warm_hist = nullptr;
+        return PD_OK;
+    }
+    if (!dev_u_prev || !dev_dmg_prev) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    const int64_t n = c->p.N_int;
+    if (!c->warm_hist && cudaMalloc(&c->warm_hist, 3 * n * sizeof(double)) != cudaSuccess) {
+        c->warm_hist = nullptr;
+        return set_err(c, PD_ERR_NOMEM, "warm-start history");
+    }
+    int rc = pd_damage(c, stream);
+    if (rc) return rc;
+    k_warm_record<<<(unsigned)std::min<int64_t>((n + 255) / 256, 4096), 256, 0, s>>>(
+        n, c->nf[PD_F_UX], c->nf[PD_F_UY], c->nf[PD_F_DMG], dev_u_prev, dev_dmg_prev, delta / U_prev, 1.0 / U_prev,
+        c->warm_hist);
+    c->launches++;
+    return cuda_err(c, cudaGetLastError(), "pd_warm_record");
 }
 
 // Candidate increments of the free nodes: features, forward pass, then
 // du = u * delta / U + U * output (x components, then y components), and the
 // skip term u * delta / U alone.
-int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref, int smooth_passes, double* dev_du,
-                    void* stream) {
+int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, int smooth_passes, double* dev_du, void* stream) {
     if (!c || !n || !dev_du || smooth_passes < 0) return PD_ERR_ARG;
     if (smooth_passes > 0 && (c->p.model != PD_MODEL_BOND || !c->family))
         return set_err(c, PD_ERR_STATE, "smoothing the correction needs a bond-based family");
@@ -747,7 +794,7 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, double nn_ref,
         cudaFreeAsync(x, s);
         return set_err(c, PD_ERR_NOMEM, "warm outputs");
     }
-    int rc = pd_warm_features(c, U, delta, nn_ref, x, s);
+    int rc = pd_warm_features(c, U, delta, x, s);
     const int64_t l0 = n->launches;
     if (!rc) rc = pd_mlp_forward(n, x, ni, y, s);
     c->launches += n->launches - l0;  // the network's kernels count as the context's

@@ -216,6 +216,7 @@ struct pd_ctx {
     int tune_chunked = 0;   // 1: contiguous slice runs per warp
     int tune_split = 1;     // warps sharing one slice's slots (2-D bond kernels)
     int layout_pref = pdg::LAYOUT_AUTO;  // bond-based SELL layout requested (pd_set_force_layout)
+    double* warm_hist = nullptr;  // [3 N_int] learned warm start: the previous increment's history (pd_warm_record)
 };
 
 namespace pdg {

@@ -9,15 +9,18 @@ increment ``delta * net(features)`` and is kept only when its residual is
 not larger than the plain start's, so the converged answer is the plain
 method's.  Features (``pd_warm_features``) and targets are normalised:
 features use the accumulated boundary displacement U of the previous
-increment.  The prediction is ``u * delta / U + U * net(features)``: a
+increment and the history of the increment before (its departure from
+proportionality and the damage it added, ``pd_warm_record``).  The
+prediction is ``u * delta / U + U * net(features)``: a
 skip term, the proportional (secant) increment, plus the network's output
 scaled by U (optionally smoothed over the bond family, ``smooth``), so the
 target of training is ``(du - u * delta / U) / U`` -- the departure from
 proportionality per unit of load, which the bonds' geometric nonlinearity
 keeps nearly constant along the loading (u = a U + b U^2 departs by
-b U delta per increment).  Training uses the increments before the first
-crack advance of each run; after a crack has grown the plate is outside what
-the network saw, and the residual rule decides: pd_load_step receives two
+b U delta per increment); consecutive increments depart alike away from a
+growing crack, which the history feature carries.  Training uses every
+increment of each run, crack advances included; the residual rule decides
+between the starts: pd_load_step receives two
 candidates, the network's prediction and the skip term alone; a candidate
 whose starting residual exceeds the plain start's is dropped, and of two
 admissible ones the start with the smaller residual is used (``probe`` > 0
@@ -117,11 +120,6 @@ class Net:
         return loss.value
 
 
-def nn_reference(eng):
-    """Bulk family size (the largest row of the free nodes)."""
-    return float(eng.get("NN")[: eng.p.N_int].max())
-
-
 def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1e-6, max_iters=400000,
                    check_every=100, keep=0.25, seed=0, start=0, probe=0, smooth=SMOOTH_PASSES):
     """Solve n_inc load increments on a set-up engine.
@@ -130,12 +128,12 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     pd_warm_predict, network + skip term and skip term alone, against the
     plain start; the admissible one with the smaller residual is used; net
     required); "network" / "secant" (one of the two alone, for ablations);
-    "extrapolate" (previous solution plus the previous increment: used to
-    generate training states quickly).  smooth: passes of family averaging
-    applied to the network's correction (pd_warm_predict).
-    collect: a list that receives (features, targets) device
-    tensors of a random ``keep`` fraction of the free nodes per increment,
-    up to the first increment in which a crack advances.
+    "extrapolate" (previous solution plus the previous increment).  Every
+    solved increment is recorded as the history of the next prediction
+    (pd_warm_record).  smooth: passes of family averaging applied to the
+    network's correction (pd_warm_predict).  collect: a list that receives
+    (features, targets) device tensors of a random ``keep`` fraction of the
+    free nodes of every increment with U > 0, crack advances included.
     Returns the per-increment statistics of pd_load_step."""
     import torch
 
@@ -143,30 +141,24 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     p = eng.p
     ni = p.N_int
     delta = meta["delta"]
-    nnref = nn_reference(eng)
     rng = np.random.default_rng(seed)
     du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")  # two candidates
     X = torch.zeros((ni, 16), dtype=torch.bfloat16, device="cuda") if collect is not None else None
     prev = None
-    grown = False  # a crack has advanced in this run
     out = []
     for k in range(start, start + n_inc):
         U = k * delta  # accumulated boundary displacement before this increment
         ptr = None
-        u0 = None
-        if U > 0.0 and (mode in ("learned", "network", "secant") or collect is not None):
-            eng.damage()
+        eng.damage()
+        u0 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+        d0 = eng.get("DMG")[:ni].copy()
         if U > 0.0 and collect is not None:
-            check(L.pd_warm_features(eng.ctx, U, delta, nnref, X.data_ptr(), eng.stream), eng.ctx,
-                  "pd_warm_features")
-        if collect is not None or mode == "extrapolate":
-            u0 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+            check(L.pd_warm_features(eng.ctx, U, delta, X.data_ptr(), eng.stream), eng.ctx, "pd_warm_features")
         t0 = time.perf_counter()
         ncand = 1
-        if collect is not None:
-            broken0 = int((eng.get("FAIL") == 0).sum())
+        broken0 = int((eng.get("FAIL") == 0).sum())
         if mode in ("learned", "network", "secant") and U > 0.0:
-            check(L.pd_warm_predict(eng.ctx, net.h, U, delta, nnref, smooth, du.data_ptr(), eng.stream), eng.ctx,
+            check(L.pd_warm_predict(eng.ctx, net.h, U, delta, smooth, du.data_ptr(), eng.stream), eng.ctx,
                   "pd_warm_predict")
             ptr = du.data_ptr()  # "network": the network's start against the plain start
             if mode == "learned":  # both candidates
@@ -179,19 +171,21 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
         st = eng.load_step(delta, ptr, tol, max_iters, check_every, ncand, probe if ncand > 1 else 0)
         st["wall_ms"] = (time.perf_counter() - t0) * 1e3
         st["increment"] = k
-        if u0 is not None:
-            u1 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
-            prev = u1 - u0
-            if collect is not None and U > 0.0:
-                tt = (prev - u0 * (delta / U)) / U  # departure from proportionality per unit load
-                st["max_target"] = float(np.abs(tt).max())
-                st["advanced"] = int((eng.get("FAIL") == 0).sum()) - broken0  # bonds broken in the increment
-                grown = grown or st["advanced"] > 0
-                if not grown:
-                    idx = np.sort(rng.choice(ni, max(1, int(keep * ni)), replace=False))
-                    t = np.stack([tt[idx], tt[ni + idx]], axis=1).astype(np.float32)
-                    ii = torch.from_numpy(idx).cuda()
-                    collect.append((X.index_select(0, ii).clone(), torch.from_numpy(t).cuda()))
+        st["advanced"] = int((eng.get("FAIL") == 0).sum()) - broken0  # bonds broken in the increment
+        u1 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+        prev = u1 - u0
+        if U > 0.0 and collect is not None:
+            tt = (prev - u0 * (delta / U)) / U  # departure from proportionality per unit load
+            st["max_target"] = float(np.abs(tt).max())
+            idx = np.sort(rng.choice(ni, max(1, int(keep * ni)), replace=False))
+            t = np.stack([tt[idx], tt[ni + idx]], axis=1).astype(np.float32)
+            ii = torch.from_numpy(idx).cuda()
+            collect.append((X.index_select(0, ii).clone(), torch.from_numpy(t).cuda()))
+        # this increment is the history of the next prediction
+        up = torch.from_numpy(u0).cuda()
+        dp = torch.from_numpy(d0).cuda()
+        check(L.pd_warm_record(eng.ctx, U, delta, up.data_ptr(), dp.data_ptr(), eng.stream), eng.ctx,
+              "pd_warm_record")
         out.append(st)
     return out
 
@@ -216,14 +210,22 @@ def train(X, T, steps=3000, batch=16384, lr=2e-3, seed=0, log=None):
     return net
 
 
-TRAIN_RUNS = [  # (scale, crack fraction, seed): 100k-1M-node plates of the same set-up
-    (0.32, 0.20, 1), (0.32, 0.15, 2), (0.32, 0.25, 3), (0.5, 0.20, 4),
+# (scale, crack fraction, seed): 41k-104k-node plates of the same set-up,
+# loaded through their first crack advances within 60 increments
+TRAIN_RUNS = [
+    (0.2, 0.15, 1), (0.2, 0.2, 2), (0.2, 0.25, 3), (0.25, 0.2, 4), (0.32, 0.2, 5),
 ]
+# the network's outputs and history features are the departure per unit load
+# times this factor (kHistScale of csrc/mlp.cu)
+OUT_SCALE = 256.0
 
 
-def generate(runs=TRAIN_RUNS, n_inc=200, keep=0.25, tol=1e-6, log=print):
-    """Converged states of seeded load-stepping runs (ADR to tol) -> (X, T)
-    device tensors."""
+def generate(runs=TRAIN_RUNS, n_inc=60, keep=0.25, tol=1e-8, log=print):
+    """Converged states of seeded load-stepping runs -> (X, T) device tensors.
+    Every increment starts from the previous solution (the plain method) and
+    runs ADR to tol, crack advances included, so the targets are the plain
+    method's converged increments; the features carry the history that
+    pd_warm_record keeps."""
     import torch
 
     data = []
@@ -232,18 +234,18 @@ def generate(runs=TRAIN_RUNS, n_inc=200, keep=0.25, tol=1e-6, log=print):
         with Engine(p) as eng:
             setup(eng)
             t0 = time.perf_counter()
-            st = run_increments(eng, meta, n_inc, mode="extrapolate", collect=data, keep=keep, seed=seed, tol=tol)
+            n0 = len(data)
+            st = run_increments(eng, meta, n_inc, mode="plain", collect=data, keep=keep, seed=seed, tol=tol)
             broken = int((eng.get("FAIL") == 0).sum())
-        jumps = [(s["increment"], s["iters"], s.get("advanced", 0), round(s.get("max_target", 0.0), 2))
-                 for s in st if s.get("advanced", 0) > 0]
+        T = torch.cat([d[1] for d in data[n0:]])
+        Xh = torch.cat([d[0][:, 5:7].float() for d in data[n0:]])
         log(json.dumps({"run": [scale, frac, seed], "nodes": p.N, "increments": n_inc,
                         "iters": int(sum(s["iters"] for s in st)), "max_iters": int(max(s["iters"] for s in st)),
                         "seconds": round(time.perf_counter() - t0, 1), "broken_bonds": broken,
-                        "left_out": jumps[:20], "n_left_out": len(jumps),
-                        "max_target_kept": round(max([s.get("max_target", 0.0) for s in st
-                                                      if s.get("advanced", 1) == 0] + [0.0]), 3)}))
+                        "advances": [(s["increment"], s["iters"], s["advanced"]) for s in st if s["advanced"] > 0],
+                        "target_std": float(T.std()) * OUT_SCALE, "history_std": float(Xh.std())}))
     X = torch.cat([d[0] for d in data])
-    T = torch.cat([d[1] for d in data])
+    T = torch.cat([d[1] for d in data]) * OUT_SCALE
     return X, T
 
 
@@ -253,7 +255,7 @@ def main():
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--steps", type=int, default=3000)
     ap.add_argument("--increments", type=int, default=60)
-    ap.add_argument("--tol", type=float, default=1e-6, help="ADR tolerance of the training runs")
+    ap.add_argument("--tol", type=float, default=1e-8, help="ADR tolerance of the training runs")
     args = ap.parse_args()
     t0 = time.perf_counter()
     X, T = generate(n_inc=args.increments, tol=args.tol)
