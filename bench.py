@@ -771,13 +771,17 @@ def batch_arm(args):
 
 
 # ---- learned ADR warm start ---------------------------------------------------------------------
-def warm_arm(args):
+def warm_measure(scale, K, W, smooth, e2e=True, with_clocks=True):
     """ADR wall-time per load increment to a 1e-6 relative residual on the
-    1M-node warm-start plate: plain start (previous solution) against the
-    learned start (network shipped in pd_gpu1_gb300/data).  Increments
-    0..W-1 are solved first (untimed: increment 0 has no history); each timed
-    increment W+j is then solved twice from the same converged state (a
-    snapshot), once from each start, and the learned run's state carries on."""
+    warm-start plate (1M nodes at scale 1): plain start (previous solution),
+    the skip term alone (proportional, secant, increment) and the learned
+    start (network shipped in pd_gpu1_gb300/data, offered beside the skip
+    term; the smaller starting residual wins).  Increments 0..W-1 are solved
+    first with the learned start (untimed: increment 0 has no history); each
+    timed increment W+j is then solved three times from the same converged
+    state (a snapshot): plain and skip-only leave the increment history alone,
+    the learned run records it and its state carries on.  Returns the dict of
+    the JSON line (without the common keys)."""
     import os
     import tempfile
 
@@ -788,6 +792,100 @@ def warm_arm(args):
     from pd_gpu1_gb300._abi import FIELD
     from pd_gpu1_gb300._lib import lib
 
+    L = lib()
+    p, setup, meta = presets.build_warm_start_plate(scale=scale)
+    net = warm.Net.load()
+    snap_dir = tempfile.mkdtemp()
+    snap = os.path.join(snap_dir, "state.snap")
+    snap_e2e = os.path.join(snap_dir, "start.snap")
+    clocks = ClockSampler(torch.cuda.current_device()) if with_clocks else None
+    rows = []
+    learned_launches = 0  # kernels of the timed (learned-start) increments
+    with E.Engine(p) as eng:
+        setup(eng)
+        B = int(eng.get("ROWPTR")[p.N_int])
+        last_pre = {}
+        pre = warm.run_increments(eng, meta, W, mode="learned", net=net, smooth=smooth, last=last_pre)
+        eng.snapshot_save(snap_e2e)  # the state before the timed increments, replayed for e2e
+        if clocks:
+            clocks.start()
+        for j in range(K):
+            eng.snapshot_save(snap)
+            plain = warm.run_increments(eng, meta, 1, mode="plain", start=W + j, record=False)[0]
+            eng.snapshot_load(snap)
+            skip = warm.run_increments(eng, meta, 1, mode="secant", net=net, start=W + j, record=False)[0]
+            eng.snapshot_load(snap)
+            l0 = eng.kernel_launches
+            learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=smooth)[0]
+            learned_launches += eng.kernel_launches - l0
+            rows.append((plain, skip, learned))
+        clk = clocks.stop() if clocks else None
+        # the network's inference alone (features, four tcgen05 products, candidates)
+        du = torch.zeros(4 * p.N_int, dtype=torch.float64, device="cuda")
+        eng.damage()
+        U = (W + K) * meta["delta"]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(5):
+            L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], smooth, du.data_ptr(), None)
+        e1.record()
+        torch.cuda.synchronize()
+        infer_ms = e0.elapsed_time(e1) / 5
+        e2e_ms = None
+        if e2e:
+            # the same timed increments again, from the same state and history,
+            # through the C ABI with the displacement field read back to pinned
+            # host memory after each one (an increment's input is its load step)
+            eng.snapshot_load(snap_e2e)
+            warm.restore_history(eng, meta, last_pre)
+            n = p.N
+            pin = torch.zeros(n, dtype=torch.float64).pin_memory()
+            t0 = time.perf_counter()
+            for j in range(K):
+                warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=smooth)
+                eng._c(L.pd_get_field(eng.ctx, FIELD["UY"], pin.data_ptr(), n, None), "pd_get_field")
+            e2e_ms = (time.perf_counter() - t0) * 1e3 / K
+    os.remove(snap)
+    os.remove(snap_e2e)
+    os.rmdir(snap_dir)
+    plain_ms = np.array([r[0]["ms"] for r in rows])
+    skip_ms = np.array([r[1]["ms"] for r in rows])
+    learned_ms = np.array([r[2]["ms"] for r in rows])
+    flops = 2.0 * p.N_int * (16 * 128 + 2 * 128 * 128 + 128 * 16)
+    peaks, peak_kind = measured_peaks()
+    return {
+        "value": float(learned_ms.mean()), "unit": "ms", "steps": K, "warmup": W,
+        "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "increment_m": meta["delta"],
+                   "tol": 1e-6, "timed_increments": list(range(W, W + K)), "smooth_passes": smooth,
+                   "untimed_increments_first": W, "untimed_iters": [s["iters"] for s in pre],
+                   "untimed_candidate_used": [s["warm_used"] for s in pre]},
+        "plain": {"ms_per_increment": float(plain_ms.mean()), "iters": [r[0]["iters"] for r in rows]},
+        "skip_only": {"ms_per_increment": float(skip_ms.mean()), "iters": [r[1]["iters"] for r in rows],
+                      "what": "the proportional (secant) increment alone, against the plain start"},
+        "learned": {"ms_per_increment": float(learned_ms.mean()), "iters": [r[2]["iters"] for r in rows],
+                    "candidate_used": [r[2]["warm_used"] for r in rows],
+                    "candidates": "0 plain, 1 network (skip term + network correction), 2 skip term alone",
+                    "r_start_over_r_plain": [r[2]["r_start"] / r[2]["r_plain"] for r in rows],
+                    "bonds_broken": [r[2]["advanced"] for r in rows]},
+        "speedup_vs_plain": float(plain_ms.mean() / learned_ms.mean()),
+        "speedup_vs_skip_only": float(skip_ms.mean() / learned_ms.mean()),
+        "roofline": {"bound": "tensor", "kernel": "k_gemm (network inference, all four layers)",
+                     "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks.get("bf16_tflops"),
+                     "unit": "TFLOP/s", "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1.0),
+                     "traffic": None, "peak_source": peak_kind, "inference_ms": infer_ms,
+                     "note": "inference is <1 % of an increment; an increment is bound by the ADR force kernel"},
+        "e2e": None if e2e_ms is None else {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 0,
+                                            "d2h_bytes_per_step": p.N * 8},
+        "gpu_launches": learned_launches // max(K, 1),
+        "gpu_launches_what": "per timed increment (ADR steps in CUDA graphs, features, network, candidates)",
+        "clocks": clk,
+    }
+
+
+def warm_arm(args):
+    """--workload warm_start: warm_measure on the 1M-node plate as its own line."""
+    import torch
+
     rank, world, local = rank_info()
     if args.impl == "reference":
         if rank == 0:
@@ -796,86 +894,63 @@ def warm_arm(args):
                               "--workload plate_tensile and batch"}), flush=True)
         return 0
     torch.cuda.set_device(local)
-    L = lib()
-    p, setup, meta = presets.build_warm_start_plate(scale=args.scale)
-    net = warm.Net.load()
-    K, W = args.increments, args.warm_increments
-    snap_dir = tempfile.mkdtemp()
-    snap = os.path.join(snap_dir, "state.snap")
-    snap_e2e = os.path.join(snap_dir, "start.snap")
-    clocks = ClockSampler(torch.cuda.current_device())
-    rows = []
-    learned_launches = 0  # kernels of the timed (learned-start) increments
-    with E.Engine(p) as eng:
-        setup(eng)
-        B = int(eng.get("ROWPTR")[p.N_int])
-        pre = warm.run_increments(eng, meta, W, mode="learned", net=net, smooth=args.smooth)
-        eng.snapshot_save(snap_e2e)  # the state before the timed increments, replayed for e2e
-        clocks.start()
-        for j in range(K):
-            eng.snapshot_save(snap)
-            plain = warm.run_increments(eng, meta, 1, mode="plain", start=W + j)[0]
-            eng.snapshot_load(snap)
-            l0 = eng.kernel_launches
-            learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=args.smooth)[0]
-            learned_launches += eng.kernel_launches - l0
-            rows.append((plain, learned))
-        clk = clocks.stop()
-        # the network's inference alone (features, four tcgen05 products, candidates)
-        du = torch.zeros(4 * p.N_int, dtype=torch.float64, device="cuda")
-        eng.damage()
-        U = (W + K) * meta["delta"]
-        nnref = warm.nn_reference(eng)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(5):
-            L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], nnref, args.smooth, du.data_ptr(), None)
-        e1.record()
-        torch.cuda.synchronize()
-        infer_ms = e0.elapsed_time(e1) / 5
-        # e2e: the same timed increments again, from the same state, through the
-        # C ABI with the displacement field read back to pinned host memory after
-        # each one (an increment's input is its load step, a scalar argument)
-        eng.snapshot_load(snap_e2e)
-        n = p.N
-        pin = torch.zeros(n, dtype=torch.float64).pin_memory()
-        t0 = time.perf_counter()
-        for j in range(K):
-            warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=args.smooth)
-            eng._c(L.pd_get_field(eng.ctx, FIELD["UY"], pin.data_ptr(), n, None), "pd_get_field")
-        e2e_ms = (time.perf_counter() - t0) * 1e3 / K
-    os.remove(snap)
-    os.remove(snap_e2e)
-    plain_ms = np.array([r[0]["ms"] for r in rows])
-    learned_ms = np.array([r[1]["ms"] for r in rows])
-    flops = 2.0 * p.N_int * (16 * 128 + 2 * 128 * 128 + 128 * 16)
-    peaks, peak_kind = measured_peaks()
-    line = {
-        "metric": "ADR wall-time to a 1e-6 relative residual per load increment, learned start",
-        "value": float(learned_ms.mean()), "unit": "ms", "n_gpus": world, "steps": K, "warmup": W,
-        "ms_per_step": float(learned_ms.mean()), "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64 (solver); bf16 x bf16 -> f32 (network)", "data": "synthetic (deterministic lattice)",
-        "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "increment_m": meta["delta"],
-                   "tol": 1e-6, "timed_increments": list(range(W, W + K)),
-                   "untimed_increments_first": W, "untimed_iters": [s["iters"] for s in pre]},
-        "plain": {"ms_per_increment": float(plain_ms.mean()), "iters": [r[0]["iters"] for r in rows]},
-        "learned": {"ms_per_increment": float(learned_ms.mean()), "iters": [r[1]["iters"] for r in rows],
-                    "candidate_used": [r[1]["warm_used"] for r in rows],
-                    "r_start_over_r_plain": [r[1]["r_start"] / r[1]["r_plain"] for r in rows]},
-        "speedup_vs_plain": float(plain_ms.mean() / learned_ms.mean()),
-        "roofline": {"bound": "tensor", "kernel": "k_gemm (network inference, all four layers)",
-                     "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks.get("bf16_tflops"),
-                     "unit": "TFLOP/s", "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1.0),
-                     "traffic": None, "peak_source": peak_kind, "inference_ms": infer_ms,
-                     "note": "inference is <1 % of an increment; an increment is bound by the ADR force kernel"},
-        "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": p.N * 8},
-        "gpu_launches": learned_launches // K, "gpu_launches_what": "per timed increment (ADR steps in CUDA graphs, "
-                                                                   "features, network, candidates)",
-        "clocks": clk, "cpu_baseline": None,
-    }
+    m = warm_measure(args.scale, args.increments, args.warm_increments, args.smooth)
+    line = {"metric": "ADR wall-time to a 1e-6 relative residual per load increment, learned start",
+            "value": m.pop("value"), "unit": m.pop("unit"), "n_gpus": world, "steps": m.pop("steps"),
+            "warmup": m.pop("warmup"), "ms_per_step": None, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64 (solver); bf16 x bf16 -> f32 (network)",
+            "data": "synthetic (deterministic lattice)", "cpu_baseline": None}
+    line["ms_per_step"] = line["value"]
+    line.update(m)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def batch_block(steps, warmup, count=256):
+    """The batch workload (256 seeded uneven plates, ADR) as a block
+    of the default line: set-up, the autotuned launch shape, warmup + steps
+    ADR steps timed with CUDA events on the launch stream (batch_arm gives the
+    full line with its comparisons)."""
+    import torch
+
+    from pd_gpu1_gb300 import engine as E
+    from pd_gpu1_gb300 import presets
+
+    base, specs, meta = presets.build_batch(count=count, nt=steps)
+    stream = torch.cuda.Stream()
+    t0 = time.perf_counter()
+    with torch.cuda.stream(stream):
+        bat = E.Batch(base, specs, stream=stream.cuda_stream)
+        bat.sync()
+    setup_s = time.perf_counter() - t0
+    p = bat.p
+    B = int(bat.get("ROWPTR")[p.N_int])
+    with torch.cuda.stream(stream):
+        tuned = bat.autotune(reps=5)
+        bat.run_adr(0, warmup, meta["load"])
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    with torch.cuda.stream(stream):
+        bat.run_adr(warmup, steps, meta["load"])
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    with torch.cuda.stream(stream):
+        kern_ms, step_ms = bat.profile_steps(0, warmup + steps, min(50, steps), meta["load"])
+    torch.cuda.synchronize()
+    layout = bat.force_layout()
+    bat.close()
+    return {"metric": "bond-updates/s", "value": B * steps / (ms * 1e-3), "unit": "bond-updates/s",
+            "steps": steps, "warmup": warmup, "ms_per_step": ms / steps,
+            "config": {"workload": meta["workload"], "specimens": len(specs), "seed": meta["seed"], "nodes": p.N,
+                       "bonds": B, "setup_s": setup_s, "force_layout": layout,
+                       "launch": {"block": tuned[0], "chunked": tuned[1], "waves": tuned[2], "split": tuned[3]}},
+            "kernel": "k_bond_compact<EPI_ADR>" if layout == "compact" else "k_bond_force<2, EPI_ADR>",
+            "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / step_ms,
+            "what": "bench.py --workload batch gives this workload's own line with the one-plate-after-another "
+                    "and reference-kernel comparisons"}
 
 
 # ----------------------------------------------------------------------------------------------
@@ -1054,6 +1129,16 @@ def gb300_arm(args):
                "sample": f"{steps} time steps of the same {p.N}-node plate ({secs:.1f} s of host time), "
                          f"the oracle's OpenMP loops"}
 
+    # the other two workloads of the headline metric, as blocks of the same line:
+    # the second half of the metric (ADR wall-time to a 1e-6 residual, learned
+    # start against plain and skip-only starts) and the batch of uneven plates
+    extras = {}
+    if rank == 0 and world == 1 and not args.no_extras and meta["workload"].startswith("crack_branching"):
+        eng.close()
+        eng = None
+        extras["adr_warm_start"] = warm_measure(1.0, 2, 10, args.smooth, e2e=False)
+        extras["batch"] = batch_block(200, 5)
+
     if rank == 0:
         line = {
             "metric": "bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": world,
@@ -1076,8 +1161,10 @@ def gb300_arm(args):
                          "fp64": fp64_block(p.model, p.dim, B, kern_ms, gfma.value)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk, "reference_cuda": ref_cuda,
         }
+        line.update(extras)
         print(json.dumps(line), flush=True)
-    eng.close()
+    if eng is not None:
+        eng.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
@@ -1101,13 +1188,19 @@ def main():
     ap.add_argument("--seq-steps", type=int, default=100, help="batch workload: steps per plate when run one "
                                                                 "after another")
     ap.add_argument("--increments", type=int, default=3, help="warm_start workload: timed load increments")
-    ap.add_argument("--smooth", type=int, default=0, help="warm_start workload: family-averaging passes of the "
+    ap.add_argument("--smooth", type=int, default=None, help="warm_start workload: family-averaging passes of the "
                                                            "network's correction")
     ap.add_argument("--warm-increments", type=int, default=10, help="warm_start workload: increments solved "
                                                                      "before the timed ones")
+    ap.add_argument("--no-extras", action="store_true", help="default workload: leave out the batch and "
+                                                                  "learned-warm-start blocks of the line")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.smooth is None:
+        from pd_gpu1_gb300.warm import SMOOTH_PASSES
+
+        args.smooth = SMOOTH_PASSES
     if args.steps is None:
         args.steps = {"crack_branching": 1800, "plate_tensile": 1000, "kalthoff_winkler": 1350,
                       "kalthoff_winkler_bond": 1350,

@@ -346,18 +346,22 @@ __global__ void k_warm_record(int64_t n, const double* __restrict__ ux, const do
     }
 }
 
-// du = u * (delta / U) + U * net: the skip term is the proportional (secant)
-// increment, added in FP64; the network predicts the departure from
-// proportionality per unit of accumulated boundary displacement (for a
-// response u = a U + b U^2 the departure of an increment is 2 b U delta - b U delta
-// = b U delta, i.e. U * (b delta): a load-independent target).  The skip term
-// alone is written as the second candidate.
+// Candidates of the free nodes: du = u (delta / U) + U (h + net / kHistScale),
+// the skip term (the proportional, secant, increment) plus the previous
+// increment's departure from proportionality per unit load h (zero without a
+// history) and the network's correction of it; the skip term alone is
+// written as the second candidate.  The network predicts how the departure
+// changes from one increment to the next, so its output, and with it the
+// BF16 network's node-to-node rounding noise, is a small correction on top of
+// smooth FP64 terms.
 __global__ void k_scale_out(int64_t n, const float* __restrict__ y, double U, double ratio,
-                            const double* __restrict__ ux, const double* __restrict__ uy, double* __restrict__ du) {
+                            const double* __restrict__ ux, const double* __restrict__ uy,
+                            const double* __restrict__ hist, double* __restrict__ du) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double sx = ux[i] * ratio, sy = uy[i] * ratio;
-        du[i] = fma(U, (double)y[i * kOut] * (1.0 / kHistScale), sx);
-        du[n + i] = fma(U, (double)y[i * kOut + 1] * (1.0 / kHistScale), sy);
+        const double hx = hist ? hist[i] : 0.0, hy = hist ? hist[n + i] : 0.0;
+        du[i] = fma(U, hx + (double)y[i * kOut] * (1.0 / kHistScale), sx);
+        du[n + i] = fma(U, hy + (double)y[i * kOut + 1] * (1.0 / kHistScale), sy);
         du[2 * n + i] = sx;
         du[3 * n + i] = sy;
     }
@@ -410,12 +414,14 @@ __global__ void k_smooth(int64_t nslices, int64_t n, const int* __restrict__ wid
 
 // Candidates from a smoothed correction: the skip term u * delta / U plus
 // the correction, and the skip term alone.
-__global__ void k_combine(int64_t n, const double* __restrict__ corr, double ratio, const double* __restrict__ ux,
-                          const double* __restrict__ uy, double* __restrict__ du) {
+__global__ void k_combine(int64_t n, const double* __restrict__ corr, double U, double ratio,
+                          const double* __restrict__ ux, const double* __restrict__ uy, const double* __restrict__ hist,
+                          double* __restrict__ du) {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const double sx = ux[i] * ratio, sy = uy[i] * ratio;
-        du[i] = sx + corr[i];
-        du[n + i] = sy + corr[n + i];
+        const double hx = hist ? hist[i] : 0.0, hy = hist ? hist[n + i] : 0.0;
+        du[i] = fma(U, hx, sx) + corr[i];
+        du[n + i] = fma(U, hy, sy) + corr[n + i];
         du[2 * n + i] = sx;
         du[3 * n + i] = sy;
     }
@@ -800,7 +806,7 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, int smooth_pas
     c->launches += n->launches - l0;  // the network's kernels count as the context's
     const unsigned g = (unsigned)std::min<int64_t>((ni + 255) / 256, 4096);
     if (!rc && smooth_passes == 0) {
-        k_scale_out<<<g, 256, 0, s>>>(ni, y, U, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], dev_du);
+        k_scale_out<<<g, 256, 0, s>>>(ni, y, U, delta / U, c->nf[PD_F_UX], c->nf[PD_F_UY], c->warm_hist, dev_du);
         c->launches++;
         rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
     } else if (!rc) {
@@ -821,8 +827,8 @@ int pd_warm_predict(pd_ctx* c, pd_mlp* n, double U, double delta, int smooth_pas
                 k_smooth<<<gs, 256, 0, s>>>(ns, ni, S.width, S.base, S.fbase, cols, stride, S.bits, in, out);
                 c->launches++;
             }
-            k_combine<<<g, 256, 0, s>>>(ni, cb + (smooth_passes & 1) * 2 * ni, delta / U, c->nf[PD_F_UX],
-                                        c->nf[PD_F_UY], dev_du);
+            k_combine<<<g, 256, 0, s>>>(ni, cb + (smooth_passes & 1) * 2 * ni, U, delta / U, c->nf[PD_F_UX],
+                                        c->nf[PD_F_UY], c->warm_hist, dev_du);
             c->launches++;
             rc = cuda_err(c, cudaGetLastError(), "pd_warm_predict");
             cudaFreeAsync(cb, s);

@@ -121,7 +121,8 @@ class Net:
 
 
 def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1e-6, max_iters=400000,
-                   check_every=100, keep=0.25, seed=0, start=0, probe=0, smooth=SMOOTH_PASSES):
+                   check_every=100, keep=0.25, seed=0, start=0, probe=0, smooth=SMOOTH_PASSES, record=True,
+                   last=None):
     """Solve n_inc load increments on a set-up engine.
 
     mode: "plain" (previous solution); "learned" (the two candidates of
@@ -134,6 +135,10 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     network's correction (pd_warm_predict).  collect: a list that receives
     (features, targets) device tensors of a random ``keep`` fraction of the
     free nodes of every increment with U > 0, crack advances included.
+    record=False leaves the context's history as it was (a comparison run
+    from a snapshot that another run continues from); last: a dict that
+    receives the state before the last increment (u0, d0, U), from which
+    restore_history rebuilds that increment's history after a snapshot load.
     Returns the per-increment statistics of pd_load_step."""
     import torch
 
@@ -145,6 +150,7 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")  # two candidates
     X = torch.zeros((ni, 16), dtype=torch.bfloat16, device="cuda") if collect is not None else None
     prev = None
+    hist = None  # the departure recorded as the history of this increment (host copy), None: no history
     out = []
     for k in range(start, start + n_inc):
         U = k * delta  # accumulated boundary displacement before this increment
@@ -174,20 +180,53 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
         st["advanced"] = int((eng.get("FAIL") == 0).sum()) - broken0  # bonds broken in the increment
         u1 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
         prev = u1 - u0
-        if U > 0.0 and collect is not None:
-            tt = (prev - u0 * (delta / U)) / U  # departure from proportionality per unit load
-            st["max_target"] = float(np.abs(tt).max())
+        tt = (prev - u0 * (delta / U)) / U if U > 0.0 else None  # departure from proportionality per unit load
+        if tt is not None and collect is not None and st["advanced"] == 0:
+            # target: the change of the departure from the recorded history (the
+            # network corrects the history term); increments in which the crack
+            # advanced are left out (their jump is not predictable from the state)
+            dt = tt - hist if hist is not None else tt
+            st["max_target"] = float(np.abs(dt).max())
             idx = np.sort(rng.choice(ni, max(1, int(keep * ni)), replace=False))
-            t = np.stack([tt[idx], tt[ni + idx]], axis=1).astype(np.float32)
+            t = np.stack([dt[idx], dt[ni + idx]], axis=1).astype(np.float32)
             ii = torch.from_numpy(idx).cuda()
             collect.append((X.index_select(0, ii).clone(), torch.from_numpy(t).cuda()))
-        # this increment is the history of the next prediction
-        up = torch.from_numpy(u0).cuda()
-        dp = torch.from_numpy(d0).cuda()
-        check(L.pd_warm_record(eng.ctx, U, delta, up.data_ptr(), dp.data_ptr(), eng.stream), eng.ctx,
-              "pd_warm_record")
+        # this increment is the history of the next prediction, unless the crack
+        # advanced in it (its departure is that jump, which the next increment does
+        # not repeat) or it has no proportional reference (U = 0)
+        if record:
+            if tt is not None and st["advanced"] == 0:
+                record_history(eng, U, delta, u0, d0)
+                hist = tt
+            else:
+                check(L.pd_warm_record(eng.ctx, 0.0, delta, None, None, eng.stream), eng.ctx, "pd_warm_record")
+                hist = None
+        if last is not None:
+            last.update(u0=u0, d0=d0, U=U if (tt is not None and st["advanced"] == 0) else 0.0)
         out.append(st)
     return out
+
+
+def record_history(eng, U_prev, delta, u_prev, dmg_prev):
+    """pd_warm_record from host arrays: the increment that led from (u_prev,
+    dmg_prev) at accumulated boundary displacement U_prev to the context's
+    current state."""
+    import torch
+
+    up = torch.from_numpy(np.ascontiguousarray(u_prev, dtype=np.float64)).cuda()
+    dp = torch.from_numpy(np.ascontiguousarray(dmg_prev, dtype=np.float64)).cuda()
+    check(lib().pd_warm_record(eng.ctx, U_prev, delta, up.data_ptr(), dp.data_ptr(), eng.stream), eng.ctx,
+          "pd_warm_record")
+
+
+def restore_history(eng, meta, last):
+    """The history of the increment described by ``last`` (run_increments),
+    for a context whose state was just restored to the end of that increment
+    (none when that increment recorded none)."""
+    if last["U"] > 0.0:
+        record_history(eng, last["U"], meta["delta"], last["u0"], last["d0"])
+    else:
+        check(lib().pd_warm_record(eng.ctx, 0.0, meta["delta"], None, None, eng.stream), eng.ctx, "pd_warm_record")
 
 
 def train(X, T, steps=3000, batch=16384, lr=2e-3, seed=0, log=None):
@@ -223,9 +262,10 @@ OUT_SCALE = 256.0
 def generate(runs=TRAIN_RUNS, n_inc=60, keep=0.25, tol=1e-8, log=print):
     """Converged states of seeded load-stepping runs -> (X, T) device tensors.
     Every increment starts from the previous solution (the plain method) and
-    runs ADR to tol, crack advances included, so the targets are the plain
-    method's converged increments; the features carry the history that
-    pd_warm_record keeps."""
+    runs ADR to tol, through the crack's advances, so the targets are the
+    plain method's converged increments: the change of the departure from
+    proportionality from the recorded history (run_increments).  The features
+    carry the history that pd_warm_record keeps."""
     import torch
 
     data = []
