@@ -247,9 +247,11 @@ struct BondOut {
 
 // The force contribution of one 2-D bond from its exact offsets eta (pairs),
 // its offset class T and its record values (dl, k2 / 2 as a pair).
-PD_BT_HD BondOut bond2(const f2 eta[2], const Tpl& T, float dl, f2 k2half) {
-    BondOut o;
-    f2 w[2], v[2];
+// The stretch of one 2-D bond from its exact offsets eta (pairs), its
+// offset class T and dl = l0 - l0t: the bond vector W = xf + eta, 1/L and the
+// extension e = L - l0, all as pairs.
+PD_BT_HD void stretch2(const f2 eta[2], const Tpl& T, float dl, f2 w[2], f2& y, f2& e) {
+    f2 v[2];
     float m[2], lo[2];
 #if defined(__CUDACC__)
 #pragma unroll
@@ -262,9 +264,9 @@ PD_BT_HD BondOut bond2(const f2 eta[2], const Tpl& T, float dl, f2 k2half) {
         v[a] = f2{s.h, s.l + eta[a].l};
         // eta_a V_a: exact product of the high parts, cross terms in the low part
         m[a] = eta[a].h * v[a].h;
-        float e = fmaf(eta[a].h, v[a].h, -m[a]);
-        e = fmaf(eta[a].h, v[a].l, e);
-        lo[a] = fmaf(eta[a].l, v[a].h, e);
+        float r = fmaf(eta[a].h, v[a].h, -m[a]);
+        r = fmaf(eta[a].h, v[a].l, r);
+        lo[a] = fmaf(eta[a].l, v[a].h, r);
     }
     // S = eta . V (the sum of the high parts exact; S_low carries the rest)
     const f2 s = two_sum(m[0], m[1]);
@@ -277,16 +279,28 @@ PD_BT_HD BondOut bond2(const f2 eta[2], const Tpl& T, float dl, f2 k2half) {
     const f2 qq = two_sum(T.q0h, s.h);
     const f2 L2 = fast_sum(qq.h, (qq.l + s_low) + T.q0l);
     // 1/L, L, L + l0, e = D / (L + l0)
-    const f2 y = rsqrt2(L2);
+    y = rsqrt2(L2);
     const f2 L = mul(L2, y);
     const f2 lp = two_sum(L.h, T.l0h);
     const f2 Lp = fast_sum(lp.h, ((lp.l + L.l) + T.l0l) + dl);
-    o.e = mul(D, rcp2(Lp));
+    e = mul(D, rcp2(Lp));
+}
+
+PD_BT_HD BondOut bond2(const f2 eta[2], const Tpl& T, float dl, f2 k2half) {
+    BondOut o;
+    f2 w[2], y;
+    stretch2(eta, T, dl, w, y, o.e);
     // t = (k2 / 2) e / L, f = t W
     const f2 t = mul(mul(k2half, o.e), y);
     o.f[0] = mul(t, w[0]);
     o.f[1] = mul(t, w[1]);
     return o;
+}
+
+// a + b for pairs (TwoSum of the high parts, renormalized).
+PD_BT_HD f2 add(f2 a, f2 b) {
+    const f2 s = two_sum(a.h, b.h);
+    return fast_sum(s.h, s.l + (a.l + b.l));
 }
 
 // Accumulate a pair into a running sum, renormalized at every addition (the

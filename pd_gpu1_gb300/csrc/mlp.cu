@@ -312,8 +312,9 @@ __global__ void k_loss(const float* __restrict__ Y, const float* __restrict__ T,
 // Features of the free nodes (see pd_warm_features).  hist (may be null):
 // the previous increment's departure from proportionality per unit load, x
 // then y (2 n), and its damage increase (n); kHistScale brings the departure
-// (of the order of 1e-3 on the warm-start plates) near one.
-constexpr double kHistScale = 256.0;
+// (of the order of 1e-5 on the warm-start plates, its change from one
+// increment to the next 1e-6) near one.
+constexpr double kHistScale = 65536.0;
 __global__ void k_features(int64_t n, const double* __restrict__ y, const double* __restrict__ ux,
                            const double* __restrict__ uy, const double* __restrict__ dmg,
                            const double* __restrict__ hist, double inv_u, double inc, double edge,

@@ -150,7 +150,7 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")  # two candidates
     X = torch.zeros((ni, 16), dtype=torch.bfloat16, device="cuda") if collect is not None else None
     prev = None
-    hist = None  # the departure recorded as the history of this increment (host copy), None: no history
+    hist = getattr(eng, "warm_history", None)  # the context's recorded departure (host copy), None: no history
     out = []
     for k in range(start, start + n_inc):
         U = k * delta  # accumulated boundary displacement before this increment
@@ -169,8 +169,11 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
             ptr = du.data_ptr()  # "network": the network's start against the plain start
             if mode == "learned":  # both candidates
                 ncand = 2
-            if mode == "secant":  # the skip term alone
+            if mode == "secant" or (mode == "learned" and hist is None and record):
+                # the skip term alone; the learned start too when there is no
+                # history (the first increments, and the one after a crack advance)
                 ptr = du.data_ptr() + 2 * ni * 8
+                ncand = 1
         elif mode == "extrapolate" and prev is not None:
             du[: 2 * ni].copy_(torch.from_numpy(prev))
             ptr = du.data_ptr()
@@ -197,10 +200,9 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
         if record:
             if tt is not None and st["advanced"] == 0:
                 record_history(eng, U, delta, u0, d0)
-                hist = tt
             else:
-                check(L.pd_warm_record(eng.ctx, 0.0, delta, None, None, eng.stream), eng.ctx, "pd_warm_record")
-                hist = None
+                clear_history(eng, delta)
+            hist = eng.warm_history
         if last is not None:
             last.update(u0=u0, d0=d0, U=U if (tt is not None and st["advanced"] == 0) else 0.0)
         out.append(st)
@@ -210,13 +212,22 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
 def record_history(eng, U_prev, delta, u_prev, dmg_prev):
     """pd_warm_record from host arrays: the increment that led from (u_prev,
     dmg_prev) at accumulated boundary displacement U_prev to the context's
-    current state."""
+    current state.  A host copy of the recorded departure stays on the engine
+    (``warm_history``)."""
     import torch
 
     up = torch.from_numpy(np.ascontiguousarray(u_prev, dtype=np.float64)).cuda()
     dp = torch.from_numpy(np.ascontiguousarray(dmg_prev, dtype=np.float64)).cuda()
     check(lib().pd_warm_record(eng.ctx, U_prev, delta, up.data_ptr(), dp.data_ptr(), eng.stream), eng.ctx,
           "pd_warm_record")
+    ni = eng.p.N_int
+    u = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+    eng.warm_history = ((u - u_prev) - u_prev * (delta / U_prev)) / U_prev
+
+
+def clear_history(eng, delta):
+    check(lib().pd_warm_record(eng.ctx, 0.0, delta, None, None, eng.stream), eng.ctx, "pd_warm_record")
+    eng.warm_history = None
 
 
 def restore_history(eng, meta, last):
@@ -226,7 +237,7 @@ def restore_history(eng, meta, last):
     if last["U"] > 0.0:
         record_history(eng, last["U"], meta["delta"], last["u0"], last["d0"])
     else:
-        check(lib().pd_warm_record(eng.ctx, 0.0, meta["delta"], None, None, eng.stream), eng.ctx, "pd_warm_record")
+        clear_history(eng, meta["delta"])
 
 
 def train(X, T, steps=3000, batch=16384, lr=2e-3, seed=0, log=None):
@@ -252,11 +263,11 @@ def train(X, T, steps=3000, batch=16384, lr=2e-3, seed=0, log=None):
 # (scale, crack fraction, seed): 41k-104k-node plates of the same set-up,
 # loaded through their first crack advances within 60 increments
 TRAIN_RUNS = [
-    (0.2, 0.15, 1), (0.2, 0.2, 2), (0.2, 0.25, 3), (0.25, 0.2, 4), (0.32, 0.2, 5),
+    (0.2, 0.15, 1), (0.2, 0.18, 2), (0.2, 0.25, 3), (0.25, 0.2, 4), (0.32, 0.2, 5),
 ]
 # the network's outputs and history features are the departure per unit load
 # times this factor (kHistScale of csrc/mlp.cu)
-OUT_SCALE = 256.0
+OUT_SCALE = 65536.0
 
 
 def generate(runs=TRAIN_RUNS, n_inc=60, keep=0.25, tol=1e-8, log=print):
