@@ -1050,7 +1050,8 @@ int pd_set_force_layout(pd_ctx* c, int layout) {
 
 int pd_get_force_layout(const pd_ctx* c, int* layout) {
     if (!c || !layout) return PD_ERR_ARG;
-    *layout = c->sell.rec16 ? PD_LAYOUT_COMPACT : c->sell.rec ? PD_LAYOUT_RECORDS : PD_LAYOUT_AUTO;
+    const pdg::Sell& S = c->sell;
+    *layout = (S.rec16 || S.srec) ? PD_LAYOUT_COMPACT : (S.rec || S.sgeo) ? PD_LAYOUT_RECORDS : PD_LAYOUT_AUTO;
     return PD_OK;
 }
 

@@ -106,6 +106,9 @@ struct ForceArgs {
     const int* inst_tbase;    // batch: first template of each specimen (null: one specimen)
     const int* slice_inst;    // batch: specimen of each slice
     const double* node_s0;    // batch: critical stretch per node (null: P.critical_s)
+    // 2-D state-based compact layout (null: the three 32-byte records)
+    const bt::Rec* srec;      // column, dl and class id, dilatation weight as a pair
+    const float4* sfrc;       // c1, c2 as pairs
 };
 
 namespace {
@@ -1108,6 +1111,143 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
 }
 
 
+// ---- 2-D state-based passes on the compact layout -------------------------
+//
+// Per slot a 16-byte geometry record (column; dl with the offset class id;
+// the dilatation weight as a pair), read by both passes, and in the force
+// pass a 16-byte record of c1 and c2; the stretch arithmetic is bt::stretch2
+// on the class template.  The dilatation pass forms the reference vector
+// x_c - x_i from the gathered coordinates (the reference's FP64 subtraction)
+// instead of storing it; e still goes from the first pass to the second in a
+// pair per slot.  2 x 16 + 8 bytes per slot per pass, against 64 + 8.
+
+// One bond's exact offsets from its class's float reference vector.
+__device__ __forceinline__ void offsets2(const bt::Tpl& T, const double d[2], bt::f2 eta[2]) {
+#pragma unroll
+    for (int a = 0; a < 2; a++) {
+        const uint64_t xb = T.xd[a];
+        if (xb == 0)
+            eta[a] = bt::split_bits(d[a]);
+        else if (!bt::offset_pair(d[a], xb, eta[a]))
+            eta[a] = bt::split_bits(d[a] - bt::dfrom(xb));  // exact by Sterbenz's lemma
+    }
+}
+
+// Dilatation pass (kernel_cal_theta_2D, Force_State.cu:56-85) on every row of
+// [0, N), every bond of the family (the 2-D kernel counts broken bonds too).
+__global__ void __launch_bounds__(kForceBlock) k_theta_compact(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const KParams& P = A.P;
+    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
+         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+        const int64_t r = s * 32 + lane;
+        const bool row = r < P.N;
+        const int64_t rr = row ? r : P.N - 1;
+        const int nn = row ? A.NN[rr] : 0;
+        const double xi = A.x[rr], yi = A.y[rr], uxi = A.ux[rr], uyi = A.uy[rr];
+        const int W = A.width[s];
+        const int64_t b = A.base[s];
+        const int4* rp = reinterpret_cast<const int4*>(A.srec + b) + lane;
+        bt::f2 acc{0.0f, 0.0f};  // sum of the weighted extensions, times 2^sth_exp
+        for (int k = 0; k < W; k++) {
+            if (k < nn) {
+                const int4 rq = __ldg(rp + (int64_t)k * 32);
+                const int c = rq.x;
+                const uint32_t dlb = (uint32_t)rq.y;
+                const bt::Tpl& T = A.tpl[dlb & 0xffu];
+                const float dl = __uint_as_float(dlb & ~0xffu);
+                // d = ((x_c - x_i) + u_c) - u_i, the dilatation pass's operand order
+                const double d[2] = {((__ldg(A.x + c) - xi) + __ldg(A.ux + c)) - uxi,
+                                     ((__ldg(A.y + c) - yi) + __ldg(A.uy + c)) - uyi};
+                bt::f2 eta[2], w[2], y, e;
+                offsets2(T, d, eta);
+                bt::stretch2(eta, T, dl, w, y, e);
+                A.e[b + (int64_t)k * 32 + lane] = make_float2(e.h, e.l);
+                acc = bt::add(acc, bt::mul(bt::f2{__int_as_float(rq.z), __int_as_float(rq.w)}, e));
+            }
+        }
+        if (row) {
+            // theta = acc / m and theta / m through 1/m (nb, IEEE-rounded at set-up)
+            const double m = A.m[r], rm = A.nb[r];
+            const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
+            const double th = div_recip(a, m, rm);
+            A.theta[r] = th;
+            const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
+            A.na[r] = make_float2(na.h, na.l);
+        }
+    }
+}
+
+// State-based force pass (kernel_state_force_2D, Force_State.cu:88-134) on
+// rows [0, N_int): t_i + t_j = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i +
+// 1/m_j) per bond with e from the dilatation pass, the length and direction
+// in the force pass's operand order.
+template <int EPI>
+__global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    const double s0 = P.critical_s;
+    const float s0f = __double2float_rn(s0);
+    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
+         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+        const int64_t r = s * 32 + lane;
+        const bool force_row = r < A.nforce;
+        if (s * 32 < A.nforce) {
+            const int64_t rr = force_row ? r : A.nforce - 1;
+            const double xi = A.x[rr], yi = A.y[rr];
+            const double uxi = A.ux[rr], uyi = A.uy[rr];
+            const float2 na_i = A.na[rr], nb_i = A.nb2[rr];
+            const bt::f2 nai{na_i.x, na_i.y}, nbi{nb_i.x, nb_i.y};
+            bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
+            const int W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            const int4* rp = reinterpret_cast<const int4*>(A.srec + b) + lane;
+            for (int k = 0; k < W; k++) {
+                const int64_t slot = b + (int64_t)k * 32 + lane;
+                const uint32_t word = wbits[k];
+                const bool alive = force_row && ((word >> lane) & 1u);
+                bool brk = false;
+                if (alive) {
+                    const int4 rq = __ldg(rp + (int64_t)k * 32);
+                    const int c = rq.x;
+                    const uint32_t dlb = (uint32_t)rq.y;
+                    const bt::Tpl& T = A.tpl[dlb & 0xffu];
+                    const float dl = __uint_as_float(dlb & ~0xffu);
+                    // d = (P_c - x_i) - u_i, the force pass's operand order
+                    const double d[2] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi};
+                    bt::f2 eta[2], w[2], y, ef;
+                    offsets2(T, d, eta);
+                    bt::stretch2(eta, T, dl, w, y, ef);
+                    // T = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j), times 2^-st_exp
+                    const float4 cc = __ldg(A.sfrc + slot);
+                    const float2 ec = A.e[slot], nac = A.na[c], nbc = A.nb2[c];
+                    const bt::f2 Tt = bt::add(bt::mul(bt::f2{cc.x, cc.y}, bt::add(nai, bt::f2{nac.x, nac.y})),
+                                              bt::mul(bt::mul(bt::f2{cc.z, cc.w}, bt::f2{ec.x, ec.y}),
+                                                      bt::add(nbi, bt::f2{nbc.x, nbc.y})));
+                    // t = T / (2 L) and f += t d
+                    const bt::f2 t = bt::mul(Tt, bt::f2{0.5f * y.h, 0.5f * y.l});
+                    bt::acc_add(fxa, bt::mul(t, w[0]));
+                    bt::acc_add(fya, bt::mul(t, w[1]));
+                    brk = bt::exceeds(ef, s0, s0f, T, dl);
+                }
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+            }
+            // undo the power-of-two scale of T (exact)
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
+            if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
+        }
+        if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<2>(A, r);
+    }
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
 // Standalone kernel_cnn + cal_cn (Integrate.cu:7-49, :108-129) on the current forces.
 template <int DIM>
 __global__ void __launch_bounds__(kForceBlock) k_adr_cnn(const ForceArgs A) {
@@ -1250,6 +1390,8 @@ static ForceArgs make_args(pd_ctx* c) {
     A.inst_tbase = S.inst_tbase;
     A.slice_inst = c->batch.slice_inst;
     A.node_s0 = c->batch.node_s0;
+    A.srec = S.srec;
+    A.sfrc = S.sfrc;
     return A;
 }
 
@@ -1269,7 +1411,9 @@ static unsigned resident_grid(pd_ctx* c, const void* kernel, int64_t nslices, in
 
 int launch_theta(pd_ctx* c, cudaStream_t s) {
     ForceArgs A = make_args(c);
-    if (A.P.dim == 2)
+    if (A.P.dim == 2 && A.srec)
+        k_theta_compact<<<resident_grid(c, (const void*)k_theta_compact, A.nslices), kForceBlock, 0, s>>>(A);
+    else if (A.P.dim == 2)
         k_theta<2><<<resident_grid(c, (const void*)k_theta<2>, A.nslices), kForceBlock, 0, s>>>(A);
     else
         k_theta<3><<<resident_grid(c, (const void*)k_theta<3>, A.nslices), kForceBlock, 0, s>>>(A);
@@ -1416,10 +1560,21 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
             else PD_LAUNCH(KER, 3, EPI_ADR);              \
         }                                                 \
     } while (0)
-    if (state)
+    if (state && !d3 && A.srec) {
+        if (f.epi == EPI_NONE)
+            k_state_compact<EPI_NONE><<<resident_grid(c, (const void*)k_state_compact<EPI_NONE>, A.nslices, blk,
+                                                      waves), blk, 0, s>>>(A);
+        else if (f.epi == EPI_VERLET)
+            k_state_compact<EPI_VERLET><<<resident_grid(c, (const void*)k_state_compact<EPI_VERLET>, A.nslices, blk,
+                                                        waves), blk, 0, s>>>(A);
+        else
+            k_state_compact<EPI_ADR><<<resident_grid(c, (const void*)k_state_compact<EPI_ADR>, A.nslices, blk,
+                                                     waves), blk, 0, s>>>(A);
+    } else if (state) {
         PD_DISPATCH(k_state_force);
-    else
+    } else {
         PD_DISPATCH(k_bond_force);
+    }
 #undef PD_DISPATCH
 #undef PD_LAUNCH
     c->launches++;

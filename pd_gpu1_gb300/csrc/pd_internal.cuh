@@ -132,6 +132,12 @@ struct Sell {
     bt::Tpl* tpl = nullptr;    // [ntpl] templates of all specimens
     int ntpl = 0;
     int* inst_tbase = nullptr; // batch: first template of each specimen (null: one specimen)
+    // 2-D state-based compact layout: per slot a 16-byte geometry record
+    // (column, dl and class id, the dilatation weight as a pair) read by both
+    // passes and a 16-byte force record (c1, c2 as pairs); the extension e of
+    // the dilatation pass stays in e; sgeo/sth/sfo are not allocated
+    bt::Rec* srec = nullptr;   // [S]
+    float4* sfrc = nullptr;    // [S]
 };
 
 // Layout of the bond-based force path (pd_set_force_layout).

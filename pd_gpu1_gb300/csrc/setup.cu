@@ -478,6 +478,69 @@ __global__ void k_rec16_fill(KParams P, int64_t nslices, const int* __restrict__
     }
 }
 
+// Records of the 2-D state-based compact layout (the coefficients of
+// k_sell_fill's state records, on offset-class templates): rec = {column, dl
+// with the class id, the dilatation weight cth as a pair}, frc = {c1, c2 as
+// pairs}; *bad as in k_rec16_fill.
+__global__ void k_state_compact_fill(KParams P, int64_t nslices, const int* __restrict__ width,
+                                     const int64_t* __restrict__ base, const int* __restrict__ csr,
+                                     const int* __restrict__ NL, const double* __restrict__ x,
+                                     const double* __restrict__ y, const double* __restrict__ idist,
+                                     const double* __restrict__ fac, const double* __restrict__ w,
+                                     const unsigned long long* __restrict__ keys, const int* __restrict__ ids,
+                                     const bt::Tpl* __restrict__ tpl, int sn_exp, int sth_exp, int st_exp,
+                                     bt::Rec* __restrict__ rec, float4* __restrict__ frc, int* __restrict__ bad) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int64_t slot = b + t;
+        const int q = csr[slot];
+        const int64_t r = s * 32 + (t & 31);
+        bt::Rec R;
+        if (q < 0) {
+            R.col = (int)(r < P.N ? r : 0);
+            R.dl = 0.0f;
+            R.k2h = R.k2l = 0.0f;
+            rec[slot] = R;
+            frc[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            continue;
+        }
+        const int64_t c = NL[q];
+        const unsigned long long key = class_key(x[c] - x[r], y[c] - y[r]);
+        unsigned h = class_hash(key);
+        int id = -1;
+        for (int probe = 0; probe < kRegion; probe++, h = (h + 1) & (kRegion - 1)) {
+            if (keys[h] == key) {
+                id = ids[h];
+                break;
+            }
+            if (keys[h] == kEmptyKey) break;
+        }
+        const double L0 = idist[q];
+        const double dlv = id >= 0 ? L0 - tpl[id].l0d : 0.0;
+        const float dl = __double2float_rn(dlv);
+        const unsigned dlb = __float_as_uint(dl);
+        if (id < 0 || id > 255 || (double)dl != dlv || (dlb & 0xffu) != 0u) atomicExch(bad, 1);
+        // the coefficients of the state records (k_sell_fill), 2-D
+        const double pr = P.pratio;
+        const double a_coef = (2.0 * pr - 1.0) / (pr - 1.0) * (2.0 * P.K - 32.0 * P.G / 9.0);
+        const double b_coef = 8.0 * P.G;
+        const double th_coef = 2.0 * (2.0 * pr - 1.0) / (pr - 1.0);
+        const double wf = w[q] * fac[q] * P.vol;
+        const ff cth = ff_split(th_coef * w[q] * L0 * fac[q] * P.vol * ldexp(1.0, sth_exp));
+        const double cs = ldexp(1.0, sn_exp - st_exp);
+        const ff c1 = ff_split(2.0 * a_coef * wf * L0 * cs), c2 = ff_split(2.0 * b_coef * wf * cs);
+        R.col = (int)c;
+        R.dl = __uint_as_float((dlb & ~0xffu) | (unsigned)(id & 0xff));
+        R.k2h = cth.h;
+        R.k2l = cth.l;
+        rec[slot] = R;
+        frc[slot] = make_float4(c1.h, c1.l, c2.h, c2.l);
+    }
+}
+
 // Intact flags: CSR int32 <-> SELL bit words.
 __global__ void k_bits_from_csr(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
                                 const int64_t* __restrict__ fbase, const int* __restrict__ csr,
@@ -640,6 +703,8 @@ static void free_sell(Sell& S) {
     free_ptr(S.rec16);
     free_ptr(S.tpl);
     free_ptr(S.inst_tbase);
+    free_ptr(S.srec);
+    free_ptr(S.sfrc);
     S.ntpl = 0;
     S.nslices = S.S = S.F = 0;
 }
@@ -669,10 +734,13 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         cudaFreeAsync(ids, s);
         cudaFreeAsync(flags, s);
     };
+    const bool state = c->p.model == PD_MODEL_STATE;
     auto release = [&]() {
         free_ptr(S.tpl);
         free_ptr(S.rec16);
         free_ptr(S.inst_tbase);
+        free_ptr(S.srec);
+        free_ptr(S.sfrc);
         S.ntpl = 0;
     };
     if (cudaMallocAsync(&keys, tsize * 8, s) || cudaMallocAsync(&l0min, tsize * 8, s) ||
@@ -748,8 +816,10 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: no bonds");
     }
     S.ntpl = (int)tp.size();
+    const size_t nrec = (size_t)std::max<int64_t>(S.S, 1);
     if (cudaMalloc(&S.tpl, tp.size() * sizeof(bt::Tpl)) ||
-        cudaMalloc(&S.rec16, (size_t)std::max<int64_t>(S.S, 1) * sizeof(bt::Rec)) ||
+        (!state && cudaMalloc(&S.rec16, nrec * sizeof(bt::Rec))) ||
+        (state && (cudaMalloc(&S.srec, nrec * sizeof(bt::Rec)) || cudaMalloc(&S.sfrc, nrec * sizeof(float4)))) ||
         (regions > 1 && cudaMalloc(&S.inst_tbase, regions * sizeof(int)))) {
         cleanup();
         release();
@@ -758,9 +828,14 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.tpl, tp.data(), tp.size() * sizeof(bt::Tpl), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(ids, hid.data(), tsize * 4, cudaMemcpyHostToDevice, s);
     if (S.inst_tbase) cudaMemcpyAsync(S.inst_tbase, tbase.data(), regions * sizeof(int), cudaMemcpyHostToDevice, s);
-    k_rec16_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
-                                               c->nf[PD_F_Y], c->idist, c->fac, c->scr, c->batch.node_bc, keys, ids,
-                                               S.inst_tbase, S.tpl, 0.5 * S.kscale_inv, S.rec16, flags + 1);
+    if (state)
+        k_state_compact_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X],
+                                                           c->nf[PD_F_Y], c->idist, c->fac, c->w, keys, ids, S.tpl,
+                                                           S.sn_exp, S.sth_exp, S.st_exp, S.srec, S.sfrc, flags + 1);
+    else
+        k_rec16_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
+                                                   c->nf[PD_F_Y], c->idist, c->fac, c->scr, c->batch.node_bc, keys,
+                                                   ids, S.inst_tbase, S.tpl, 0.5 * S.kscale_inv, S.rec16, flags + 1);
     c->launches++;
     cudaMemcpyAsync(hflags + 1, flags + 1, 4, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
@@ -816,12 +891,13 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
     bool ok = !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
-    // 2-D bond-based problems try the compact layout first (16-byte records on
-    // offset-class templates); the 48-byte records are the general layout
-    const bool try_compact = !state && P.dim == 2 && c->layout_pref != LAYOUT_RECORDS;
+    // 2-D problems try the compact layout first (16-byte records on
+    // offset-class templates); the 48-byte (bond-based) and three 32-byte
+    // (state-based) records are the general layout
+    const bool try_compact = P.dim == 2 && c->layout_pref != LAYOUT_RECORDS;
     if (c->layout_pref == LAYOUT_COMPACT && !try_compact) {
         free_sell(S);
-        return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 2-D bond-based problems");
+        return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 2-D problems");
     }
     if (ok && !state && !try_compact)
         ok = !cudaMalloc(&S.rec, n8 * 6);
@@ -849,9 +925,9 @@ int prepare(pd_ctx* c, cudaStream_t s) {
         S.sth_exp = -lg(std::fabs(th_coef) * P.delta * P.vol);
         S.st_exp = S.sn_exp + lg(std::fabs(2.0 * b_coef) * P.vol);
     }
-    if (ok && state)
-        ok = !cudaMalloc(&S.sgeo, n8 * 4) && !cudaMalloc(&S.sth, n8 * 4) && !cudaMalloc(&S.sfo, n8 * 4) &&
-             !cudaMalloc(&S.e, n8);
+    if (ok && state) ok = !cudaMalloc(&S.e, n8) && !cudaMemsetAsync(S.e, 0, n8, s);
+    if (ok && state && !try_compact)
+        ok = !cudaMalloc(&S.sgeo, n8 * 4) && !cudaMalloc(&S.sth, n8 * 4) && !cudaMalloc(&S.sfo, n8 * 4);
     if (!ok) {
         free_sell(S);
         return set_err(c, PD_ERR_NOMEM, "SELL bond arrays");
@@ -869,9 +945,10 @@ int prepare(pd_ctx* c, cudaStream_t s) {
             return rc;
         }
         if (rc) {
-            // the general layout: 48-byte records
+            // the general layout
             c->err.clear();
-            if (cudaMalloc(&S.rec, n8 * 6)) {
+            if (state ? (cudaMalloc(&S.sgeo, n8 * 4) || cudaMalloc(&S.sth, n8 * 4) || cudaMalloc(&S.sfo, n8 * 4))
+                      : cudaMalloc(&S.rec, n8 * 6) != cudaSuccess) {
                 free_sell(S);
                 return set_err(c, PD_ERR_NOMEM, "SELL bond arrays");
             }

@@ -564,10 +564,10 @@ def helpers_ell(values, NN, MN):
 
 
 def test_compact_layout_selection(E):
-    """Where the compact layout applies: 2-D bond-based problems take it by
-    default; 3-D and state-based ones keep the records, and asking for the
-    compact layout there is refused (PD_ERR_UNSUPPORTED, -8) without
-    disturbing the context, which then runs on the records."""
+    """Where the compact layout applies: 2-D problems (bond- and state-based)
+    take it by default; 3-D ones keep the records, and asking for the compact
+    layout there is refused (PD_ERR_UNSUPPORTED, -8) without disturbing the
+    context, which then runs on the records."""
     from pd_gpu1_gb300 import presets
     from pd_gpu1_gb300._abi import PD_MODEL_BOND
 
@@ -586,4 +586,45 @@ def test_compact_layout_selection(E):
     p, setup, meta = presets.build_crack_grow(scale=0.1, nt=10)
     with E.Engine(p) as eng:
         setup(eng)
-        assert eng.force_layout() is None  # state-based: neither bond-based layout
+        assert eng.force_layout() == "compact"
+        eng.set_force_layout("records")
+        eng.prepare()
+        assert eng.force_layout() == "records"
+
+
+def test_state_compact_layout_matches_records(E):
+    """The 2-D state-based passes on the compact layout against the three
+    32-byte records, on the cracked crack-grow plate with boundary rows:
+    dilatation and forces within 2e-13 norm-relative, the same intact flags
+    after two passes at strains of a few percent, and 20 explicit steps with
+    the boundary rows moving within 1e-11 (the two differ in their pair
+    arithmetic only)."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_grow(scale=0.2, nt=20)
+    rng = np.random.default_rng(12)
+    u = rng.standard_normal((2, p.N)) * 2.5e-6  # dx = 1e-4: bond strains of a few percent
+    out = {}
+    with E.Engine(p) as eng:
+        for layout in ("compact", "records"):
+            eng.set_force_layout(layout)
+            setup(eng)
+            assert eng.force_layout() == layout
+            fail0 = eng.get("FAIL")
+            eng.set("UX", u[0])
+            eng.set("UY", u[1])
+            eng.state_force_gpu()
+            first = (eng.get("FX"), eng.get("FY"), eng.get("THETA"))
+            eng.state_force_gpu()
+            second = (eng.get("FX"), eng.get("FY"), eng.get("FAIL"))
+            setup(eng)
+            eng.run_explicit(20, load=meta["load"])
+            out[layout] = first + second + (eng.get("UY"), eng.get("FAIL"))
+        n = p.N_int
+        for k, what in ((0, "fx"), (1, "fy"), (3, "fx 2"), (4, "fy 2")):
+            assert_close_norm(out["compact"][k][:n], out["records"][k][:n], 2e-13, what)
+        assert_close_norm(out["compact"][2], out["records"][2], 2e-13, "theta")
+        np.testing.assert_array_equal(out["compact"][5], out["records"][5])
+        assert (out["compact"][5] == 0).sum() > (fail0 == 0).sum()  # bonds broke beyond the pre-crack
+        assert_close_norm(out["compact"][6], out["records"][6], 1e-11, "uy after 20 steps")
+        np.testing.assert_array_equal(out["compact"][7], out["records"][7])
