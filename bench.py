@@ -771,17 +771,21 @@ def batch_arm(args):
 
 
 # ---- learned ADR warm start ---------------------------------------------------------------------
-def warm_measure(scale, K, W, smooth, e2e=True, with_clocks=True):
+def warm_measure(scale, K, smooth, n_plain=1, e2e=True, with_clocks=True):
     """ADR wall-time per load increment to a 1e-6 relative residual on the
-    warm-start plate (1M nodes at scale 1): plain start (previous solution),
-    the skip term alone (proportional, secant, increment) and the learned
-    start (network shipped in pd_gpu1_gb300/data, offered beside the skip
-    term; the smaller starting residual wins).  Increments 0..W-1 are solved
-    first with the learned start (untimed: increment 0 has no history); each
-    timed increment W+j is then solved three times from the same converged
-    state (a snapshot): plain and skip-only leave the increment history alone,
-    the learned run records it and its state carries on.  Returns the dict of
-    the JSON line (without the common keys)."""
+    warm-start plate (1M nodes at scale 1).  Increment 0 (no displacement yet,
+    so no proportional start) is solved first, untimed, and its converged
+    state kept (a snapshot).  From that state each start then solves its own
+    chain of increments 1..K, timed: the learned start (network shipped in
+    pd_gpu1_gb300/data, offered beside the skip term; the smaller starting
+    residual wins; every solved increment without crack advance becomes the
+    next prediction's history) and the skip term alone (proportional, secant,
+    increment).  A chain is the fair comparison: the state an increment
+    converges to seeds the next prediction, so each start inherits its own
+    earlier stopping error.  The plain start (previous solution) needs the
+    same ~23k ADR steps on every increment; n_plain of them are timed from
+    the same state.  Returns the dict of the JSON line (without the common
+    keys)."""
     import os
     import tempfile
 
@@ -797,78 +801,80 @@ def warm_measure(scale, K, W, smooth, e2e=True, with_clocks=True):
     net = warm.Net.load()
     snap_dir = tempfile.mkdtemp()
     snap = os.path.join(snap_dir, "state.snap")
-    snap_e2e = os.path.join(snap_dir, "start.snap")
     clocks = ClockSampler(torch.cuda.current_device()) if with_clocks else None
-    rows = []
-    learned_launches = 0  # kernels of the timed (learned-start) increments
+    delta = meta["delta"]
     with E.Engine(p) as eng:
         setup(eng)
         B = int(eng.get("ROWPTR")[p.N_int])
-        last_pre = {}
-        pre = warm.run_increments(eng, meta, W, mode="learned", net=net, smooth=smooth, last=last_pre)
-        eng.snapshot_save(snap_e2e)  # the state before the timed increments, replayed for e2e
+        first = warm.run_increments(eng, meta, 1, mode="plain")[0]  # increment 0; clears the history
+        eng.snapshot_save(snap)
         if clocks:
             clocks.start()
-        for j in range(K):
-            eng.snapshot_save(snap)
-            plain = warm.run_increments(eng, meta, 1, mode="plain", start=W + j, record=False)[0]
+        l0 = eng.kernel_launches
+        learned = warm.run_increments(eng, meta, K, mode="learned", net=net, start=1, smooth=smooth)
+        learned_launches = eng.kernel_launches - l0
+        eng.snapshot_load(snap)
+        warm.clear_history(eng, delta)
+        skip = warm.run_increments(eng, meta, K, mode="secant", net=net, start=1, record=False)
+        plain = []
+        for _ in range(n_plain):
             eng.snapshot_load(snap)
-            skip = warm.run_increments(eng, meta, 1, mode="secant", net=net, start=W + j, record=False)[0]
-            eng.snapshot_load(snap)
-            l0 = eng.kernel_launches
-            learned = warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=smooth)[0]
-            learned_launches += eng.kernel_launches - l0
-            rows.append((plain, skip, learned))
+            plain += warm.run_increments(eng, meta, 1, mode="plain", start=1, record=False)
         clk = clocks.stop() if clocks else None
         # the network's inference alone (features, four tcgen05 products, candidates)
         du = torch.zeros(4 * p.N_int, dtype=torch.float64, device="cuda")
         eng.damage()
-        U = (W + K) * meta["delta"]
+        U = 1 * delta
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
         for _ in range(5):
-            L.pd_warm_predict(eng.ctx, net.h, U, meta["delta"], smooth, du.data_ptr(), None)
+            L.pd_warm_predict(eng.ctx, net.h, U, delta, smooth, du.data_ptr(), None)
         e1.record()
         torch.cuda.synchronize()
         infer_ms = e0.elapsed_time(e1) / 5
         e2e_ms = None
         if e2e:
-            # the same timed increments again, from the same state and history,
-            # through the C ABI with the displacement field read back to pinned
-            # host memory after each one (an increment's input is its load step)
-            eng.snapshot_load(snap_e2e)
-            warm.restore_history(eng, meta, last_pre)
+            # the learned chain again, from the same state, through the C ABI
+            # with the displacement field read back to pinned host memory after
+            # each increment (an increment's input is its load step)
+            eng.snapshot_load(snap)
+            warm.clear_history(eng, delta)
             n = p.N
             pin = torch.zeros(n, dtype=torch.float64).pin_memory()
             t0 = time.perf_counter()
             for j in range(K):
-                warm.run_increments(eng, meta, 1, mode="learned", net=net, start=W + j, smooth=smooth)
+                warm.run_increments(eng, meta, 1, mode="learned", net=net, start=1 + j, smooth=smooth)
                 eng._c(L.pd_get_field(eng.ctx, FIELD["UY"], pin.data_ptr(), n, None), "pd_get_field")
             e2e_ms = (time.perf_counter() - t0) * 1e3 / K
     os.remove(snap)
-    os.remove(snap_e2e)
     os.rmdir(snap_dir)
-    plain_ms = np.array([r[0]["ms"] for r in rows])
-    skip_ms = np.array([r[1]["ms"] for r in rows])
-    learned_ms = np.array([r[2]["ms"] for r in rows])
+    plain_ms = float(np.mean([s["ms"] for s in plain]))
+    skip_ms = float(np.sum([s["ms"] for s in skip]))
+    learned_ms = float(np.sum([s["ms"] for s in learned]))
     flops = 2.0 * p.N_int * (16 * 128 + 2 * 128 * 128 + 128 * 16)
     peaks, peak_kind = measured_peaks()
     return {
-        "value": float(learned_ms.mean()), "unit": "ms", "steps": K, "warmup": W,
-        "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "increment_m": meta["delta"],
-                   "tol": 1e-6, "timed_increments": list(range(W, W + K)), "smooth_passes": smooth,
-                   "untimed_increments_first": W, "untimed_iters": [s["iters"] for s in pre],
-                   "untimed_candidate_used": [s["warm_used"] for s in pre]},
-        "plain": {"ms_per_increment": float(plain_ms.mean()), "iters": [r[0]["iters"] for r in rows]},
-        "skip_only": {"ms_per_increment": float(skip_ms.mean()), "iters": [r[1]["iters"] for r in rows],
-                      "what": "the proportional (secant) increment alone, against the plain start"},
-        "learned": {"ms_per_increment": float(learned_ms.mean()), "iters": [r[2]["iters"] for r in rows],
-                    "candidate_used": [r[2]["warm_used"] for r in rows],
-                    "candidates": "0 plain, 1 network (skip term + network correction), 2 skip term alone",
-                    "r_start_over_r_plain": [r[2]["r_start"] / r[2]["r_plain"] for r in rows],
-                    "bonds_broken": [r[2]["advanced"] for r in rows]},
-        "speedup_vs_plain": float(plain_ms.mean() / learned_ms.mean()),
-        "speedup_vs_skip_only": float(skip_ms.mean() / learned_ms.mean()),
+        "value": learned_ms / K, "unit": "ms", "steps": K, "warmup": 1,
+        "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "increment_m": delta,
+                   "tol": 1e-6, "timed_increments": list(range(1, K + 1)), "smooth_passes": smooth,
+                   "untimed": "increment 0 (plain start, %d ADR steps); every chain starts from its state"
+                              % first["iters"]},
+        "plain": {"ms_per_increment": plain_ms, "iters": [s["iters"] for s in plain],
+                  "what": "increment 1 from the previous solution"},
+        "skip_only": {"ms_per_increment": skip_ms / K, "iters": [s["iters"] for s in skip],
+                      "total_iters": int(sum(s["iters"] for s in skip)),
+                      "what": "the proportional (secant) increment alone, against the plain start, increments 1..%d"
+                              % K},
+        "learned": {"ms_per_increment": learned_ms / K, "iters": [s["iters"] for s in learned],
+                    "total_iters": int(sum(s["iters"] for s in learned)),
+                    "candidate_used": [s["warm_used"] for s in learned],
+                    "candidates": "0 plain, 1 network (skip term + history + network correction), 2 skip term "
+                                  "alone (also the only one offered when there is no history: increment 1 and the "
+                                  "one after a crack advance)",
+                    "r_start_over_r_plain": [s["r_start"] / s["r_plain"] for s in learned],
+                    "bonds_broken": [s["advanced"] for s in learned]},
+        "speedup_vs_plain": plain_ms / (learned_ms / K),
+        "speedup_vs_skip_only": skip_ms / learned_ms,
         "roofline": {"bound": "tensor", "kernel": "k_gemm (network inference, all four layers)",
                      "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks.get("bf16_tflops"),
                      "unit": "TFLOP/s", "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1.0),
@@ -894,7 +900,7 @@ def warm_arm(args):
                               "--workload plate_tensile and batch"}), flush=True)
         return 0
     torch.cuda.set_device(local)
-    m = warm_measure(args.scale, args.increments, args.warm_increments, args.smooth)
+    m = warm_measure(args.scale, args.increments, args.smooth, n_plain=args.plain_increments)
     line = {"metric": "ADR wall-time to a 1e-6 relative residual per load increment, learned start",
             "value": m.pop("value"), "unit": m.pop("unit"), "n_gpus": world, "steps": m.pop("steps"),
             "warmup": m.pop("warmup"), "ms_per_step": None, "higher_is_better": False, "scaling": "weak",
@@ -1136,7 +1142,7 @@ def gb300_arm(args):
     if rank == 0 and world == 1 and not args.no_extras and meta["workload"].startswith("crack_branching"):
         eng.close()
         eng = None
-        extras["adr_warm_start"] = warm_measure(1.0, 2, 10, args.smooth, e2e=False)
+        extras["adr_warm_start"] = warm_measure(1.0, 10, args.smooth, e2e=False)
         extras["batch"] = batch_block(200, 5)
 
     if rank == 0:
@@ -1187,11 +1193,12 @@ def main():
     ap.add_argument("--count", type=int, default=256, help="batch workload: number of specimens")
     ap.add_argument("--seq-steps", type=int, default=100, help="batch workload: steps per plate when run one "
                                                                 "after another")
-    ap.add_argument("--increments", type=int, default=3, help="warm_start workload: timed load increments")
+    ap.add_argument("--increments", type=int, default=10, help="warm_start workload: chained load increments "
+                                                                "timed per start")
     ap.add_argument("--smooth", type=int, default=None, help="warm_start workload: family-averaging passes of the "
                                                            "network's correction")
-    ap.add_argument("--warm-increments", type=int, default=10, help="warm_start workload: increments solved "
-                                                                     "before the timed ones")
+    ap.add_argument("--plain-increments", type=int, default=1, help="warm_start workload: plain-start increments "
+                                                                     "timed (each ~23k ADR steps at 1M nodes)")
     ap.add_argument("--no-extras", action="store_true", help="default workload: leave out the batch and "
                                                                   "learned-warm-start blocks of the line")
     args = ap.parse_args()

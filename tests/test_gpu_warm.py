@@ -76,7 +76,9 @@ def test_network_beats_the_skip_term_through_crack_advances(W):
 def test_bad_prediction_falls_back_to_plain(W):
     rng = np.random.default_rng(0)
     p = W.init_params(1)
-    p[-258:] = rng.standard_normal(258).astype(np.float32) * 5000.0  # output layer: large, wrong corrections
+    # output layer: large, wrong corrections (outputs ~1e7, i.e. ~100 U per
+    # node after the 2^-16 history scale, against an increment of U / k)
+    p[-258:] = rng.standard_normal(258).astype(np.float32) * 1e6
     bad = W.Net(65536, p)
     st, _ = _run(W, "network", 3, bad, smooth=0)
     for s in st[1:]:
