@@ -300,8 +300,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
         for (int a = 0; a < 3 && ok; a++) ok = cudaMalloc(&c->pos[b][a], nb) == cudaSuccess;
     ok = ok && cudaMalloc(&c->NN, (size_t)p->N * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&c->rowptr, ((size_t)p->N + 1) * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->node_a, nb) == cudaSuccess && cudaMalloc(&c->node_b, nb) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->node_c, nb) == cudaSuccess;
+    ok = ok && cudaMalloc(&c->node_a, 2 * nb) == cudaSuccess && cudaMalloc(&c->node_b, nb) == cudaSuccess;
     ok = ok && cudaMalloc(&c->partials, (size_t)kMaxPartials * 4 * 8) == cudaSuccess;
     ok = ok && cudaMalloc(&c->ticket, 4 * sizeof(unsigned)) == cudaSuccess;
     ok = ok && cudaMalloc(&c->cn, 8) == cudaSuccess && cudaMalloc(&c->red_out, 8) == cudaSuccess;
@@ -317,9 +316,8 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
         for (int a = 0; a < 3; a++) cudaMemset(c->pos[b][a], 0, nb);
     cudaMemset(c->NN, 0, (size_t)p->N * 4);
     cudaMemset(c->rowptr, 0, ((size_t)p->N + 1) * 8);
-    cudaMemset(c->node_a, 0, nb);
+    cudaMemset(c->node_a, 0, 2 * nb);
     cudaMemset(c->node_b, 0, nb);
-    cudaMemset(c->node_c, 0, nb);
     cudaMemset(c->ticket, 0, 4 * sizeof(unsigned));
     cudaMemset(c->cn, 0, 8);
     cudaMemset(c->res, 0, 8);
@@ -341,7 +339,7 @@ int pd_destroy(pd_ctx* c) {
     for (int b = 0; b < 2; b++)
         for (int a = 0; a < 3; a++)
             if (c->pos[b][a]) cudaFree(c->pos[b][a]);
-    void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->node_c, c->partials, c->ticket, c->cn,
+    void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->partials, c->ticket, c->cn,
                     c->red_out, c->res, c->cyl, c->NL, c->idist, c->fac, c->scr, c->w, c->e, c->fail,
                     c->warm_hist};
     for (void* q : ptrs)

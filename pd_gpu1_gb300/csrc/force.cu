@@ -78,9 +78,11 @@ struct ForceArgs {
     const double *bx, *by, *bz;
     const double *fox, *foy, *foz;
     const double *vhx, *vhy, *vhz;
-    float2* na;         // state: theta/m times 2^-sn_exp as a float pair
+    // state: per node {theta/m, 1/m} times 2^-sn_exp as float pairs (one
+    // 16-byte gather per bond in the force pass); the dilatation pass writes
+    // the first pair, the set-up the second
+    float4* nab;
     const double* nb;   // state: 1/m (IEEE-rounded)
-    const float2* nb2;  // state: 1/m times 2^-sn_exp as a float pair
     const double* m;
     double* theta;
     const double* dmg;
@@ -107,8 +109,9 @@ struct ForceArgs {
     const int* slice_inst;    // batch: specimen of each slice
     const double* node_s0;    // batch: critical stretch per node (null: P.critical_s)
     // 2-D state-based compact layout (null: the three 32-byte records)
-    const bt::Rec* srec;      // column, dl and class id, dilatation weight as a pair
-    const float4* sfrc;       // c1, c2 as pairs
+    const int4* srec;         // dilatation pass: column, dl and class id, kx, ky
+    const int2* srec8;        // force pass: column, dl and class id
+    const StateTpl* stpl;     // per class: c1, c2, cth as pairs
 };
 
 namespace {
@@ -1019,7 +1022,7 @@ __device__ __forceinline__ void theta_pass(const ForceArgs& A) {
             const double th = div_recip(a, m, rm);
             A.theta[r] = th;
             const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
-            A.na[r] = make_float2(na.h, na.l);
+            *reinterpret_cast<float2*>(A.nab + r) = make_float2(na.h, na.l);
         }
     }
 }
@@ -1054,8 +1057,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
             const int64_t rr = force_row ? r : A.nforce - 1;
             const double xi = A.x[rr], yi = A.y[rr], zi = DIM == 3 ? A.z[rr] : 0.0;
             const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = DIM == 3 ? A.uz[rr] : 0.0;
-            const float2 na_i = A.na[rr], nb_i = A.nb2[rr];
-            const ff nai{na_i.x, na_i.y}, nbi{nb_i.x, nb_i.y};
+            const float4 nab_i = A.nab[rr];
+            const ff nai{nab_i.x, nab_i.y}, nbi{nab_i.z, nab_i.w};
             double fxr = 0.0, fyr = 0.0, fzr = 0.0;
             ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
             const int W = A.width[s];
@@ -1085,9 +1088,10 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                     pair_stretch<DIM>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
                     // T = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j), times 2^-st_exp,
                     // in pair arithmetic on the scaled pairs (no FP64 instruction)
-                    const float2 ec = A.e[slot], nac = A.na[c], nbc = A.nb2[c];
-                    const ff T = ff_add(ff_mul(ff{w4.x, w4.y}, ff_add(nai, ff{nac.x, nac.y})),
-                                        ff_mul(ff_mul(ff{w4.z, w4.w}, ff{ec.x, ec.y}), ff_add(nbi, ff{nbc.x, nbc.y})));
+                    const float2 ec = A.e[slot];
+                    const float4 nc = __ldg(A.nab + c);
+                    const ff T = ff_add(ff_mul(ff{w4.x, w4.y}, ff_add(nai, ff{nc.x, nc.y})),
+                                        ff_mul(ff_mul(ff{w4.z, w4.w}, ff{ec.x, ec.y}), ff_add(nbi, ff{nc.z, nc.w})));
                     // t = T / (2 L) and f += t d in pair arithmetic (as in the bond-based kernel)
                     const ff t = ff_mul(T, ff{0.5f * y.h, 0.5f * y.l});
                     fxa = ff_add(fxa, ff_mul(t, dp[0]));
@@ -1113,13 +1117,18 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
 
 // ---- 2-D state-based passes on the compact layout -------------------------
 //
-// Per slot a 16-byte geometry record (column; dl with the offset class id;
-// the dilatation weight as a pair), read by both passes, and in the force
-// pass a 16-byte record of c1 and c2; the stretch arithmetic is bt::stretch2
-// on the class template.  The dilatation pass forms the reference vector
-// x_c - x_i from the gathered coordinates (the reference's FP64 subtraction)
-// instead of storing it; e still goes from the first pass to the second in a
-// pair per slot.  2 x 16 + 8 bytes per slot per pass, against 64 + 8.
+// Per slot a 16-byte record for the dilatation pass (column; dl with the
+// offset class id; kx, ky) and an 8-byte record for the force pass (column;
+// dl with the class id).  The reference vector x_c - x_i, as the reference
+// rounds it in the dilatation pass, is the class's float vector as a double
+// moved by kx, ky representable doubles: an integer addition on the bit
+// pattern instead of an FP64 subtraction and two gathered coordinates.  The
+// bond coefficients come from the class (StateTpl); the stretch arithmetic is
+// bt::stretch2 on the class template; e goes from the first pass to the
+// second in a pair per slot (recomputing it in the force pass would take the
+// dilatation order's bond vector, four more FP64 instructions per bond, on
+// the pipe that bounds the dilatation pass).  Per slot and step: 16 + 8
+// bytes in the dilatation pass, 8 + 8 in the force pass.
 
 // One bond's exact offsets from its class's float reference vector.
 __device__ __forceinline__ void offsets2(const bt::Tpl& T, const double d[2], bt::f2 eta[2]) {
@@ -1138,33 +1147,42 @@ __device__ __forceinline__ void offsets2(const bt::Tpl& T, const double d[2], bt
 __global__ void __launch_bounds__(kForceBlock) k_theta_compact(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
     const KParams& P = A.P;
-    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
-         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+    for (int64_t s = (int64_t)blockIdx.x * wpb + wib; s < A.nslices; s += (int64_t)gridDim.x * wpb) {
         const int64_t r = s * 32 + lane;
         const bool row = r < P.N;
         const int64_t rr = row ? r : P.N - 1;
         const int nn = row ? A.NN[rr] : 0;
-        const double xi = A.x[rr], yi = A.y[rr], uxi = A.ux[rr], uyi = A.uy[rr];
+        const double uxi = A.ux[rr], uyi = A.uy[rr];
         const int W = A.width[s];
         const int64_t b = A.base[s];
-        const int4* rp = reinterpret_cast<const int4*>(A.srec + b) + lane;
+        const int4* rp = A.srec + b + lane;
         bt::f2 acc{0.0f, 0.0f};  // sum of the weighted extensions, times 2^sth_exp
+        // the next slot's record loaded one iteration ahead
+        int4 rq_next = nn > 0 ? __ldg(rp) : make_int4(0, 0, 0, 0);
         for (int k = 0; k < W; k++) {
+            const int4 rq = rq_next;
+            if (k + 1 < nn) rq_next = __ldg(rp + (int64_t)(k + 1) * 32);
             if (k < nn) {
-                const int4 rq = __ldg(rp + (int64_t)k * 32);
                 const int c = rq.x;
                 const uint32_t dlb = (uint32_t)rq.y;
-                const bt::Tpl& T = A.tpl[dlb & 0xffu];
+                const int id = (int)(dlb & 0xffu);
+                const bt::Tpl& T = A.tpl[id];
                 const float dl = __uint_as_float(dlb & ~0xffu);
-                // d = ((x_c - x_i) + u_c) - u_i, the dilatation pass's operand order
-                const double d[2] = {((__ldg(A.x + c) - xi) + __ldg(A.ux + c)) - uxi,
-                                     ((__ldg(A.y + c) - yi) + __ldg(A.uy + c)) - uyi};
+                // x_c - x_i as the reference rounds it, then d = (that + u_c) - u_i,
+                // the dilatation pass's operand order
+                const double xa = __longlong_as_double((long long)T.xd[0] + rq.z);
+                const double ya = __longlong_as_double((long long)T.xd[1] + rq.w);
+                const double d[2] = {(xa + __ldg(A.ux + c)) - uxi, (ya + __ldg(A.uy + c)) - uyi};
                 bt::f2 eta[2], w[2], y, e;
                 offsets2(T, d, eta);
                 bt::stretch2(eta, T, dl, w, y, e);
                 A.e[b + (int64_t)k * 32 + lane] = make_float2(e.h, e.l);
-                acc = bt::add(acc, bt::mul(bt::f2{__int_as_float(rq.z), __int_as_float(rq.w)}, e));
+                // cth of the class moved to this bond's length: cth (1 + g1 dl)
+                const float4 ct = __ldg(reinterpret_cast<const float4*>(A.stpl + id) + 1);
+                const bt::f2 cth{ct.x, fmaf(ct.x, ct.z * dl, ct.y)};
+                acc = bt::add(acc, bt::mul(cth, e));
             }
         }
         if (row) {
@@ -1174,7 +1192,7 @@ __global__ void __launch_bounds__(kForceBlock) k_theta_compact(const ForceArgs A
             const double th = div_recip(a, m, rm);
             A.theta[r] = th;
             const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
-            A.na[r] = make_float2(na.h, na.l);
+            *reinterpret_cast<float2*>(A.nab + r) = make_float2(na.h, na.l);
         }
     }
 }
@@ -1187,35 +1205,39 @@ template <int EPI>
 __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(const ForceArgs A) {
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
     const KParams& P = A.P;
     double red[3] = {0.0, 0.0, 0.0};
     const double s0 = P.critical_s;
     const float s0f = __double2float_rn(s0);
-    for (int64_t s = (int64_t)blockIdx.x * kWarpsPerBlock + wib; s < A.nslices;
-         s += (int64_t)gridDim.x * kWarpsPerBlock) {
+    for (int64_t s = (int64_t)blockIdx.x * wpb + wib; s < A.nslices; s += (int64_t)gridDim.x * wpb) {
         const int64_t r = s * 32 + lane;
         const bool force_row = r < A.nforce;
         if (s * 32 < A.nforce) {
             const int64_t rr = force_row ? r : A.nforce - 1;
             const double xi = A.x[rr], yi = A.y[rr];
             const double uxi = A.ux[rr], uyi = A.uy[rr];
-            const float2 na_i = A.na[rr], nb_i = A.nb2[rr];
-            const bt::f2 nai{na_i.x, na_i.y}, nbi{nb_i.x, nb_i.y};
+            const float4 nab_i = A.nab[rr];
+            const bt::f2 nai{nab_i.x, nab_i.y}, nbi{nab_i.z, nab_i.w};
             bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f};
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
-            const int4* rp = reinterpret_cast<const int4*>(A.srec + b) + lane;
+            const int2* rp = A.srec8 + b + lane;
+            // the next slot's record loaded one iteration ahead
+            int2 rq_next = W > 0 ? __ldg(rp) : make_int2(0, 0);
             for (int k = 0; k < W; k++) {
                 const int64_t slot = b + (int64_t)k * 32 + lane;
+                const int2 rq = rq_next;
+                if (k + 1 < W) rq_next = __ldg(rp + (int64_t)(k + 1) * 32);
                 const uint32_t word = wbits[k];
                 const bool alive = force_row && ((word >> lane) & 1u);
                 bool brk = false;
                 if (alive) {
-                    const int4 rq = __ldg(rp + (int64_t)k * 32);
                     const int c = rq.x;
                     const uint32_t dlb = (uint32_t)rq.y;
-                    const bt::Tpl& T = A.tpl[dlb & 0xffu];
+                    const int id = (int)(dlb & 0xffu);
+                    const bt::Tpl& T = A.tpl[id];
                     const float dl = __uint_as_float(dlb & ~0xffu);
                     // d = (P_c - x_i) - u_i, the force pass's operand order
                     const double d[2] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi};
@@ -1223,11 +1245,15 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
                     offsets2(T, d, eta);
                     bt::stretch2(eta, T, dl, w, y, ef);
                     // T = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j), times 2^-st_exp
-                    const float4 cc = __ldg(A.sfrc + slot);
-                    const float2 ec = A.e[slot], nac = A.na[c], nbc = A.nb2[c];
-                    const bt::f2 Tt = bt::add(bt::mul(bt::f2{cc.x, cc.y}, bt::add(nai, bt::f2{nac.x, nac.y})),
-                                              bt::mul(bt::mul(bt::f2{cc.z, cc.w}, bt::f2{ec.x, ec.y}),
-                                                      bt::add(nbi, bt::f2{nbc.x, nbc.y})));
+                    // c1, c2 of the class moved to this bond's length (1 + g dl)
+                    const float4 cc = __ldg(reinterpret_cast<const float4*>(A.stpl + id));
+                    const float2 gg = __ldg(reinterpret_cast<const float2*>(A.stpl + id) + 3);
+                    const bt::f2 c1{cc.x, fmaf(cc.x, gg.x * dl, cc.y)}, c2{cc.z, fmaf(cc.z, gg.y * dl, cc.w)};
+                    const float2 ec = A.e[slot];
+                    const float4 nc = __ldg(A.nab + c);
+                    const bt::f2 Tt = bt::add(bt::mul(c1, bt::add(nai, bt::f2{nc.x, nc.y})),
+                                              bt::mul(bt::mul(c2, bt::f2{ec.x, ec.y}),
+                                                      bt::add(nbi, bt::f2{nc.z, nc.w})));
                     // t = T / (2 L) and f += t d
                     const bt::f2 t = bt::mul(Tt, bt::f2{0.5f * y.h, 0.5f * y.l});
                     bt::acc_add(fxa, bt::mul(t, w[0]));
@@ -1370,9 +1396,8 @@ static ForceArgs make_args(pd_ctx* c) {
     A.vhx = c->nf[PD_F_VHX];
     A.vhy = c->nf[PD_F_VHY];
     A.vhz = c->nf[PD_F_VHZ];
-    A.na = c->node_a;
+    A.nab = c->node_a;
     A.nb = c->node_b;
-    A.nb2 = c->node_c;
     A.m = c->nf[PD_F_M];
     A.theta = c->nf[PD_F_THETA];
     A.dmg = c->nf[PD_F_DMG];
@@ -1391,7 +1416,8 @@ static ForceArgs make_args(pd_ctx* c) {
     A.slice_inst = c->batch.slice_inst;
     A.node_s0 = c->batch.node_s0;
     A.srec = S.srec;
-    A.sfrc = S.sfrc;
+    A.srec8 = S.srec8;
+    A.stpl = S.stpl;
     return A;
 }
 
@@ -1411,8 +1437,12 @@ static unsigned resident_grid(pd_ctx* c, const void* kernel, int64_t nslices, in
 
 int launch_theta(pd_ctx* c, cudaStream_t s) {
     ForceArgs A = make_args(c);
-    if (A.P.dim == 2 && A.srec)
-        k_theta_compact<<<resident_grid(c, (const void*)k_theta_compact, A.nslices), kForceBlock, 0, s>>>(A);
+    if (A.P.dim == 2 && A.srec) {
+        // the launch shape's block size (at most kForceBlock) and waves
+        const int blk = std::min(c->tune_block, kForceBlock);
+        k_theta_compact<<<resident_grid(c, (const void*)k_theta_compact, A.nslices, blk, c->tune_waves), blk, 0, s>>>(
+            A);
+    }
     else if (A.P.dim == 2)
         k_theta<2><<<resident_grid(c, (const void*)k_theta<2>, A.nslices), kForceBlock, 0, s>>>(A);
     else
@@ -1502,8 +1532,11 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         return cuda_err(c, cudaGetLastError(), "node post");
     }
     const bool bond = !state;
-    const int blk = bond ? c->tune_block : kForceBlock;
-    const int waves = bond ? c->tune_waves : 1;
+    // the launch shape applies to the bond kernels and to the 2-D state passes
+    // of the compact layout (block at most kForceBlock there)
+    const bool shaped = bond || (!d3 && A.srec);
+    const int blk = bond ? c->tune_block : shaped ? std::min(c->tune_block, kForceBlock) : kForceBlock;
+    const int waves = shaped ? c->tune_waves : 1;
     A.chunked = bond ? c->tune_chunked : 0;
     if (bond && !d3 && A.rec16) return launch_compact(c, A, f, blk, waves, s);
     if (bond && c->tune_split > 1) {

@@ -102,6 +102,20 @@ struct alignas(16) StateForce {
 static_assert(sizeof(StateGeo) == 32 && sizeof(StateTheta) == 32 && sizeof(StateForce) == 32,
               "state records are two 16-byte words each");
 
+// Coefficients of the 2-D state-based bonds of one offset class, at the
+// class's reference length l0t, as float pairs carrying the context's
+// power-of-two scales: c1 and c2 of the force pass (T = c1 (theta_i/m_i +
+// theta_j/m_j) + c2 e (1/m_i + 1/m_j)), cth of the dilatation pass.  They
+// depend on the bond length only: c2 on the weight exp(-l0^2/delta^2) and the
+// partial-volume factor, c1 and cth on those times l0.  The bond lengths of a
+// class differ from l0t by dl, a few ulps, so a bond's coefficient is the
+// class's times 1 + g dl, g the logarithmic derivative at l0t (g1 for c1 and
+// cth, g2 for c2; checked per slot at set-up to 2^-45).
+struct alignas(16) StateTpl {
+    float c1h, c1l, c2h, c2l;
+    float cth_h, cth_l, g1, g2;
+};
+
 struct Sell {
     int64_t nslices = 0;     // ceil(N / 32)
     int64_t S = 0;           // total slots (sum of 32 * width)
@@ -132,12 +146,16 @@ struct Sell {
     bt::Tpl* tpl = nullptr;    // [ntpl] templates of all specimens
     int ntpl = 0;
     int* inst_tbase = nullptr; // batch: first template of each specimen (null: one specimen)
-    // 2-D state-based compact layout: per slot a 16-byte geometry record
-    // (column, dl and class id, the dilatation weight as a pair) read by both
-    // passes and a 16-byte force record (c1, c2 as pairs); the extension e of
-    // the dilatation pass stays in e; sgeo/sth/sfo are not allocated
-    bt::Rec* srec = nullptr;   // [S]
-    float4* sfrc = nullptr;    // [S]
+    // 2-D state-based compact layout: per slot a 16-byte record for the
+    // dilatation pass (column, dl and class id, the reference vector's
+    // distance from its class's float vector in doubles, per component) and an
+    // 8-byte record for the force pass (column, dl and class id); the bond
+    // coefficients (functions of the bond length only) live in one StateTpl
+    // per class; the extension e of the dilatation pass stays in e;
+    // sgeo/sth/sfo are not allocated
+    int4* srec = nullptr;       // [S]
+    int2* srec8 = nullptr;      // [S]
+    StateTpl* stpl = nullptr;   // [ntpl]
 };
 
 // Layout of the bond-based force path (pd_set_force_layout).
@@ -186,9 +204,8 @@ struct pd_ctx {
     int parity = 0;          // pos[parity] is current
     bool pos_valid = false;  // pos[parity] == x + u
     int* NN = nullptr;
-    float2* node_a = nullptr;  // state-based: theta/m times 2^-sn_exp, as a float pair
+    float4* node_a = nullptr;  // state-based: {theta/m, 1/m} times 2^-sn_exp, as float pairs
     double* node_b = nullptr;  // state-based: 1/m (IEEE-rounded)
-    float2* node_c = nullptr;  // state-based: 1/m times 2^-sn_exp, as a float pair
 
     // CSR bond family
     int64_t B = 0;

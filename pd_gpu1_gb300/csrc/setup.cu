@@ -478,10 +478,30 @@ __global__ void k_rec16_fill(KParams P, int64_t nslices, const int* __restrict__
     }
 }
 
-// Records of the 2-D state-based compact layout (the coefficients of
-// k_sell_fill's state records, on offset-class templates): rec = {column, dl
-// with the class id, the dilatation weight cth as a pair}, frc = {c1, c2 as
-// pairs}; *bad as in k_rec16_fill.
+// The coefficients of one 2-D state-based bond (the state records of
+// k_sell_fill), with the context's power-of-two scales, in doubles.
+__device__ __forceinline__ void state_coefs(const KParams& P, double L0, double w, double fac, int sn_exp,
+                                            int sth_exp, int st_exp, double& cth, double& c1, double& c2) {
+    const double pr = P.pratio;
+    const double a_coef = (2.0 * pr - 1.0) / (pr - 1.0) * (2.0 * P.K - 32.0 * P.G / 9.0);
+    const double b_coef = 8.0 * P.G;
+    const double th_coef = 2.0 * (2.0 * pr - 1.0) / (pr - 1.0);
+    const double wf = w * fac * P.vol;
+    cth = th_coef * w * L0 * fac * P.vol * ldexp(1.0, sth_exp);
+    const double cs = ldexp(1.0, sn_exp - st_exp);
+    c1 = 2.0 * a_coef * wf * L0 * cs;
+    c2 = 2.0 * b_coef * wf * cs;
+}
+
+// Records of the 2-D state-based compact layout: rec = {column, dl with the
+// class id, kx, ky}, where the reference vector x_c - x_i as the reference
+// rounds it (a double) is the class's float vector (as a double) moved by kx
+// and ky representable doubles (the difference of the bit patterns); rec8 =
+// {column, dl with the class id}.  A slot whose bond has the class's
+// reference length (dl = 0; every class has one) writes the class's
+// coefficients into stpl (such slots compute identical values).  *bad as in
+// k_rec16_fill, and also where kx or ky leaves the int32 range or the signs
+// differ.
 __global__ void k_state_compact_fill(KParams P, int64_t nslices, const int* __restrict__ width,
                                      const int64_t* __restrict__ base, const int* __restrict__ csr,
                                      const int* __restrict__ NL, const double* __restrict__ x,
@@ -489,7 +509,8 @@ __global__ void k_state_compact_fill(KParams P, int64_t nslices, const int* __re
                                      const double* __restrict__ fac, const double* __restrict__ w,
                                      const unsigned long long* __restrict__ keys, const int* __restrict__ ids,
                                      const bt::Tpl* __restrict__ tpl, int sn_exp, int sth_exp, int st_exp,
-                                     bt::Rec* __restrict__ rec, float4* __restrict__ frc, int* __restrict__ bad) {
+                                     int4* __restrict__ rec, int2* __restrict__ rec8, StateTpl* __restrict__ stpl,
+                                     int* __restrict__ bad) {
     const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
     if (s >= nslices) return;
     const int W = width[s];
@@ -498,17 +519,15 @@ __global__ void k_state_compact_fill(KParams P, int64_t nslices, const int* __re
         const int64_t slot = b + t;
         const int q = csr[slot];
         const int64_t r = s * 32 + (t & 31);
-        bt::Rec R;
         if (q < 0) {
-            R.col = (int)(r < P.N ? r : 0);
-            R.dl = 0.0f;
-            R.k2h = R.k2l = 0.0f;
-            rec[slot] = R;
-            frc[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const int col = (int)(r < P.N ? r : 0);
+            rec[slot] = make_int4(col, 0, 0, 0);
+            rec8[slot] = make_int2(col, 0);
             continue;
         }
         const int64_t c = NL[q];
-        const unsigned long long key = class_key(x[c] - x[r], y[c] - y[r]);
+        const double xa = x[c] - x[r], ya = y[c] - y[r];  // the reference's rounding (Force_State.cu:71-72)
+        const unsigned long long key = class_key(xa, ya);
         unsigned h = class_hash(key);
         int id = -1;
         for (int probe = 0; probe < kRegion; probe++, h = (h + 1) & (kRegion - 1)) {
@@ -522,22 +541,60 @@ __global__ void k_state_compact_fill(KParams P, int64_t nslices, const int* __re
         const double dlv = id >= 0 ? L0 - tpl[id].l0d : 0.0;
         const float dl = __double2float_rn(dlv);
         const unsigned dlb = __float_as_uint(dl);
-        if (id < 0 || id > 255 || (double)dl != dlv || (dlb & 0xffu) != 0u) atomicExch(bad, 1);
-        // the coefficients of the state records (k_sell_fill), 2-D
-        const double pr = P.pratio;
-        const double a_coef = (2.0 * pr - 1.0) / (pr - 1.0) * (2.0 * P.K - 32.0 * P.G / 9.0);
-        const double b_coef = 8.0 * P.G;
-        const double th_coef = 2.0 * (2.0 * pr - 1.0) / (pr - 1.0);
-        const double wf = w[q] * fac[q] * P.vol;
-        const ff cth = ff_split(th_coef * w[q] * L0 * fac[q] * P.vol * ldexp(1.0, sth_exp));
-        const double cs = ldexp(1.0, sn_exp - st_exp);
-        const ff c1 = ff_split(2.0 * a_coef * wf * L0 * cs), c2 = ff_split(2.0 * b_coef * wf * cs);
-        R.col = (int)c;
-        R.dl = __uint_as_float((dlb & ~0xffu) | (unsigned)(id & 0xff));
-        R.k2h = cth.h;
-        R.k2l = cth.l;
-        rec[slot] = R;
-        frc[slot] = make_float4(c1.h, c1.l, c2.h, c2.l);
+        bool fail = id < 0 || id > 255 || (double)dl != dlv || (dlb & 0xffu) != 0u;
+        long long k[2] = {0, 0};
+        if (!fail) {
+            const double xv[2] = {xa, ya};
+            for (int a = 0; a < 2; a++) {
+                const long long xb = (long long)tpl[id].xd[a];
+                const long long vb = __double_as_longlong(xv[a]);
+                k[a] = vb - xb;
+                if ((vb < 0) != (xb < 0) || k[a] < INT_MIN || k[a] > INT_MAX) fail = true;
+            }
+        }
+        if (fail) atomicExch(bad, 1);
+        const int dlw = (int)((dlb & ~0xffu) | (unsigned)(id & 0xff));
+        rec[slot] = make_int4((int)c, dlw, (int)k[0], (int)k[1]);
+        rec8[slot] = make_int2((int)c, dlw);
+        if (!fail && dlv == 0.0) {
+            double cth, c1, c2;
+            state_coefs(P, L0, w[q], fac[q], sn_exp, sth_exp, st_exp, cth, c1, c2);
+            const ff a = ff_split(c1), bb = ff_split(c2), t3 = ff_split(cth);
+            StateTpl& T = stpl[id];  // g1, g2 come from the host
+            T.c1h = a.h, T.c1l = a.l, T.c2h = bb.h, T.c2l = bb.l;
+            T.cth_h = t3.h, T.cth_l = t3.l;
+        }
+    }
+}
+
+// Every slot's coefficients against its class's moved to the slot's length
+// (c (1 + g dl)): *bad where one differs from the bond's own by more than
+// 2^-45 of it.
+__global__ void k_state_compact_check(KParams P, int64_t nslices, const int* __restrict__ width,
+                                      const int64_t* __restrict__ base, const int* __restrict__ csr,
+                                      const double* __restrict__ idist, const double* __restrict__ fac,
+                                      const double* __restrict__ w, const int2* __restrict__ rec8,
+                                      const StateTpl* __restrict__ stpl, int sn_exp, int sth_exp, int st_exp,
+                                      int* __restrict__ bad) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int64_t slot = b + t;
+        const int q = csr[slot];
+        if (q < 0) continue;
+        const unsigned dlb = (unsigned)rec8[slot].y;
+        const StateTpl T = stpl[dlb & 0xffu];
+        const double dl = (double)__uint_as_float(dlb & ~0xffu);
+        double cth, c1, c2;
+        state_coefs(P, idist[q], w[q], fac[q], sn_exp, sth_exp, st_exp, cth, c1, c2);
+        const double tol = ldexp(1.0, -45);
+        const double f1 = 1.0 + (double)T.g1 * dl, f2 = 1.0 + (double)T.g2 * dl;
+        const double d1 = fabs(((double)T.c1h + (double)T.c1l) * f1 - c1);
+        const double d2 = fabs(((double)T.c2h + (double)T.c2l) * f2 - c2);
+        const double d3 = fabs(((double)T.cth_h + (double)T.cth_l) * f1 - cth);
+        if (!(d1 <= tol * fabs(c1)) || !(d2 <= tol * fabs(c2)) || !(d3 <= tol * fabs(cth))) atomicExch(bad, 1);
     }
 }
 
@@ -577,13 +634,13 @@ __global__ void k_csr_from_bits(int64_t nslices, const int* __restrict__ width, 
 // 1/m per node (IEEE-rounded, the dilatation pass's divisor reciprocal) and
 // the same times 2^-sn as a float pair (the force pass's operand).
 __global__ void k_inv_m(int64_t N, const double* __restrict__ m, double sn_scale, double* __restrict__ inv,
-                        float2* __restrict__ inv_pair) {
+                        float4* __restrict__ nab) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i < N) {
         const double v = 1.0 / m[i];
         inv[i] = v;
         const ff p = ff_split(v * sn_scale);
-        inv_pair[i] = make_float2(p.h, p.l);
+        reinterpret_cast<float2*>(nab + i)[1] = make_float2(p.h, p.l);  // the second pair of {theta/m, 1/m}
     }
 }
 
@@ -704,7 +761,8 @@ static void free_sell(Sell& S) {
     free_ptr(S.tpl);
     free_ptr(S.inst_tbase);
     free_ptr(S.srec);
-    free_ptr(S.sfrc);
+    free_ptr(S.srec8);
+    free_ptr(S.stpl);
     S.ntpl = 0;
     S.nslices = S.S = S.F = 0;
 }
@@ -740,7 +798,8 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         free_ptr(S.rec16);
         free_ptr(S.inst_tbase);
         free_ptr(S.srec);
-        free_ptr(S.sfrc);
+        free_ptr(S.srec8);
+        free_ptr(S.stpl);
         S.ntpl = 0;
     };
     if (cudaMallocAsync(&keys, tsize * 8, s) || cudaMallocAsync(&l0min, tsize * 8, s) ||
@@ -819,7 +878,8 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
     const size_t nrec = (size_t)std::max<int64_t>(S.S, 1);
     if (cudaMalloc(&S.tpl, tp.size() * sizeof(bt::Tpl)) ||
         (!state && cudaMalloc(&S.rec16, nrec * sizeof(bt::Rec))) ||
-        (state && (cudaMalloc(&S.srec, nrec * sizeof(bt::Rec)) || cudaMalloc(&S.sfrc, nrec * sizeof(float4)))) ||
+        (state && (cudaMalloc(&S.srec, nrec * sizeof(int4)) || cudaMalloc(&S.srec8, nrec * sizeof(int2)) ||
+                   cudaMalloc(&S.stpl, tp.size() * sizeof(StateTpl)))) ||
         (regions > 1 && cudaMalloc(&S.inst_tbase, regions * sizeof(int)))) {
         cleanup();
         release();
@@ -828,11 +888,31 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.tpl, tp.data(), tp.size() * sizeof(bt::Tpl), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(ids, hid.data(), tsize * 4, cudaMemcpyHostToDevice, s);
     if (S.inst_tbase) cudaMemcpyAsync(S.inst_tbase, tbase.data(), regions * sizeof(int), cudaMemcpyHostToDevice, s);
-    if (state)
+    if (state) {
+        // logarithmic derivatives of the coefficients at each class's l0t: the
+        // weight exp(-l0^2/delta^2) gives -2 l0 / delta^2; the partial-volume
+        // factor (delta + dx/2 - l0) / dx (kernel_vol_Corr, Surf_Corr.cu:26-31)
+        // above delta - dx/2 gives -1 / (delta + dx/2 - l0); l0 itself 1 / l0
+        std::vector<StateTpl> st(tp.size());
+        const double dlt = c->p.delta, hdx = c->p.dx / 2.0;
+        for (size_t k = 0; k < tp.size(); k++) {
+            const double l0t = tp[k].l0d;
+            double g2 = -2.0 * l0t / (dlt * dlt);
+            if (l0t > dlt - hdx) g2 -= 1.0 / (dlt + hdx - l0t);
+            st[k] = StateTpl{};
+            st[k].g2 = (float)g2;
+            st[k].g1 = (float)(g2 + 1.0 / l0t);
+        }
+        cudaMemcpyAsync(S.stpl, st.data(), st.size() * sizeof(StateTpl), cudaMemcpyHostToDevice, s);
         k_state_compact_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X],
                                                            c->nf[PD_F_Y], c->idist, c->fac, c->w, keys, ids, S.tpl,
-                                                           S.sn_exp, S.sth_exp, S.st_exp, S.srec, S.sfrc, flags + 1);
-    else
+                                                           S.sn_exp, S.sth_exp, S.st_exp, S.srec, S.srec8, S.stpl,
+                                                           flags + 1);
+        k_state_compact_check<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->idist, c->fac,
+                                                            c->w, S.srec8, S.stpl, S.sn_exp, S.sth_exp, S.st_exp,
+                                                            flags + 1);
+        c->launches++;
+    } else
         k_rec16_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
                                                    c->nf[PD_F_Y], c->idist, c->fac, c->scr, c->batch.node_bc, keys,
                                                    ids, S.inst_tbase, S.tpl, 0.5 * S.kscale_inv, S.rec16, flags + 1);
@@ -961,7 +1041,7 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     }
     if (state) {
         k_inv_m<<<(unsigned)((P.N + 255) / 256), 256, 0, s>>>(P.N, c->nf[PD_F_M], std::ldexp(1.0, -S.sn_exp),
-                                                             c->node_b, c->node_c);
+                                                             c->node_b, c->node_a);
         c->launches++;
     }
     c->bits_current = false;

@@ -308,7 +308,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("cmd", choices=["train"])
     ap.add_argument("--out", default=WEIGHTS)
-    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--increments", type=int, default=60)
     ap.add_argument("--tol", type=float, default=1e-8, help="ADR tolerance of the training runs")
     args = ap.parse_args()

@@ -628,3 +628,31 @@ def test_state_compact_layout_matches_records(E):
         assert (out["compact"][5] == 0).sum() > (fail0 == 0).sum()  # bonds broke beyond the pre-crack
         assert_close_norm(out["compact"][6], out["records"][6], 1e-11, "uy after 20 steps")
         np.testing.assert_array_equal(out["compact"][7], out["records"][7])
+
+
+def test_state_compact_launch_shapes_bitwise(E):
+    """The 2-D state-based passes of the compact layout under several launch
+    shapes (block size, waves of resident blocks): one warp per slice and a
+    fixed slot order, so dilatation, forces, intact flags and 20 explicit
+    steps agree bit for bit."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_grow(scale=0.2, nt=20)
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal((2, p.N)) * 2.5e-6
+    outs = []
+    with E.Engine(p) as eng:
+        for shape in ((256, 0, 1, 1), (128, 0, 8, 1), (256, 0, 4, 1)):
+            setup(eng)
+            assert eng.force_layout() == "compact"
+            eng.set_launch(*shape)
+            eng.set("UX", u[0])
+            eng.set("UY", u[1])
+            eng.state_force_gpu()
+            got = [eng.get(f) for f in ("FX", "FY", "THETA", "FAIL")]
+            setup(eng)
+            eng.run_explicit(20, load=meta["load"])
+            outs.append(got + [eng.get("UY"), eng.get("FAIL")])
+    for o in outs[1:]:
+        for a, b in zip(outs[0], o):
+            np.testing.assert_array_equal(a, b)
