@@ -1115,6 +1115,96 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
 }
 
 
+// The 3-D state-based force pass without epilogue (the explicit step's node
+// pass follows it), each warp on R = 32 / Q rows of a slice: lane j + R p
+// takes row j's slots p, p + Q, p + 2Q, ... and the Q partial sums of a row
+// are added as a tree over the lane groups (pair addition is commutative, so
+// every lane of the row gets the same sum).  The impact slab has 5,652 slices
+// of about 104 slots against 4,864 warps resident at this kernel's 64
+// registers: one warp per slice leaves a second round of 788 slices on a
+// nearly empty GPU; units of a quarter slice fill five rounds of a quarter
+// the length.  The sum order depends on Q only, not on the launch shape.
+// Intact flags of other units of the slice share the words, so breaks clear
+// their bits with atomicAnd.
+constexpr int kStatePhases3 = 4;
+template <int Q>
+__global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force3_phased(const ForceArgs A) {
+    constexpr int R = 32 / Q;
+    static_assert(Q >= 2 && Q <= 8 && 32 % Q == 0, "2 to 8 phases");
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const int j = lane % R, ph = lane / R;
+    const int64_t units = A.nslices * Q;
+    double red[3] = {0.0, 0.0, 0.0};
+    for (int64_t u = (int64_t)blockIdx.x * wpb + wib; u < units; u += (int64_t)gridDim.x * wpb) {
+        const int64_t s = u / Q;
+        const int h = (int)(u - s * Q);
+        if (s * 32 + h * R >= A.nforce) continue;  // warp-uniform: no force row in the unit
+        const int rl = h * R + j;  // the row's lane in the slice
+        const int64_t r = s * 32 + rl;
+        const bool force_row = r < A.nforce;
+        const int64_t rr = force_row ? r : A.nforce - 1;
+        const double xi = A.x[rr], yi = A.y[rr], zi = A.z[rr];
+        const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = A.uz[rr];
+        const float4 nab_i = A.nab[rr];
+        const ff nai{nab_i.x, nab_i.y}, nbi{nab_i.z, nab_i.w};
+        ff fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
+        const int W = A.width[s];
+        const int64_t b = A.base[s];
+        uint32_t* wbits = A.bits + A.fbase[s];
+        const int iters = (W + Q - 1) / Q;
+        for (int i = 0; i < iters; i++) {
+            const int k = i * Q + ph;
+            const int64_t slot = b + (int64_t)k * 32 + rl;
+            const uint32_t word = k < W ? wbits[k] : 0u;
+            const bool alive = force_row && ((word >> rl) & 1u);
+            bool brk = false;
+            if (alive) {
+                const float4 w0 = srec_w(A.sgeo, slot, 0), w1 = srec_w(A.sgeo, slot, 1);
+                const float4 w4 = srec_w(A.sfo, slot, 0), w5 = srec_w(A.sfo, slot, 1);
+                const int c = __float_as_int(w0.x);
+                const float xf[3] = {w0.y, w0.z, w0.w};
+                // as k_state_force<3>: the force pass's operand order, the z term of
+                // the length in the dilatation pass's (Force_State.cu:272)
+                ff eta[3], dp[3], y, e2, etaz;
+                eta[0] = bond_offset(A.pcx[c], xi, uxi, xf[0]);
+                eta[1] = bond_offset(A.pcy[c], yi, uyi, xf[1]);
+                eta[2] = exact_offset((hi_f64(w5) + A.uz[c]) - uzi, xf[2]);
+                etaz = bond_offset(A.pcz[c], zi, uzi, xf[2]);
+                pair_stretch<3>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
+                const float2 ec = A.e[slot];
+                const float4 nc = __ldg(A.nab + c);
+                const ff T = ff_add(ff_mul(ff{w4.x, w4.y}, ff_add(nai, ff{nc.x, nc.y})),
+                                    ff_mul(ff_mul(ff{w4.z, w4.w}, ff{ec.x, ec.y}), ff_add(nbi, ff{nc.z, nc.w})));
+                const ff t = ff_mul(T, ff{0.5f * y.h, 0.5f * y.l});
+                fxa = ff_add(fxa, ff_mul(t, dp[0]));
+                fya = ff_add(fya, ff_mul(t, dp[1]));
+                fza = ff_add(fza, ff_mul(t, ff_add_f(xf[2], etaz)));
+                brk = pair_exceeds(e2, lo_f64(w5));
+            }
+            const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+            if (broke && j == 0 && !A.nobreak) {
+                const uint32_t mine = (broke >> (ph * R)) & ((1u << R) - 1u);
+                if (mine) atomicAnd(wbits + k, ~(mine << (h * R)));
+            }
+        }
+#pragma unroll
+        for (int off = R; off < 32; off <<= 1) {
+            fxa = ff_add(fxa, ff{__shfl_xor_sync(0xffffffffu, fxa.h, off), __shfl_xor_sync(0xffffffffu, fxa.l, off)});
+            fya = ff_add(fya, ff{__shfl_xor_sync(0xffffffffu, fya.h, off), __shfl_xor_sync(0xffffffffu, fya.l, off)});
+            fza = ff_add(fza, ff{__shfl_xor_sync(0xffffffffu, fza.h, off), __shfl_xor_sync(0xffffffffu, fza.l, off)});
+        }
+        if (ph == 0 && force_row) {
+            // undo the power-of-two scale of T (exact)
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
+            const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.st_scale;
+            row_epilogue<3, EPI_NONE>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+        }
+    }
+}
+
 // ---- 2-D state-based passes on the compact layout -------------------------
 //
 // Per slot a 16-byte record for the dilatation pass (column; dl with the
@@ -1603,6 +1693,10 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         else
             k_state_compact<EPI_ADR><<<resident_grid(c, (const void*)k_state_compact<EPI_ADR>, A.nslices, blk,
                                                      waves), blk, 0, s>>>(A);
+    } else if (state && d3 && f.epi == EPI_NONE) {
+        constexpr int Q = kStatePhases3;
+        k_state_force3_phased<Q><<<resident_grid(c, (const void*)k_state_force3_phased<Q>, A.nslices * Q), kForceBlock,
+                                   0, s>>>(A);
     } else if (state) {
         PD_DISPATCH(k_state_force);
     } else {
