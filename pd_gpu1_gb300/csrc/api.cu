@@ -1049,7 +1049,7 @@ int pd_set_force_layout(pd_ctx* c, int layout) {
 int pd_get_force_layout(const pd_ctx* c, int* layout) {
     if (!c || !layout) return PD_ERR_ARG;
     const pdg::Sell& S = c->sell;
-    *layout = (S.rec16 || S.srec) ? PD_LAYOUT_COMPACT : (S.rec || S.sgeo) ? PD_LAYOUT_RECORDS : PD_LAYOUT_AUTO;
+    *layout = (S.rec16 || S.srec || S.sk) ? PD_LAYOUT_COMPACT : (S.rec || S.sgeo) ? PD_LAYOUT_RECORDS : PD_LAYOUT_AUTO;
     return PD_OK;
 }
 

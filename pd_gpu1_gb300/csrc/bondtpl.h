@@ -61,6 +61,19 @@ struct alignas(16) Tpl {
 };
 static_assert(sizeof(Tpl) == 64, "four 16-byte words");
 
+// One 3-D offset class: the same quantities as Tpl with three components
+// (five 16-byte words).
+struct alignas(16) Tpl3 {
+    uint64_t xd[3];  // xf as double bit patterns
+    float xf[3];     // the class's float reference vector
+    float xf2[3];    // 2 xf (exact)
+    float c0h, c0l;  // |xf|^2 - l0t^2 as a pair (computed exactly)
+    float q0h, q0l;  // |xf|^2 as a pair
+    float l0h, l0l;  // l0t as a pair
+    double l0d;      // l0t
+};
+static_assert(sizeof(Tpl3) == 80, "five 16-byte words");
+
 // Per-slot record: 16 bytes, one 128-bit load.
 struct alignas(16) Rec {
     int col;      // neighbour id (the row itself for padding)
@@ -286,6 +299,40 @@ PD_BT_HD void stretch2(const f2 eta[2], const Tpl& T, float dl, f2 w[2], f2& y, 
     e = mul(D, rcp2(Lp));
 }
 
+// The stretch of one 3-D bond, as stretch2 with three components: the
+// length from the exact offsets eta of the bond vector whose length the
+// caller wants (w = xf + eta per component), 1/L and e = L - l0.
+PD_BT_HD void stretch3(const f2 eta[3], const Tpl3& T, float dl, f2 w[3], f2& y, f2& e) {
+    float m[3], lo[3];
+#if defined(__CUDACC__)
+#pragma unroll
+#endif
+    for (int a = 0; a < 3; a++) {
+        f2 s = two_sum(T.xf[a], eta[a].h);
+        w[a] = f2{s.h, s.l + eta[a].l};
+        s = two_sum(T.xf2[a], eta[a].h);
+        const f2 v{s.h, s.l + eta[a].l};
+        m[a] = eta[a].h * v.h;
+        float r = fmaf(eta[a].h, v.h, -m[a]);
+        r = fmaf(eta[a].h, v.l, r);
+        lo[a] = fmaf(eta[a].l, v.h, r);
+    }
+    // S = eta . (2 xf + eta): the high parts summed exactly in two steps
+    const f2 s01 = two_sum(m[0], m[1]);
+    const f2 s = two_sum(s01.h, m[2]);
+    const float s_low = ((lo[0] + lo[1]) + lo[2]) + (s01.l + s.l);
+    const f2 dd = two_sum(s.h, T.c0h);
+    const float d_low = ((s_low + dd.l) + T.c0l) + (-2.0f * T.l0h) * dl;
+    const f2 D = fast_sum(dd.h, d_low);
+    const f2 qq = two_sum(T.q0h, s.h);
+    const f2 L2 = fast_sum(qq.h, (qq.l + s_low) + T.q0l);
+    y = rsqrt2(L2);
+    const f2 L = mul(L2, y);
+    const f2 lp = two_sum(L.h, T.l0h);
+    const f2 Lp = fast_sum(lp.h, ((lp.l + L.l) + T.l0l) + dl);
+    e = mul(D, rcp2(Lp));
+}
+
 PD_BT_HD BondOut bond2(const f2 eta[2], const Tpl& T, float dl, f2 k2half) {
     BondOut o;
     f2 w[2], y;
@@ -316,7 +363,8 @@ PD_BT_HD void acc_add(f2& acc, f2 v) {
 // of the threshold (tf = s0f * l0h is within 4 ulps of ecrit), then on the
 // double sum of the pair against the double threshold, the test of the
 // reference-rounded kernels.
-PD_BT_HD bool exceeds(f2 e, double s0, float s0f, const Tpl& T, float dl) {
+template <class TT>
+PD_BT_HD bool exceeds(f2 e, double s0, float s0f, const TT& T, float dl) {
     const float tf = s0f * T.l0h;
     const int hb = (int)fbits(e.h), tb = (int)fbits(tf);
     if (hb >= tb + 8) return true;   // e >= e.h - ulp/2 > tf (1 + 2^-21) > ecrit

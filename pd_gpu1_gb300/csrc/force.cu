@@ -112,6 +112,10 @@ struct ForceArgs {
     const int4* srec;         // dilatation pass: column, dl and class id, kx, ky
     const int2* srec8;        // force pass: column, dl and class id
     const StateTpl* stpl;     // per class: c1, c2, cth as pairs
+    // 3-D state-based compact layout (srec8 and stpl as above)
+    const bt::Tpl3* tpl3;     // 3-D class templates
+    const int4* sk;           // dilatation pass: kx, ky, kz, flags
+    const int2* skz;          // force pass: kz, flags
 };
 
 namespace {
@@ -1364,6 +1368,186 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
+// ---- 3-D state-based passes on the compact layout -------------------------
+//
+// Per slot an 8-byte record (column; dl with the offset class id) read by
+// both passes, {kx, ky, kz, flags} read by the dilatation pass and {kz,
+// flags} by the force pass; 80-byte class templates (bt::Tpl3) and the class
+// coefficients (StateTpl) as in 2-D.  Per slot and step: 8 + 16 + 8 bytes in
+// the dilatation pass, 8 + 8 + 8 in the force pass, against 72 and 72 with
+// the three 32-byte records.
+
+// d - x exactly as a pair, x the double value of a float (bit pattern xb).
+__device__ __forceinline__ bt::f2 offset1(double d, uint64_t xb) {
+    bt::f2 eta;
+    if (xb == 0)
+        eta = bt::split_bits(d);
+    else if (!bt::offset_pair(d, xb, eta))
+        eta = bt::split_bits(d - bt::dfrom(xb));  // exact by Sterbenz's lemma
+    return eta;
+}
+// One bond's exact offsets from its class's float reference vector.
+template <int N, class TT>
+__device__ __forceinline__ void offsets_n(const TT& T, const double* d, bt::f2* eta) {
+#pragma unroll
+    for (int a = 0; a < N; a++) eta[a] = offset1(d[a], T.xd[a]);
+}
+
+// Dilatation pass (kernel_cal_theta_3D, Force_State.cu:200-239) on rows [0,
+// N): the reference kernel skips broken bonds (its fail test); boundary rows,
+// which carry no flags in the reference (Memory.cu:39), count every bond.
+__global__ void __launch_bounds__(kForceBlock, 5) k_theta_compact3(const ForceArgs A) {
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const KParams& P = A.P;
+    for (int64_t s = (int64_t)blockIdx.x * wpb + wib; s < A.nslices; s += (int64_t)gridDim.x * wpb) {
+        const int64_t r = s * 32 + lane;
+        const bool row = r < P.N;
+        const int64_t rr = row ? r : P.N - 1;
+        const int nn = row ? A.NN[rr] : 0;
+        const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = A.uz[rr];
+        const bool check_bits = r < P.N_int;
+        const int W = A.width[s];
+        const int64_t b = A.base[s];
+        const uint32_t* wbits = A.bits + A.fbase[s];
+        const int2* rp = A.srec8 + b + lane;
+        const int4* kp = A.sk + b + lane;
+        bt::f2 acc{0.0f, 0.0f};  // sum of the weighted extensions, times 2^sth_exp
+        for (int k = 0; k < W; k++) {
+            bool use = k < nn;
+            if (check_bits) use = use && ((wbits[k] >> lane) & 1u);
+            if (use) {
+                const int2 rq = __ldg(rp + (int64_t)k * 32);
+                const int4 kq = __ldg(kp + (int64_t)k * 32);
+                const int c = rq.x;
+                const uint32_t dlb = (uint32_t)rq.y;
+                const int id = (int)(dlb & 0xffu);
+                const bt::Tpl3& T = A.tpl3[id];
+                const float dl = __uint_as_float(dlb & ~0xffu);
+                // x_c - x_i as the reference rounds it (the class vector moved by
+                // kx, ky, kz doubles), then d = (that + u_c) - u_i
+                const double xa = __longlong_as_double((long long)T.xd[0] + kq.x);
+                const double ya = __longlong_as_double((long long)T.xd[1] + kq.y);
+                const double za = __longlong_as_double((long long)T.xd[2] + kq.z);
+                const double d[3] = {(xa + __ldg(A.ux + c)) - uxi, (ya + __ldg(A.uy + c)) - uyi,
+                                     (za + __ldg(A.uz + c)) - uzi};
+                bt::f2 eta[3], w[3], y, e;
+                offsets_n<3>(T, d, eta);
+                bt::stretch3(eta, T, dl, w, y, e);
+                A.e[b + (int64_t)k * 32 + lane] = make_float2(e.h, e.l);
+                const float4 ct = __ldg(reinterpret_cast<const float4*>(A.stpl + id) + 1);
+                const bt::f2 cth{ct.x, fmaf(ct.x, ct.z * dl, ct.y)};
+                acc = bt::add(acc, bt::mul(cth, e));
+            }
+        }
+        if (row) {
+            const double m = A.m[r], rm = A.nb[r];
+            const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
+            const double th = div_recip(a, m, rm);
+            A.theta[r] = th;
+            const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
+            *reinterpret_cast<float2*>(A.nab + r) = make_float2(na.h, na.l);
+        }
+    }
+}
+
+// Force pass (kernel_state_force_3D, Force_State.cu:242-306) on rows [0,
+// N_int), on quarter-slice units as k_state_force3_phased: the length takes
+// x and y in the force pass's operand order and z in the dilatation pass's
+// (Force_State.cu:270-272), the direction the force pass's order in all three.
+// Epilogues without the next step's half-kick (the explicit step runs the
+// node pass after this kernel: the length gathers u_z of the neighbours).
+template <int EPI>
+__global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3(const ForceArgs A) {
+    constexpr int Q = kStatePhases3, R = 32 / Q;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const int j = lane % R, ph = lane / R;
+    const int64_t units = A.nslices * Q;
+    const double s0 = A.P.critical_s;
+    const float s0f = __double2float_rn(s0);
+    double red[3] = {0.0, 0.0, 0.0};
+    for (int64_t u = (int64_t)blockIdx.x * wpb + wib; u < units; u += (int64_t)gridDim.x * wpb) {
+        const int64_t s = u / Q;
+        const int h = (int)(u - s * Q);
+        if (s * 32 + h * R >= A.nforce) continue;  // warp-uniform: no force row in the unit
+        const int rl = h * R + j;
+        const int64_t r = s * 32 + rl;
+        const bool force_row = r < A.nforce;
+        const int64_t rr = force_row ? r : A.nforce - 1;
+        const double xi = A.x[rr], yi = A.y[rr], zi = A.z[rr];
+        const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = A.uz[rr];
+        const float4 nab_i = A.nab[rr];
+        const bt::f2 nai{nab_i.x, nab_i.y}, nbi{nab_i.z, nab_i.w};
+        bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
+        const int W = A.width[s];
+        const int64_t b = A.base[s];
+        uint32_t* wbits = A.bits + A.fbase[s];
+        const int iters = (W + Q - 1) / Q;
+        for (int i = 0; i < iters; i++) {
+            const int k = i * Q + ph;
+            const int64_t slot = b + (int64_t)k * 32 + rl;
+            const uint32_t word = k < W ? wbits[k] : 0u;
+            const bool alive = force_row && ((word >> rl) & 1u);
+            bool brk = false;
+            if (alive) {
+                const int2 rq = __ldg(A.srec8 + slot);
+                const int2 kz = __ldg(A.skz + slot);
+                const int c = rq.x;
+                const uint32_t dlb = (uint32_t)rq.y;
+                const int id = (int)(dlb & 0xffu);
+                const bt::Tpl3& T = A.tpl3[id];
+                const float dl = __uint_as_float(dlb & ~0xffu);
+                const double za = __longlong_as_double((long long)T.xd[2] + kz.x);
+                // the length's components: x, y in the force order, z in the
+                // dilatation order; then the force order's z for the direction
+                const double dlen[3] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi,
+                                        (za + __ldg(A.uz + c)) - uzi};
+                const double dzf = (__ldg(A.pcz + c) - zi) - uzi;
+                bt::f2 eta[3], w[3], y, ef, etz;
+                offsets_n<3>(T, dlen, eta);
+                etz = offset1(dzf, T.xd[2]);
+                bt::stretch3(eta, T, dl, w, y, ef);
+                const bt::f2 sz = bt::two_sum(T.xf[2], etz.h);
+                const bt::f2 wz{sz.h, sz.l + etz.l};
+                // c1, c2 of the class moved to this bond's length (1 + g dl)
+                const float4 cc = __ldg(reinterpret_cast<const float4*>(A.stpl + id));
+                const float2 gg = __ldg(reinterpret_cast<const float2*>(A.stpl + id) + 3);
+                const bt::f2 c1{cc.x, fmaf(cc.x, gg.x * dl, cc.y)}, c2{cc.z, fmaf(cc.z, gg.y * dl, cc.w)};
+                const float2 ec = A.e[slot];
+                const float4 nc = __ldg(A.nab + c);
+                const bt::f2 Tt = bt::add(bt::mul(c1, bt::add(nai, bt::f2{nc.x, nc.y})),
+                                          bt::mul(bt::mul(c2, bt::f2{ec.x, ec.y}), bt::add(nbi, bt::f2{nc.z, nc.w})));
+                const bt::f2 t = bt::mul(Tt, bt::f2{0.5f * y.h, 0.5f * y.l});
+                bt::acc_add(fxa, bt::mul(t, w[0]));
+                bt::acc_add(fya, bt::mul(t, w[1]));
+                bt::acc_add(fza, bt::mul(t, wz));
+                brk = (kz.y & 1) && bt::exceeds(ef, s0, s0f, T, dl);
+            }
+            const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+            if (broke && j == 0 && !A.nobreak) {
+                const uint32_t mine = (broke >> (ph * R)) & ((1u << R) - 1u);
+                if (mine) atomicAnd(wbits + k, ~(mine << (h * R)));
+            }
+        }
+#pragma unroll
+        for (int off = R; off < 32; off <<= 1) {
+            fxa = bt::add(fxa, bt::f2{__shfl_xor_sync(0xffffffffu, fxa.h, off), __shfl_xor_sync(0xffffffffu, fxa.l, off)});
+            fya = bt::add(fya, bt::f2{__shfl_xor_sync(0xffffffffu, fya.h, off), __shfl_xor_sync(0xffffffffu, fya.l, off)});
+            fza = bt::add(fza, bt::f2{__shfl_xor_sync(0xffffffffu, fza.h, off), __shfl_xor_sync(0xffffffffu, fza.l, off)});
+        }
+        if (ph == 0 && force_row) {
+            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
+            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
+            const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.st_scale;
+            row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+        }
+    }
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+}
+
 // Standalone kernel_cnn + cal_cn (Integrate.cu:7-49, :108-129) on the current forces.
 template <int DIM>
 __global__ void __launch_bounds__(kForceBlock) k_adr_cnn(const ForceArgs A) {
@@ -1508,6 +1692,9 @@ static ForceArgs make_args(pd_ctx* c) {
     A.srec = S.srec;
     A.srec8 = S.srec8;
     A.stpl = S.stpl;
+    A.tpl3 = S.tpl3;
+    A.sk = S.sk;
+    A.skz = S.skz;
     return A;
 }
 
@@ -1535,6 +1722,8 @@ int launch_theta(pd_ctx* c, cudaStream_t s) {
     }
     else if (A.P.dim == 2)
         k_theta<2><<<resident_grid(c, (const void*)k_theta<2>, A.nslices), kForceBlock, 0, s>>>(A);
+    else if (A.sk)
+        k_theta_compact3<<<resident_grid(c, (const void*)k_theta_compact3, A.nslices), kForceBlock, 0, s>>>(A);
     else
         k_theta<3><<<resident_grid(c, (const void*)k_theta<3>, A.nslices), kForceBlock, 0, s>>>(A);
     c->launches++;
@@ -1693,6 +1882,17 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         else
             k_state_compact<EPI_ADR><<<resident_grid(c, (const void*)k_state_compact<EPI_ADR>, A.nslices, blk,
                                                      waves), blk, 0, s>>>(A);
+    } else if (state && d3 && A.sk) {
+        constexpr int Q = kStatePhases3;
+        if (f.epi == EPI_NONE)
+            k_state_compact3<EPI_NONE><<<resident_grid(c, (const void*)k_state_compact3<EPI_NONE>, A.nslices * Q),
+                                         kForceBlock, 0, s>>>(A);
+        else if (f.epi == EPI_VERLET)
+            k_state_compact3<EPI_VERLET><<<resident_grid(c, (const void*)k_state_compact3<EPI_VERLET>, A.nslices * Q),
+                                           kForceBlock, 0, s>>>(A);
+        else
+            k_state_compact3<EPI_ADR><<<resident_grid(c, (const void*)k_state_compact3<EPI_ADR>, A.nslices * Q),
+                                        kForceBlock, 0, s>>>(A);
     } else if (state && d3 && f.epi == EPI_NONE) {
         constexpr int Q = kStatePhases3;
         k_state_force3_phased<Q><<<resident_grid(c, (const void*)k_state_force3_phased<Q>, A.nslices * Q), kForceBlock,

@@ -156,6 +156,13 @@ struct Sell {
     int4* srec = nullptr;       // [S]
     int2* srec8 = nullptr;      // [S]
     StateTpl* stpl = nullptr;   // [ntpl]
+    // 3-D state-based compact layout: srec8 and stpl as in 2-D, 3-D class
+    // templates, and per slot {kx, ky, kz, flags} for the dilatation pass and
+    // {kz, flags} for the force pass (flags bit 0: the bond may break; the 3-D
+    // kernels spare bonds with an end below y = -0.04)
+    bt::Tpl3* tpl3 = nullptr;   // [ntpl]
+    int4* sk = nullptr;         // [S]
+    int2* skz = nullptr;        // [S]
 };
 
 // Layout of the bond-based force path (pd_set_force_layout).

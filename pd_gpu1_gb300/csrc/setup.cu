@@ -391,12 +391,28 @@ __device__ __forceinline__ unsigned long long class_key(double xa, double ya) {
 __device__ __forceinline__ unsigned class_hash(unsigned long long k) {
     return (unsigned)((k * 0x9E3779B97F4A7C15ull) >> 56);  // 8 bits
 }
+// 3-D: a 64-bit mix of the three float components.  Not injective: the
+// inserting thread stores its float vector beside the key, and the record
+// fill checks every member's vector against its class's (a collision makes
+// the layout unsupported, never a wrong class).
+__device__ __forceinline__ unsigned long long class_key3(double xa, double ya, double za) {
+    unsigned long long k = ((unsigned long long)__float_as_uint(__double2float_rn(xa)) << 32) |
+                           (unsigned long long)__float_as_uint(__double2float_rn(ya));
+    k ^= (unsigned long long)__float_as_uint(__double2float_rn(za)) * 0xD6E8FEB86659FD93ull;
+    k ^= k >> 31;
+    k *= 0xBF58476D1CE4E5B9ull;
+    k ^= k >> 29;
+    return k == kEmptyKey ? 0ull : k;
+}
 
+// z null: 2-D keys (the float vector itself); otherwise 3-D keys, and the
+// thread that inserts a key writes its float vector into vec.
 __global__ void k_class_insert(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
                                const int* __restrict__ csr, const int* __restrict__ NL, const int* __restrict__ grp,
                                const double* __restrict__ x, const double* __restrict__ y,
-                               const double* __restrict__ idist, unsigned long long* __restrict__ keys,
-                               unsigned long long* __restrict__ l0min, int* __restrict__ overflow) {
+                               const double* __restrict__ z, const double* __restrict__ idist,
+                               unsigned long long* __restrict__ keys, unsigned long long* __restrict__ l0min,
+                               float4* __restrict__ vec, int* __restrict__ overflow) {
     const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
     if (s >= nslices) return;
     const int W = width[s];
@@ -406,7 +422,8 @@ __global__ void k_class_insert(int64_t nslices, const int* __restrict__ width, c
         if (q < 0) continue;
         const int64_t r = s * 32 + (t & 31), c = NL[q];
         const int64_t region = grp ? grp[r] : 0;
-        const unsigned long long key = class_key(x[c] - x[r], y[c] - y[r]);
+        const double xa = x[c] - x[r], ya = y[c] - y[r], za = z ? z[c] - z[r] : 0.0;
+        const unsigned long long key = z ? class_key3(xa, ya, za) : class_key(xa, ya);
         const unsigned long long lb = (unsigned long long)__double_as_longlong(idist[q]);
         unsigned h = class_hash(key);
         bool done = false;
@@ -415,6 +432,8 @@ __global__ void k_class_insert(int64_t nslices, const int* __restrict__ width, c
             const unsigned long long prev = atomicCAS(keys + i, kEmptyKey, key);
             if (prev == kEmptyKey || prev == key) {
                 atomicMin(l0min + i, lb);  // positive doubles order like their bit patterns
+                if (prev == kEmptyKey && vec)
+                    vec[i] = make_float4(__double2float_rn(xa), __double2float_rn(ya), __double2float_rn(za), 0.0f);
                 done = true;
             }
         }
@@ -478,14 +497,21 @@ __global__ void k_rec16_fill(KParams P, int64_t nslices, const int* __restrict__
     }
 }
 
-// The coefficients of one 2-D state-based bond (the state records of
+// The coefficients of one state-based bond (the state records of
 // k_sell_fill), with the context's power-of-two scales, in doubles.
 __device__ __forceinline__ void state_coefs(const KParams& P, double L0, double w, double fac, int sn_exp,
                                             int sth_exp, int st_exp, double& cth, double& c1, double& c2) {
     const double pr = P.pratio;
-    const double a_coef = (2.0 * pr - 1.0) / (pr - 1.0) * (2.0 * P.K - 32.0 * P.G / 9.0);
-    const double b_coef = 8.0 * P.G;
-    const double th_coef = 2.0 * (2.0 * pr - 1.0) / (pr - 1.0);
+    double a_coef, b_coef, th_coef;
+    if (P.dim == 2) {
+        a_coef = (2.0 * pr - 1.0) / (pr - 1.0) * (2.0 * P.K - 32.0 * P.G / 9.0);
+        b_coef = 8.0 * P.G;
+        th_coef = 2.0 * (2.0 * pr - 1.0) / (pr - 1.0);
+    } else {
+        a_coef = 3.0 * P.K - 5.0 * P.G;  // 3K th w L0/m + 15G/m w (e - th L0/3)
+        b_coef = 15.0 * P.G;
+        th_coef = 3.0;
+    }
     const double wf = w * fac * P.vol;
     cth = th_coef * w * L0 * fac * P.vol * ldexp(1.0, sth_exp);
     const double cs = ldexp(1.0, sn_exp - st_exp);
@@ -556,6 +582,84 @@ __global__ void k_state_compact_fill(KParams P, int64_t nslices, const int* __re
         const int dlw = (int)((dlb & ~0xffu) | (unsigned)(id & 0xff));
         rec[slot] = make_int4((int)c, dlw, (int)k[0], (int)k[1]);
         rec8[slot] = make_int2((int)c, dlw);
+        if (!fail && dlv == 0.0) {
+            double cth, c1, c2;
+            state_coefs(P, L0, w[q], fac[q], sn_exp, sth_exp, st_exp, cth, c1, c2);
+            const ff a = ff_split(c1), bb = ff_split(c2), t3 = ff_split(cth);
+            StateTpl& T = stpl[id];  // g1, g2 come from the host
+            T.c1h = a.h, T.c1l = a.l, T.c2h = bb.h, T.c2l = bb.l;
+            T.cth_h = t3.h, T.cth_l = t3.l;
+        }
+    }
+}
+
+// Records of the 3-D state-based compact layout: rec8 = {column, dl with
+// the class id}; sk = {kx, ky, kz, flags} (the reference vector x_c - x_i as
+// the class's float vector moved by kx, ky, kz representable doubles; flags
+// bit 0: the bond may break, both ends at y >= -0.04, Force_State.cu:283);
+// skz = {kz, flags}.  The class coefficients come from the slots with dl = 0
+// as in k_state_compact_fill.  *bad also where a slot's float vector is not
+// its class's (a key collision).
+__global__ void k_state_compact3_fill(KParams P, int64_t nslices, const int* __restrict__ width,
+                                      const int64_t* __restrict__ base, const int* __restrict__ csr,
+                                      const int* __restrict__ NL, const double* __restrict__ x,
+                                      const double* __restrict__ y, const double* __restrict__ z,
+                                      const double* __restrict__ idist, const double* __restrict__ fac,
+                                      const double* __restrict__ w, const unsigned long long* __restrict__ keys,
+                                      const int* __restrict__ ids, const bt::Tpl3* __restrict__ tpl, int sn_exp,
+                                      int sth_exp, int st_exp, int2* __restrict__ rec8, int4* __restrict__ sk,
+                                      int2* __restrict__ skz, StateTpl* __restrict__ stpl, int* __restrict__ bad) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int64_t slot = b + t;
+        const int q = csr[slot];
+        const int64_t r = s * 32 + (t & 31);
+        if (q < 0) {
+            rec8[slot] = make_int2((int)(r < P.N ? r : 0), 0);
+            sk[slot] = make_int4(0, 0, 0, 0);
+            skz[slot] = make_int2(0, 0);
+            continue;
+        }
+        const int64_t c = NL[q];
+        // the reference's roundings of the reference vector (Force_State.cu:217-219)
+        const double xv[3] = {x[c] - x[r], y[c] - y[r], z[c] - z[r]};
+        const unsigned long long key = class_key3(xv[0], xv[1], xv[2]);
+        unsigned h = class_hash(key);
+        int id = -1;
+        for (int probe = 0; probe < kRegion; probe++, h = (h + 1) & (kRegion - 1)) {
+            if (keys[h] == key) {
+                id = ids[h];
+                break;
+            }
+            if (keys[h] == kEmptyKey) break;
+        }
+        bool fail = id < 0 || id > 255;
+        const double L0 = idist[q];
+        double dlv = 0.0;
+        long long k[3] = {0, 0, 0};
+        if (!fail) {
+            const bt::Tpl3& T = tpl[id];
+            dlv = L0 - T.l0d;
+            for (int a = 0; a < 3; a++) {
+                if (__double2float_rn(xv[a]) != T.xf[a]) fail = true;  // another vector under the same key
+                const long long xb = (long long)T.xd[a];
+                const long long vb = __double_as_longlong(xv[a]);
+                k[a] = vb - xb;
+                if ((vb < 0) != (xb < 0) || k[a] < INT_MIN || k[a] > INT_MAX) fail = true;
+            }
+        }
+        const float dl = __double2float_rn(dlv);
+        const unsigned dlb = __float_as_uint(dl);
+        if ((double)dl != dlv || (dlb & 0xffu) != 0u) fail = true;
+        if (fail) atomicExch(bad, 1);
+        const int dlw = (int)((dlb & ~0xffu) | (unsigned)(id & 0xff));
+        const int flags = (y[r] >= P.break_ymin && y[c] >= P.break_ymin) ? 1 : 0;
+        rec8[slot] = make_int2((int)c, dlw);
+        sk[slot] = make_int4((int)k[0], (int)k[1], (int)k[2], flags);
+        skz[slot] = make_int2((int)k[2], flags);
         if (!fail && dlv == 0.0) {
             double cth, c1, c2;
             state_coefs(P, L0, w[q], fac[q], sn_exp, sth_exp, st_exp, cth, c1, c2);
@@ -763,6 +867,9 @@ static void free_sell(Sell& S) {
     free_ptr(S.srec);
     free_ptr(S.srec8);
     free_ptr(S.stpl);
+    free_ptr(S.tpl3);
+    free_ptr(S.sk);
+    free_ptr(S.skz);
     S.ntpl = 0;
     S.nslices = S.S = S.F = 0;
 }
@@ -772,27 +879,33 @@ void release_sell(pd_ctx* c) {
     free_sell(c->sell);
 }
 
-// The compact layout of a 2-D bond-based problem (S.csr filled): offset
-// classes per specimen, their templates and the 16-byte slot records.
-// Returns PD_ERR_UNSUPPORTED (arrays released) where the problem does not fit
-// it: more than 255 classes in a specimen (or a region of the hash table
-// full), or a bond length that differs from its class's smallest by more
-// than a float with a free low byte can hold.
+// The compact layout (S.csr filled): offset classes per specimen, their
+// templates and the slot records, for 2-D bond-based problems (one specimen
+// or a batch) and state-based problems in 2-D and 3-D.  Returns
+// PD_ERR_UNSUPPORTED (arrays released) where the problem does not fit it:
+// more than 255 classes in a specimen (or a region of the hash table full), a
+// bond length that differs from its class's smallest by more than a float
+// with a free low byte can hold, a reference vector too far from its class's
+// float vector, a coefficient off its class's by more than 2^-45, or (3-D) a
+// key shared by two float vectors.
 int build_compact(pd_ctx* c, cudaStream_t s) {
     const KParams P = kparams(c->p);
     Sell& S = c->sell;
     const int* grp = c->batch.node_group;
     const int64_t regions = c->batch.count > 0 ? c->batch.count : 1;
     const int64_t tsize = regions * kRegion;
+    const bool state = c->p.model == PD_MODEL_STATE;
+    const bool d3 = c->p.dim == 3;
     unsigned long long *keys = nullptr, *l0min = nullptr;
     int *ids = nullptr, *flags = nullptr;
+    float4* vec = nullptr;
     auto cleanup = [&]() {
         cudaFreeAsync(keys, s);
         cudaFreeAsync(l0min, s);
         cudaFreeAsync(ids, s);
         cudaFreeAsync(flags, s);
+        if (vec) cudaFreeAsync(vec, s);
     };
-    const bool state = c->p.model == PD_MODEL_STATE;
     auto release = [&]() {
         free_ptr(S.tpl);
         free_ptr(S.rec16);
@@ -800,25 +913,34 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         free_ptr(S.srec);
         free_ptr(S.srec8);
         free_ptr(S.stpl);
+        free_ptr(S.tpl3);
+        free_ptr(S.sk);
+        free_ptr(S.skz);
         S.ntpl = 0;
     };
+    if (d3 && !state) return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 3-D state-based problems");
     if (cudaMallocAsync(&keys, tsize * 8, s) || cudaMallocAsync(&l0min, tsize * 8, s) ||
-        cudaMallocAsync(&ids, tsize * 4, s) || cudaMallocAsync(&flags, 2 * 4, s)) {
+        cudaMallocAsync(&ids, tsize * 4, s) || cudaMallocAsync(&flags, 2 * 4, s) ||
+        (d3 && cudaMallocAsync(&vec, tsize * sizeof(float4), s))) {
         cleanup();
         return set_err(c, PD_ERR_NOMEM, "offset-class table");
     }
     cudaMemsetAsync(keys, 0xff, tsize * 8, s);
     cudaMemsetAsync(l0min, 0xff, tsize * 8, s);
     cudaMemsetAsync(flags, 0, 2 * 4, s);
+    if (vec) cudaMemsetAsync(vec, 0, tsize * sizeof(float4), s);
     const unsigned gx = (unsigned)std::min<int64_t>(S.nslices, 65535);
     const unsigned gy = (unsigned)((S.nslices + gx - 1) / gx);
     k_class_insert<<<dim3(gx, gy), 256, 0, s>>>(S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
-                                                 c->nf[PD_F_Y], c->idist, keys, l0min, flags);
+                                                 c->nf[PD_F_Y], d3 ? c->nf[PD_F_Z] : nullptr, c->idist, keys, l0min,
+                                                 vec, flags);
     c->launches++;
     std::vector<unsigned long long> hk((size_t)tsize), hl((size_t)tsize);
+    std::vector<float4> hv(d3 ? (size_t)tsize : 0);
     int hflags[2] = {0, 0};
     cudaMemcpyAsync(hk.data(), keys, tsize * 8, cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hl.data(), l0min, tsize * 8, cudaMemcpyDeviceToHost, s);
+    if (d3) cudaMemcpyAsync(hv.data(), vec, tsize * sizeof(float4), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(hflags, flags, 2 * 4, cudaMemcpyDeviceToHost, s);
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
@@ -829,8 +951,12 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         cleanup();
         return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: a specimen with more offset classes than its table");
     }
-    // templates, numbered per specimen in key order
+    // templates, numbered per specimen in key order: a float vector xf and
+    // the smallest bond length l0t of the class; |xf|^2, |xf|^2 - l0t^2 and
+    // l0t as exact pairs
     std::vector<bt::Tpl> tp;
+    std::vector<bt::Tpl3> tp3;
+    std::vector<double> l0ts;
     std::vector<int> hid((size_t)tsize, -1), tbase((size_t)regions, 0);
     for (int64_t g = 0; g < regions; g++) {
         std::vector<std::pair<unsigned long long, int64_t>> used;
@@ -842,81 +968,122 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
             return set_err(c, PD_ERR_UNSUPPORTED,
                            "compact layout: " + std::to_string(used.size()) + " offset classes in a specimen");
         }
-        tbase[g] = (int)tp.size();
+        tbase[g] = (int)l0ts.size();
         for (size_t k = 0; k < used.size(); k++) {
             const unsigned long long key = used[k].first;
-            hid[used[k].second] = (int)k;
-            bt::Tpl T;
-            const float xf[2] = {bt::ffrom((uint32_t)(key >> 32)), bt::ffrom((uint32_t)key)};
+            const int64_t slot = used[k].second;
+            hid[slot] = (int)k;
+            float xf[3] = {0.0f, 0.0f, 0.0f};
+            if (d3) {
+                xf[0] = hv[slot].x, xf[1] = hv[slot].y, xf[2] = hv[slot].z;
+            } else {
+                xf[0] = bt::ffrom((uint32_t)(key >> 32)), xf[1] = bt::ffrom((uint32_t)key);
+            }
+            const int nd = d3 ? 3 : 2;
             double sh = 0.0, sl = 0.0;
-            for (int a = 0; a < 2; a++) {
-                T.xf[a] = xf[a];
-                T.xf2[a] = 2.0f * xf[a];
-                T.xd[a] = bt::dbits((double)xf[a]);
+            for (int a = 0; a < nd; a++) {
                 const double sq = (double)xf[a] * (double)xf[a];  // exact: 24-bit significands
                 const double t = sh + sq, bb = t - sh;
                 sl += (sh - (t - bb)) + (sq - bb);
                 sh = t;
             }
-            const double l0t = bt::dfrom(hl[used[k].second]);
+            const double l0t = bt::dfrom(hl[slot]);
             const double ph = l0t * l0t, pl = std::fma(l0t, l0t, -ph);
             const bt::f2 c0 = bt::split_bits((sh - ph) + (sl - pl));  // sh - ph exact (Sterbenz)
             const bt::f2 q0 = bt::split_bits(sh + sl);
             const bt::f2 l0 = bt::split_bits(l0t);
-            T.c0h = c0.h, T.c0l = c0.l;
-            T.q0h = q0.h, T.q0l = q0.l;
-            T.l0h = l0.h, T.l0l = l0.l;
-            T.l0d = l0t;
-            tp.push_back(T);
+            l0ts.push_back(l0t);
+            if (d3) {
+                bt::Tpl3 T;
+                for (int a = 0; a < 3; a++) {
+                    T.xf[a] = xf[a];
+                    T.xf2[a] = 2.0f * xf[a];
+                    T.xd[a] = bt::dbits((double)xf[a]);
+                }
+                T.c0h = c0.h, T.c0l = c0.l, T.q0h = q0.h, T.q0l = q0.l, T.l0h = l0.h, T.l0l = l0.l;
+                T.l0d = l0t;
+                tp3.push_back(T);
+            } else {
+                bt::Tpl T;
+                for (int a = 0; a < 2; a++) {
+                    T.xf[a] = xf[a];
+                    T.xf2[a] = 2.0f * xf[a];
+                    T.xd[a] = bt::dbits((double)xf[a]);
+                }
+                T.c0h = c0.h, T.c0l = c0.l, T.q0h = q0.h, T.q0l = q0.l, T.l0h = l0.h, T.l0l = l0.l;
+                T.l0d = l0t;
+                tp.push_back(T);
+            }
         }
     }
-    if (tp.empty()) {
+    const size_t ntpl = l0ts.size();
+    if (ntpl == 0) {
         cleanup();
         return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: no bonds");
     }
-    S.ntpl = (int)tp.size();
+    S.ntpl = (int)ntpl;
     const size_t nrec = (size_t)std::max<int64_t>(S.S, 1);
-    if (cudaMalloc(&S.tpl, tp.size() * sizeof(bt::Tpl)) ||
-        (!state && cudaMalloc(&S.rec16, nrec * sizeof(bt::Rec))) ||
-        (state && (cudaMalloc(&S.srec, nrec * sizeof(int4)) || cudaMalloc(&S.srec8, nrec * sizeof(int2)) ||
-                   cudaMalloc(&S.stpl, tp.size() * sizeof(StateTpl)))) ||
-        (regions > 1 && cudaMalloc(&S.inst_tbase, regions * sizeof(int)))) {
+    bool ok = true;
+    if (d3)
+        ok = !cudaMalloc(&S.tpl3, ntpl * sizeof(bt::Tpl3)) && !cudaMalloc(&S.srec8, nrec * sizeof(int2)) &&
+             !cudaMalloc(&S.sk, nrec * sizeof(int4)) && !cudaMalloc(&S.skz, nrec * sizeof(int2)) &&
+             !cudaMalloc(&S.stpl, ntpl * sizeof(StateTpl));
+    else if (state)
+        ok = !cudaMalloc(&S.tpl, ntpl * sizeof(bt::Tpl)) && !cudaMalloc(&S.srec, nrec * sizeof(int4)) &&
+             !cudaMalloc(&S.srec8, nrec * sizeof(int2)) && !cudaMalloc(&S.stpl, ntpl * sizeof(StateTpl));
+    else
+        ok = !cudaMalloc(&S.tpl, ntpl * sizeof(bt::Tpl)) && !cudaMalloc(&S.rec16, nrec * sizeof(bt::Rec));
+    if (ok && regions > 1) ok = !cudaMalloc(&S.inst_tbase, regions * sizeof(int));
+    if (!ok) {
         cleanup();
         release();
         return set_err(c, PD_ERR_NOMEM, "compact records");
     }
-    cudaMemcpyAsync(S.tpl, tp.data(), tp.size() * sizeof(bt::Tpl), cudaMemcpyHostToDevice, s);
+    if (d3)
+        cudaMemcpyAsync(S.tpl3, tp3.data(), ntpl * sizeof(bt::Tpl3), cudaMemcpyHostToDevice, s);
+    else
+        cudaMemcpyAsync(S.tpl, tp.data(), ntpl * sizeof(bt::Tpl), cudaMemcpyHostToDevice, s);
     cudaMemcpyAsync(ids, hid.data(), tsize * 4, cudaMemcpyHostToDevice, s);
     if (S.inst_tbase) cudaMemcpyAsync(S.inst_tbase, tbase.data(), regions * sizeof(int), cudaMemcpyHostToDevice, s);
+    std::vector<StateTpl> st;
     if (state) {
         // logarithmic derivatives of the coefficients at each class's l0t: the
         // weight exp(-l0^2/delta^2) gives -2 l0 / delta^2; the partial-volume
         // factor (delta + dx/2 - l0) / dx (kernel_vol_Corr, Surf_Corr.cu:26-31)
         // above delta - dx/2 gives -1 / (delta + dx/2 - l0); l0 itself 1 / l0
-        std::vector<StateTpl> st(tp.size());
+        st.resize(ntpl);
         const double dlt = c->p.delta, hdx = c->p.dx / 2.0;
-        for (size_t k = 0; k < tp.size(); k++) {
-            const double l0t = tp[k].l0d;
+        for (size_t k = 0; k < ntpl; k++) {
+            const double l0t = l0ts[k];
             double g2 = -2.0 * l0t / (dlt * dlt);
             if (l0t > dlt - hdx) g2 -= 1.0 / (dlt + hdx - l0t);
             st[k] = StateTpl{};
             st[k].g2 = (float)g2;
             st[k].g1 = (float)(g2 + 1.0 / l0t);
         }
-        cudaMemcpyAsync(S.stpl, st.data(), st.size() * sizeof(StateTpl), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(S.stpl, st.data(), ntpl * sizeof(StateTpl), cudaMemcpyHostToDevice, s);
+    }
+    if (d3) {
+        k_state_compact3_fill<<<dim3(gx, gy), 256, 0, s>>>(
+            P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac,
+            c->w, keys, ids, S.tpl3, S.sn_exp, S.sth_exp, S.st_exp, S.srec8, S.sk, S.skz, S.stpl, flags + 1);
+    } else if (state) {
         k_state_compact_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X],
                                                            c->nf[PD_F_Y], c->idist, c->fac, c->w, keys, ids, S.tpl,
                                                            S.sn_exp, S.sth_exp, S.st_exp, S.srec, S.srec8, S.stpl,
                                                            flags + 1);
+    } else {
+        k_rec16_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
+                                                   c->nf[PD_F_Y], c->idist, c->fac, c->scr, c->batch.node_bc, keys,
+                                                   ids, S.inst_tbase, S.tpl, 0.5 * S.kscale_inv, S.rec16, flags + 1);
+    }
+    c->launches++;
+    if (state) {
         k_state_compact_check<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->idist, c->fac,
                                                             c->w, S.srec8, S.stpl, S.sn_exp, S.sth_exp, S.st_exp,
                                                             flags + 1);
         c->launches++;
-    } else
-        k_rec16_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, grp, c->nf[PD_F_X],
-                                                   c->nf[PD_F_Y], c->idist, c->fac, c->scr, c->batch.node_bc, keys,
-                                                   ids, S.inst_tbase, S.tpl, 0.5 * S.kscale_inv, S.rec16, flags + 1);
-    c->launches++;
+    }
     cudaMemcpyAsync(hflags + 1, flags + 1, 4, cudaMemcpyDeviceToHost, s);
     e = cudaStreamSynchronize(s);
     cleanup();
@@ -926,7 +1093,7 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
     }
     if (hflags[1]) {
         release();
-        return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: a bond length outside its class's float range");
+        return set_err(c, PD_ERR_UNSUPPORTED, "compact layout: a bond outside its offset class's ranges");
     }
     return PD_OK;
 }
@@ -971,13 +1138,15 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
     bool ok = !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
-    // 2-D problems try the compact layout first (16-byte records on
-    // offset-class templates); the 48-byte (bond-based) and three 32-byte
-    // (state-based) records are the general layout
-    const bool try_compact = P.dim == 2 && c->layout_pref != LAYOUT_RECORDS;
+    // 2-D problems and 3-D state-based ones try the compact layout first
+    // (small per-slot records on offset-class templates); the 48-byte
+    // (bond-based) and three 32-byte (state-based) records are the general
+    // layout
+    const bool fits_compact = P.dim == 2 || state;
+    const bool try_compact = fits_compact && c->layout_pref != LAYOUT_RECORDS;
     if (c->layout_pref == LAYOUT_COMPACT && !try_compact) {
         free_sell(S);
-        return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 2-D problems");
+        return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 2-D problems and 3-D state-based ones");
     }
     if (ok && !state && !try_compact)
         ok = !cudaMalloc(&S.rec, n8 * 6);

@@ -565,9 +565,10 @@ def helpers_ell(values, NN, MN):
 
 def test_compact_layout_selection(E):
     """Where the compact layout applies: 2-D problems (bond- and state-based)
-    take it by default; 3-D ones keep the records, and asking for the compact
-    layout there is refused (PD_ERR_UNSUPPORTED, -8) without disturbing the
-    context, which then runs on the records."""
+    and 3-D state-based ones take it by default; 3-D bond-based ones keep the
+    records, and asking for the compact layout there is refused
+    (PD_ERR_UNSUPPORTED, -8) without disturbing the context, which then runs
+    on the records."""
     from pd_gpu1_gb300 import presets
     from pd_gpu1_gb300._abi import PD_MODEL_BOND
 
@@ -590,6 +591,10 @@ def test_compact_layout_selection(E):
         eng.set_force_layout("records")
         eng.prepare()
         assert eng.force_layout() == "records"
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10)
+    with E.Engine(p) as eng:
+        setup(eng)
+        assert eng.force_layout() == "compact"
 
 
 def test_state_compact_layout_matches_records(E):
@@ -656,3 +661,45 @@ def test_state_compact_launch_shapes_bitwise(E):
     for o in outs[1:]:
         for a, b in zip(outs[0], o):
             np.testing.assert_array_equal(a, b)
+
+
+def test_state_compact_3d_matches_records(E):
+    """The 3-D state-based passes on the compact layout against the three
+    32-byte records, on the notched impact slab: dilatation and forces within
+    2e-13 norm-relative at strains of a few percent, the same intact flags
+    after a second pass (the y >= -0.04 guard included), and 30 explicit steps
+    with the impactor in contact within 1e-11."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=30)
+    rng = np.random.default_rng(7)
+    u = rng.standard_normal((3, p.N)) * 5e-5  # dx = 2e-3: bond strains of a few percent
+    out = {}
+    with E.Engine(p) as eng:
+        for layout in ("compact", "records"):
+            eng.set_force_layout(layout)
+            setup(eng)
+            assert eng.force_layout() == layout
+            fail0 = eng.get("FAIL")
+            for k, f in enumerate(("UX", "UY", "UZ")):
+                eng.set(f, u[k])
+            eng.state_force_gpu()
+            first = (eng.get("FX"), eng.get("FY"), eng.get("FZ"), eng.get("THETA"))
+            eng.state_force_gpu()
+            second = (eng.get("FX"), eng.get("FY"), eng.get("FZ"), eng.get("FAIL"))
+            setup(eng)
+            c2 = meta["cylinder"]
+            c2.disp[1] = -0.3 * p.dx
+            eng.cylinder_init(c2)
+            eng.run_explicit(30)
+            out[layout] = first + second + (eng.get("UY"), eng.get("UZ"), eng.get("FAIL"), eng.cylinder().vel[1])
+        n = p.N_int
+        for k, what in ((0, "fx"), (1, "fy"), (2, "fz"), (4, "fx 2"), (5, "fy 2"), (6, "fz 2")):
+            assert_close_norm(out["compact"][k][:n], out["records"][k][:n], 2e-13, what)
+        assert_close_norm(out["compact"][3], out["records"][3], 2e-13, "theta")
+        np.testing.assert_array_equal(out["compact"][7], out["records"][7])
+        assert (out["compact"][7] == 0).sum() > (fail0 == 0).sum()  # bonds broke beyond the notch
+        assert_close_norm(out["compact"][8], out["records"][8], 1e-11, "uy after 30 steps")
+        assert_close_norm(out["compact"][9], out["records"][9], 1e-11, "uz after 30 steps")
+        np.testing.assert_array_equal(out["compact"][10], out["records"][10])
+        assert out["compact"][11] == pytest.approx(out["records"][11], rel=1e-12)
