@@ -59,11 +59,28 @@ FP64_EXEC_PER_BOND = {(1, 2): 4, (1, 3): 6, (2, 2): 8, (2, 3): 14}  # (model, di
 # scaled to the timed launch's bonds and nodes; a zero per-node figure means the
 # node traffic is folded into the per-bond one
 TRAFFIC = {
-    "crack_branching_2d_pmb_verlet": (48.6, 139.8, "k_bond_force<2,1>, 800k-node half plate, 2026-12-03"),
-    "batch_plate_adr_2d_pmb": (54.5, 0.0, "k_bond_force<2,2>, 64-plate batch, 2026-12-03"),
+    "crack_branching_2d_pmb_verlet": (21.1, 0.0, "k_bond_compact<1>, 400k-node quarter-size plate (node traffic folded "
+                                                 "into the per-bond figure), 2026-12-04"),
+    "batch_plate_adr_2d_pmb": (22.5, 0.0, "k_bond_compact<2>, 64-plate batch (node traffic folded in), 2026-12-04"),
     "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0, "k_bond_split3, full slab, 2026-12-03"),
-    "plate_crack_grow_2d_state_verlet": (153.3, 0.0, "k_theta<2> + k_state_force<2,1>, full plate, 2026-12-03"),
-    "kalthoff_winkler_3d_state_verlet": (148.9, 0.0, "k_theta<3> + k_state_force<3,0>, full slab, 2026-12-03")}
+    "plate_crack_grow_2d_state_verlet": (42.5, 0.0, "k_theta_compact + k_state_compact<1>, full plate, 2026-12-04"),
+    "kalthoff_winkler_3d_state_verlet": (59.7, 0.0, "k_theta_compact3 + k_state_compact3<0>, full slab, 2026-12-04")}
+
+
+def layout_info(model, dim, layout, epi):
+    """(kernel names of the step's force launches, per-slot bytes the step
+    reads and writes in them) for the force layout in use."""
+    compact = layout == "compact"
+    if model == 1:
+        if dim == 2:
+            return ("k_bond_compact<%s>" % epi, 16) if compact else ("k_bond_force<2, %s>" % epi, 48)
+        return "k_bond_force<3, %s> / k_bond_split3 (the autotuner's pick)" % epi, 48
+    if dim == 2:
+        # dilatation: 16-byte record + e written; force: 8-byte record + e read
+        return ("k_theta_compact + k_state_compact<%s>" % epi, 16 + 8 + 8 + 8) if compact else \
+            ("k_theta<2> + k_state_force<2, %s>" % epi, 64 + 8 + 64 + 8)
+    return ("k_theta_compact3 + k_state_compact3<EPI_NONE>", 8 + 16 + 8 + 8 + 8 + 8) if compact else \
+        ("k_theta<3> + k_state_force3_phased<4>", 64 + 8 + 64 + 8)
 
 
 def traffic_of(workload, bonds, nodes):
@@ -654,6 +671,7 @@ def batch_arm(args):
     # step loop: CUDA events on the launch stream around each step's launch
     with torch.cuda.stream(stream):
         kern_ms, step_ms = bat.profile_steps(0, args.warmup + args.steps, min(50, args.steps), load)
+    layout = bat.force_layout()
     torch.cuda.synchronize()
     alg_bytes = ALG_BYTES_PER_NODE_2D_ADR * p.N_int + ALG_BYTES_PER_BOND_2D * B
     peaks, peak_kind = measured_peaks()
@@ -744,6 +762,7 @@ def batch_arm(args):
                              f"host time), the oracle's OpenMP loops"}
 
     if rank == 0:
+        kname, slot_bytes = layout_info(1, 2, layout, "EPI_ADR")
         line = {
             "metric": "bond-updates/s", "value": value, "unit": "bond-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": secs_max * 1e3 / args.steps,
@@ -752,12 +771,13 @@ def batch_arm(args):
             "config": {"workload": meta["workload"], "specimens": len(specs), "nodes": p.N, "interior": p.N_int,
                        "bonds": B, "dx": p.dx, "dt": p.dt, "parallelism": "replicas" if world > 1 else "single",
                        "launch": {"block": tuned[0], "chunked": tuned[1], "waves": tuned[2], "split": tuned[3]},
-                       "l2": "inputs larger than L2: bond arrays %.2f GB per step" % (B * 28 / 1e9),
+                       "force_layout": layout,
+                       "l2": "inputs larger than L2: per-slot records %.2f GB read per step" % (B * slot_bytes / 1e9),
                        "setup_s": setup_s, "broken_bond_fraction": broken},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
                          "peak_source": peak_kind,
-                         "kernel": "k_bond_force<2, ADR>", "kernel_ms": kern_ms,
+                         "kernel": kname, "kernel_ms": kern_ms,
                          "kernel_share_of_step": kern_ms / step_ms, "autotune_ms": tuned[4],
                          "alg_bytes_per_launch": alg_bytes,
                          "fp64": fp64_block(1, 2, B, kern_ms, gfma.value)},
@@ -1026,6 +1046,8 @@ def gb300_arm(args):
     kind = 0 if meta["workload"].startswith("plate_tensile") else 1
     with torch.cuda.stream(stream):
         kern_ms, step_ms = eng.profile_steps(kind, args.warmup + args.steps, kern_steps, meta["load"])
+    layout = eng.force_layout()
+    kname, slot_bytes = layout_info(p.model, p.dim, layout, "EPI_ADR" if kind == 0 else "EPI_VERLET")
     torch.cuda.synchronize()
     state = p.model == 2
     if state:  # dilatation + force passes (the 3-D state-based byte model; 2-D by the same count)
@@ -1153,15 +1175,15 @@ def gb300_arm(args):
             "data": "synthetic (deterministic lattice, seeded nothing: the geometry fixes every input)",
             "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "dt": p.dt,
                        "parallelism": "replicas" if world > 1 else "single",
-                       "l2": "inputs larger than L2: per-slot records %.2f GB read per step"
-                             % (B * (48 if p.model == 1 else 2 * 64 + 16) / 1e9),
+                       "force_layout": layout,
+                       "l2": "inputs larger than L2: per-slot records %.2f GB read per step" % (B * slot_bytes / 1e9),
                        "setup_s": setup_s,
                        "launch": None if tuned is None else {"block": tuned[0], "chunked": tuned[1],
                                                              "waves": tuned[2], "split": tuned[3]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                          "frac": achieved / peaks["hbm_gbs"], "traffic": traffic, "traffic_source": traffic_src,
                          "peak_source": peak_kind,
-                         "kernel": "k_bond_force" if p.model == 1 else "k_theta + k_state_force",
+                         "kernel": kname,
                          "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / step_ms,
                          "alg_bytes_per_launch": alg_bytes,
                          "fp64": fp64_block(p.model, p.dim, B, kern_ms, gfma.value)},
