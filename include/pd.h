@@ -314,7 +314,7 @@ int pd_mlp_gemm_wait_check(const void* dev_a, const void* dev_b, int64_t M, int6
  * features, 8 zeros): previous displacement / U (x, y), increment / U,
  * damage, loaded-edge flag, and the history of the previous increment
  * (pd_warm_record): its departure from proportionality per unit load (x, y,
- * times 256) and the damage it added (zeros without a history).  U is the
+ * times 65536) and the damage it added (zeros without a history).  U is the
  * accumulated boundary displacement before the increment. */
 int pd_warm_features(pd_ctx* ctx, double U, double delta, void* dev_x, void* stream);
 /* The increment just solved becomes the history of the next prediction:
@@ -328,17 +328,19 @@ int pd_warm_features(pd_ctx* ctx, double U, double delta, void* dev_x, void* str
 int pd_warm_record(pd_ctx* ctx, double U_prev, double delta, const double* dev_u_prev, const double* dev_dmg_prev,
                    void* stream);
 /* Candidate increments for pd_load_step (ncand = 2): dev_du[0 .. 2*N_int) =
- * u * delta / U + U * net(features), dev_du[2*N_int .. 4*N_int) = u * delta / U.
- * The skip term is the proportional (secant) increment, exact for a linear
- * response loaded proportionally from rest; the network predicts the
+ * u * delta / U + U * (h + net(features) / 65536), dev_du[2*N_int ..
+ * 4*N_int) = u * delta / U.  The skip term is the proportional (secant)
+ * increment, exact for a linear response loaded proportionally from rest; h
+ * is the recorded history (pd_warm_record: the previous increment's
  * departure from proportionality per unit of accumulated boundary
- * displacement, from the local state and the previous increment's departure
- * and damage (pd_warm_record); it is trained on converged states of
- * loadings that include crack advances.  smooth_passes > 0 (bond-based
- * contexts): the correction U * net is first averaged that many times over
- * each free node's intact family (prescribed rows count as zero), which
- * removes the node-to-node rounding noise of the BF16 network that the
- * residual amplifies. */
+ * displacement, zero without a history), and the network predicts how that
+ * departure changes from one increment to the next, from the local state and
+ * the history; it is trained on converged states of loadings through crack
+ * advances (the increments in which a crack advanced left out).
+ * smooth_passes > 0 (bond-based contexts): the correction U * net / 65536 is
+ * first averaged that many times over each free node's intact family
+ * (prescribed rows count as zero), which removes the node-to-node rounding
+ * noise of the BF16 network that the residual amplifies. */
 int pd_warm_predict(pd_ctx* ctx, pd_mlp* net, double U, double delta, int smooth_passes, double* dev_du,
                     void* stream);
 

@@ -304,14 +304,49 @@ def generate(runs=TRAIN_RUNS, n_inc=60, keep=0.25, tol=1e-8, log=print):
     return X, T
 
 
+# (scale, crack fraction): plates the training runs do not include
+EVAL_PLATES = [(0.2, 0.22), (0.28, 0.18)]
+
+
+def evaluate(net, scale, frac, n_inc=50, smooths=(0, 16, 32), tol=1e-6):
+    """Chained load increments on one plate, each start method on its own
+    chain from rest: plain, the skip term alone, skip + history without the
+    network (a zero output layer) and the learned start at each smoothing
+    count.  Returns {method: per-increment ADR steps, candidates used, bonds
+    broken, seconds}."""
+    p, setup, meta = presets.build_warm_start_plate(scale=scale, crack_frac=frac)
+    zero = Net(65536, init_params(0))
+    runs = [("plain", "plain", 0, net), ("skip", "secant", 0, net), ("history", "learned", 0, zero)]
+    runs += [("learned_s%d" % sm, "learned", sm, net) for sm in smooths]
+    res = {}
+    for name, mode, sm, nt in runs:
+        with Engine(p) as eng:
+            setup(eng)
+            t0 = time.perf_counter()
+            st = run_increments(eng, meta, n_inc, mode=mode, net=nt, smooth=sm, tol=tol)
+        res[name] = {"seconds": round(time.perf_counter() - t0, 2), "iters": [s["iters"] for s in st],
+                     "used": [s["start"] for s in st], "bonds_broken": [s["advanced"] for s in st],
+                     "total_iters": int(sum(s["iters"] for s in st[1:]))}
+    zero.close()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("cmd", choices=["train"])
+    ap.add_argument("cmd", choices=["train", "evaluate"])
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--steps", type=int, default=5000)
     ap.add_argument("--increments", type=int, default=60)
     ap.add_argument("--tol", type=float, default=1e-8, help="ADR tolerance of the training runs")
     args = ap.parse_args()
+    if args.cmd == "evaluate":
+        # the shipped (or --out) weights against the skip term and the history
+        # alone, 50 chained increments on each plate of EVAL_PLATES
+        net = Net.load(args.out)
+        for scale, frac in EVAL_PLATES:
+            r = evaluate(net, scale, frac)
+            print(json.dumps({"plate": [scale, frac], "results": r}), flush=True)
+        return
     t0 = time.perf_counter()
     X, T = generate(n_inc=args.increments, tol=args.tol)
     print(json.dumps({"samples": int(X.shape[0]), "seconds": round(time.perf_counter() - t0, 1)}), flush=True)
