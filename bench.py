@@ -887,10 +887,10 @@ def warm_measure(scale, K, smooth, n_plain=1, e2e=True, with_clocks=True):
                               % K},
         "learned": {"ms_per_increment": learned_ms / K, "iters": [s["iters"] for s in learned],
                     "total_iters": int(sum(s["iters"] for s in learned)),
-                    "candidate_used": [s["warm_used"] for s in learned],
-                    "candidates": "0 plain, 1 network (skip term + history + network correction), 2 skip term "
-                                  "alone (also the only one offered when there is no history: increment 1 and the "
-                                  "one after a crack advance)",
+                    "start_used": [s["start"] for s in learned],
+                    "starts": "plain: the previous solution; network: skip term + history + network correction; "
+                              "skip: the skip term alone (the only candidate offered without a history: "
+                              "increment 1 and the one after a crack advance)",
                     "r_start_over_r_plain": [s["r_start"] / s["r_plain"] for s in learned],
                     "bonds_broken": [s["advanced"] for s in learned]},
         "speedup_vs_plain": plain_ms / (learned_ms / K),
