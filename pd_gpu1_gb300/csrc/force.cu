@@ -1129,7 +1129,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
 // nearly empty GPU; units of a quarter slice fill five rounds of a quarter
 // the length.  The sum order depends on Q only, not on the launch shape.
 // Intact flags of other units of the slice share the words, so breaks clear
-// their bits with atomicAnd.
+// their bits with atomicAnd.  Measured on the compact layout (impact slab,
+// ms per step): Q = 2: 0.789, 4: 0.770, 8: 0.841.
 constexpr int kStatePhases3 = 4;
 template <int Q>
 __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force3_phased(const ForceArgs A) {
@@ -1236,50 +1237,68 @@ __device__ __forceinline__ void offsets2(const bt::Tpl& T, const double d[2], bt
     }
 }
 
+// Pair sums of a row spread over Q lane groups (lane j + R p, R = 32 / Q),
+// added as a lane tree: pair addition is commutative, so every lane of the
+// row gets the same sum.
+template <int Q>
+__device__ __forceinline__ bt::f2 phase_sum(bt::f2 v) {
+#pragma unroll
+    for (int off = 32 / Q; off < 32; off <<= 1)
+        v = bt::add(v, bt::f2{__shfl_xor_sync(0xffffffffu, v.h, off), __shfl_xor_sync(0xffffffffu, v.l, off)});
+    return v;
+}
+
 // Dilatation pass (kernel_cal_theta_2D, Force_State.cu:56-85) on every row of
 // [0, N), every bond of the family (the 2-D kernel counts broken bonds too).
+// Work units of R = 32 / Q rows of a slice: lane j + R p takes row j's slots
+// p, p + Q, ... (Q = 1: one warp per slice); the sum order depends on Q only.
+template <int Q>
 __global__ void __launch_bounds__(kForceBlock) k_theta_compact(const ForceArgs A) {
+    constexpr int R = 32 / Q;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
+    const int j = lane % R, ph = lane / R;
     const KParams& P = A.P;
-    for (int64_t s = (int64_t)blockIdx.x * wpb + wib; s < A.nslices; s += (int64_t)gridDim.x * wpb) {
-        const int64_t r = s * 32 + lane;
+    const int64_t units = A.nslices * Q;
+    for (int64_t u = (int64_t)blockIdx.x * wpb + wib; u < units; u += (int64_t)gridDim.x * wpb) {
+        const int64_t s = u / Q;
+        const int h = (int)(u - s * Q);
+        const int rl = h * R + j;
+        const int64_t r = s * 32 + rl;
         const bool row = r < P.N;
         const int64_t rr = row ? r : P.N - 1;
         const int nn = row ? A.NN[rr] : 0;
         const double uxi = A.ux[rr], uyi = A.uy[rr];
-        const int W = A.width[s];
         const int64_t b = A.base[s];
-        const int4* rp = A.srec + b + lane;
+        const int4* rp = A.srec + b + rl;
         bt::f2 acc{0.0f, 0.0f};  // sum of the weighted extensions, times 2^sth_exp
-        // the next slot's record loaded one iteration ahead
-        int4 rq_next = nn > 0 ? __ldg(rp) : make_int4(0, 0, 0, 0);
-        for (int k = 0; k < W; k++) {
+        // the lane's next slot's record loaded one iteration ahead
+        int4 rq_next = ph < nn ? __ldg(rp + (int64_t)ph * 32) : make_int4(0, 0, 0, 0);
+        for (int k = ph; k < nn; k += Q) {
             const int4 rq = rq_next;
-            if (k + 1 < nn) rq_next = __ldg(rp + (int64_t)(k + 1) * 32);
-            if (k < nn) {
-                const int c = rq.x;
-                const uint32_t dlb = (uint32_t)rq.y;
-                const int id = (int)(dlb & 0xffu);
-                const bt::Tpl& T = A.tpl[id];
-                const float dl = __uint_as_float(dlb & ~0xffu);
-                // x_c - x_i as the reference rounds it, then d = (that + u_c) - u_i,
-                // the dilatation pass's operand order
-                const double xa = __longlong_as_double((long long)T.xd[0] + rq.z);
-                const double ya = __longlong_as_double((long long)T.xd[1] + rq.w);
-                const double d[2] = {(xa + __ldg(A.ux + c)) - uxi, (ya + __ldg(A.uy + c)) - uyi};
-                bt::f2 eta[2], w[2], y, e;
-                offsets2(T, d, eta);
-                bt::stretch2(eta, T, dl, w, y, e);
-                A.e[b + (int64_t)k * 32 + lane] = make_float2(e.h, e.l);
-                // cth of the class moved to this bond's length: cth (1 + g1 dl)
-                const float4 ct = __ldg(reinterpret_cast<const float4*>(A.stpl + id) + 1);
-                const bt::f2 cth{ct.x, fmaf(ct.x, ct.z * dl, ct.y)};
-                acc = bt::add(acc, bt::mul(cth, e));
-            }
+            if (k + Q < nn) rq_next = __ldg(rp + (int64_t)(k + Q) * 32);
+            const int c = rq.x;
+            const uint32_t dlb = (uint32_t)rq.y;
+            const int id = (int)(dlb & 0xffu);
+            const bt::Tpl& T = A.tpl[id];
+            const float dl = __uint_as_float(dlb & ~0xffu);
+            // x_c - x_i as the reference rounds it, then d = (that + u_c) - u_i,
+            // the dilatation pass's operand order
+            const double xa = __longlong_as_double((long long)T.xd[0] + rq.z);
+            const double ya = __longlong_as_double((long long)T.xd[1] + rq.w);
+            const double d[2] = {(xa + __ldg(A.ux + c)) - uxi, (ya + __ldg(A.uy + c)) - uyi};
+            bt::f2 eta[2], w[2], y, e;
+            offsets2(T, d, eta);
+            bt::stretch2(eta, T, dl, w, y, e);
+            A.e[b + (int64_t)k * 32 + rl] = make_float2(e.h, e.l);
+            // cth of the class moved to this bond's length: cth (1 + g1 dl)
+            const float4 ct = __ldg(reinterpret_cast<const float4*>(A.stpl + id) + 1);
+            const bt::f2 cth{ct.x, fmaf(ct.x, ct.z * dl, ct.y)};
+            acc = bt::add(acc, bt::mul(cth, e));
         }
-        if (row) {
+        if (Q > 1) acc = phase_sum<Q>(acc);
+        if (row && ph == 0) {
             // theta = acc / m and theta / m through 1/m (nb, IEEE-rounded at set-up)
             const double m = A.m[r], rm = A.nb[r];
             const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
@@ -1294,20 +1313,28 @@ __global__ void __launch_bounds__(kForceBlock) k_theta_compact(const ForceArgs A
 // State-based force pass (kernel_state_force_2D, Force_State.cu:88-134) on
 // rows [0, N_int): t_i + t_j = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i +
 // 1/m_j) per bond with e from the dilatation pass, the length and direction
-// in the force pass's operand order.
-template <int EPI>
+// in the force pass's operand order.  Work units as k_theta_compact<Q>;
+// with Q > 1 the units of a slice share its intact-flag words, so breaks
+// clear their bits with atomicAnd.
+template <int EPI, int Q>
 __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(const ForceArgs A) {
+    constexpr int R = 32 / Q;
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
+    const int j = lane % R, ph = lane / R;
     const KParams& P = A.P;
     double red[3] = {0.0, 0.0, 0.0};
     const double s0 = P.critical_s;
     const float s0f = __double2float_rn(s0);
-    for (int64_t s = (int64_t)blockIdx.x * wpb + wib; s < A.nslices; s += (int64_t)gridDim.x * wpb) {
-        const int64_t r = s * 32 + lane;
+    const int64_t units = A.nslices * Q;
+    for (int64_t u = (int64_t)blockIdx.x * wpb + wib; u < units; u += (int64_t)gridDim.x * wpb) {
+        const int64_t s = u / Q;
+        const int h = (int)(u - s * Q);
+        const int rl = h * R + j;
+        const int64_t r = s * 32 + rl;
         const bool force_row = r < A.nforce;
-        if (s * 32 < A.nforce) {
+        if (s * 32 + h * R < A.nforce) {  // warp-uniform: the unit holds a force row
             const int64_t rr = force_row ? r : A.nforce - 1;
             const double xi = A.x[rr], yi = A.y[rr];
             const double uxi = A.ux[rr], uyi = A.uy[rr];
@@ -1317,15 +1344,17 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
             const int W = A.width[s];
             const int64_t b = A.base[s];
             uint32_t* wbits = A.bits + A.fbase[s];
-            const int2* rp = A.srec8 + b + lane;
-            // the next slot's record loaded one iteration ahead
-            int2 rq_next = W > 0 ? __ldg(rp) : make_int2(0, 0);
-            for (int k = 0; k < W; k++) {
-                const int64_t slot = b + (int64_t)k * 32 + lane;
+            const int2* rp = A.srec8 + b + rl;
+            const int iters = (W + Q - 1) / Q;
+            // the lane's next slot's record loaded one iteration ahead
+            int2 rq_next = ph < W ? __ldg(rp + (int64_t)ph * 32) : make_int2(0, 0);
+            for (int i = 0; i < iters; i++) {
+                const int k = i * Q + ph;
+                const int64_t slot = b + (int64_t)k * 32 + rl;
                 const int2 rq = rq_next;
-                if (k + 1 < W) rq_next = __ldg(rp + (int64_t)(k + 1) * 32);
-                const uint32_t word = wbits[k];
-                const bool alive = force_row && ((word >> lane) & 1u);
+                if (k + Q < W) rq_next = __ldg(rp + (int64_t)(k + Q) * 32);
+                const uint32_t word = k < W ? wbits[k] : 0u;
+                const bool alive = force_row && ((word >> rl) & 1u);
                 bool brk = false;
                 if (alive) {
                     const int c = rq.x;
@@ -1338,7 +1367,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
                     bt::f2 eta[2], w[2], y, ef;
                     offsets2(T, d, eta);
                     bt::stretch2(eta, T, dl, w, y, ef);
-                    // T = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j), times 2^-st_exp
+                    // T = c1 (theta_i/m_i + theta_j/m_j) + c2 e (1/m_i + 1/m_j), times 2^-st_exp;
                     // c1, c2 of the class moved to this bond's length (1 + g dl)
                     const float4 cc = __ldg(reinterpret_cast<const float4*>(A.stpl + id));
                     const float2 gg = __ldg(reinterpret_cast<const float2*>(A.stpl + id) + 3);
@@ -1355,14 +1384,26 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
                     brk = bt::exceeds(ef, s0, s0f, T, dl);
                 }
                 const uint32_t broke = __ballot_sync(0xffffffffu, brk);
-                if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+                if (Q == 1) {
+                    if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
+                } else if (broke && j == 0 && !A.nobreak) {
+                    constexpr uint32_t kRows = R >= 32 ? 0xffffffffu : ((1u << (R % 32)) - 1u);
+                    const uint32_t mine = (broke >> (ph * R)) & kRows;
+                    if (mine) atomicAnd(wbits + k, ~(mine << (h * R)));
+                }
             }
-            // undo the power-of-two scale of T (exact)
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
-            if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
+            if (Q > 1) {
+                fxa = phase_sum<Q>(fxa);
+                fya = phase_sum<Q>(fya);
+            }
+            if (ph == 0) {
+                // undo the power-of-two scale of T (exact)
+                const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
+                const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
+                if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
+            }
         }
-        if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<2>(A, r);
+        if (EPI == EPI_VERLET && A.do_next && ph == 0 && !force_row && r < P.N) boundary_row<2>(A, r);
     }
     if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
@@ -1712,13 +1753,23 @@ static unsigned resident_grid(pd_ctx* c, const void* kernel, int64_t nslices, in
     return (unsigned)std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(want, cap), kMaxPartials));
 }
 
+// Slot phases of the 2-D state passes on the compact layout (the Q of
+// k_theta_compact<Q> / k_state_compact<EPI, Q>).  Measured on the crack-grow
+// plate (7,906 slices of ~28 slots against 4,864-6,080 resident warps),
+// dilatation / force phases 1/1: 0.192 ms per step; 2/1: 0.198; 1/4: 0.212;
+// 2/2: 0.205; 4/4: 0.233.  Short rows gain nothing from the shorter rounds:
+// each unit repeats its rows' set-up, and a warp's loads spread over Q slot
+// rows.  (The 3-D force pass, ~104 slots per row, takes kStatePhases3.)
+constexpr int kStatePhases2 = 1;
+
 int launch_theta(pd_ctx* c, cudaStream_t s) {
     ForceArgs A = make_args(c);
     if (A.P.dim == 2 && A.srec) {
         // the launch shape's block size (at most kForceBlock) and waves
         const int blk = std::min(c->tune_block, kForceBlock);
-        k_theta_compact<<<resident_grid(c, (const void*)k_theta_compact, A.nslices, blk, c->tune_waves), blk, 0, s>>>(
-            A);
+        constexpr int Q = kStatePhases2;
+        k_theta_compact<Q><<<resident_grid(c, (const void*)k_theta_compact<Q>, A.nslices * Q, blk, c->tune_waves), blk,
+                             0, s>>>(A);
     }
     else if (A.P.dim == 2)
         k_theta<2><<<resident_grid(c, (const void*)k_theta<2>, A.nslices), kForceBlock, 0, s>>>(A);
@@ -1873,15 +1924,16 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
         }                                                 \
     } while (0)
     if (state && !d3 && A.srec) {
+        constexpr int Q = kStatePhases2;
         if (f.epi == EPI_NONE)
-            k_state_compact<EPI_NONE><<<resident_grid(c, (const void*)k_state_compact<EPI_NONE>, A.nslices, blk,
-                                                      waves), blk, 0, s>>>(A);
+            k_state_compact<EPI_NONE, Q><<<resident_grid(c, (const void*)k_state_compact<EPI_NONE, Q>, A.nslices * Q,
+                                                         blk, waves), blk, 0, s>>>(A);
         else if (f.epi == EPI_VERLET)
-            k_state_compact<EPI_VERLET><<<resident_grid(c, (const void*)k_state_compact<EPI_VERLET>, A.nslices, blk,
-                                                        waves), blk, 0, s>>>(A);
+            k_state_compact<EPI_VERLET, Q><<<resident_grid(c, (const void*)k_state_compact<EPI_VERLET, Q>,
+                                                           A.nslices * Q, blk, waves), blk, 0, s>>>(A);
         else
-            k_state_compact<EPI_ADR><<<resident_grid(c, (const void*)k_state_compact<EPI_ADR>, A.nslices, blk,
-                                                     waves), blk, 0, s>>>(A);
+            k_state_compact<EPI_ADR, Q><<<resident_grid(c, (const void*)k_state_compact<EPI_ADR, Q>, A.nslices * Q,
+                                                        blk, waves), blk, 0, s>>>(A);
     } else if (state && d3 && A.sk) {
         constexpr int Q = kStatePhases3;
         if (f.epi == EPI_NONE)

@@ -11,8 +11,6 @@
 // (Neighbor.cu:42-80).  The family predicate is the reference's expression,
 // |xj - xi|^2 < delta^2, and this file is compiled without FMA contraction, so
 // the membership test rounds exactly like the reference's host code.
-#include <cub/cub.cuh>
-
 #include "pd_internal.cuh"
 
 namespace pdg {
@@ -214,19 +212,104 @@ void free_ptr(T*& p) {
 
 }  // namespace
 
-// Exclusive scan of n int32 counts into n+1 int64 offsets (out[n] = total).
+namespace {
+
+// ---- exclusive scan of int32 counts into int64 offsets ----------------------
+//
+// Three passes over tiles of kScanTile counts: the sum of every tile, an
+// exclusive scan of the tile sums in one block, then every tile rescanned
+// from its offset.  Integer sums: exact and independent of the launch.
+constexpr int kScanThreads = 512, kScanItems = 8, kScanTile = kScanThreads * kScanItems;
+constexpr int kScanWarps = kScanThreads / 32;
+
+// Inclusive scan of one value per thread over the block (every thread
+// calls it); total receives the block's sum.
+__device__ int64_t block_inclusive_scan(int64_t v, int64_t* sm, int64_t& total) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int off = 1; off < 32; off <<= 1) {
+        const int64_t t = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += t;
+    }
+    if (lane == 31) sm[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int64_t q = lane < kScanWarps ? sm[lane] : 0;
+        for (int off = 1; off < 32; off <<= 1) {
+            const int64_t t = __shfl_up_sync(0xffffffffu, q, off);
+            if (lane >= off) q += t;
+        }
+        if (lane < kScanWarps) sm[lane] = q;
+    }
+    __syncthreads();
+    total = sm[kScanWarps - 1];
+    const int64_t r = v + (w > 0 ? sm[w - 1] : 0);
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_sums(const int* __restrict__ in, int64_t n,
+                                                                 int64_t* __restrict__ tile_sum) {
+    __shared__ int64_t sm[kScanWarps];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int64_t v = 0;
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < n) v += in[base + k];
+    int64_t total;
+    block_inclusive_scan(v, sm, total);
+    if (threadIdx.x == 0) tile_sum[blockIdx.x] = total;
+}
+
+// One block: the tile sums become their exclusive prefix sums, in place.
+__global__ void __launch_bounds__(kScanThreads) k_scan_tile_offsets(int64_t* __restrict__ tile_sum, int64_t ntiles) {
+    __shared__ int64_t sm[kScanWarps];
+    int64_t carry = 0;
+    for (int64_t b = 0; b < ntiles; b += kScanThreads) {
+        const int64_t i = b + threadIdx.x;
+        const int64_t v = i < ntiles ? tile_sum[i] : 0;
+        int64_t total;
+        const int64_t inc = block_inclusive_scan(v, sm, total);
+        if (i < ntiles) tile_sum[i] = carry + inc - v;
+        carry += total;
+    }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int* __restrict__ in, int64_t n,
+                                                             const int64_t* __restrict__ tile_off,
+                                                             int64_t* __restrict__ out) {
+    __shared__ int64_t sm[kScanWarps];
+    const int64_t base = (int64_t)blockIdx.x * kScanTile + (int64_t)threadIdx.x * kScanItems;
+    int c[kScanItems];
+    int64_t v = 0;
+    for (int k = 0; k < kScanItems; k++) {
+        c[k] = base + k < n ? in[base + k] : 0;
+        v += c[k];
+    }
+    int64_t total;
+    const int64_t inc = block_inclusive_scan(v, sm, total);
+    int64_t run = tile_off[blockIdx.x] + inc - v;
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < n) {
+            out[base + k] = run;
+            run += c[k];
+        }
+}
+
+}  // namespace
+
+// Exclusive scan of n int32 counts into int64 offsets out[0 .. n) (the
+// callers form out[n] themselves).
 static int scan_counts(pd_ctx* c, const int* in, int64_t* out, int64_t n, cudaStream_t s) {
-    size_t tmp = 0;
-    cudaError_t e = cub::DeviceScan::ExclusiveSum(nullptr, tmp, in, out, (int)(n + 1), s);
-    if (e != cudaSuccess) return cuda_err(c, e, "scan size");
-    void* t = nullptr;
-    if ((e = cudaMallocAsync(&t, tmp, s)) != cudaSuccess) return cuda_err(c, e, "scan alloc");
-    // scan n+1 elements where the (n+1)-th input is read as zero: scan n, then add the last count
-    e = cub::DeviceScan::ExclusiveSum(t, tmp, in, out, (int)n, s);
-    cudaFreeAsync(t, s);
-    if (e != cudaSuccess) return cuda_err(c, e, "scan");
-    c->launches += 1;
-    return PD_OK;
+    if (n <= 0) return PD_OK;
+    const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+    int64_t* tiles = nullptr;
+    cudaError_t e = cudaMallocAsync(&tiles, ntiles * sizeof(int64_t), s);
+    if (e != cudaSuccess) return cuda_err(c, e, "scan alloc");
+    k_scan_tile_sums<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tiles);
+    k_scan_tile_offsets<<<1, kScanThreads, 0, s>>>(tiles, ntiles);
+    k_scan_apply<<<(unsigned)ntiles, kScanThreads, 0, s>>>(in, n, tiles, out);
+    cudaFreeAsync(tiles, s);
+    c->launches += 3;
+    return cuda_err(c, cudaGetLastError(), "scan");
 }
 
 int build_family(pd_ctx* c, cudaStream_t s) {
