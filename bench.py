@@ -74,7 +74,8 @@ def layout_info(model, dim, layout, epi):
     if model == 1:
         if dim == 2:
             return ("k_bond_compact<%s>" % epi, 16) if compact else ("k_bond_force<2, %s>" % epi, 48)
-        return "k_bond_force<3, %s> / k_bond_split3 (the autotuner's pick)" % epi, 48
+        return ("k_bond_compact3<%s>" % epi, 16) if compact else \
+            ("k_bond_force<3, %s> / k_bond_split3 (the autotuner's pick)" % epi, 48)
     if dim == 2:
         # dilatation: 16-byte record + e written; force: 8-byte record + e read
         return ("k_theta_compact + k_state_compact<%s>" % epi, 16 + 8 + 8 + 8) if compact else \
@@ -998,6 +999,7 @@ def gb300_arm(args):
     p, setup, meta = build_workload(args.workload, args.scale)
     stream = torch.cuda.Stream()
     eng = E.Engine(p, stream=stream.cuda_stream)
+    eng.set_force_layout(args.layout)
     t0 = time.perf_counter()
     with torch.cuda.stream(stream):
         setup(eng)
@@ -1221,6 +1223,8 @@ def main():
                                                            "network's correction")
     ap.add_argument("--plain-increments", type=int, default=1, help="warm_start workload: plain-start increments "
                                                                      "timed (each ~23k ADR steps at 1M nodes)")
+    ap.add_argument("--layout", default="auto", choices=["auto", "compact", "records"],
+                    help="force layout of the bond kernels (auto: compact where it fits)")
     ap.add_argument("--no-extras", action="store_true", help="default workload: leave out the batch and "
                                                                   "learned-warm-start blocks of the line")
     args = ap.parse_args()

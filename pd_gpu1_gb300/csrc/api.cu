@@ -1118,6 +1118,14 @@ int pd_autotune(pd_ctx* c, int reps, double* best_ms, void* stream) {
     for (int blk : {128, 256, 512})
         for (int sp : {2, 4})
             for (int wv : {1, 2}) shapes.push_back({blk, 0, wv, sp});
+    if (c->p.dim == 3 && S.rec16) {
+        // the 3-D compact kernel has its own unit order (quarter slices): only
+        // block size and waves apply
+        std::vector<Shape> kept;
+        for (const Shape& sh : shapes)
+            if (sh.chunked == 0 && sh.split == 1) kept.push_back(sh);
+        shapes.swap(kept);
+    }
     for (size_t ish = 0; ish < shapes.size() && !rc; ish++) {
                 c->tune_block = shapes[ish].block;
                 c->tune_chunked = shapes[ish].chunked;

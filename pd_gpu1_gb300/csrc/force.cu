@@ -813,6 +813,125 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
+// Pair sums of a row spread over Q lane groups (lane j + R p, R = 32 / Q),
+// added as a lane tree: pair addition is commutative, so every lane of the
+// row gets the same sum.
+template <int Q>
+__device__ __forceinline__ bt::f2 phase_sum(bt::f2 v) {
+#pragma unroll
+    for (int off = 32 / Q; off < 32; off <<= 1)
+        v = bt::add(v, bt::f2{__shfl_xor_sync(0xffffffffu, v.h, off), __shfl_xor_sync(0xffffffffu, v.l, off)});
+    return v;
+}
+
+// d - x exactly as a pair, x the double value of a float (bit pattern xb).
+__device__ __forceinline__ bt::f2 offset1(double d, uint64_t xb) {
+    bt::f2 eta;
+    if (xb == 0)
+        eta = bt::split_bits(d);
+    else if (!bt::offset_pair(d, xb, eta))
+        eta = bt::split_bits(d - bt::dfrom(xb));  // exact by Sterbenz's lemma
+    return eta;
+}
+// One bond's exact offsets from its class's float reference vector.
+template <int N, class TT>
+__device__ __forceinline__ void offsets_n(const TT& T, const double* d, bt::f2* eta) {
+#pragma unroll
+    for (int a = 0; a < N; a++) eta[a] = offset1(d[a], T.xd[a]);
+}
+
+// The 3-D bond force (kernel_bond_force_3D, Force_Bond.cu:87-141) on the
+// compact layout: one 16-byte record per slot (k2 / 2 negated where the
+// bond may not break, the y >= -0.04 guard of Force_Bond.cu:117) and 80-byte
+// class templates; the bond vector with the reference's roundings (6 FP64
+// instructions), the stretch in pairs (bt::stretch3).  Work units of 32 / Q
+// rows with Q slot phases, as k_state_compact3; the sum order depends on Q
+// only (not on block size, waves or slice order).  Measured on the impact
+// slab (ms per step, the autotuner's shape): Q = 1: 0.361, 2: 0.379, 4: 0.440,
+// 8: 0.552; the 48-byte records: 0.385.  So one warp per slice here.
+constexpr int kBondPhases3 = 1;
+template <int EPI>
+__global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compact3(const ForceArgs A) {
+    constexpr int Q = kBondPhases3, R = 32 / Q;
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int wpb = blockDim.x >> 5;
+    const int j = lane % R, ph = lane / R;
+    const KParams& P = A.P;
+    double red[3] = {0.0, 0.0, 0.0};
+    const double s0 = P.critical_s;
+    const float s0f = __double2float_rn(s0);
+    const int64_t units = A.nslices * Q;
+    for (int64_t u = (int64_t)blockIdx.x * wpb + wib; u < units; u += (int64_t)gridDim.x * wpb) {
+        const int64_t s = u / Q;
+        const int h = (int)(u - s * Q);
+        const int rl = h * R + j;
+        const int64_t r = s * 32 + rl;
+        const bool force_row = r < A.nforce;
+        if (s * 32 + h * R < A.nforce) {  // warp-uniform: the unit holds a force row
+            const int64_t rr = force_row ? r : A.nforce - 1;
+            const double xi = A.x[rr], yi = A.y[rr], zi = A.z[rr];
+            const double uxi = A.ux[rr], uyi = A.uy[rr], uzi = A.uz[rr];
+            bt::f2 fxa{0.0f, 0.0f}, fya{0.0f, 0.0f}, fza{0.0f, 0.0f};
+            const int W = A.width[s];
+            const int64_t b = A.base[s];
+            uint32_t* wbits = A.bits + A.fbase[s];
+            const int4* rp = reinterpret_cast<const int4*>(A.rec16 + b) + rl;
+            const int iters = (W + Q - 1) / Q;
+            // the lane's next slot's record loaded one iteration ahead
+            int4 rq_next = ph < W ? __ldg(rp + (int64_t)ph * 32) : make_int4(0, 0, 0, 0);
+            for (int i = 0; i < iters; i++) {
+                const int k = i * Q + ph;
+                const int4 rq = rq_next;
+                if (k + Q < W) rq_next = __ldg(rp + (int64_t)(k + Q) * 32);
+                const uint32_t word = k < W ? wbits[k] : 0u;
+                const bool alive = force_row && ((word >> rl) & 1u);
+                bool brk = false;
+                if (alive) {
+                    const int c = rq.x;
+                    const uint32_t dlb = (uint32_t)rq.y;
+                    const bt::Tpl3& T = A.tpl3[dlb & 0xffu];
+                    const float dl = __uint_as_float(dlb & ~0xffu);
+                    // d = (P_c - x_i) - u_i with the reference's roundings
+                    const double d[3] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi,
+                                         (__ldg(A.pcz + c) - zi) - uzi};
+                    bt::f2 eta[3], w[3], y, e;
+                    offsets_n<3>(T, d, eta);
+                    bt::stretch3(eta, T, dl, w, y, e);
+                    const bool spared = __int_as_float(rq.z) < 0.0f;
+                    const bt::f2 k2half = spared ? bt::f2{-__int_as_float(rq.z), -__int_as_float(rq.w)}
+                                                 : bt::f2{__int_as_float(rq.z), __int_as_float(rq.w)};
+                    // t = (k2 / 2) e / L, f = t W
+                    const bt::f2 t = bt::mul(bt::mul(k2half, e), y);
+                    bt::acc_add(fxa, bt::mul(t, w[0]));
+                    bt::acc_add(fya, bt::mul(t, w[1]));
+                    bt::acc_add(fza, bt::mul(t, w[2]));
+                    brk = !spared && bt::exceeds(e, s0, s0f, T, dl);
+                }
+                const uint32_t broke = __ballot_sync(0xffffffffu, brk);
+                if (broke && j == 0 && !A.nobreak) {
+                    constexpr uint32_t kRows = R >= 32 ? 0xffffffffu : ((1u << (R % 32)) - 1u);
+                    const uint32_t mine = (broke >> (ph * R)) & kRows;
+                    if (mine) atomicAnd(wbits + k, ~(mine << ((h * R) % 32)));
+                }
+            }
+            fxa = phase_sum<Q>(fxa);
+            fya = phase_sum<Q>(fya);
+            fza = phase_sum<Q>(fza);
+            if (ph == 0 && force_row) {
+                // undo the power-of-two scaling of the bond coefficient (exact)
+                const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
+                const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+                const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
+                row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
+            }
+        }
+        if (EPI == EPI_VERLET && A.do_next && ph == 0 && !force_row && r < P.N) boundary_row<3>(A, r);
+    }
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
+}
+
 // The compact layout with several warps per slice (as k_bond_split): warp
 // `sub` computes the slots sub, sub + split, ... into shared memory and the
 // group's first warp adds them in slot order (bit for bit the one-warp sums).
@@ -1130,12 +1249,12 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
 // the length.  The sum order depends on Q only, not on the launch shape.
 // Intact flags of other units of the slice share the words, so breaks clear
 // their bits with atomicAnd.  Measured on the compact layout (impact slab,
-// ms per step): Q = 2: 0.789, 4: 0.770, 8: 0.841.
+// ms per step): Q = 1: 0.823, 2: 0.789, 4: 0.770, 8: 0.841.
 constexpr int kStatePhases3 = 4;
 template <int Q>
 __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force3_phased(const ForceArgs A) {
     constexpr int R = 32 / Q;
-    static_assert(Q >= 2 && Q <= 8 && 32 % Q == 0, "2 to 8 phases");
+    static_assert(Q >= 1 && Q <= 8 && 32 % Q == 0, "1 to 8 phases");
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int wpb = blockDim.x >> 5;
@@ -1190,8 +1309,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force3_p
             }
             const uint32_t broke = __ballot_sync(0xffffffffu, brk);
             if (broke && j == 0 && !A.nobreak) {
-                const uint32_t mine = (broke >> (ph * R)) & ((1u << R) - 1u);
-                if (mine) atomicAnd(wbits + k, ~(mine << (h * R)));
+                constexpr uint32_t kRows = R >= 32 ? 0xffffffffu : ((1u << (R % 32)) - 1u);
+                const uint32_t mine = (broke >> (ph * R)) & kRows;
+                if (mine) atomicAnd(wbits + k, ~(mine << ((h * R) % 32)));
             }
         }
 #pragma unroll
@@ -1235,17 +1355,6 @@ __device__ __forceinline__ void offsets2(const bt::Tpl& T, const double d[2], bt
         else if (!bt::offset_pair(d[a], xb, eta[a]))
             eta[a] = bt::split_bits(d[a] - bt::dfrom(xb));  // exact by Sterbenz's lemma
     }
-}
-
-// Pair sums of a row spread over Q lane groups (lane j + R p, R = 32 / Q),
-// added as a lane tree: pair addition is commutative, so every lane of the
-// row gets the same sum.
-template <int Q>
-__device__ __forceinline__ bt::f2 phase_sum(bt::f2 v) {
-#pragma unroll
-    for (int off = 32 / Q; off < 32; off <<= 1)
-        v = bt::add(v, bt::f2{__shfl_xor_sync(0xffffffffu, v.h, off), __shfl_xor_sync(0xffffffffu, v.l, off)});
-    return v;
 }
 
 // Dilatation pass (kernel_cal_theta_2D, Force_State.cu:56-85) on every row of
@@ -1418,22 +1527,6 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
 // the dilatation pass, 8 + 8 + 8 in the force pass, against 72 and 72 with
 // the three 32-byte records.
 
-// d - x exactly as a pair, x the double value of a float (bit pattern xb).
-__device__ __forceinline__ bt::f2 offset1(double d, uint64_t xb) {
-    bt::f2 eta;
-    if (xb == 0)
-        eta = bt::split_bits(d);
-    else if (!bt::offset_pair(d, xb, eta))
-        eta = bt::split_bits(d - bt::dfrom(xb));  // exact by Sterbenz's lemma
-    return eta;
-}
-// One bond's exact offsets from its class's float reference vector.
-template <int N, class TT>
-__device__ __forceinline__ void offsets_n(const TT& T, const double* d, bt::f2* eta) {
-#pragma unroll
-    for (int a = 0; a < N; a++) eta[a] = offset1(d[a], T.xd[a]);
-}
-
 // Dilatation pass (kernel_cal_theta_3D, Force_State.cu:200-239) on rows [0,
 // N): the reference kernel skips broken bonds (its fail test); boundary rows,
 // which carry no flags in the reference (Memory.cu:39), count every bond.
@@ -1569,8 +1662,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
             }
             const uint32_t broke = __ballot_sync(0xffffffffu, brk);
             if (broke && j == 0 && !A.nobreak) {
-                const uint32_t mine = (broke >> (ph * R)) & ((1u << R) - 1u);
-                if (mine) atomicAnd(wbits + k, ~(mine << (h * R)));
+                constexpr uint32_t kRows = R >= 32 ? 0xffffffffu : ((1u << (R % 32)) - 1u);
+                const uint32_t mine = (broke >> (ph * R)) & kRows;
+                if (mine) atomicAnd(wbits + k, ~(mine << ((h * R) % 32)));
             }
         }
 #pragma unroll
@@ -1869,6 +1963,23 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
     const int waves = shaped ? c->tune_waves : 1;
     A.chunked = bond ? c->tune_chunked : 0;
     if (bond && !d3 && A.rec16) return launch_compact(c, A, f, blk, waves, s);
+    if (bond && d3 && A.rec16) {
+        // the launch shape's block size and waves; order and split do not apply
+        constexpr int Q = kBondPhases3;
+        if (f.epi == EPI_VERLET)
+            k_bond_compact3<EPI_VERLET><<<resident_grid(c, (const void*)k_bond_compact3<EPI_VERLET>, A.nslices * Q,
+                                                        blk, waves), blk, 0, s>>>(A);
+        else if (f.epi == EPI_ADR)
+            k_bond_compact3<EPI_ADR><<<resident_grid(c, (const void*)k_bond_compact3<EPI_ADR>, A.nslices * Q, blk,
+                                                     waves), blk, 0, s>>>(A);
+        else
+            k_bond_compact3<EPI_NONE><<<resident_grid(c, (const void*)k_bond_compact3<EPI_NONE>, A.nslices * Q, blk,
+                                                      waves), blk, 0, s>>>(A);
+        c->launches++;
+        if (f.epi == EPI_VERLET && f.do_next) c->parity ^= 1;
+        c->csr_fail_current = false;
+        return cuda_err(c, cudaGetLastError(), "bond force (compact, 3-D)");
+    }
     if (bond && c->tune_split > 1) {
         // several warps per slice (k_bond_split / k_bond_split3), one wave of slice groups
         A.split = c->tune_split;

@@ -519,6 +519,70 @@ __device__ __forceinline__ void state_coefs(const KParams& P, double L0, double 
     c2 = 2.0 * b_coef * wf * cs;
 }
 
+// Records of the 3-D bond-based compact layout: {column, dl with the class
+// id, k2 / 2 as a pair}, the pair negated where the bond may not break (an
+// end below y = -0.04, Force_Bond.cu:117).  *bad as in k_rec16_fill, and also
+// where a slot's float vector is not its class's (a key collision).
+__global__ void k_rec16_fill3(KParams P, int64_t nslices, const int* __restrict__ width,
+                              const int64_t* __restrict__ base, const int* __restrict__ csr,
+                              const int* __restrict__ NL, const double* __restrict__ x, const double* __restrict__ y,
+                              const double* __restrict__ z, const double* __restrict__ idist,
+                              const double* __restrict__ fac, const double* __restrict__ scr,
+                              const unsigned long long* __restrict__ keys, const int* __restrict__ ids,
+                              const bt::Tpl3* __restrict__ tpl, double kscale_half_inv, bt::Rec* __restrict__ rec,
+                              int* __restrict__ bad) {
+    const int64_t s = blockIdx.y * (int64_t)gridDim.x + blockIdx.x;
+    if (s >= nslices) return;
+    const int W = width[s];
+    const int64_t b = base[s];
+    for (int t = threadIdx.x; t < W * 32; t += blockDim.x) {
+        const int64_t slot = b + t;
+        const int q = csr[slot];
+        const int64_t r = s * 32 + (t & 31);
+        bt::Rec R;
+        if (q < 0) {
+            R.col = (int)(r < P.N ? r : 0);
+            R.dl = 0.0f;  // class 0, zero coefficient: a padding slot contributes nothing
+            R.k2h = R.k2l = 0.0f;
+            rec[slot] = R;
+            continue;
+        }
+        const int64_t c = NL[q];
+        const double xv[3] = {x[c] - x[r], y[c] - y[r], z[c] - z[r]};
+        const unsigned long long key = class_key3(xv[0], xv[1], xv[2]);
+        unsigned h = class_hash(key);
+        int id = -1;
+        for (int probe = 0; probe < kRegion; probe++, h = (h + 1) & (kRegion - 1)) {
+            if (keys[h] == key) {
+                id = ids[h];
+                break;
+            }
+            if (keys[h] == kEmptyKey) break;
+        }
+        bool fail = id < 0 || id > 255;
+        const double L0 = idist[q];
+        double dlv = 0.0;
+        if (!fail) {
+            const bt::Tpl3& T = tpl[id];
+            dlv = L0 - T.l0d;
+            for (int a = 0; a < 3; a++)
+                if (__double2float_rn(xv[a]) != T.xf[a]) fail = true;  // another vector under the same key
+        }
+        const float dl = __double2float_rn(dlv);
+        const unsigned dlb = __float_as_uint(dl);
+        if ((double)dl != dlv || (dlb & 0xffu) != 0u) fail = true;
+        if (fail) atomicExch(bad, 1);
+        R.col = (int)c;
+        R.dl = __uint_as_float((dlb & ~0xffu) | (unsigned)(id & 0xff));
+        const double k2 = 2.0 * (P.vol * fac[q] * P.bc * scr[q]) / L0;
+        const ff kf = ff_split(k2 * kscale_half_inv);
+        const bool breakable = y[r] >= P.break_ymin && y[c] >= P.break_ymin;
+        R.k2h = breakable ? kf.h : -kf.h;
+        R.k2l = breakable ? kf.l : -kf.l;
+        rec[slot] = R;
+    }
+}
+
 // Records of the 2-D state-based compact layout: rec = {column, dl with the
 // class id, kx, ky}, where the reference vector x_c - x_i as the reference
 // rounds it (a double) is the class's float vector (as a double) moved by kx
@@ -918,7 +982,6 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         free_ptr(S.skz);
         S.ntpl = 0;
     };
-    if (d3 && !state) return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 3-D state-based problems");
     if (cudaMallocAsync(&keys, tsize * 8, s) || cudaMallocAsync(&l0min, tsize * 8, s) ||
         cudaMallocAsync(&ids, tsize * 4, s) || cudaMallocAsync(&flags, 2 * 4, s) ||
         (d3 && cudaMallocAsync(&vec, tsize * sizeof(float4), s))) {
@@ -1024,10 +1087,12 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
     S.ntpl = (int)ntpl;
     const size_t nrec = (size_t)std::max<int64_t>(S.S, 1);
     bool ok = true;
-    if (d3)
+    if (d3 && state)
         ok = !cudaMalloc(&S.tpl3, ntpl * sizeof(bt::Tpl3)) && !cudaMalloc(&S.srec8, nrec * sizeof(int2)) &&
              !cudaMalloc(&S.sk, nrec * sizeof(int4)) && !cudaMalloc(&S.skz, nrec * sizeof(int2)) &&
              !cudaMalloc(&S.stpl, ntpl * sizeof(StateTpl));
+    else if (d3)
+        ok = !cudaMalloc(&S.tpl3, ntpl * sizeof(bt::Tpl3)) && !cudaMalloc(&S.rec16, nrec * sizeof(bt::Rec));
     else if (state)
         ok = !cudaMalloc(&S.tpl, ntpl * sizeof(bt::Tpl)) && !cudaMalloc(&S.srec, nrec * sizeof(int4)) &&
              !cudaMalloc(&S.srec8, nrec * sizeof(int2)) && !cudaMalloc(&S.stpl, ntpl * sizeof(StateTpl));
@@ -1063,7 +1128,11 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         }
         cudaMemcpyAsync(S.stpl, st.data(), ntpl * sizeof(StateTpl), cudaMemcpyHostToDevice, s);
     }
-    if (d3) {
+    if (d3 && !state) {
+        k_rec16_fill3<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X],
+                                                    c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac, c->scr, keys, ids,
+                                                    S.tpl3, 0.5 * S.kscale_inv, S.rec16, flags + 1);
+    } else if (d3) {
         k_state_compact3_fill<<<dim3(gx, gy), 256, 0, s>>>(
             P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac,
             c->w, keys, ids, S.tpl3, S.sn_exp, S.sth_exp, S.st_exp, S.srec8, S.sk, S.skz, S.stpl, flags + 1);
@@ -1138,16 +1207,11 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     cudaMemcpyAsync(S.base, bs.data(), bs.size() * 8, cudaMemcpyHostToDevice, s);
     const size_t n8 = (size_t)std::max<int64_t>(S.S, 1) * 8, n4 = (size_t)std::max<int64_t>(S.S, 1) * 4;
     bool ok = !cudaMalloc(&S.csr, n4) && !cudaMalloc(&S.bits, (size_t)std::max<int64_t>(S.F, 1) * 4);
-    // 2-D problems and 3-D state-based ones try the compact layout first
-    // (small per-slot records on offset-class templates); the 48-byte
-    // (bond-based) and three 32-byte (state-based) records are the general
-    // layout
-    const bool fits_compact = P.dim == 2 || state;
-    const bool try_compact = fits_compact && c->layout_pref != LAYOUT_RECORDS;
-    if (c->layout_pref == LAYOUT_COMPACT && !try_compact) {
-        free_sell(S);
-        return set_err(c, PD_ERR_UNSUPPORTED, "the compact layout serves 2-D problems and 3-D state-based ones");
-    }
+    // every problem tries the compact layout first (small per-slot records on
+    // offset-class templates); the 48-byte (bond-based) and three 32-byte
+    // (state-based) records are the general layout, taken where the compact
+    // one does not fit
+    const bool try_compact = c->layout_pref != LAYOUT_RECORDS;
     if (ok && !state && !try_compact)
         ok = !cudaMalloc(&S.rec, n8 * 6);
     // power-of-two scale bringing the bond coefficient 2 vol bc / dx near one,

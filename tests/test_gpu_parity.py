@@ -273,6 +273,7 @@ def test_split_slices_match_3d(E):
     p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=30, model=PD_MODEL_BOND)
     engs = [E.Engine(p) for _ in range(4)]
     for eng in engs:
+        eng.set_force_layout("records")  # the split kernels serve the records layout
         setup(eng)
     assert engs[0].get("NN").max() > 64  # rows span three 32-slot blocks
     engs[1].set_launch(128, 0, 1, 2)
@@ -292,8 +293,9 @@ def test_split_slices_match_3d(E):
     for eng in engs:
         eng.close()
     a, b = E.Engine(p), E.Engine(p)
-    setup(a)
-    setup(b)
+    for eng in (a, b):
+        eng.set_force_layout("records")
+        setup(eng)
     b.set_launch(256, 0, 1, 4)
     a.run_explicit(30)
     b.run_explicit(30)
@@ -564,18 +566,33 @@ def helpers_ell(values, NN, MN):
 
 
 def test_compact_layout_selection(E):
-    """Where the compact layout applies: 2-D problems (bond- and state-based)
-    and 3-D state-based ones take it by default; 3-D bond-based ones keep the
-    records, and asking for the compact layout there is refused
-    (PD_ERR_UNSUPPORTED, -8) without disturbing the context, which then runs
-    on the records."""
+    """Where the compact layout applies: every problem on a lattice takes it
+    by default (2-D and 3-D, bond- and state-based) and the records on
+    request.  A plate whose nodes are jittered off the lattice has a class
+    per bond: asking for the compact layout there is refused
+    (PD_ERR_UNSUPPORTED, -8) without disturbing the context, and the default
+    falls back to the records."""
     from pd_gpu1_gb300 import presets
     from pd_gpu1_gb300._abi import PD_MODEL_BOND
 
-    p, setup, meta = presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10, model=PD_MODEL_BOND)
+    for p, setup, meta in (presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10, model=PD_MODEL_BOND),
+                           presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10),
+                           presets.build_crack_grow(scale=0.1, nt=10)):
+        with E.Engine(p) as eng:
+            setup(eng)
+            assert eng.force_layout() == "compact"
+            eng.set_force_layout("records")
+            eng.prepare()
+            assert eng.force_layout() == "records"
+    p, setup, meta = presets.build_plate_tensile(scale=0.3)
+    rng = np.random.default_rng(3)
     with E.Engine(p) as eng:
-        setup(eng)
-        assert eng.force_layout() == "records"
+        eng.coord_plate_crack()
+        for k in ("X", "Y"):  # off the lattice by up to a hundredth of a spacing
+            eng.set(k, eng.get(k) + rng.uniform(-0.01, 0.01, p.N) * p.dx)
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        eng.initial_state()
         eng.set_force_layout("compact")
         with pytest.raises(E.PDError) as ei:
             eng.prepare()
@@ -584,17 +601,6 @@ def test_compact_layout_selection(E):
         eng.prepare()
         assert eng.force_layout() == "records"
         eng.bond_force_gpu()
-    p, setup, meta = presets.build_crack_grow(scale=0.1, nt=10)
-    with E.Engine(p) as eng:
-        setup(eng)
-        assert eng.force_layout() == "compact"
-        eng.set_force_layout("records")
-        eng.prepare()
-        assert eng.force_layout() == "records"
-    p, setup, meta = presets.build_kalthoff_winkler(scale=0.25, dx=2e-3, nt=10)
-    with E.Engine(p) as eng:
-        setup(eng)
-        assert eng.force_layout() == "compact"
 
 
 def test_state_compact_layout_matches_records(E):
@@ -703,3 +709,50 @@ def test_state_compact_3d_matches_records(E):
         assert_close_norm(out["compact"][9], out["records"][9], 1e-11, "uz after 30 steps")
         np.testing.assert_array_equal(out["compact"][10], out["records"][10])
         assert out["compact"][11] == pytest.approx(out["records"][11], rel=1e-12)
+
+
+def test_compact_3d_bond_matches_records(E):
+    """The 3-D bond kernel on the compact layout (16-byte records, 80-byte
+    class templates, quarter-slice units) against the 48-byte records on the
+    notched impact slab: forces within 2e-13 norm-relative, the same intact
+    flags after two passes at strains around s0 (the y >= -0.04 guard
+    included), the same results under two launch shapes bit for bit, and 30
+    impact steps within 1e-11 (the impactor's velocity 1e-12)."""
+    from pd_gpu1_gb300 import presets
+    from pd_gpu1_gb300._abi import PD_MODEL_BOND
+
+    p, setup, meta = presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=30, model=PD_MODEL_BOND)
+    rng = np.random.default_rng(11)
+    u = rng.standard_normal((3, p.N)) * 8e-6  # strains of a few 1e-3, around s0 (4e-3 at dx = 2e-3)
+    out = {}
+    with E.Engine(p) as eng:
+        for layout, shape in (("compact", (256, 0, 1, 1)), ("compact", (128, 0, 8, 1)), ("records", (256, 0, 1, 1))):
+            eng.set_force_layout(layout)
+            setup(eng)
+            assert eng.force_layout() == layout
+            eng.set_launch(*shape)
+            fail0 = eng.get("FAIL")
+            for a, k in enumerate(("UX", "UY", "UZ")):
+                eng.set(k, u[a])
+            eng.bond_force_gpu()
+            eng.bond_force_gpu()  # sees the bonds the first pass broke
+            got = [eng.get(k) for k in ("FX", "FY", "FZ", "FAIL")]
+            setup(eng)
+            eng.set_launch(*shape)
+            c2 = meta["cylinder"]
+            c2.disp[1] = -0.3 * p.dx
+            eng.cylinder_init(c2)
+            eng.run_explicit(30)
+            out[(layout, shape)] = got + [eng.get("UY"), eng.get("UZ"), eng.get("FAIL"), eng.cylinder().vel[1]]
+    a, b, rec = out[("compact", (256, 0, 1, 1))], out[("compact", (128, 0, 8, 1))], out[("records", (256, 0, 1, 1))]
+    for x, y in zip(a[:4], b[:4]):
+        np.testing.assert_array_equal(x, y)
+    n = p.N_int
+    for k, what in ((0, "fx"), (1, "fy"), (2, "fz")):
+        assert_close_norm(a[k][:n], rec[k][:n], 2e-13, what)
+    np.testing.assert_array_equal(a[3], rec[3])
+    assert (a[3] == 0).sum() > (fail0 == 0).sum()  # bonds broke beyond the notch
+    assert_close_norm(a[4], rec[4], 1e-11, "uy after 30 steps")
+    assert_close_norm(a[5], rec[5], 1e-11, "uz after 30 steps")
+    np.testing.assert_array_equal(a[6], rec[6])
+    assert a[7] == pytest.approx(rec[7], rel=1e-12)
