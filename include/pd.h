@@ -393,23 +393,32 @@ int pd_batch_get_cn(pd_ctx* ctx, double* cn, void* stream);
  * differ in the last bits.  Default 256 / 0 / 1 / 1.  The reference's two
  * mappings, thread per node (kernel_particle_force_2D, Force_Bond.cu:52-85)
  * and warp per node (kernel_bond_force_2D, :6-50), correspond to split 1 and
- * to the widest split. */
+ * to the widest split.  On the compact layout the 3-D bond kernel and the
+ * state-based passes take the block size (at most 256 for the state-based
+ * passes) and the waves; their unit order is fixed (the 3-D state-based
+ * force pass: quarter slices with four slot phases). */
 int pd_set_launch(pd_ctx* ctx, int block, int chunked, int waves, int split);
 int pd_get_launch(const pd_ctx* ctx, int* block, int* chunked, int* waves, int* split);
-/* Per-bond storage of the bond-based force kernels.  PD_LAYOUT_RECORDS: one
- * 48-byte record per bond slot (column, float reference vector, c0, l0, k2,
- * break threshold), any geometry, 2-D and 3-D.  PD_LAYOUT_COMPACT (2-D): one
- * 16-byte record per slot (column, l0 - l0t with the offset class id, k2 / 2)
- * plus one template per offset class (bonds whose reference vectors round to
- * the same float vector, one class per lattice offset on the reference's
- * regular grids), for problems with at most 255 classes whose bond lengths
- * differ from the class's smallest by a float with a free low byte;
- * pd_prepare returns PD_ERR_UNSUPPORTED when a problem does not fit.
- * PD_LAYOUT_AUTO (default): compact where it fits, records otherwise.  Both
- * layouts give the reference's intact flags and forces to the same bars; the
- * forces of the two differ in the last bits (different pair arithmetic).  No
- * counterpart in the reference, whose bond arrays are padded ELL
- * (Memory.cu:38-43).  Changing the layout releases the prepared arrays. */
+/* Per-bond storage of the force kernels.  PD_LAYOUT_RECORDS: per bond slot
+ * one 48-byte record (bond-based: column, float reference vector, c0, l0, k2,
+ * break threshold) or three 32-byte records (state-based), any geometry.
+ * PD_LAYOUT_COMPACT: one template per offset class (bonds whose reference
+ * vectors round to the same float vector, one class per lattice offset on
+ * the reference's regular grids: float vector, |xf|^2, |xf|^2 - l0t^2 and the
+ * class's smallest length l0t) and small per-slot records: bond-based 16
+ * bytes (column, l0 - l0t with the class id, k2 / 2; in 3-D the sign of k2
+ * marks bonds the y >= -0.04 guard spares); state-based the column, l0 - l0t
+ * with the class id and the reference vector's distance from the class's in
+ * representable doubles (2-D 16 + 8 bytes, 3-D 8 + 16 + 8), the bond
+ * coefficients per class.  For problems with at most 255 classes per
+ * specimen whose bond lengths differ from their class's smallest by a float
+ * with a free low byte; pd_prepare returns PD_ERR_UNSUPPORTED when a problem
+ * does not fit.  PD_LAYOUT_AUTO (default): compact where it fits, records
+ * otherwise.  Both layouts give the reference's intact flags and forces to
+ * the same bars; the forces of the two differ in the last bits (different
+ * pair arithmetic).  No counterpart in the reference, whose bond arrays are
+ * padded ELL (Memory.cu:38-43).  Changing the layout releases the prepared
+ * arrays. */
 #define PD_LAYOUT_AUTO 0
 #define PD_LAYOUT_RECORDS 1
 #define PD_LAYOUT_COMPACT 2
@@ -418,7 +427,8 @@ int pd_set_force_layout(pd_ctx* ctx, int layout);
 int pd_get_force_layout(const pd_ctx* ctx, int* layout);
 /* Times the bond-force kernel (reps launches per shape, at the current
  * displacements) over the shapes above (24 with split 1: 1, 2, 4 or 8 waves;
- * 12 more with split 2 and 4) and keeps the fastest; *best_ms receives its time per
+ * 12 more with split 2 and 4; a 3-D compact context only the 12 strided
+ * one-warp shapes) and keeps the fastest; *best_ms receives its time per
  * launch.  Intact flags and forces are restored, so a run continues exactly
  * as without the call.  Bond-based contexts only. */
 int pd_autotune(pd_ctx* ctx, int reps, double* best_ms, void* stream);
