@@ -62,7 +62,8 @@ TRAFFIC = {
     "crack_branching_2d_pmb_verlet": (21.1, 0.0, "k_bond_compact<1>, 400k-node quarter-size plate (node traffic folded "
                                                  "into the per-bond figure), 2026-12-04"),
     "batch_plate_adr_2d_pmb": (22.5, 0.0, "k_bond_compact<2>, 64-plate batch (node traffic folded in), 2026-12-04"),
-    "kalthoff_winkler_3d_pmb_verlet": (52.7, 0.0, "k_bond_split3, full slab, 2026-12-03"),
+    "kalthoff_winkler_3d_pmb_verlet": (17.5, 0.0, "k_bond_compact3<EPI_NONE>, full slab (the Verlet and contact "
+                                                  "epilogue's node traffic not included), 2026-12-04"),
     "plate_crack_grow_2d_state_verlet": (42.5, 0.0, "k_theta_compact + k_state_compact<1>, full plate, 2026-12-04"),
     "kalthoff_winkler_3d_state_verlet": (59.7, 0.0, "k_theta_compact3 + k_state_compact3<0>, full slab, 2026-12-04")}
 
