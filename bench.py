@@ -936,7 +936,7 @@ def warm_arm(args):
 
 
 def batch_block(steps, warmup, count=256):
-    """The batch workload (SURVEY C4: 256 seeded uneven plates, ADR) as a block
+    """The batch workload (256 seeded uneven plates, ADR) as a block
     of the default line: set-up, the autotuned launch shape, warmup + steps
     ADR steps timed with CUDA events on the launch stream (batch_arm gives the
     full line with its comparisons)."""
