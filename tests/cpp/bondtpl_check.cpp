@@ -1,5 +1,6 @@
-// Host check of the per-bond arithmetic of the 2-D template path
-// (pd_gpu1_gb300/csrc/bondtpl.h) against quadruple precision.
+// Host check of the per-bond arithmetic of the template path
+// (pd_gpu1_gb300/csrc/bondtpl.h) against quadruple precision: the 2-D bond
+// (bond2, exceeds) and the 3-D stretch (stretch3).
 //
 // Bonds of regular lattices (dx from 5e-5 to 1e-3, horizon 3.015 dx, the
 // plate coordinates (i + 1/2) dx - L/2 of the reference's generators) under
@@ -16,6 +17,7 @@
 // fl(e.h + e.l) > fl(s0 l0) on extensions placed around the threshold.
 #include <quadmath.h>
 
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <random>
@@ -54,6 +56,123 @@ static void make_tpl(Tpl& T, const double xa[2], double l0t) {
     const f2 lp = split_bits(l0t);
     T.l0h = lp.h, T.l0l = lp.l;
     T.l0d = l0t;
+}
+
+// The 3-D class template from a representative reference vector and l0t.
+static void make_tpl3(Tpl3& T, const double xa[3], double l0t) {
+    q sq = 0;
+    for (int a = 0; a < 3; a++) {
+        T.xf[a] = (float)xa[a];
+        T.xf2[a] = 2.0f * T.xf[a];
+        T.xd[a] = dbits((double)T.xf[a]);
+        sq += (q)T.xf[a] * (q)T.xf[a];
+    }
+    const q c = sq - (q)l0t * (q)l0t;
+    double sh = (double)sq, ch = (double)c;
+    f2 sp = split_bits(sh), cp = split_bits(ch);
+    sp.l = (float)((q)sp.l + (sq - (q)sh));
+    cp.l = (float)((q)cp.l + (c - (q)ch));
+    T.q0h = sp.h, T.q0l = sp.l, T.c0h = cp.h, T.c0l = cp.l;
+    const f2 lp = split_bits(l0t);
+    T.l0h = lp.h, T.l0l = lp.l;
+    T.l0d = l0t;
+}
+
+// stretch3 on the bonds of a 3-D lattice (the offsets within 3.015 spacings,
+// coordinates i dx - L/2 per axis), the force direction w = xf + eta, 1/L and
+// e against __float128, relative to the field's strain scale.
+static bool check3(std::mt19937_64& rng, double& worst_e, double& worst_f) {
+    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    const double dxs[] = {1e-3, 2e-3};
+    const double strains[] = {1e-6, 1e-4, 1e-2};
+    worst_e = worst_f = 0.0;
+    for (double dx : dxs) {
+        const int n = 60;
+        const double L = n * dx, delta = 3.015 * dx;
+        std::vector<std::array<int, 3>> offs;
+        for (int oz = -3; oz <= 3; oz++)
+            for (int oy = -3; oy <= 3; oy++)
+                for (int ox = -3; ox <= 3; ox++)
+                    if ((ox || oy || oz) &&
+                        (ox * dx) * (ox * dx) + (oy * dx) * (oy * dx) + (oz * dx) * (oz * dx) < delta * delta)
+                        offs.push_back({ox, oy, oz});
+        auto coord = [&](int i) { return i * dx - L / 2.0; };
+        for (double strain : strains) {
+            const int rows = 1500;
+            std::vector<std::array<int, 3>> rr(rows);
+            for (auto& v : rr)
+                for (int a = 0; a < 3; a++) v[a] = 3 + (int)(rng() % (n - 6));
+            std::vector<double> l0min(offs.size(), 1e300);
+            std::vector<std::array<double, 3>> rep(offs.size());
+            for (size_t o = 0; o < offs.size(); o++)
+                for (int k = 0; k < rows; k++) {
+                    double xa[3], l2 = 0.0;
+                    for (int a = 0; a < 3; a++) {
+                        xa[a] = coord(rr[k][a] + offs[o][a]) - coord(rr[k][a]);
+                        l2 += xa[a] * xa[a];
+                    }
+                    const double l0 = std::sqrt(l2);
+                    if (k == 0) rep[o] = {xa[0], xa[1], xa[2]};
+                    if (l0 < l0min[o]) l0min[o] = l0;
+                }
+            std::vector<Tpl3> tpl(offs.size());
+            for (size_t o = 0; o < offs.size(); o++) make_tpl3(tpl[o], rep[o].data(), l0min[o]);
+            for (int k = 0; k < rows; k++) {
+                double g[3][3];
+                for (int a = 0; a < 3; a++)
+                    for (int b = 0; b < 3; b++) g[a][b] = strain * U(rng);
+                for (size_t o = 0; o < offs.size(); o++) {
+                    double xi[3], xc[3], ui[3], uc[3], xa[3], l2 = 0.0;
+                    for (int a = 0; a < 3; a++) {
+                        xi[a] = coord(rr[k][a]);
+                        xc[a] = coord(rr[k][a] + offs[o][a]);
+                    }
+                    for (int a = 0; a < 3; a++) {
+                        ui[a] = g[a][0] * xi[0] + g[a][1] * xi[1] + g[a][2] * xi[2] + 0.1 * strain * dx * U(rng);
+                        uc[a] = g[a][0] * xc[0] + g[a][1] * xc[1] + g[a][2] * xc[2] + 0.1 * strain * dx * U(rng);
+                        xa[a] = xc[a] - xi[a];
+                        l2 += xa[a] * xa[a];
+                    }
+                    const double l0 = std::sqrt(l2);
+                    const Tpl3& T = tpl[o];
+                    const double dlv = l0 - T.l0d;
+                    const float dl = (float)dlv;
+                    if ((double)dl != dlv) {
+                        std::printf("3-D: dl not a float: %g\n", dlv);
+                        return false;
+                    }
+                    double d[3];
+                    f2 eta[3];
+                    for (int a = 0; a < 3; a++) {
+                        d[a] = ((xc[a] + uc[a]) - xi[a]) - ui[a];
+                        if (T.xd[a] == 0)
+                            eta[a] = split_bits(d[a]);
+                        else if (!offset_pair(d[a], T.xd[a], eta[a]))
+                            eta[a] = split_bits(d[a] - dfrom(T.xd[a]));
+                    }
+                    f2 w[3], y, e;
+                    stretch3(eta, T, dl, w, y, e);
+                    const q Lq = sqrtq((q)d[0] * (q)d[0] + (q)d[1] * (q)d[1] + (q)d[2] * (q)d[2]);
+                    const q eq = Lq - (q)l0;
+                    const q escale = qabs(eq) > (q)(strain * l0) ? qabs(eq) : (q)(strain * l0);
+                    const double re = (double)(qabs((q)e.h + (q)e.l - eq) / escale);
+                    // the force direction w / L against d / L
+                    q fd = 0;
+                    for (int a = 0; a < 3; a++) {
+                        const q got = ((q)w[a].h + (q)w[a].l) * ((q)y.h + (q)y.l);
+                        const q want = (q)d[a] / Lq;
+                        fd += (got - want) * (got - want);
+                    }
+                    // the force's error relative to its strain-scale magnitude: e times the
+                    // direction error, plus the extension error (already in re)
+                    const double rf = (double)(sqrtq(fd) * qabs(eq) / escale);
+                    if (re > worst_e) worst_e = re;
+                    if (rf > worst_f) worst_f = rf;
+                }
+            }
+        }
+    }
+    return true;
 }
 
 int main() {
@@ -194,7 +313,10 @@ int main() {
         if (want != got) bad++;
     }
     std::printf("break decisions: %ld checked, %ld differ from the double test\n", checked, bad);
-    const bool ok = worst_e <= 2e-13 && worst_f <= 2e-13 && bad == 0;
+    double e3 = 0.0, f3 = 0.0;
+    const bool ok3 = check3(rng, e3, f3);
+    std::printf("3-D stretch: worst extension %.2e, worst direction term %.2e\n", e3, f3);
+    const bool ok = ok3 && worst_e <= 2e-13 && worst_f <= 2e-13 && e3 <= 2e-13 && f3 <= 2e-13 && bad == 0;
     std::printf(ok ? "OK\n" : "FAIL\n");
     return ok ? 0 : 1;
 }

@@ -1,9 +1,10 @@
-"""The per-bond arithmetic of the 2-D compact-record force path
+"""The per-bond arithmetic of the compact-record force paths
 (pd_gpu1_gb300/csrc/bondtpl.h), compiled for the host and checked against
-quadruple precision on three million lattice bonds (extension and force
-within 2e-13 of the strain scale, hardware-like reciprocal seeds), and its
-break decision against the double test on two million extensions around
-the threshold."""
+quadruple precision: the 2-D bond on three million lattice bonds (extension
+and force within 2e-13 of the strain scale, hardware-like reciprocal seeds),
+its break decision against the double test on two million extensions around
+the threshold, and the 3-D stretch (extension, 1/L and direction) on the
+bonds of a 3-D lattice."""
 import os
 import shutil
 import subprocess
@@ -26,3 +27,4 @@ def test_bond_arithmetic_against_quad_precision(tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
     assert out.returncode == 0, out.stdout + out.stderr
     assert "break decisions: 2000000 checked, 0 differ" in out.stdout
+    assert "3-D stretch: worst extension" in out.stdout
