@@ -297,7 +297,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     bool ok = true;
     for (int f = 0; f < kNodeDoubleFields && ok; f++) ok = cudaMalloc(&c->nf[f], nb) == cudaSuccess;
     for (int b = 0; b < 2 && ok; b++)
-        for (int a = 0; a < 3 && ok; a++) ok = cudaMalloc(&c->pos[b][a], nb) == cudaSuccess;
+        ok = cudaMalloc(&c->posxy[b], 2 * nb) == cudaSuccess && cudaMalloc(&c->posz[b], nb) == cudaSuccess;
     ok = ok && cudaMalloc(&c->NN, (size_t)p->N * 4) == cudaSuccess;
     ok = ok && cudaMalloc(&c->rowptr, ((size_t)p->N + 1) * 8) == cudaSuccess;
     ok = ok && cudaMalloc(&c->node_a, 2 * nb) == cudaSuccess && cudaMalloc(&c->node_b, nb) == cudaSuccess;
@@ -313,7 +313,7 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     }
     for (int f = 0; f < kNodeDoubleFields; f++) cudaMemset(c->nf[f], 0, nb);
     for (int b = 0; b < 2; b++)
-        for (int a = 0; a < 3; a++) cudaMemset(c->pos[b][a], 0, nb);
+        cudaMemset(c->posxy[b], 0, 2 * nb), cudaMemset(c->posz[b], 0, nb);
     cudaMemset(c->NN, 0, (size_t)p->N * 4);
     cudaMemset(c->rowptr, 0, ((size_t)p->N + 1) * 8);
     cudaMemset(c->node_a, 0, 2 * nb);
@@ -336,9 +336,10 @@ int pd_destroy(pd_ctx* c) {
     drop_graphs(c);
     for (int f = 0; f < kNodeDoubleFields; f++)
         if (c->nf[f]) cudaFree(c->nf[f]);
-    for (int b = 0; b < 2; b++)
-        for (int a = 0; a < 3; a++)
-            if (c->pos[b][a]) cudaFree(c->pos[b][a]);
+    for (int b = 0; b < 2; b++) {
+        if (c->posxy[b]) cudaFree(c->posxy[b]);
+        if (c->posz[b]) cudaFree(c->posz[b]);
+    }
     void* ptrs[] = {c->NN,  c->rowptr, c->node_a, c->node_b, c->partials, c->ticket, c->cn,
                     c->red_out, c->res, c->cyl, c->NL, c->idist, c->fac, c->scr, c->w, c->e, c->fail,
                     c->warm_hist};

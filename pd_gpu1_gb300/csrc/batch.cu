@@ -67,7 +67,8 @@ __global__ void k_batch_cn(int count, const int64_t* __restrict__ inst_slices, c
 
 struct BatchArgs {
     KParams P;
-    double *x, *y, *ux, *uy, *vx, *vy, *fx, *fy, *bx, *by, *vhx, *vhy, *fox, *foy, *px, *py;
+    double *x, *y, *ux, *uy, *vx, *vy, *fx, *fy, *bx, *by, *vhx, *vhy, *fox, *foy;
+    double2* pxy;  // current positions, x and y interleaved
     const double* mass;
     const double* c1;  // 2 dt / mass per node
     const double* sign;
@@ -123,8 +124,7 @@ __global__ void k_batch_update(BatchArgs A, int ct, int do_next, double load) {
         } else if (do_next && load != 0.0) {
             move_boundary(A, i, load);
         }
-        A.px[i] = A.x[i] + A.ux[i];
-        A.py[i] = A.y[i] + A.uy[i];
+        A.pxy[i] = make_double2(A.x[i] + A.ux[i], A.y[i] + A.uy[i]);
     }
 }
 
@@ -133,8 +133,7 @@ __global__ void k_batch_prologue(BatchArgs A, double load) {
     const KParams& P = A.P;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
         if (i >= P.N_int && load != 0.0) move_boundary(A, i, load);
-        A.px[i] = A.x[i] + A.ux[i];
-        A.py[i] = A.y[i] + A.uy[i];
+        A.pxy[i] = make_double2(A.x[i] + A.ux[i], A.y[i] + A.uy[i]);
     }
 }
 
@@ -145,7 +144,7 @@ BatchArgs batch_args(pd_ctx* c) {
     a.x = f[PD_F_X], a.y = f[PD_F_Y], a.ux = f[PD_F_UX], a.uy = f[PD_F_UY], a.vx = f[PD_F_VX], a.vy = f[PD_F_VY];
     a.fx = f[PD_F_FX], a.fy = f[PD_F_FY], a.bx = f[PD_F_BX], a.by = f[PD_F_BY];
     a.vhx = f[PD_F_VHX], a.vhy = f[PD_F_VHY], a.fox = f[PD_F_FOX], a.foy = f[PD_F_FOY];
-    a.px = c->pos[c->parity][0], a.py = c->pos[c->parity][1];
+    a.pxy = c->posxy[c->parity];
     a.mass = c->batch.node_mass;
     a.c1 = c->batch.node_c1;
     a.sign = c->batch.load_sign;

@@ -70,8 +70,10 @@ struct ForceArgs {
     const int* NN;
     const double *x, *y, *z;
     double *ux, *uy, *uz;
-    const double *pcx, *pcy, *pcz;
-    double *pnx, *pny, *pnz;
+    const double2* pc;  // current positions, x and y interleaved
+    const double* pcz;
+    double2* pn;        // next positions (the other ping-pong buffer)
+    double* pnz;
     double *fx, *fy, *fz;
     double *vx, *vy, *vz;
     double *ax, *ay, *az;
@@ -352,8 +354,7 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
             if (DIM == 3) A.uz[r] = uz;
         }
         if (A.do_next) {
-            A.pnx[r] = xi + ux;
-            A.pny[r] = yi + uy;
+            A.pn[r] = make_double2(xi + ux, yi + uy);
             if (DIM == 3) A.pnz[r] = zi + uz;
         }
     }
@@ -388,8 +389,7 @@ __device__ __forceinline__ void boundary_row(const ForceArgs& A, int64_t r) {
             uy -= A.load * P.dt;
         A.uy[r] = uy;
     }
-    A.pnx[r] = A.pcx[r];
-    A.pny[r] = A.y[r] + uy;
+    A.pn[r] = make_double2(A.pc[r].x, A.y[r] + uy);
     if (DIM == 3) A.pnz[r] = A.pcz[r];
 }
 
@@ -492,7 +492,8 @@ template <int DIM>
 __device__ __forceinline__ bool bond3(const ForceArgs& A, int4 q0, float4 q1, float4 q2, double xi, double yi,
                                       double zi, double uxi, double uyi, double uzi, ff cf[3]) {
     const int c = q0.x;
-    const double pc[3] = {__ldg(A.pcx + c), __ldg(A.pcy + c), DIM == 3 ? __ldg(A.pcz + c) : 0.0};
+    const double2 pxy = __ldg(A.pc + c);
+    const double pc[3] = {pxy.x, pxy.y, DIM == 3 ? __ldg(A.pcz + c) : 0.0};
     const double xr[3] = {xi, yi, zi}, ur[3] = {uxi, uyi, uzi};
     const float xfs[3] = {__int_as_float(q0.y), __int_as_float(q0.z), __int_as_float(q0.w)};
     ff eta[3], dp[3], y, e2;
@@ -712,7 +713,8 @@ __device__ __forceinline__ bool bond_compact_p(const bt::Tpl* __restrict__ tpls,
 }
 __device__ __forceinline__ bool bond_compact(const ForceArgs& A, const bt::Tpl* __restrict__ tpls, int4 rq, double xi,
                                              double yi, double uxi, double uyi, double s0, float s0f, bt::f2 cf[2]) {
-    return bond_compact_p(tpls, rq, __ldg(A.pcx + rq.x), __ldg(A.pcy + rq.x), xi, yi, uxi, uyi, s0, s0f, cf);
+    const double2 pxy = __ldg(A.pc + rq.x);
+    return bond_compact_p(tpls, rq, pxy.x, pxy.y, xi, yi, uxi, uyi, s0, s0f, cf);
 }
 
 // The compact kernel's software pipeline: records two slots ahead and the
@@ -761,15 +763,17 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
             if (kGatherAhead) {
                 const int4 z4 = make_int4(0, 0, 0, 0);
                 int4 rq_a = W > 0 ? __ldg(rp) : z4, rq_b = W > 1 ? __ldg(rp + 32) : z4;
-                double gx = W > 0 ? __ldg(A.pcx + rq_a.x) : 0.0, gy = W > 0 ? __ldg(A.pcy + rq_a.x) : 0.0;
+                const double2 g0 = W > 0 ? __ldg(A.pc + rq_a.x) : make_double2(0.0, 0.0);
+                double gx = g0.x, gy = g0.y;
                 for (int k = 0; k < W; k++) {
                     const int4 rq = rq_a;
                     const double pcx = gx, pcy = gy;
                     rq_a = rq_b;
                     if (k + 2 < W) rq_b = __ldg(rp + (int64_t)(k + 2) * 32);
                     if (k + 1 < W) {
-                        gx = __ldg(A.pcx + rq_a.x);
-                        gy = __ldg(A.pcy + rq_a.x);
+                        const double2 g1 = __ldg(A.pc + rq_a.x);
+                        gx = g1.x;
+                        gy = g1.y;
                     }
                     const uint32_t word = wbits[k];
                     const bool alive = force_row && ((word >> lane) & 1u);
@@ -893,8 +897,8 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
                     const bt::Tpl3& T = A.tpl3[dlb & 0xffu];
                     const float dl = __uint_as_float(dlb & ~0xffu);
                     // d = (P_c - x_i) - u_i with the reference's roundings
-                    const double d[3] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi,
-                                         (__ldg(A.pcz + c) - zi) - uzi};
+                    const double2 pxy = __ldg(A.pc + c);
+                    const double d[3] = {(pxy.x - xi) - uxi, (pxy.y - yi) - uyi, (__ldg(A.pcz + c) - zi) - uzi};
                     bt::f2 eta[3], w[3], y, e;
                     offsets_n<3>(T, d, eta);
                     bt::stretch3(eta, T, dl, w, y, e);
@@ -1200,8 +1204,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                     // d = (P_c - x_i) - u_i, the force pass's operand order, then its
                     // exact offsets from xf and the stretch in pairs
                     ff eta[3], dp[3], y, e2, etaz{0.0f, 0.0f};
-                    eta[0] = bond_offset(A.pcx[c], xi, uxi, xf[0]);
-                    eta[1] = bond_offset(A.pcy[c], yi, uyi, xf[1]);
+                    const double2 pxy = A.pc[c];
+                    eta[0] = bond_offset(pxy.x, xi, uxi, xf[0]);
+                    eta[1] = bond_offset(pxy.y, yi, uyi, xf[1]);
                     if (DIM == 3) {
                         // the reference's 3-D force kernel takes the z term of the
                         // length in the dilatation pass's operand order (Force_State.cu:272)
@@ -1292,8 +1297,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force3_p
                 // as k_state_force<3>: the force pass's operand order, the z term of
                 // the length in the dilatation pass's (Force_State.cu:272)
                 ff eta[3], dp[3], y, e2, etaz;
-                eta[0] = bond_offset(A.pcx[c], xi, uxi, xf[0]);
-                eta[1] = bond_offset(A.pcy[c], yi, uyi, xf[1]);
+                const double2 pxy = A.pc[c];
+                eta[0] = bond_offset(pxy.x, xi, uxi, xf[0]);
+                eta[1] = bond_offset(pxy.y, yi, uyi, xf[1]);
                 eta[2] = exact_offset((hi_f64(w5) + A.uz[c]) - uzi, xf[2]);
                 etaz = bond_offset(A.pcz[c], zi, uzi, xf[2]);
                 pair_stretch<3>(eta, xf, make_float2(w1.x, w1.y), make_float2(w1.z, w1.w), dp, y, e2);
@@ -1472,7 +1478,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
                     const bt::Tpl& T = A.tpl[id];
                     const float dl = __uint_as_float(dlb & ~0xffu);
                     // d = (P_c - x_i) - u_i, the force pass's operand order
-                    const double d[2] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi};
+                    const double2 pxy = __ldg(A.pc + c);
+                    const double d[2] = {(pxy.x - xi) - uxi, (pxy.y - yi) - uyi};
                     bt::f2 eta[2], w[2], y, ef;
                     offsets2(T, d, eta);
                     bt::stretch2(eta, T, dl, w, y, ef);
@@ -1637,8 +1644,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
                 const double za = __longlong_as_double((long long)T.xd[2] + kz.x);
                 // the length's components: x, y in the force order, z in the
                 // dilatation order; then the force order's z for the direction
-                const double dlen[3] = {(__ldg(A.pcx + c) - xi) - uxi, (__ldg(A.pcy + c) - yi) - uyi,
-                                        (za + __ldg(A.uz + c)) - uzi};
+                const double2 pxy = __ldg(A.pc + c);
+                const double dlen[3] = {(pxy.x - xi) - uxi, (pxy.y - yi) - uyi, (za + __ldg(A.uz + c)) - uzi};
                 const double dzf = (__ldg(A.pcz + c) - zi) - uzi;
                 bt::f2 eta[3], w[3], y, ef, etz;
                 offsets_n<3>(T, dlen, eta);
@@ -1781,12 +1788,10 @@ static ForceArgs make_args(pd_ctx* c) {
     A.ux = c->nf[PD_F_UX];
     A.uy = c->nf[PD_F_UY];
     A.uz = c->nf[PD_F_UZ];
-    A.pcx = c->pos[c->parity][0];
-    A.pcy = c->pos[c->parity][1];
-    A.pcz = c->pos[c->parity][2];
-    A.pnx = c->pos[c->parity ^ 1][0];
-    A.pny = c->pos[c->parity ^ 1][1];
-    A.pnz = c->pos[c->parity ^ 1][2];
+    A.pc = c->posxy[c->parity];
+    A.pcz = c->posz[c->parity];
+    A.pn = c->posxy[c->parity ^ 1];
+    A.pnz = c->posz[c->parity ^ 1];
     A.fx = c->nf[PD_F_FX];
     A.fy = c->nf[PD_F_FY];
     A.fz = c->nf[PD_F_FZ];

@@ -28,7 +28,8 @@ struct NodeArgs {
     KParams P;
     double *x, *y, *z, *ux, *uy, *uz, *vx, *vy, *vz, *ax, *ay, *az, *fx, *fy, *fz, *bx, *by, *bz;
     double *vhx, *vhy, *vhz, *fox, *foy, *foz;
-    double *px, *py, *pz;
+    double2* pxy;  // current positions, x and y interleaved
+    double* pz;
     const double* cn;
     CylDev* cyl;
 };
@@ -45,7 +46,7 @@ NodeArgs node_args(pd_ctx* c) {
     a.bx = f[PD_F_BX], a.by = f[PD_F_BY], a.bz = f[PD_F_BZ];
     a.vhx = f[PD_F_VHX], a.vhy = f[PD_F_VHY], a.vhz = f[PD_F_VHZ];
     a.fox = f[PD_F_FOX], a.foy = f[PD_F_FOY], a.foz = f[PD_F_FOZ];
-    a.px = c->pos[c->parity][0], a.py = c->pos[c->parity][1], a.pz = c->pos[c->parity][2];
+    a.pxy = c->posxy[c->parity], a.pz = c->posz[c->parity];
     a.cn = c->cn;
     a.cyl = c->cyl;
     return a;
@@ -54,8 +55,7 @@ NodeArgs node_args(pd_ctx* c) {
 __global__ void k_refresh_pos(NodeArgs A) {
     const KParams& P = A.P;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
-        A.px[i] = A.x[i] + A.ux[i];
-        A.py[i] = A.y[i] + A.uy[i];
+        A.pxy[i] = make_double2(A.x[i] + A.ux[i], A.y[i] + A.uy[i]);
         if (P.dim == 3) A.pz[i] = A.z[i] + A.uz[i];
     }
 }
@@ -83,8 +83,7 @@ __global__ void k_prologue(NodeArgs A, double load, int first_verlet, int cyl_st
             A.uy[i] = fma(A.vy[i], P.dt, A.uy[i]);
             if (P.dim == 3) A.uz[i] = fma(A.vz[i], P.dt, A.uz[i]);
         }
-        A.px[i] = A.x[i] + A.ux[i];
-        A.py[i] = A.y[i] + A.uy[i];
+        A.pxy[i] = make_double2(A.x[i] + A.ux[i], A.y[i] + A.uy[i]);
         if (P.dim == 3) A.pz[i] = A.z[i] + A.uz[i];
     }
     if (cyl_step && blockIdx.x == 0 && threadIdx.x == 0) {
@@ -128,8 +127,7 @@ __global__ void k_adr_update(NodeArgs A, int ct, int do_next, double load) {
         } else if (do_next && load != 0.0) {
             quick_load_row(P, i, load, A.uy);
         }
-        A.px[i] = A.x[i] + A.ux[i];
-        A.py[i] = A.y[i] + A.uy[i];
+        A.pxy[i] = make_double2(A.x[i] + A.ux[i], A.y[i] + A.uy[i]);
         if (P.dim == 3) A.pz[i] = A.z[i] + A.uz[i];
     }
 }

@@ -207,7 +207,10 @@ struct pd_ctx {
 
     // node fields, indexed by pd_field for ids < PD_F_NN (N doubles each)
     double* nf[PD_F_NN] = {};
-    double* pos[2][3] = {};  // ping-pong current position P = x + u
+    // ping-pong current position P = x + u: x and y interleaved (one 16-byte
+    // gather per neighbour), z apart
+    double2* posxy[2] = {};
+    double* posz[2] = {};
     int parity = 0;          // pos[parity] is current
     bool pos_valid = false;  // pos[parity] == x + u
     int* NN = nullptr;
