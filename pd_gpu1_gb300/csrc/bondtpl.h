@@ -48,29 +48,31 @@ struct f2 {
     float h, l;  // value h + l
 };
 
-// One offset class: four 16-byte words (the fourth is read only by the
+// One offset class: four 16-byte words, ordered so that a bond's stretch
+// reads the first three (the fourth holds l0t as a double, read only by the
 // break test's exact path).
 struct alignas(16) Tpl {
     uint64_t xd[2];  // xf as double bit patterns
     float xf[2];     // the class's float reference vector
-    float xf2[2];    // 2 xf (exact)
     float c0h, c0l;  // |xf|^2 - l0t^2 as a pair (computed exactly)
     float q0h, q0l;  // |xf|^2 as a pair
     float l0h, l0l;  // l0t as a pair
     double l0d;      // l0t
+    double pad;
 };
 static_assert(sizeof(Tpl) == 64, "four 16-byte words");
 
 // One 3-D offset class: the same quantities as Tpl with three components
-// (five 16-byte words).
+// (five 16-byte words; a stretch reads the first four).
 struct alignas(16) Tpl3 {
     uint64_t xd[3];  // xf as double bit patterns
     float xf[3];     // the class's float reference vector
-    float xf2[3];    // 2 xf (exact)
     float c0h, c0l;  // |xf|^2 - l0t^2 as a pair (computed exactly)
     float q0h, q0l;  // |xf|^2 as a pair
     float l0h, l0l;  // l0t as a pair
+    float pad;
     double l0d;      // l0t
+    double pad2;
 };
 static_assert(sizeof(Tpl3) == 80, "five 16-byte words");
 
@@ -273,7 +275,7 @@ PD_BT_HD void stretch2(const f2 eta[2], const Tpl& T, float dl, f2 w[2], f2& y, 
         // W = xf + eta and V = 2 xf + eta as pairs (TwoSum of the high parts)
         f2 s = two_sum(T.xf[a], eta[a].h);
         w[a] = f2{s.h, s.l + eta[a].l};
-        s = two_sum(T.xf2[a], eta[a].h);
+        s = two_sum(2.0f * T.xf[a], eta[a].h);  // 2 xf (exact)
         v[a] = f2{s.h, s.l + eta[a].l};
         // eta_a V_a: exact product of the high parts, cross terms in the low part
         m[a] = eta[a].h * v[a].h;
@@ -310,7 +312,7 @@ PD_BT_HD void stretch3(const f2 eta[3], const Tpl3& T, float dl, f2 w[3], f2& y,
     for (int a = 0; a < 3; a++) {
         f2 s = two_sum(T.xf[a], eta[a].h);
         w[a] = f2{s.h, s.l + eta[a].l};
-        s = two_sum(T.xf2[a], eta[a].h);
+        s = two_sum(2.0f * T.xf[a], eta[a].h);  // 2 xf (exact)
         const f2 v{s.h, s.l + eta[a].l};
         m[a] = eta[a].h * v.h;
         float r = fmaf(eta[a].h, v.h, -m[a]);

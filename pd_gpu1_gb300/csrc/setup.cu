@@ -1057,20 +1057,18 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
             const bt::f2 l0 = bt::split_bits(l0t);
             l0ts.push_back(l0t);
             if (d3) {
-                bt::Tpl3 T;
+                bt::Tpl3 T{};
                 for (int a = 0; a < 3; a++) {
                     T.xf[a] = xf[a];
-                    T.xf2[a] = 2.0f * xf[a];
                     T.xd[a] = bt::dbits((double)xf[a]);
                 }
                 T.c0h = c0.h, T.c0l = c0.l, T.q0h = q0.h, T.q0l = q0.l, T.l0h = l0.h, T.l0l = l0.l;
                 T.l0d = l0t;
                 tp3.push_back(T);
             } else {
-                bt::Tpl T;
+                bt::Tpl T{};
                 for (int a = 0; a < 2; a++) {
                     T.xf[a] = xf[a];
-                    T.xf2[a] = 2.0f * xf[a];
                     T.xd[a] = bt::dbits((double)xf[a]);
                 }
                 T.c0h = c0.h, T.c0l = c0.l, T.q0h = q0.h, T.q0l = q0.l, T.l0h = l0.h, T.l0l = l0.l;

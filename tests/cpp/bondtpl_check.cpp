@@ -41,7 +41,6 @@ struct Class {
 static void make_tpl(Tpl& T, const double xa[2], double l0t) {
     for (int a = 0; a < 2; a++) {
         T.xf[a] = (float)xa[a];
-        T.xf2[a] = 2.0f * T.xf[a];
         T.xd[a] = dbits((double)T.xf[a]);
     }
     // |xf|^2 and |xf|^2 - l0t^2 exactly in quad, then as pairs
@@ -63,7 +62,6 @@ static void make_tpl3(Tpl3& T, const double xa[3], double l0t) {
     q sq = 0;
     for (int a = 0; a < 3; a++) {
         T.xf[a] = (float)xa[a];
-        T.xf2[a] = 2.0f * T.xf[a];
         T.xd[a] = dbits((double)T.xf[a]);
         sq += (q)T.xf[a] * (q)T.xf[a];
     }
