@@ -870,9 +870,11 @@ def warm_measure(scale, K, smooth, n_plain=1, e2e=True, with_clocks=True):
             e2e_ms = (time.perf_counter() - t0) * 1e3 / K
     os.remove(snap)
     os.rmdir(snap_dir)
-    plain_ms = float(np.mean([s["ms"] for s in plain]))
-    skip_ms = float(np.sum([s["ms"] for s in skip]))
-    learned_ms = float(np.sum([s["ms"] for s in learned]))
+    # per increment: the prediction (features, network, smoothing, candidates),
+    # the solve and the history record (run_increments' ms_total)
+    plain_ms = float(np.mean([s["ms_total"] for s in plain]))
+    skip_ms = float(np.sum([s["ms_total"] for s in skip]))
+    learned_ms = float(np.sum([s["ms_total"] for s in learned]))
     flops = 2.0 * p.N_int * (16 * 128 + 2 * 128 * 128 + 128 * 16)
     peaks, peak_kind = measured_peaks()
     return {

@@ -483,6 +483,10 @@ int pd_save_kw(pd_ctx* ctx, double rad, const char* path, void* stream);
  * bit for bit. */
 int pd_snapshot_save(pd_ctx* ctx, const char* path, void* stream);
 int pd_snapshot_load(pd_ctx* ctx, const char* path, void* stream);
+/* Number of broken bonds (intact flag 0) over the whole family, counted on
+ * the device; the caller's copy is one integer.  No counterpart in the
+ * reference, whose drivers read the fail array back to the host. */
+int pd_count_broken(pd_ctx* ctx, int64_t* count, void* stream);
 /* Crack tip from the damage field: the interior node with the largest x among
  * those with dmg > threshold (lowest index among ties); tip_xy receives its
  * reference coordinates, NaN when no node is damaged.  The reference's tracker

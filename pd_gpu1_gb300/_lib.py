@@ -32,6 +32,7 @@ _SIGS = {
     "pd_get_field": (I32, [VP, I32, VP, SZ, VP]),
     "pd_set_field": (I32, [VP, I32, VP, SZ, VP]),
     "pd_field_ptr": (I32, [VP, I32, P(VP), P(SZ)]),
+    "pd_count_broken": (I32, [VP, P(I64), VP]),
     "pd_num_bonds": (I64, [VP]),
     "pd_sync": (I32, [VP, VP]),
     "pd_coord_plate": (I32, [VP, VP]),

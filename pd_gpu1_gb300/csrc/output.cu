@@ -16,6 +16,34 @@
 namespace pdg {
 namespace {
 
+// Broken bonds from the SELL intact bits: slots of the family (csr >= 0)
+// whose bit is clear; one warp per slice, one atomic per warp.
+__global__ void k_count_broken_bits(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
+                                    const int64_t* __restrict__ fbase, const int* __restrict__ csr,
+                                    const uint32_t* __restrict__ bits, unsigned long long* __restrict__ out) {
+    const int lane = threadIdx.x & 31;
+    for (int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; s < nslices;
+         s += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+        unsigned cnt = 0;
+        const int W = width[s];
+        for (int k = 0; k < W; k++) {
+            const bool valid = csr[base[s] + (int64_t)k * 32 + lane] >= 0;
+            const bool alive = (bits[fbase[s] + k] >> lane) & 1u;
+            cnt += __popc(__ballot_sync(0xffffffffu, valid && !alive));
+        }
+        if (lane == 0 && cnt) atomicAdd(out, (unsigned long long)cnt);
+    }
+}
+
+// Broken bonds from the CSR flags (fail == 0).
+__global__ void k_count_broken_csr(int64_t B, const int* __restrict__ fail, unsigned long long* __restrict__ out) {
+    unsigned cnt = 0;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < B; q += (int64_t)gridDim.x * blockDim.x)
+        cnt += fail[q] == 0;
+    for (int off = 16; off > 0; off >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, off);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(out, (unsigned long long)cnt);
+}
+
 // std::ostream << double with the default format: %g with precision 6.
 void put(FILE* f, double v) { std::fprintf(f, "%g", v); }
 
@@ -221,6 +249,32 @@ int pd_snapshot_load(pd_ctx* c, const char* path, void* stream) {
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     c->pos_valid = false;
     return cuda_err(c, e, "pd_snapshot_load");
+}
+
+int pd_count_broken(pd_ctx* c, int64_t* count, void* stream) {
+    if (!c || !count) return PD_ERR_ARG;
+    *count = 0;
+    if (!c->family || c->B == 0) return PD_OK;
+    cudaStream_t s = st(stream);
+    unsigned long long* w = reinterpret_cast<unsigned long long*>(c->partials);
+    cudaError_t e = cudaMemsetAsync(w, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return cuda_err(c, e, "pd_count_broken");
+    const Sell& S = c->sell;
+    if (c->bits_current && S.bits) {
+        const unsigned g = (unsigned)std::max<int64_t>(
+            1, std::min<int64_t>((S.nslices * 32 + 255) / 256, (int64_t)c->num_sms * 16));
+        k_count_broken_bits<<<g, 256, 0, s>>>(S.nslices, S.width, S.base, S.fbase, S.csr, S.bits, w);
+    } else {
+        const unsigned g = (unsigned)std::max<int64_t>(1, std::min<int64_t>((c->B + 255) / 256, (int64_t)c->num_sms * 16));
+        k_count_broken_csr<<<g, 256, 0, s>>>(c->B, c->fail, w);
+    }
+    c->launches++;
+    unsigned long long out = 0;
+    e = cudaMemcpyAsync(&out, w, sizeof(out), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_err(c, e, "pd_count_broken");
+    *count = (int64_t)out;
+    return PD_OK;
 }
 
 int pd_crack_tip(pd_ctx* c, double threshold, double* tip_xy, void* stream) {

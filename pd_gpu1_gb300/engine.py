@@ -106,6 +106,27 @@ class Engine:
         self._c(self._lib.pd_field_ptr(self.ctx, FIELD[name], C.byref(ptr), C.byref(n)), "pd_field_ptr")
         return ptr.value, n.value
 
+    def count_broken(self):
+        """Broken bonds over the whole family (pd_count_broken: counted on the
+        device, one integer copied back)."""
+        v = C.c_int64()
+        self._c(self._lib.pd_count_broken(self.ctx, C.byref(v), self.stream), "pd_count_broken")
+        return v.value
+
+    def device_view(self, name, count=None):
+        """A torch tensor on the field's device memory (no copy); count
+        elements from the start (all by default)."""
+        import torch
+
+        ptr, n = self.device_ptr(name)
+        n = n if count is None else count
+        dt = {np.dtype(np.float64): "<f8", np.dtype(np.int32): "<i4"}[np.dtype(FIELD_DTYPE[name])]
+
+        class _View:
+            __cuda_array_interface__ = {"shape": (n,), "typestr": dt, "data": (ptr, False), "version": 2}
+
+        return torch.as_tensor(_View(), device="cuda")
+
     @property
     def num_bonds(self):
         return self._lib.pd_num_bonds(self.ctx)

@@ -135,102 +135,124 @@ def run_increments(eng, meta, n_inc, mode="plain", net=None, collect=None, tol=1
     (pd_warm_record).  smooth: passes of family averaging applied to the
     network's correction (pd_warm_predict).  collect: a list that receives
     (features, targets) device tensors of a random ``keep`` fraction of the
-    free nodes of every increment with U > 0, crack advances included.
+    free nodes of every increment with U > 0 and no crack advance.
     record=False leaves the context's history as it was (a comparison run
     from a snapshot that another run continues from); last: a dict that
-    receives the state before the last increment (u0, d0, U), from which
-    restore_history rebuilds that increment's history after a snapshot load.
-    Returns the per-increment statistics of pd_load_step."""
+    receives the state before the last increment (u0, d0, U: device tensors
+    and a float), from which restore_history rebuilds that increment's
+    history after a snapshot load.
+    Returns the per-increment statistics of pd_load_step, with "start" (the
+    start used), "advanced" (bonds broken in the increment) and "ms_total"
+    (wall time of the prediction, the solve and the history record; the
+    bookkeeping copies of this function are outside it)."""
     import torch
 
     L = lib()
-    p = eng.p
-    ni = p.N_int
+    ni = eng.p.N_int
     delta = meta["delta"]
     rng = np.random.default_rng(seed)
     du = torch.zeros(4 * ni, dtype=torch.float64, device="cuda")  # two candidates
     X = torch.zeros((ni, 16), dtype=torch.bfloat16, device="cuda") if collect is not None else None
+    ux, uy, dmg = eng.device_view("UX", ni), eng.device_view("UY", ni), eng.device_view("DMG", ni)
+    u0 = torch.empty(2 * ni, dtype=torch.float64, device="cuda")
+    d0 = torch.empty(ni, dtype=torch.float64, device="cuda")
     prev = None
-    hist = getattr(eng, "warm_history", None)  # the context's recorded departure (host copy), None: no history
     out = []
     for k in range(start, start + n_inc):
         U = k * delta  # accumulated boundary displacement before this increment
         ptr = None
         eng.damage()
-        u0 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
-        d0 = eng.get("DMG")[:ni].copy()
+        eng.sync()
+        # the state before the increment, kept on the device
+        u0[:ni].copy_(ux)
+        u0[ni:].copy_(uy)
+        d0.copy_(dmg)
         if U > 0.0 and collect is not None:
             check(L.pd_warm_features(eng.ctx, U, delta, X.data_ptr(), eng.stream), eng.ctx, "pd_warm_features")
+        broken0 = eng.count_broken()
+        hist_set = getattr(eng, "has_history", False)
+        hist = getattr(eng, "warm_history", None) if collect is not None else None
+        torch.cuda.synchronize()
         t0 = time.perf_counter()
         ncand = 1
-        broken0 = int((eng.get("FAIL") == 0).sum())
         if mode in ("learned", "network", "secant") and U > 0.0:
             check(L.pd_warm_predict(eng.ctx, net.h, U, delta, smooth, du.data_ptr(), eng.stream), eng.ctx,
                   "pd_warm_predict")
             ptr = du.data_ptr()  # "network": the network's start against the plain start
             if mode == "learned":  # both candidates
                 ncand = 2
-            if mode == "secant" or (mode == "learned" and hist is None and record):
+            if mode == "secant" or (mode == "learned" and not hist_set and record):
                 # the skip term alone; the learned start too when there is no
                 # history (the first increments, and the one after a crack advance)
                 ptr = du.data_ptr() + 2 * ni * 8
                 ncand = 1
         elif mode == "extrapolate" and prev is not None:
-            du[: 2 * ni].copy_(torch.from_numpy(prev))
+            du[: 2 * ni].copy_(prev)
             ptr = du.data_ptr()
         offered = ("plain",) if ptr is None else ("network", "skip") if ncand == 2 else \
             ("skip",) if (mode == "secant" or ptr != du.data_ptr()) else (mode,)
         st = eng.load_step(delta, ptr, tol, max_iters, check_every, ncand, probe if ncand > 1 else 0)
+        advanced = eng.count_broken() - broken0  # bonds broken in the increment
+        # this increment is the history of the next prediction, unless the crack
+        # advanced in it (its departure is that jump, which the next increment does
+        # not repeat) or it has no proportional reference (U = 0)
+        recordable = U > 0.0 and advanced == 0
+        if record:
+            if recordable:
+                record_history(eng, U, delta, u0, d0, host=collect is not None)
+            else:
+                clear_history(eng, delta)
+        eng.sync()
+        st["ms_total"] = (time.perf_counter() - t0) * 1e3
         st["start"] = "plain" if st["warm_used"] == 0 else offered[st["warm_used"] - 1]
-        st["wall_ms"] = (time.perf_counter() - t0) * 1e3
         st["increment"] = k
-        st["advanced"] = int((eng.get("FAIL") == 0).sum()) - broken0  # bonds broken in the increment
-        u1 = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
+        st["advanced"] = advanced
+        u1 = torch.cat([ux, uy])
         prev = u1 - u0
-        tt = (prev - u0 * (delta / U)) / U if U > 0.0 else None  # departure from proportionality per unit load
-        if tt is not None and collect is not None and st["advanced"] == 0:
-            # target: the change of the departure from the recorded history (the
-            # network corrects the history term); increments in which the crack
-            # advanced are left out (their jump is not predictable from the state)
+        if collect is not None and U > 0.0 and advanced == 0:
+            # target: the change of the departure from proportionality from the
+            # recorded history (the network corrects the history term); increments
+            # in which the crack advanced are left out (their jump is not
+            # predictable from the state)
+            tt = ((prev - u0 * (delta / U)) / U).cpu().numpy()
             dt = tt - hist if hist is not None else tt
             st["max_target"] = float(np.abs(dt).max())
             idx = np.sort(rng.choice(ni, max(1, int(keep * ni)), replace=False))
             t = np.stack([dt[idx], dt[ni + idx]], axis=1).astype(np.float32)
             ii = torch.from_numpy(idx).cuda()
             collect.append((X.index_select(0, ii).clone(), torch.from_numpy(t).cuda()))
-        # this increment is the history of the next prediction, unless the crack
-        # advanced in it (its departure is that jump, which the next increment does
-        # not repeat) or it has no proportional reference (U = 0)
-        if record:
-            if tt is not None and st["advanced"] == 0:
-                record_history(eng, U, delta, u0, d0)
-            else:
-                clear_history(eng, delta)
-            hist = eng.warm_history
         if last is not None:
-            last.update(u0=u0, d0=d0, U=U if (tt is not None and st["advanced"] == 0) else 0.0)
+            last.update(u0=u0.clone(), d0=d0.clone(), U=U if recordable else 0.0)
         out.append(st)
     return out
 
 
-def record_history(eng, U_prev, delta, u_prev, dmg_prev):
-    """pd_warm_record from host arrays: the increment that led from (u_prev,
-    dmg_prev) at accumulated boundary displacement U_prev to the context's
-    current state.  A host copy of the recorded departure stays on the engine
-    (``warm_history``)."""
+def record_history(eng, U_prev, delta, u_prev, dmg_prev, host=False):
+    """pd_warm_record: the increment that led from (u_prev, dmg_prev) at
+    accumulated boundary displacement U_prev to the context's current state
+    (u_prev, dmg_prev: device tensors, or host arrays that are uploaded).
+    host=True also keeps a host copy of the recorded departure on the engine
+    (``warm_history``, for training targets)."""
     import torch
 
-    up = torch.from_numpy(np.ascontiguousarray(u_prev, dtype=np.float64)).cuda()
-    dp = torch.from_numpy(np.ascontiguousarray(dmg_prev, dtype=np.float64)).cuda()
+    up = u_prev if torch.is_tensor(u_prev) else torch.from_numpy(np.ascontiguousarray(u_prev, np.float64)).cuda()
+    dp = dmg_prev if torch.is_tensor(dmg_prev) else \
+        torch.from_numpy(np.ascontiguousarray(dmg_prev, np.float64)).cuda()
     check(lib().pd_warm_record(eng.ctx, U_prev, delta, up.data_ptr(), dp.data_ptr(), eng.stream), eng.ctx,
           "pd_warm_record")
-    ni = eng.p.N_int
-    u = np.concatenate([eng.get("UX")[:ni], eng.get("UY")[:ni]])
-    eng.warm_history = ((u - u_prev) - u_prev * (delta / U_prev)) / U_prev
+    eng.has_history = True
+    if host:
+        eng.sync()
+        ni = eng.p.N_int
+        u = torch.cat([eng.device_view("UX", ni), eng.device_view("UY", ni)])
+        eng.warm_history = (((u - up) - up * (delta / U_prev)) / U_prev).cpu().numpy()
+    else:
+        eng.warm_history = None
 
 
 def clear_history(eng, delta):
     check(lib().pd_warm_record(eng.ctx, 0.0, delta, None, None, eng.stream), eng.ctx, "pd_warm_record")
+    eng.has_history = False
     eng.warm_history = None
 
 
