@@ -756,3 +756,23 @@ def test_compact_3d_bond_matches_records(E):
     assert_close_norm(a[5], rec[5], 1e-11, "uz after 30 steps")
     np.testing.assert_array_equal(a[6], rec[6])
     assert a[7] == pytest.approx(rec[7], rel=1e-12)
+
+
+def test_count_broken_matches_the_flags(E):
+    """pd_count_broken (counted on the device from the intact bits) equals
+    the number of zero intact flags, on the cracked crack-grow plate before
+    and after a force pass that breaks bonds."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_crack_grow(scale=0.2, nt=20)
+    with E.Engine(p) as eng:
+        setup(eng)
+        n0 = eng.count_broken()
+        assert n0 == int((eng.get("FAIL") == 0).sum()) > 0  # the pre-crack
+        rng = np.random.default_rng(21)
+        eng.set("UX", rng.standard_normal(p.N) * 2.5e-6)
+        eng.set("UY", rng.standard_normal(p.N) * 2.5e-6)
+        eng.state_force_gpu()
+        n = eng.count_broken()
+        assert n == int((eng.get("FAIL") == 0).sum())
+        assert n > n0  # bonds broke
