@@ -227,6 +227,21 @@ __global__ void __launch_bounds__(kThreads) k_gemm(GemmArgs g) {
                 : "r"(taddr));
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (m >= g.M) continue;
+            if (g.epi == E_GELU && !g.Z && n0 + c0 + 16 <= g.N && (g.ldh & 7) == 0) {
+                // inference: the row's 16 activations as BF16 in two 16-byte stores
+                // (the pre-activation is kept only for the backward pass)
+                uint32_t h[8];
+                for (int j = 0; j < 8; j++) {
+                    const float z0 = __uint_as_float(v[2 * j]) + g.bias[n0 + c0 + 2 * j];
+                    const float z1 = __uint_as_float(v[2 * j + 1]) + g.bias[n0 + c0 + 2 * j + 1];
+                    const __nv_bfloat162 b2 = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+                    h[j] = *reinterpret_cast<const uint32_t*>(&b2);
+                }
+                uint4* dst = reinterpret_cast<uint4*>(g.H + m * g.ldh + n0 + c0);
+                dst[0] = make_uint4(h[0], h[1], h[2], h[3]);
+                dst[1] = make_uint4(h[4], h[5], h[6], h[7]);
+                continue;
+            }
             for (int j = 0; j < 16; j++) {
                 const int64_t n = n0 + c0 + j;
                 if (n >= g.N) break;
@@ -240,7 +255,7 @@ __global__ void __launch_bounds__(kThreads) k_gemm(GemmArgs g) {
                         break;
                     case E_GELU: {
                         const float z = d + g.bias[n];
-                        g.Z[m * g.ldh + n] = z;
+                        if (g.Z) g.Z[m * g.ldh + n] = z;
                         g.H[m * g.ldh + n] = __float2bfloat16_rn(gelu(z));
                         break;
                     }
@@ -538,17 +553,18 @@ GemmArgs gemm(const __nv_bfloat16* A, int64_t sam, int64_t sak, const __nv_bfloa
     return a;
 }
 
-// forward over M rows of X (BF16 [M][16]); Y (FP32 [M][16]) receives the outputs
-int forward(pd_mlp* n, const __nv_bfloat16* X, int64_t M, cudaStream_t s) {
+// forward over M rows of X (BF16 [M][16]); Y (FP32 [M][16]) receives the outputs;
+// keep_z: store the pre-activations for a backward pass
+int forward(pd_mlp* n, const __nv_bfloat16* X, int64_t M, cudaStream_t s, bool keep_z = true) {
     int rc;
     GemmArgs a = gemm(X, kInPad, 1, n->W1, kInPad, 1, M, kHid, kInPad);
-    a.epi = E_GELU, a.bias = n->b1, a.Z = n->Z1, a.H = n->H1, a.ldh = kHid;
+    a.epi = E_GELU, a.bias = n->b1, a.Z = keep_z ? n->Z1 : nullptr, a.H = n->H1, a.ldh = kHid;
     if ((rc = launch_gemm(n, a, 128, s))) return rc;
     a = gemm(n->H1, kHid, 1, n->W2, kHid, 1, M, kHid, kHid);
-    a.epi = E_GELU, a.bias = n->b2, a.Z = n->Z2, a.H = n->H2, a.ldh = kHid;
+    a.epi = E_GELU, a.bias = n->b2, a.Z = keep_z ? n->Z2 : nullptr, a.H = n->H2, a.ldh = kHid;
     if ((rc = launch_gemm(n, a, 128, s))) return rc;
     a = gemm(n->H2, kHid, 1, n->W3, kHid, 1, M, kHid, kHid);
-    a.epi = E_GELU, a.bias = n->b3, a.Z = n->Z3, a.H = n->H3, a.ldh = kHid;
+    a.epi = E_GELU, a.bias = n->b3, a.Z = keep_z ? n->Z3 : nullptr, a.H = n->H3, a.ldh = kHid;
     if ((rc = launch_gemm(n, a, 128, s))) return rc;
     a = gemm(n->H3, kHid, 1, n->W4, kHid, 1, M, kOutPad, kHid);
     a.epi = E_F32, a.bias = n->b4, a.D = n->Y, a.ldd = kOutPad;
@@ -698,7 +714,7 @@ int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* 
     cudaStream_t s = st(stream);
     for (int64_t r0 = 0; r0 < M; r0 += n->max_rows) {
         const int64_t m = std::min<int64_t>(n->max_rows, M - r0);
-        int rc = forward(n, reinterpret_cast<const __nv_bfloat16*>(dev_x) + r0 * kInPad, m, s);
+        int rc = forward(n, reinterpret_cast<const __nv_bfloat16*>(dev_x) + r0 * kInPad, m, s, false);
         if (rc) return rc;
         if (cudaMemcpy2DAsync(dev_y + r0 * kOut, kOut * sizeof(float), n->Y, kOutPad * sizeof(float),
                               kOut * sizeof(float), m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
