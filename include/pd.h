@@ -288,8 +288,14 @@ int pd_mlp_num_params(void);
 /* set (also resets the Adam state) / get the FP32 master parameters */
 int pd_mlp_set_params(pd_mlp* net, const float* host, int64_t count);
 int pd_mlp_get_params(pd_mlp* net, float* host, int64_t count);
-/* y[M][2] = net(x[M][16]) (device pointers; any M, processed in max_rows blocks) */
+/* y[M][2] = net(x[M][16]) (device pointers, x 16-byte and y 8-byte aligned;
+ * any M): one persistent kernel runs the four layers per 128-row tile with
+ * the weights resident in shared memory and the activations kept on chip. */
 int pd_mlp_forward(pd_mlp* net, const void* dev_x, int64_t M, float* dev_y, void* stream);
+/* The same forward pass layer by layer (one tensor-core product per layer
+ * over max_rows blocks, activations through device memory): a check of
+ * pd_mlp_forward, whose outputs it equals bit for bit. */
+int pd_mlp_forward_layers(pd_mlp* net, const void* dev_x, int64_t M, float* dev_y, void* stream);
 /* Gradient of loss = sum over rows and outputs of (y - t)^2 / (2 M), t[M][2] on
  * the device, M <= max_rows; flat gradient to host_grad (may be NULL). */
 int pd_mlp_grad(pd_mlp* net, const void* dev_x, const float* dev_t, int64_t M, float* host_grad, float* loss,

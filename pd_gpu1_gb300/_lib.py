@@ -72,6 +72,7 @@ _SIGS = {
     "pd_mlp_set_params": (I32, [VP, VP, I64]),
     "pd_mlp_get_params": (I32, [VP, VP, I64]),
     "pd_mlp_forward": (I32, [VP, VP, I64, VP, VP]),
+    "pd_mlp_forward_layers": (I32, [VP, VP, I64, VP, VP]),
     "pd_mlp_grad": (I32, [VP, VP, VP, I64, VP, P(C.c_float), VP]),
     "pd_mlp_train_step": (I32, [VP, VP, VP, I64, C.c_float, P(C.c_float), VP]),
     "pd_mlp_gemm": (I32, [VP, VP, I64, I64, I64, VP, I32, VP]),

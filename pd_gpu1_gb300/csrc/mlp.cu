@@ -443,6 +443,171 @@ __global__ void k_combine(int64_t n, const double* __restrict__ corr, double U, 
     }
 }
 
+// ---- fused forward pass (inference) ------------------------------------------
+//
+// All four layers per 128-row tile in one persistent kernel: the BF16
+// weights stay in shared memory in the canonical K-major layout (staged once
+// per CTA), each layer's product goes to the same 128 TMEM columns, and its
+// epilogue (bias, GELU, BF16) writes the activations back into shared memory
+// as the next product's A operand, so activations never leave the SM.  The
+// products, their order of K steps and the epilogue arithmetic are those of
+// k_gemm, so the outputs equal the layer-by-layer pass bit for bit.
+// Shared memory: W1 4 KB (K = 16, core-matrix groups 256 B apart), W2 and W3
+// 32 KB each, W4 4 KB, the activation tile 32 KB (two 64-wide K chunks; the
+// input tile uses chunk 0) and the biases: 106 KB, two CTAs per SM.
+constexpr int kFusedSmem = 4096 + 2 * 32768 + 4096 + 32768 + 2048;  // + the biases (1,600 bytes)
+
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+        "l"(da), "l"(db), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t v[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+          "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+struct FusedArgs {
+    const __nv_bfloat16* X;  // [M][16]
+    int64_t M;
+    const __nv_bfloat16 *W1, *W2, *W3, *W4;
+    const float *b1, *b2, *b3, *b4;
+    float* Y;  // [M][2]
+    int* err;
+    long long spin_limit;
+};
+
+__global__ void __launch_bounds__(kThreads) k_mlp_fused(FusedArgs g) {
+    extern __shared__ __align__(1024) unsigned char fsm[];
+    unsigned char* sW1 = fsm;                  // 128 x 16, groups 256 B apart
+    unsigned char* sW2 = sW1 + 4096;           // 2 chunks x 16 KB
+    unsigned char* sW3 = sW2 + 32768;          // 2 chunks x 16 KB
+    unsigned char* sW4 = sW3 + 32768;          // 2 chunks x 2 KB (16 rows)
+    unsigned char* sH = sW4 + 4096;            // 2 chunks x 16 KB
+    float* sb = reinterpret_cast<float*>(sH + 32768);  // b1, b2, b3 (128 each), b4 (16)
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int failed;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t bar_a = smem_addr(&bar);
+
+    if (threadIdx.x == 0) {
+        failed = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_slot)),
+                     "r"(128)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    // weights and biases, once per CTA
+    for (int i = threadIdx.x; i < kHid * 2; i += kThreads) {  // W1: 16-byte vectors (row, half)
+        const int r = i >> 1, h = i & 1;
+        *reinterpret_cast<uint4*>(sW1 + (r >> 3) * 256 + h * 128 + (r & 7) * 16) =
+            *reinterpret_cast<const uint4*>(g.W1 + r * kInPad + h * 8);
+    }
+    for (int c = 0; c < 2; c++) {
+        load_tile(sW2 + c * 16384, g.W2, kHid, 1, 0, kHid, kHid, c * kChunkK, kHid);
+        load_tile(sW3 + c * 16384, g.W3, kHid, 1, 0, kHid, kHid, c * kChunkK, kHid);
+        load_tile(sW4 + c * 2048, g.W4, kHid, 1, 0, kOutPad, kOutPad, c * kChunkK, kHid);
+    }
+    for (int i = threadIdx.x; i < kHid; i += kThreads) {
+        sb[i] = g.b1[i];
+        sb[kHid + i] = g.b2[i];
+        sb[2 * kHid + i] = g.b3[i];
+        if (i < kOutPad) sb[3 * kHid + i] = g.b4[i];
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = tmem_slot;
+    const uint32_t a0 = smem_addr(sH), w1 = smem_addr(sW1), w2 = smem_addr(sW2), w3 = smem_addr(sW3),
+                   w4 = smem_addr(sW4);
+    constexpr uint32_t kIdH = make_idesc(kTileM, kHid), kIdO = make_idesc(kTileM, kOutPad);
+    uint32_t phase = 0;
+    const int64_t ntiles = (g.M + kTileM - 1) / kTileM;
+    const int r = 32 * warp + lane;  // this thread's row of the tile
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t m = tile * kTileM + r;
+        // input row -> chunk 0 of the activation tile (K = 16)
+        uint4 x0 = make_uint4(0, 0, 0, 0), x1 = x0;
+        if (m < g.M) {
+            x0 = *reinterpret_cast<const uint4*>(g.X + m * kInPad);
+            x1 = *reinterpret_cast<const uint4*>(g.X + m * kInPad + 8);
+        }
+        *reinterpret_cast<uint4*>(sH + tile_off(r, 0)) = x0;
+        *reinterpret_cast<uint4*>(sH + tile_off(r, 8)) = x1;
+        for (int layer = 0; layer < 4; layer++) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                if (layer == 0) {
+                    mma_f16(tmem, make_desc(a0, 128, 1024), make_desc(w1, 128, 256), kIdH, 0u);
+                } else {
+                    const uint32_t wb = layer == 1 ? w2 : layer == 2 ? w3 : w4;
+                    const uint32_t wchunk = layer == 3 ? 2048 : 16384;
+                    for (int c = 0; c < 2; c++)
+                        for (int j = 0; j < kChunkK / 16; j++)
+                            mma_f16(tmem, make_desc(a0 + c * 16384 + j * 256, 128, 1024),
+                                    make_desc(wb + c * wchunk + j * 256, 128, 1024), layer == 3 ? kIdO : kIdH,
+                                    (c > 0 || j > 0) ? 1u : 0u);
+                }
+                asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                 bar_a)
+                             : "memory");
+            }
+            if (!mbar_wait(bar_a, phase, g.spin_limit)) failed = 1;
+            phase ^= 1;
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (failed) break;
+            const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+            if (layer < 3) {
+                // bias, GELU, BF16 -> the next product's A operand
+                const float* bias = sb + layer * kHid;
+                for (int c0 = 0; c0 < kHid; c0 += 16) {
+                    uint32_t v[16];
+                    tmem_ld16(trow + (uint32_t)c0, v);
+                    uint32_t h[8];
+                    for (int jj = 0; jj < 8; jj++) {
+                        const float z0 = __uint_as_float(v[2 * jj]) + bias[c0 + 2 * jj];
+                        const float z1 = __uint_as_float(v[2 * jj + 1]) + bias[c0 + 2 * jj + 1];
+                        const __nv_bfloat162 b2 = __floats2bfloat162_rn(gelu(z0), gelu(z1));
+                        h[jj] = *reinterpret_cast<const uint32_t*>(&b2);
+                    }
+                    unsigned char* chunk = sH + (c0 / kChunkK) * 16384;
+                    *reinterpret_cast<uint4*>(chunk + tile_off(r, c0 % kChunkK)) = make_uint4(h[0], h[1], h[2], h[3]);
+                    *reinterpret_cast<uint4*>(chunk + tile_off(r, c0 % kChunkK + 8)) =
+                        make_uint4(h[4], h[5], h[6], h[7]);
+                }
+            } else {
+                uint32_t v[16];
+                tmem_ld16(trow, v);
+                if (m < g.M)
+                    *reinterpret_cast<float2*>(g.Y + m * kOut) =
+                        make_float2(__uint_as_float(v[0]) + sb[3 * kHid], __uint_as_float(v[1]) + sb[3 * kHid + 1]);
+            }
+        }
+        if (failed) break;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");
+    if (threadIdx.x == 0 && failed) atomicExch(g.err, 1);
+}
+
 }  // namespace mlp
 }  // namespace pdg
 
@@ -709,7 +874,7 @@ int pd_mlp_get_params(pd_mlp* n, float* host, int64_t count) {
                                                                                                  : PD_ERR_CUDA;
 }
 
-int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* stream) {
+int pd_mlp_forward_layers(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* stream) {
     if (!n || !dev_x || !dev_y || M < 1) return PD_ERR_ARG;
     cudaStream_t s = st(stream);
     for (int64_t r0 = 0; r0 < M; r0 += n->max_rows) {
@@ -720,6 +885,37 @@ int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* 
                               kOut * sizeof(float), m, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
             return PD_ERR_CUDA;
     }
+    int herr = 0;
+    cudaMemcpyAsync(&herr, n->err, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) return PD_ERR_CUDA;
+    return herr ? PD_ERR_TIMEOUT : PD_OK;
+}
+
+int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* stream) {
+    if (!n || !dev_x || !dev_y || M < 1) return PD_ERR_ARG;
+    if ((reinterpret_cast<uintptr_t>(dev_x) & 15) || (reinterpret_cast<uintptr_t>(dev_y) & 7)) return PD_ERR_ARG;
+    cudaStream_t s = st(stream);
+    // the fused pass: two CTAs per SM, persistent over the 128-row tiles
+    static int configured = 0;
+    if (!configured) {
+        if (cudaFuncSetAttribute((const void*)k_mlp_fused, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kFusedSmem) != cudaSuccess)
+            return PD_ERR_CUDA;
+        configured = 1;
+    }
+    int dev = 0, sms = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const int64_t ntiles = (M + kTileM - 1) / kTileM;
+    FusedArgs a;
+    a.X = reinterpret_cast<const __nv_bfloat16*>(dev_x), a.M = M;
+    a.W1 = n->W1, a.W2 = n->W2, a.W3 = n->W3, a.W4 = n->W4;
+    a.b1 = n->b1, a.b2 = n->b2, a.b3 = n->b3, a.b4 = n->b4;
+    a.Y = dev_y, a.err = n->err, a.spin_limit = kSpinLimit;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, 2 * (int64_t)sms));
+    k_mlp_fused<<<grid, kThreads, kFusedSmem, s>>>(a);
+    n->launches++;
+    if (cudaGetLastError() != cudaSuccess) return PD_ERR_CUDA;
     int herr = 0;
     cudaMemcpyAsync(&herr, n->err, sizeof(int), cudaMemcpyDeviceToHost, s);
     if (cudaStreamSynchronize(s) != cudaSuccess) return PD_ERR_CUDA;
