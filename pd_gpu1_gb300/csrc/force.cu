@@ -117,7 +117,8 @@ struct ForceArgs {
     // 3-D state-based compact layout (srec8 and stpl as above)
     const bt::Tpl3* tpl3;     // 3-D class templates
     const int4* sk;           // dilatation pass: kx, ky, kz, flags
-    const int2* skz;          // force pass: kz, flags
+    float4* e4;               // per slot: e and the exact z offset of the dilatation-order bond vector
+    const uint32_t* bbits;    // per (slice, slot): "may break" bits
 };
 
 namespace {
@@ -1576,7 +1577,8 @@ __global__ void __launch_bounds__(kForceBlock, 5) k_theta_compact3(const ForceAr
                 bt::f2 eta[3], w[3], y, e;
                 offsets_n<3>(T, d, eta);
                 bt::stretch3(eta, T, dl, w, y, e);
-                A.e[b + (int64_t)k * 32 + lane] = make_float2(e.h, e.l);
+                // e for T and the exact z offset for the force pass's length
+                A.e4[b + (int64_t)k * 32 + lane] = make_float4(e.h, e.l, eta[2].h, eta[2].l);
                 const float4 ct = __ldg(reinterpret_cast<const float4*>(A.stpl + id) + 1);
                 const bt::f2 cth{ct.x, fmaf(ct.x, ct.z * dl, ct.y)};
                 acc = bt::add(acc, bt::mul(cth, e));
@@ -1626,6 +1628,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
         const int W = A.width[s];
         const int64_t b = A.base[s];
         uint32_t* wbits = A.bits + A.fbase[s];
+        const uint32_t* bbits = A.bbits + A.fbase[s];
         const int iters = (W + Q - 1) / Q;
         for (int i = 0; i < iters; i++) {
             const int k = i * Q + ph;
@@ -1635,20 +1638,22 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
             bool brk = false;
             if (alive) {
                 const int2 rq = __ldg(A.srec8 + slot);
-                const int2 kz = __ldg(A.skz + slot);
                 const int c = rq.x;
                 const uint32_t dlb = (uint32_t)rq.y;
                 const int id = (int)(dlb & 0xffu);
                 const bt::Tpl3& T = A.tpl3[id];
                 const float dl = __uint_as_float(dlb & ~0xffu);
-                const double za = __longlong_as_double((long long)T.xd[2] + kz.x);
-                // the length's components: x, y in the force order, z in the
-                // dilatation order; then the force order's z for the direction
+                // the length's components: x, y in the force order; z in the
+                // dilatation order, whose exact offset the dilatation pass kept
+                // (the same FP64 expression on the same values); then the force
+                // order's z for the direction
+                const float4 ez = A.e4[slot];
                 const double2 pxy = __ldg(A.pc + c);
-                const double dlen[3] = {(pxy.x - xi) - uxi, (pxy.y - yi) - uyi, (za + __ldg(A.uz + c)) - uzi};
+                const double dlen[2] = {(pxy.x - xi) - uxi, (pxy.y - yi) - uyi};
                 const double dzf = (__ldg(A.pcz + c) - zi) - uzi;
                 bt::f2 eta[3], w[3], y, ef, etz;
-                offsets_n<3>(T, dlen, eta);
+                offsets_n<2>(T, dlen, eta);
+                eta[2] = bt::f2{ez.z, ez.w};
                 etz = offset1(dzf, T.xd[2]);
                 bt::stretch3(eta, T, dl, w, y, ef);
                 const bt::f2 sz = bt::two_sum(T.xf[2], etz.h);
@@ -1657,15 +1662,14 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
                 const float4 cc = __ldg(reinterpret_cast<const float4*>(A.stpl + id));
                 const float2 gg = __ldg(reinterpret_cast<const float2*>(A.stpl + id) + 3);
                 const bt::f2 c1{cc.x, fmaf(cc.x, gg.x * dl, cc.y)}, c2{cc.z, fmaf(cc.z, gg.y * dl, cc.w)};
-                const float2 ec = A.e[slot];
                 const float4 nc = __ldg(A.nab + c);
                 const bt::f2 Tt = bt::add(bt::mul(c1, bt::add(nai, bt::f2{nc.x, nc.y})),
-                                          bt::mul(bt::mul(c2, bt::f2{ec.x, ec.y}), bt::add(nbi, bt::f2{nc.z, nc.w})));
+                                          bt::mul(bt::mul(c2, bt::f2{ez.x, ez.y}), bt::add(nbi, bt::f2{nc.z, nc.w})));
                 const bt::f2 t = bt::mul(Tt, bt::f2{0.5f * y.h, 0.5f * y.l});
                 bt::acc_add(fxa, bt::mul(t, w[0]));
                 bt::acc_add(fya, bt::mul(t, w[1]));
                 bt::acc_add(fza, bt::mul(t, wz));
-                brk = (kz.y & 1) && bt::exceeds(ef, s0, s0f, T, dl);
+                brk = ((bbits[k] >> rl) & 1u) && bt::exceeds(ef, s0, s0f, T, dl);
             }
             const uint32_t broke = __ballot_sync(0xffffffffu, brk);
             if (broke && j == 0 && !A.nobreak) {
@@ -1834,7 +1838,8 @@ static ForceArgs make_args(pd_ctx* c) {
     A.stpl = S.stpl;
     A.tpl3 = S.tpl3;
     A.sk = S.sk;
-    A.skz = S.skz;
+    A.e4 = S.e4;
+    A.bbits = S.bbits;
     return A;
 }
 

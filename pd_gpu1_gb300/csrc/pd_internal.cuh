@@ -163,6 +163,12 @@ struct Sell {
     bt::Tpl3* tpl3 = nullptr;   // [ntpl]
     int4* sk = nullptr;         // [S]
     int2* skz = nullptr;        // [S]
+    // 3-D state-based compact layout: per slot the dilatation pass's
+    // extension and the exact offset of its z component (the length's z term
+    // of the force pass, Force_State.cu:272), both as float pairs; per
+    // (slice, slot) a word of "may break" bits
+    float4* e4 = nullptr;       // [S]
+    uint32_t* bbits = nullptr;  // [F]
 };
 
 // Layout of the bond-based force path (pd_set_force_layout).

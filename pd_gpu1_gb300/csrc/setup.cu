@@ -735,6 +735,21 @@ __global__ void k_state_compact3_fill(KParams P, int64_t nslices, const int* __r
     }
 }
 
+// The "may break" flags of the 3-D state-based records as one bit word per
+// (slice, slot), like the intact flags.
+__global__ void k_break_bits(int64_t nslices, const int* __restrict__ width, const int64_t* __restrict__ base,
+                             const int64_t* __restrict__ fbase, const int2* __restrict__ skz,
+                             uint32_t* __restrict__ bbits) {
+    const int64_t s = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (s >= nslices) return;
+    const int W = width[s];
+    for (int k = 0; k < W; k++) {
+        const uint32_t word = __ballot_sync(0xffffffffu, (skz[base[s] + (int64_t)k * 32 + lane].y & 1) != 0);
+        if (lane == 0) bbits[fbase[s] + k] = word;
+    }
+}
+
 // Every slot's coefficients against its class's moved to the slot's length
 // (c (1 + g dl)): *bad where one differs from the bond's own by more than
 // 2^-45 of it.
@@ -934,6 +949,8 @@ static void free_sell(Sell& S) {
     free_ptr(S.tpl3);
     free_ptr(S.sk);
     free_ptr(S.skz);
+    free_ptr(S.e4);
+    free_ptr(S.bbits);
     S.ntpl = 0;
     S.nslices = S.S = S.F = 0;
 }
@@ -980,6 +997,8 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         free_ptr(S.tpl3);
         free_ptr(S.sk);
         free_ptr(S.skz);
+        free_ptr(S.e4);
+        free_ptr(S.bbits);
         S.ntpl = 0;
     };
     if (cudaMallocAsync(&keys, tsize * 8, s) || cudaMallocAsync(&l0min, tsize * 8, s) ||
@@ -1088,7 +1107,9 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
     if (d3 && state)
         ok = !cudaMalloc(&S.tpl3, ntpl * sizeof(bt::Tpl3)) && !cudaMalloc(&S.srec8, nrec * sizeof(int2)) &&
              !cudaMalloc(&S.sk, nrec * sizeof(int4)) && !cudaMalloc(&S.skz, nrec * sizeof(int2)) &&
-             !cudaMalloc(&S.stpl, ntpl * sizeof(StateTpl));
+             !cudaMalloc(&S.stpl, ntpl * sizeof(StateTpl)) && !cudaMalloc(&S.e4, nrec * sizeof(float4)) &&
+             !cudaMemsetAsync(S.e4, 0, nrec * sizeof(float4), s) &&
+             !cudaMalloc(&S.bbits, (size_t)std::max<int64_t>(S.F, 1) * sizeof(uint32_t));
     else if (d3)
         ok = !cudaMalloc(&S.tpl3, ntpl * sizeof(bt::Tpl3)) && !cudaMalloc(&S.rec16, nrec * sizeof(bt::Rec));
     else if (state)
@@ -1134,6 +1155,9 @@ int build_compact(pd_ctx* c, cudaStream_t s) {
         k_state_compact3_fill<<<dim3(gx, gy), 256, 0, s>>>(
             P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->idist, c->fac,
             c->w, keys, ids, S.tpl3, S.sn_exp, S.sth_exp, S.st_exp, S.srec8, S.sk, S.skz, S.stpl, flags + 1);
+        k_break_bits<<<(unsigned)((S.nslices * 32 + 255) / 256), 256, 0, s>>>(S.nslices, S.width, S.base, S.fbase,
+                                                                                S.skz, S.bbits);
+        c->launches++;
     } else if (state) {
         k_state_compact_fill<<<dim3(gx, gy), 256, 0, s>>>(P, S.nslices, S.width, S.base, S.csr, c->NL, c->nf[PD_F_X],
                                                            c->nf[PD_F_Y], c->idist, c->fac, c->w, keys, ids, S.tpl,
