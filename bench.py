@@ -51,8 +51,9 @@ ALG_BYTES_PER_NODE_3D = 72.0
 # counted in the kernel source (csrc/force.cu): the bond vector's FP64
 # subtractions with the reference's roundings, two per component (bond_offset),
 # plus in the state-based passes the dilatation-order vector of the theta pass
-# (the 3-D force pass takes its length's z term from the theta pass).  Bonds within two float ulps of
-# their break threshold add one; per-node epilogue instructions are not counted.
+# (the 3-D force pass takes its length's z term from the theta pass).  Bonds
+# within two float ulps of their break threshold add one; per-node epilogue
+# instructions are not counted.
 FP64_EXEC_PER_BOND = {(1, 2): 4, (1, 3): 6, (2, 2): 8, (2, 3): 12}  # (model, dim), compact layouts
 # DRAM bytes per bond and per node of the step kernel: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one capture per workload (kernel, case, date below),
