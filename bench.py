@@ -66,7 +66,8 @@ TRAFFIC = {
     "kalthoff_winkler_3d_pmb_verlet": (17.5, 0.0, "k_bond_compact3<EPI_NONE>, full slab (the Verlet and contact "
                                                   "epilogue's node traffic not included), 2026-12-04"),
     "plate_crack_grow_2d_state_verlet": (42.5, 0.0, "k_theta_compact + k_state_compact<1>, full plate, 2026-12-04"),
-    "kalthoff_winkler_3d_state_verlet": (59.7, 0.0, "k_theta_compact3 + k_state_compact3<0>, full slab, 2026-12-04")}
+    "kalthoff_winkler_3d_state_verlet": (67.5, 0.0, "k_theta_compact3 + k_state_compact3<0> (z offset carried), full "
+                                                    "slab, 2026-12-04")}
 
 
 def layout_info(model, dim, layout, epi):
