@@ -154,9 +154,13 @@ int pd_find_neighbor(pd_ctx* ctx, void* stream);
 /* kernel_vol_Corr (Surf_Corr.cu:7-35): idist and fac per bond. */
 int pd_vol_corr(pd_ctx* ctx, void* stream);
 /* surface_correct_gpu (Surf_Corr.cu:235-310): vol_Corr + per-axis strain
- * energy factors fncst + per-bond scr, fused into two kernels. */
+ * energy factors fncst + per-bond scr, fused into two kernels (one family
+ * pass, then the coefficient pass, which needs both end nodes' fncst).  In a
+ * state-based context the family pass also writes w and m. */
 int pd_surface_correct(pd_ctx* ctx, void* stream);
-/* kernel_initial_weight_2D/3D (Force_State.cu:8-54): w per bond, m per node. */
+/* kernel_initial_weight_2D/3D (Force_State.cu:8-54): w per bond, m per node,
+ * in one family pass with vol_Corr's idist and fac (a preceding
+ * pd_vol_corr is not needed; after one the values are rewritten unchanged). */
 int pd_initial_weight(pd_ctx* ctx, void* stream);
 /* kernel_set_crack_2D (Base_Function.cu:39-81): cut bonds crossing a segment
  * of length clength centred at (loc_x, loc_y) at angle theta (radians). */

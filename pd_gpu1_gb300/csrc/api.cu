@@ -1259,8 +1259,7 @@ int pd_solve_plate_crack_grow(double dx, int nt, double* ux, double* uy, double*
     PD_TRY(pd_find_neighbor(c, nullptr));
     PD_TRY(pd_initial_state(c, nullptr));
     PD_TRY(pd_set_crack_2d(c, 0.01, 0.0, 0.0, 0.0, nullptr));
-    PD_TRY(pd_vol_corr(c, nullptr));
-    PD_TRY(pd_initial_weight(c, nullptr));
+    PD_TRY(pd_initial_weight(c, nullptr));  // with vol_Corr in one family pass
     PD_TRY(pd_prepare(c, nullptr));
     const double setup_ms = t.stop();
     PD_TRY(pd_run_explicit(c, nt, 20.0, 0, nullptr));

@@ -16,7 +16,9 @@
 //
 // Padding: the 8 inputs are padded to K = 16 and the 2 outputs to N = 16 with
 // zero weights; tiles are 128 rows (M) by 16 or 128 columns (N).
+#include <cuda.h>
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 
 #include <cmath>
 #include <cstring>
@@ -446,16 +448,26 @@ __global__ void k_combine(int64_t n, const double* __restrict__ corr, double U, 
 // ---- fused forward pass (inference) ------------------------------------------
 //
 // All four layers per 128-row tile in one persistent kernel: the BF16
-// weights stay in shared memory in the canonical K-major layout (staged once
-// per CTA), each layer's product goes to the same 128 TMEM columns, and its
-// epilogue (bias, GELU, BF16) writes the activations back into shared memory
-// as the next product's A operand, so activations never leave the SM.  The
-// products, their order of K steps and the epilogue arithmetic are those of
-// k_gemm, so the outputs equal the layer-by-layer pass bit for bit.
-// Shared memory: W1 4 KB (K = 16, core-matrix groups 256 B apart), W2 and W3
-// 32 KB each, W4 4 KB, the activation tile 32 KB (two 64-wide K chunks; the
-// input tile uses chunk 0) and the biases: 106 KB, two CTAs per SM.
-constexpr int kFusedSmem = 4096 + 2 * 32768 + 4096 + 32768 + 2048;  // + the biases (1,600 bytes)
+// weights stay in shared memory (loaded once per CTA by the tensor memory
+// accelerator), each layer's product goes to the same 128 TMEM columns, and
+// its epilogue (bias, GELU, BF16) writes the activations back into shared
+// memory as the next product's A operand, so activations never leave the SM.
+// The input tiles arrive by TMA as well, one tile ahead: the next tile's rows
+// are requested as soon as the first layer's product has read the current
+// ones, and land while layers 2-4 run.  The products, their order of K steps
+// and the epilogue arithmetic are those of k_gemm, so the outputs equal the
+// layer-by-layer pass bit for bit.
+//
+// TMA layout: every operand loaded by TMA comes in boxes of 8 columns (16
+// bytes) by all rows of the operand, so one box is a column of core matrices
+// (8 rows x 16 bytes each, 128 bytes apart: SBO = 128) and consecutive boxes
+// are the next 8 columns of K (LBO = rows x 16 bytes).  Every box starts at a
+// column that is a multiple of 8 BF16 elements (16 bytes).
+// Shared memory: W1 4 KB, W2 and W3 32 KB each, W4 4 KB, the activation tile
+// 32 KB (two 64-wide K chunks, written by the epilogues), the input tile 4 KB
+// and the biases: 110 KB, two CTAs per SM.
+constexpr int kFusedSmem = 4096 + 2 * 32768 + 4096 + 32768 + 4096 + 2048;  // + the biases (1,600 bytes)
+constexpr uint32_t kWeightBytes = 4096 + 2 * 32768 + 4096, kXBytes = 4096;
 
 __device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
     asm volatile(
@@ -475,33 +487,55 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t v[16]) {
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+// One 2-D tile (x = column, y = row) of a tensor map into shared memory;
+// completion is counted in bytes on the mbarrier.
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
 struct FusedArgs {
-    const __nv_bfloat16* X;  // [M][16]
+    CUtensorMap mX;   // [M][16] input rows, boxes of 8 columns x 128 rows
+    CUtensorMap mW1;  // [128][16], 8 x 128
+    CUtensorMap mW2;  // [128][128], 8 x 128
+    CUtensorMap mW3;  // [128][128], 8 x 128
+    CUtensorMap mW4;  // [16][128], 8 x 16
     int64_t M;
-    const __nv_bfloat16 *W1, *W2, *W3, *W4;
     const float *b1, *b2, *b3, *b4;
     float* Y;  // [M][2]
     int* err;
     long long spin_limit;
 };
 
-__global__ void __launch_bounds__(kThreads) k_mlp_fused(FusedArgs g) {
+__global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ FusedArgs g) {
     extern __shared__ __align__(1024) unsigned char fsm[];
-    unsigned char* sW1 = fsm;                  // 128 x 16, groups 256 B apart
-    unsigned char* sW2 = sW1 + 4096;           // 2 chunks x 16 KB
-    unsigned char* sW3 = sW2 + 32768;          // 2 chunks x 16 KB
-    unsigned char* sW4 = sW3 + 32768;          // 2 chunks x 2 KB (16 rows)
-    unsigned char* sH = sW4 + 4096;            // 2 chunks x 16 KB
-    float* sb = reinterpret_cast<float*>(sH + 32768);  // b1, b2, b3 (128 each), b4 (16)
-    __shared__ __align__(8) uint64_t bar;
+    unsigned char* sW1 = fsm;                  // 2 boxes x 2 KB (128 rows)
+    unsigned char* sW2 = sW1 + 4096;           // 16 boxes x 2 KB
+    unsigned char* sW3 = sW2 + 32768;          // 16 boxes x 2 KB
+    unsigned char* sW4 = sW3 + 32768;          // 16 boxes x 256 B (16 rows)
+    unsigned char* sH = sW4 + 4096;            // 2 chunks x 16 KB, K-major tiles (tile_off)
+    unsigned char* sX = sH + 32768;            // 2 boxes x 2 KB
+    float* sb = reinterpret_cast<float*>(sX + 4096);  // b1, b2, b3 (128 each), b4 (16)
+    __shared__ __align__(8) uint64_t bar, tbar;
     __shared__ uint32_t tmem_slot;
     __shared__ int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t bar_a = smem_addr(&bar);
+    const uint32_t bar_a = smem_addr(&bar), tbar_a = smem_addr(&tbar);
+    const uint32_t a0 = smem_addr(sH), x0 = smem_addr(sX), w1 = smem_addr(sW1), w2 = smem_addr(sW2),
+                   w3 = smem_addr(sW3), w4 = smem_addr(sW4);
+    const int64_t ntiles = (g.M + kTileM - 1) / kTileM;
 
     if (threadIdx.x == 0) {
         failed = 0;
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar_a) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tbar_a) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
@@ -510,16 +544,19 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(FusedArgs g) {
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-    // weights and biases, once per CTA
-    for (int i = threadIdx.x; i < kHid * 2; i += kThreads) {  // W1: 16-byte vectors (row, half)
-        const int r = i >> 1, h = i & 1;
-        *reinterpret_cast<uint4*>(sW1 + (r >> 3) * 256 + h * 128 + (r & 7) * 16) =
-            *reinterpret_cast<const uint4*>(g.W1 + r * kInPad + h * 8);
-    }
-    for (int c = 0; c < 2; c++) {
-        load_tile(sW2 + c * 16384, g.W2, kHid, 1, 0, kHid, kHid, c * kChunkK, kHid);
-        load_tile(sW3 + c * 16384, g.W3, kHid, 1, 0, kHid, kHid, c * kChunkK, kHid);
-        load_tile(sW4 + c * 2048, g.W4, kHid, 1, 0, kOutPad, kOutPad, c * kChunkK, kHid);
+    __syncthreads();
+    // the weights and the first input tile, by TMA (the grid never exceeds the tiles)
+    if (threadIdx.x == 0) {
+        mbar_expect_tx(tbar_a, kWeightBytes + kXBytes);
+        for (int b = 0; b < 2; b++) {
+            tma_load_2d(w1 + b * 2048, &g.mW1, 8 * b, 0, tbar_a);
+            tma_load_2d(x0 + b * 2048, &g.mX, 8 * b, (int)(blockIdx.x * kTileM), tbar_a);
+        }
+        for (int b = 0; b < 16; b++) {
+            tma_load_2d(w2 + b * 2048, &g.mW2, 8 * b, 0, tbar_a);
+            tma_load_2d(w3 + b * 2048, &g.mW3, 8 * b, 0, tbar_a);
+            tma_load_2d(w4 + b * 256, &g.mW4, 8 * b, 0, tbar_a);
+        }
     }
     for (int i = threadIdx.x; i < kHid; i += kThreads) {
         sb[i] = g.b1[i];
@@ -531,38 +568,38 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(FusedArgs g) {
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = tmem_slot;
-    const uint32_t a0 = smem_addr(sH), w1 = smem_addr(sW1), w2 = smem_addr(sW2), w3 = smem_addr(sW3),
-                   w4 = smem_addr(sW4);
     constexpr uint32_t kIdH = make_idesc(kTileM, kHid), kIdO = make_idesc(kTileM, kOutPad);
-    uint32_t phase = 0;
-    const int64_t ntiles = (g.M + kTileM - 1) / kTileM;
+    uint32_t phase = 0, tphase = 0;
+    bool pending = true;  // a TMA transaction on tbar not yet waited for (uniform across the CTA)
     const int r = 32 * warp + lane;  // this thread's row of the tile
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t m = tile * kTileM + r;
-        // input row -> chunk 0 of the activation tile (K = 16)
-        uint4 x0 = make_uint4(0, 0, 0, 0), x1 = x0;
-        if (m < g.M) {
-            x0 = *reinterpret_cast<const uint4*>(g.X + m * kInPad);
-            x1 = *reinterpret_cast<const uint4*>(g.X + m * kInPad + 8);
+        // this tile's input rows (and, on the first tile, the weights)
+        if (mbar_wait(tbar_a, tphase, g.spin_limit)) {
+            tphase ^= 1;
+            pending = false;
+        } else {
+            failed = 1;
         }
-        *reinterpret_cast<uint4*>(sH + tile_off(r, 0)) = x0;
-        *reinterpret_cast<uint4*>(sH + tile_off(r, 8)) = x1;
         for (int layer = 0; layer < 4; layer++) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             __syncthreads();
+            if (failed) break;
             if (threadIdx.x == 0) {
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
                 if (layer == 0) {
-                    mma_f16(tmem, make_desc(a0, 128, 1024), make_desc(w1, 128, 256), kIdH, 0u);
+                    mma_f16(tmem, make_desc(x0, 2048, 128), make_desc(w1, 2048, 128), kIdH, 0u);
                 } else {
-                    const uint32_t wb = layer == 1 ? w2 : layer == 2 ? w3 : w4;
-                    const uint32_t wchunk = layer == 3 ? 2048 : 16384;
                     for (int c = 0; c < 2; c++)
-                        for (int j = 0; j < kChunkK / 16; j++)
-                            mma_f16(tmem, make_desc(a0 + c * 16384 + j * 256, 128, 1024),
-                                    make_desc(wb + c * wchunk + j * 256, 128, 1024), layer == 3 ? kIdO : kIdH,
-                                    (c > 0 || j > 0) ? 1u : 0u);
+                        for (int j = 0; j < kChunkK / 16; j++) {
+                            const int kk = c * (kChunkK / 16) + j;  // K step of 16 columns = two boxes
+                            const uint64_t db = layer == 1   ? make_desc(w2 + kk * 4096, 2048, 128)
+                                                : layer == 2 ? make_desc(w3 + kk * 4096, 2048, 128)
+                                                             : make_desc(w4 + kk * 512, 256, 128);
+                            mma_f16(tmem, make_desc(a0 + c * 16384 + j * 256, 128, 1024), db,
+                                    layer == 3 ? kIdO : kIdH, (c > 0 || j > 0) ? 1u : 0u);
+                        }
                 }
                 asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                                  bar_a)
@@ -573,6 +610,15 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(FusedArgs g) {
             __syncthreads();
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
             if (failed) break;
+            if (layer == 0 && tile + gridDim.x < ntiles) {
+                // the first product has read the input tile: request the next one
+                if (threadIdx.x == 0) {
+                    mbar_expect_tx(tbar_a, kXBytes);
+                    for (int b = 0; b < 2; b++)
+                        tma_load_2d(x0 + b * 2048, &g.mX, 8 * b, (int)((tile + gridDim.x) * kTileM), tbar_a);
+                }
+                pending = true;
+            }
             const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
             if (layer < 3) {
                 // bias, GELU, BF16 -> the next product's A operand
@@ -602,6 +648,8 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(FusedArgs g) {
         }
         if (failed) break;
     }
+    // a copy still in flight lands before the CTA's shared memory goes away
+    if (pending) mbar_wait(tbar_a, tphase, g.spin_limit);
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(128) : "memory");
@@ -891,8 +939,41 @@ int pd_mlp_forward_layers(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y,
     return herr ? PD_ERR_TIMEOUT : PD_OK;
 }
 
+namespace {
+// cuTensorMapEncodeTiled, looked up through the runtime (no link against the
+// driver library)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
+// A row-major [rows][cols] BF16 matrix read in boxes of 8 columns (16 bytes)
+// by box_rows rows; rows past the end read as zero.
+bool bf16_map(CUtensorMap* m, const void* base, uint64_t rows, uint64_t cols, uint32_t box_rows) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * sizeof(__nv_bfloat16)};
+    const cuuint32_t box[2] = {8, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_NONE,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
 int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* stream) {
-    if (!n || !dev_x || !dev_y || M < 1) return PD_ERR_ARG;
+    if (!n || !dev_x || !dev_y || M < 1 || M > INT32_MAX - kTileM) return PD_ERR_ARG;
     if ((reinterpret_cast<uintptr_t>(dev_x) & 15) || (reinterpret_cast<uintptr_t>(dev_y) & 7)) return PD_ERR_ARG;
     cudaStream_t s = st(stream);
     // the fused pass: two CTAs per SM, persistent over the 128-row tiles
@@ -908,8 +989,13 @@ int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* 
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const int64_t ntiles = (M + kTileM - 1) / kTileM;
     FusedArgs a;
-    a.X = reinterpret_cast<const __nv_bfloat16*>(dev_x), a.M = M;
-    a.W1 = n->W1, a.W2 = n->W2, a.W3 = n->W3, a.W4 = n->W4;
+    if (!bf16_map(&a.mX, dev_x, (uint64_t)M, kInPad, kTileM) || !bf16_map(&a.mW1, n->W1, kHid, kInPad, kHid) ||
+        !bf16_map(&a.mW2, n->W2, kHid, kHid, kHid) || !bf16_map(&a.mW3, n->W3, kHid, kHid, kHid) ||
+        !bf16_map(&a.mW4, n->W4, kOutPad, kHid, kOutPad)) {
+        n->errmsg = "tensor map encoding failed";
+        return PD_ERR_CUDA;
+    }
+    a.M = M;
     a.b1 = n->b1, a.b2 = n->b2, a.b3 = n->b3, a.b4 = n->b4;
     a.Y = dev_y, a.err = n->err, a.spin_limit = kSpinLimit;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, 2 * (int64_t)sms));

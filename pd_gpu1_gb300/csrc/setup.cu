@@ -7,8 +7,10 @@
 //                     field and cudaMalloc/cudaFree temporaries; here one warp
 //                     per node computes idist, fac and the strain energy of all
 //                     test fields at once (u_axis = 0.001 x_axis is analytic),
-//                     then one pass forms scr per bond.
-//   initial_weight    kernel_initial_weight_2D/3D (Force_State.cu:8-54)
+//                     in a state-based context w and m as well, then one pass
+//                     forms scr per bond.
+//   initial_weight    kernel_initial_weight_2D/3D (Force_State.cu:8-54), in the
+//                     same family pass as vol_corr (k_family_setup)
 //   set_crack_*       kernel_set_crack_2D (Base_Function.cu:39-81) and the
 //                     Kalthoff-Winkler notch cut (Solve_Kalthoff_Winkler.cu:40-63)
 //   prepare           per-bond coefficients in SELL order (see pd_internal.cuh)
@@ -32,88 +34,98 @@ __device__ __forceinline__ double warp_sum(double v) {
     return __shfl_sync(0xffffffffu, v, 0);
 }
 
-__device__ __forceinline__ double bond_length(int dim, const double* x, const double* y, const double* z, int64_t i,
-                                              int64_t c) {
-    const double a = x[c] - x[i];
-    const double b = y[c] - y[i];
-    if (dim == 2) return sqrt(a * a + b * b);
-    const double d = z[c] - z[i];
-    return sqrt(a * a + b * b + d * d);
-}
-
-// idist and fac per bond (Surf_Corr.cu:17-32); one warp per node.
-__global__ void k_vol_corr(KParams P, const double* __restrict__ x, const double* __restrict__ y,
-                           const double* __restrict__ z, const int64_t* __restrict__ rowptr,
-                           const int* __restrict__ NL, double* __restrict__ idist, double* __restrict__ fac) {
+// One pass over node i's bonds, one warp per node:
+//   * idist and fac per bond (kernel_vol_Corr, Surf_Corr.cu:17-32);
+//   * with ENERGY, the strain energy density of node i under the test fields
+//     u_a = 0.001 x_a (kernel_Disp + kernel_surface_F/_3D, Surf_Corr.cu:38-158),
+//     all axes at once, and fncst_a = sedload / energy.  A batch of specimens
+//     passes bc and sedload per node (its specimen's values); bonds never
+//     cross specimens;
+//   * with WEIGHT, w per bond and m per node (kernel_initial_weight_2D/3D,
+//     Force_State.cu:8-54).
+// The reference runs these as separate passes that re-read idist and fac;
+// here they come from registers.  Every sum runs in the order a pass of its
+// own would use (lane-strided, then the warp tree), so fused and separate
+// calls give the same bits.
+template <bool ENERGY, bool WEIGHT>
+__global__ void k_family_setup(KParams P, double sedload, const double* __restrict__ node_bc,
+                               const double* __restrict__ node_sed, const double* __restrict__ x,
+                               const double* __restrict__ y, const double* __restrict__ z,
+                               const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
+                               double* __restrict__ idist, double* __restrict__ fac, double* __restrict__ fx,
+                               double* __restrict__ fy, double* __restrict__ fz, double* __restrict__ w,
+                               double* __restrict__ m) {
     const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (i >= P.N) return;
-    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
-        const int64_t c = NL[q];
-        const double L = bond_length(P.dim, x, y, z, i, c);
-        idist[q] = L;
-        double f;
-        if (L <= P.delta - P.dx / 2.0)
-            f = 1.0;
-        else if (L <= P.delta + P.dx / 2.0)
-            f = (P.delta + P.dx / 2.0 - L) / P.dx;
-        else
-            f = 0.0;
-        fac[q] = f;
-    }
-}
-
-// Strain energy density of node i under the test fields u_a = 0.001 x_a
-// (kernel_Disp + kernel_surface_F/_3D, Surf_Corr.cu:38-158), all axes in one
-// pass; fncst_a = sedload / energy.  A batch of specimens passes bc and
-// sedload per node (its specimen's values); bonds never cross specimens.
-__global__ void k_surface_energy(KParams P, double sedload, const double* __restrict__ node_bc,
-                                 const double* __restrict__ node_sed, const double* __restrict__ x,
-                                 const double* __restrict__ y, const double* __restrict__ z,
-                                 const int64_t* __restrict__ rowptr, const int* __restrict__ NL,
-                                 const double* __restrict__ idist, const double* __restrict__ fac,
-                                 double* __restrict__ fx, double* __restrict__ fy, double* __restrict__ fz) {
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= P.N) return;
-    if (node_bc) {
+    if (ENERGY && node_bc) {
         P.bc = node_bc[i];
         sedload = node_sed[i];
     }
     const int dim = P.dim;
     double st[3] = {0.0, 0.0, 0.0};
+    double acc = 0.0;
     const double xi = x[i], yi = y[i], zi = dim == 3 ? z[i] : 0.0;
     const double ui[3] = {0.001 * xi, 0.001 * yi, 0.001 * zi};
     for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
         const int64_t c = NL[q];
         const double xc = x[c], yc = y[c], zc = dim == 3 ? z[c] : 0.0;
-        const double L0 = idist[q];
-        for (int a = 0; a < dim; a++) {
-            // displacement only along axis a (the other components are zero,
-            // and adding zero is exact, so the reference's expression reduces
-            // to the plain coordinate difference on those axes)
-            const double uxc = a == 0 ? 0.001 * xc : 0.0, uxi = a == 0 ? ui[0] : 0.0;
-            const double uyc = a == 1 ? 0.001 * yc : 0.0, uyi = a == 1 ? ui[1] : 0.0;
-            const double ddx = xc + uxc - xi - uxi;
-            const double ddy = yc + uyc - yi - uyi;
-            double L;
-            if (dim == 2) {
-                L = sqrt(ddx * ddx + ddy * ddy);
-            } else {
-                const double uzc = a == 2 ? 0.001 * zc : 0.0, uzi = a == 2 ? ui[2] : 0.0;
-                const double ddz = zc + uzc - zi - uzi;
-                L = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+        const double a0 = xc - xi, b0 = yc - yi;
+        double L0;
+        if (dim == 2) {
+            L0 = sqrt(a0 * a0 + b0 * b0);
+        } else {
+            const double d0 = zc - zi;
+            L0 = sqrt(a0 * a0 + b0 * b0 + d0 * d0);
+        }
+        idist[q] = L0;
+        double f;
+        if (L0 <= P.delta - P.dx / 2.0)
+            f = 1.0;
+        else if (L0 <= P.delta + P.dx / 2.0)
+            f = (P.delta + P.dx / 2.0 - L0) / P.dx;
+        else
+            f = 0.0;
+        fac[q] = f;
+        if (ENERGY) {
+            for (int a = 0; a < dim; a++) {
+                // displacement only along axis a (the other components are
+                // zero, and adding zero is exact, so the reference's expression
+                // reduces to the plain coordinate difference on those axes)
+                const double uxc = a == 0 ? 0.001 * xc : 0.0, uxi = a == 0 ? ui[0] : 0.0;
+                const double uyc = a == 1 ? 0.001 * yc : 0.0, uyi = a == 1 ? ui[1] : 0.0;
+                const double ddx = xc + uxc - xi - uxi;
+                const double ddy = yc + uyc - yi - uyi;
+                double L;
+                if (dim == 2) {
+                    L = sqrt(ddx * ddx + ddy * ddy);
+                } else {
+                    const double uzc = a == 2 ? 0.001 * zc : 0.0, uzi = a == 2 ? ui[2] : 0.0;
+                    const double ddz = zc + uzc - zi - uzi;
+                    L = sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+                }
+                st[a] += 0.25 * P.bc * (L - L0) * (L - L0) / L0 * P.vol * f;
             }
-            st[a] += 0.25 * P.bc * (L - L0) * (L - L0) / L0 * P.vol * fac[q];
+        }
+        if (WEIGHT) {
+            const double wq = exp(-(L0 * L0) / (P.delta * P.delta));
+            w[q] = wq;
+            acc += wq * (L0 * L0) * P.vol * f;
         }
     }
-    const double sx = warp_sum(st[0]);
-    const double sy = warp_sum(st[1]);
-    const double sz = warp_sum(st[2]);
-    if (lane == 0) {
-        fx[i] = sedload / sx;
-        fy[i] = sedload / sy;
-        if (dim == 3) fz[i] = sedload / sz;
+    if (ENERGY) {
+        const double sx = warp_sum(st[0]);
+        const double sy = warp_sum(st[1]);
+        const double sz = warp_sum(st[2]);
+        if (lane == 0) {
+            fx[i] = sedload / sx;
+            fy[i] = sedload / sy;
+            if (dim == 3) fz[i] = sedload / sz;
+        }
+    }
+    if (WEIGHT) {
+        acc = warp_sum(acc);
+        if (lane == 0) m[i] = acc;
     }
 }
 
@@ -165,23 +177,6 @@ __global__ void k_surface_coeff(KParams P, const double* __restrict__ x, const d
             }
         }
     }
-}
-
-// w per bond, m per node (Force_State.cu:8-54).
-__global__ void k_weight(KParams P, const int64_t* __restrict__ rowptr, const double* __restrict__ idist,
-                         const double* __restrict__ fac, double* __restrict__ w, double* __restrict__ m) {
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
-    if (i >= P.N) return;
-    double acc = 0.0;
-    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
-        const double L0 = idist[q];
-        const double wq = exp(-(L0 * L0) / (P.delta * P.delta));
-        w[q] = wq;
-        acc += wq * (L0 * L0) * P.vol * fac[q];
-    }
-    acc = warp_sum(acc);
-    if (lane == 0) m[i] = acc;
 }
 
 // Pre-crack segment test (Base_Function.cu:39-81) on nodes [r0, r1)
@@ -837,42 +832,52 @@ void free_ptr(T*& p) {
 
 }  // namespace
 
+// The family pass with the stages asked for (energy: the surface test
+// fields; weight: w and m); idist and fac are always written.
+template <bool ENERGY, bool WEIGHT>
+static void launch_family_setup(pd_ctx* c, const KParams& P, cudaStream_t s) {
+    const double sedload = P.dim == 3 ? 0.6 * P.emod * 1.0e-6 : 0.5 * P.emod / (1.0 - P.pratio * P.pratio) * 1.0e-6;
+    k_family_setup<ENERGY, WEIGHT><<<warps_grid(P.N), 256, 0, s>>>(
+        P, sedload, c->batch.node_bc, c->batch.node_sed, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->rowptr, c->NL,
+        c->idist, c->fac, c->nf[PD_F_FNCST_X], c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z], c->w, c->nf[PD_F_M]);
+    c->launches++;
+}
+
 int vol_corr(pd_ctx* c, cudaStream_t s) {
     if (!c->family) return set_err(c, PD_ERR_STATE, "vol_corr needs the bond family");
-    const KParams P = kparams(c->p);
-    k_vol_corr<<<warps_grid(P.N), 256, 0, s>>>(P, c->nf[PD_F_X], c->nf[PD_F_Y], c->nf[PD_F_Z], c->rowptr, c->NL,
-                                                c->idist, c->fac);
-    c->launches++;
+    launch_family_setup<false, false>(c, kparams(c->p), s);
     c->volcorr = true;
     c->prepared = false;
     return cuda_err(c, cudaGetLastError(), "vol_corr");
 }
 
+// vol_Corr and the surface energies in one family pass, then the coefficient
+// pass (scr of a bond needs both end nodes' fncst: a grid-wide dependency).
+// A state-based context also gets w and m from the first pass.
 int surface_correct(pd_ctx* c, cudaStream_t s) {
-    int rc = vol_corr(c, s);
-    if (rc) return rc;
+    if (!c->family) return set_err(c, PD_ERR_STATE, "surface_correct needs the bond family");
     const KParams P = kparams(c->p);
-    const double sedload = P.dim == 3 ? 0.6 * P.emod * 1.0e-6 : 0.5 * P.emod / (1.0 - P.pratio * P.pratio) * 1.0e-6;
+    const bool state = c->p.model == PD_MODEL_STATE;
+    if (state)
+        launch_family_setup<true, true>(c, P, s);
+    else
+        launch_family_setup<true, false>(c, P, s);
     double *X = c->nf[PD_F_X], *Y = c->nf[PD_F_Y], *Z = c->nf[PD_F_Z];
-    k_surface_energy<<<warps_grid(P.N), 256, 0, s>>>(P, sedload, c->batch.node_bc, c->batch.node_sed, X, Y, Z,
-                                                      c->rowptr, c->NL, c->idist, c->fac,
-                                                      c->nf[PD_F_FNCST_X], c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z]);
     k_surface_coeff<<<warps_grid(P.N), 256, 0, s>>>(P, X, Y, Z, c->rowptr, c->NL, c->idist, c->nf[PD_F_FNCST_X],
                                                      c->nf[PD_F_FNCST_Y], c->nf[PD_F_FNCST_Z], c->scr);
-    c->launches += 2;
-    c->surfcorr = true;
+    c->launches++;
+    c->volcorr = c->surfcorr = true;
+    c->weights = c->weights || state;
     c->prepared = false;
     return cuda_err(c, cudaGetLastError(), "surface_correct");
 }
 
+// w and m in the family pass, which also (re)writes idist and fac: after a
+// vol_corr call the same values again, without one the call stands for both.
 int initial_weight(pd_ctx* c, cudaStream_t s) {
-    if (!c->volcorr) {
-        int rc = vol_corr(c, s);
-        if (rc) return rc;
-    }
-    const KParams P = kparams(c->p);
-    k_weight<<<warps_grid(P.N), 256, 0, s>>>(P, c->rowptr, c->idist, c->fac, c->w, c->nf[PD_F_M]);
-    c->launches++;
+    if (!c->family) return set_err(c, PD_ERR_STATE, "initial_weight needs the bond family");
+    launch_family_setup<false, true>(c, kparams(c->p), s);
+    c->volcorr = true;
     c->weights = true;
     c->prepared = false;
     return cuda_err(c, cudaGetLastError(), "initial_weight");
@@ -1193,9 +1198,9 @@ int prepare(pd_ctx* c, cudaStream_t s) {
     if (!c->family) return set_err(c, PD_ERR_STATE, "prepare needs the bond family");
     drop_graphs(c);  // the SELL arrays are reallocated below
     int rc;
-    if (!c->volcorr && (rc = vol_corr(c, s))) return rc;
     const bool state = c->p.model == PD_MODEL_STATE;
-    if (state && !c->weights && (rc = initial_weight(c, s))) return rc;
+    if (state && !c->weights && (rc = initial_weight(c, s))) return rc;  // vol_corr included
+    if (!c->volcorr && (rc = vol_corr(c, s))) return rc;
     // the SELL fail bits are rebuilt from the CSR flags
     if ((rc = sync_fail_to_csr(c, s))) return rc;
     const KParams P = kparams(c->p);

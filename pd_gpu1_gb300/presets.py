@@ -145,8 +145,7 @@ def build_kalthoff_winkler(scale=1.0, dx=1e-3, nt=1350, model=PD_MODEL_STATE, de
         if model == PD_MODEL_BOND:
             eng.surface_correct_gpu()
         else:
-            eng.vol_corr()
-            eng.initial_weight()
+            eng.initial_weight()  # vol_Corr's idist and fac in the same family pass
         eng.initial_state()
         eng.set_crack_kw(rad)
         eng.cylinder_init(cyl)
@@ -171,8 +170,7 @@ def build_crack_grow(scale=1.0, dx=1e-4, nt=1250, derive=None):
         eng.find_neighbor_gpu()
         eng.initial_state()
         eng.set_crack_2d(0.01 * scale, 0.0, 0.0, 0.0)
-        eng.vol_corr()
-        eng.initial_weight()
+        eng.initial_weight()  # vol_Corr's idist and fac in the same family pass
         eng.prepare()
 
     return p, setup, dict(load=20.0, nt=nt, workload="plate_crack_grow_2d_state_verlet")

@@ -94,26 +94,28 @@ def test_fused_forward_equals_layer_by_layer(L):
     """The fused forward pass (one persistent kernel, the four layers per
     128-row tile with weights and activations on chip) against the layer-by-
     layer pass (one tensor-core product per layer through device memory):
-    the same products and epilogues, so the outputs agree bit for bit, on a
-    row count that leaves a partial last tile and spans several passes of the
-    persistent grid."""
+    the same products and epilogues, so the outputs agree bit for bit.  Row
+    counts: one partial tile (the input tile's missing rows read as zero), a
+    full tile and one row, and a count that leaves a partial last tile and
+    spans several passes of the persistent grid (the next input tile is
+    fetched while the current one runs)."""
     import torch
 
-    M = 300_001
     p = mo.init_params(3)
     rng = np.random.default_rng(5)
     p = (p + 0.05 * rng.standard_normal(p.size)).astype(np.float32)
-    x, _ = _problem(9, M)
     n = _net(L, 65536)
     assert L.pd_mlp_set_params(n, p.ctypes.data, p.size) == 0
-    dx = _dev(x, torch.bfloat16)
-    y1 = torch.zeros((M, 2), dtype=torch.float32, device="cuda")
-    y2 = torch.ones((M, 2), dtype=torch.float32, device="cuda")
-    assert L.pd_mlp_forward(n, dx.data_ptr(), M, y1.data_ptr(), None) == 0
-    assert L.pd_mlp_forward_layers(n, dx.data_ptr(), M, y2.data_ptr(), None) == 0
-    a, b = y1.cpu().numpy(), y2.cpu().numpy()
-    assert np.abs(a).max() > 0.0
-    np.testing.assert_array_equal(a, b)
+    for M in (100, 129, 300_001):
+        x, _ = _problem(9, M)
+        dx = _dev(x, torch.bfloat16)
+        y1 = torch.zeros((M, 2), dtype=torch.float32, device="cuda")
+        y2 = torch.ones((M, 2), dtype=torch.float32, device="cuda")
+        assert L.pd_mlp_forward(n, dx.data_ptr(), M, y1.data_ptr(), None) == 0
+        assert L.pd_mlp_forward_layers(n, dx.data_ptr(), M, y2.data_ptr(), None) == 0
+        a, b = y1.cpu().numpy(), y2.cpu().numpy()
+        assert np.abs(a).max() > 0.0
+        np.testing.assert_array_equal(a, b, err_msg=str(M))
     L.pd_mlp_destroy(n)
 
 

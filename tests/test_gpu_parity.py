@@ -95,6 +95,42 @@ def test_weights(E, golden):
             assert_close_norm(eng.get("M"), g["m"], 1e-13, name + " m")
 
 
+def test_fused_family_pass_matches_separate_calls(E, golden):
+    """One family pass writes idist, fac, the surface energies and w, m: the
+    results are the bits of the separate calls (vol_corr, then the weights;
+    the surface correction of a bond-based context), and one launch stands
+    for vol_corr + initial_weight."""
+    from pd_gpu1_gb300 import PD_MODEL_BOND
+
+    g = golden("plate_crack_state")
+    fields = ["IDIST", "FAC", "W", "M"]
+    with engine_from_golden(E, g) as eng:
+        eng.find_neighbor_gpu()
+        eng.vol_corr()
+        eng.initial_weight()
+        sep = {k: eng.get(k) for k in fields}
+    with engine_from_golden(E, g) as eng:
+        eng.find_neighbor_gpu()
+        n0 = eng.kernel_launches
+        eng.initial_weight()
+        assert eng.kernel_launches - n0 == 1
+        for k in fields:
+            np.testing.assert_array_equal(eng.get(k), sep[k], err_msg=k)
+    p = params_from_golden(g)
+    with engine_from_golden(E, g) as eng:
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()  # state-based context: energies, scr, w and m
+        fused = {k: eng.get(k) for k in fields + ["FNCST_X", "FNCST_Y", "SCR"]}
+    p.model = PD_MODEL_BOND
+    with engine_from_golden(E, g, p) as eng:
+        eng.find_neighbor_gpu()
+        eng.surface_correct_gpu()
+        for k in ["IDIST", "FAC", "FNCST_X", "FNCST_Y", "SCR"]:
+            np.testing.assert_array_equal(fused[k], eng.get(k), err_msg=k)
+    for k in fields:
+        np.testing.assert_array_equal(fused[k], sep[k], err_msg=k)
+
+
 def test_bond_force_2d_and_breakage(E, golden):
     g = golden("plate_tensile_bond")
     with engine_from_golden(E, g) as eng:
