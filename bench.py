@@ -55,6 +55,18 @@ ALG_BYTES_PER_NODE_3D = 72.0
 # within two float ulps of their break threshold add one; per-node epilogue
 # instructions are not counted.
 FP64_EXEC_PER_BOND = {(1, 2): 4, (1, 3): 6, (2, 2): 8, (2, 3): 12}  # (model, dim), compact layouts
+# FP64 instructions per bond of the step's force launches with their per-node
+# work (epilogues, theta, divisions) included: ncu's FP64 pipe use of one
+# capture per workload (sm__inst_executed_pipe_fp64 percentage of peak x 2
+# instructions per cycle per SM x active cycles x 152 SMs), over the capture's
+# bonds (kernels and case below)
+FP64_NCU_PER_BOND = {
+    "crack_branching_2d_pmb_verlet": (4.97, "k_bond_compact<1>, 400k-node quarter-size plate, 2026-12-04"),
+    "kalthoff_winkler_3d_pmb_verlet": (7.05, "k_bond_compact3<EPI_NONE>, full slab, 2026-12-04"),
+    "plate_crack_grow_2d_state_verlet": (10.55, "k_theta_compact 4.52 + k_state_compact<1> 6.03, full plate, "
+                                                "2026-12-04"),
+    "kalthoff_winkler_3d_state_verlet": (12.60, "k_theta_compact3 6.20 + k_state_compact3<0> 6.40, full slab, "
+                                                "2026-12-04")}
 # DRAM bytes per bond and per node of the step kernel: ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one capture per workload (kernel, case, date below),
 # scaled to the timed launch's bonds and nodes; a zero per-node figure means the
@@ -96,15 +108,24 @@ def traffic_of(workload, bonds, nodes):
                                            f"scaled to this launch")
 
 
-def fp64_block(model, dim, bonds, kern_ms, gfma):
-    """FP64 pipe use of the force kernel's bond loop: executed FP64
-    instructions per second against the measured FP64 instruction rate
-    (pd_probe_fp64, dependent DFMA chains)."""
+def fp64_block(model, dim, bonds, kern_ms, gfma, workload=None):
+    """FP64 pipe use of the step's force launches: executed FP64 instructions
+    per second against the measured FP64 instruction rate (pd_probe_fp64,
+    eight independent DFMA chains per thread).  With an ncu count for the
+    workload (FP64_NCU_PER_BOND: per-node work included) that count sets the
+    fraction; otherwise the bond loop's count from the kernel source does."""
     n = FP64_EXEC_PER_BOND[(model, dim)]
     rate = n * bonds / (kern_ms * 1e-3) / 1e9
-    return {"executed_per_bond": n, "achieved_ginst_s": rate, "peak_ginst_s": gfma, "frac": rate / gfma,
-            "counted": "FP64 instructions of the bond loop, from the kernel source; epilogue not counted",
-            "peak_source": "pd_probe_fp64 (dependent DFMA chains)"}
+    out = {"executed_per_bond": n, "achieved_ginst_s": rate, "peak_ginst_s": gfma, "frac": rate / gfma,
+           "counted": "FP64 instructions of the bond loop, from the kernel source; per-node work not counted",
+           "peak_source": "pd_probe_fp64 (independent DFMA chains, all SMs)"}
+    if workload in FP64_NCU_PER_BOND:
+        m, src = FP64_NCU_PER_BOND[workload]
+        rate = m * bonds / (kern_ms * 1e-3) / 1e9
+        out.update({"executed_per_bond_ncu": m, "achieved_ginst_s": rate, "frac": rate / gfma,
+                    "counted": f"FP64 instructions per bond with the per-node work, ncu FP64 pipe use of {src}; "
+                               f"the bond loop alone executes {n} per bond (kernel source)"})
+    return out
 
 
 def rank_info():
@@ -913,7 +934,7 @@ def warm_measure(scale, K, smooth, n_plain=1, e2e=True, with_clocks=True):
                     "bonds_broken": [s["advanced"] for s in learned]},
         "speedup_vs_plain": plain_ms / (learned_ms / K),
         "speedup_vs_skip_only": skip_ms / learned_ms,
-        "roofline": {"bound": "tensor", "kernel": "k_gemm (the network's forward pass, all four layers)",
+        "roofline": {"bound": "tensor", "kernel": "k_mlp_fused (the network's forward pass: four layers per 128-row tile, TMA-fed)",
                      "achieved": flops / (infer_ms * 1e-3) / 1e12, "peak": peaks.get("bf16_tflops"),
                      "unit": "TFLOP/s", "frac": flops / (infer_ms * 1e-3) / 1e12 / peaks.get("bf16_tflops", 1.0),
                      "traffic": None, "peak_source": peak_kind, "forward_ms": infer_ms,
@@ -1227,7 +1248,7 @@ def gb300_arm(args):
                          "kernel": kname,
                          "kernel_ms": kern_ms, "kernel_share_of_step": kern_ms / step_ms,
                          "alg_bytes_per_launch": alg_bytes,
-                         "fp64": fp64_block(p.model, p.dim, B, kern_ms, gfma.value)},
+                         "fp64": fp64_block(p.model, p.dim, B, kern_ms, gfma.value, meta["workload"])},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clk, "reference_cuda": ref_cuda,
         }
         line.update(extras)
