@@ -80,6 +80,23 @@ __device__ __forceinline__ double f64_of_f32s(float f) {
     return mag < 0x00800000u ? 0.0 : v;
 }
 
+// Exact double of f * 2^e (|e| < 800; zero and subnormal floats give zero),
+// integer ops only: the power of two goes into the exponent field.
+__device__ __forceinline__ double f64_of_f32s_scaled(float f, int e) {
+    const unsigned b = __float_as_uint(f);
+    const unsigned mag = b & 0x7fffffffu;
+    const unsigned hi = (b & 0x80000000u) | ((mag >> 3) + ((unsigned)(896 + e) << 20));
+    const double v = __hiloint2double((int)hi, (int)(mag << 29));
+    return mag < 0x00800000u ? 0.0 : v;
+}
+
+// (h + l) * 2^e for a float pair in one FP64 addition: bit for bit the sum of
+// the exact doubles times 2^e, since scaling by a power of two is exact and
+// commutes with the sum's rounding while every value stays a normal double.
+__device__ __forceinline__ double f64_of_pair_scaled(float h, float l, int e) {
+    return f64_of_f32s_scaled(h, e) + f64_of_f32s_scaled(l, e);
+}
+
 __device__ __forceinline__ float rsqrt_approx_f32(float x) {
     float y;
     asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));

@@ -57,14 +57,14 @@ struct ForceArgs {
     const int64_t* base;
     const int64_t* fbase;
     const BondRec* rec;  // bond-based: per-slot record (column, float reference vector, c0, l0, k2, ecrit)
-    double kscale;      // 2^S
+    int kexp;           // sums of bond forces carry 2^-kexp (undone in the conversion to FP64)
     const StateGeo* sgeo;    // state-based: per-slot geometry (column, float reference vector, c0, l0)
     const StateTheta* sth;   // state-based: dilatation-pass record (xi, cth)
     const StateForce* sfo;   // state-based: force-pass record (c1, c2, ecrit, xi_z)
     float2* e;                // state: extension per slot as a float pair
     double sn_scale;          // state: 2^-sn_exp (theta/m and 1/m pairs)
-    double sth_inv;           // state: 2^-sth_exp (undoes the dilatation weights' scale)
-    double st_scale;          // state: 2^st_exp (undoes the force pairs' scale)
+    int sth_exp;              // state: the dilatation sums carry 2^sth_exp
+    int st_exp;               // state: the force pair sums carry 2^-st_exp
     uint32_t* bits;
     int64_t S;
     const int* NN;
@@ -586,9 +586,9 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
                 }
             }
             // undo the power-of-two scaling of the bond coefficient (exact)
-            fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-            fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
-            if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
+            fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.kexp);
+            fyr = f64_of_pair_scaled(fya.h, fya.l, A.kexp);
+            if (DIM == 3) fzr = f64_of_pair_scaled(fza.h, fza.l, A.kexp);
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
@@ -658,8 +658,8 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split(co
                 fxa = ff_add(fxa, ff{cx.x, cx.y});
                 fya = ff_add(fya, ff{cy.x, cy.y});
             }
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.kexp);
+            const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.kexp);
             if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
@@ -807,8 +807,8 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
                 }
             }
             // undo the power-of-two scaling of the bond coefficient (exact)
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.kexp);
+            const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.kexp);
             if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
@@ -925,9 +925,9 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
             fza = phase_sum<Q>(fza);
             if (ph == 0 && force_row) {
                 // undo the power-of-two scaling of the bond coefficient (exact)
-                const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-                const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
-                const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
+                const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.kexp);
+                const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.kexp);
+                const double fzr = f64_of_pair_scaled(fza.h, fza.l, A.kexp);
                 row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
             }
         }
@@ -999,8 +999,8 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact_
                 bt::acc_add(fxa, bt::f2{cx.x, cx.y});
                 bt::acc_add(fya, bt::f2{cy.x, cy.y});
             }
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
+            const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.kexp);
+            const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.kexp);
             if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
@@ -1086,9 +1086,9 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split3(c
                 fya = ff_add(fya, ff{cy.x, cy.y});
                 fza = ff_add(fza, ff{cz.x, cz.y});
             }
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.kscale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.kscale;
-            const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.kscale;
+            const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.kexp);
+            const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.kexp);
+            const double fzr = f64_of_pair_scaled(fza.h, fza.l, A.kexp);
             if (force_row) row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
             if (EPI == EPI_ADR && A.slice_part) slice_partials(A, s, red);
         }
@@ -1146,7 +1146,7 @@ __device__ __forceinline__ void theta_pass(const ForceArgs& A) {
         if (row) {
             // theta = acc / m and theta / m through 1/m (nb, IEEE-rounded at set-up)
             const double m = A.m[r], rm = A.nb[r];
-            const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
+            const double a = f64_of_pair_scaled(acc.h, acc.l, -A.sth_exp);
             const double th = div_recip(a, m, rm);
             A.theta[r] = th;
             const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
@@ -1232,9 +1232,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
                 if (broke && lane == 0 && !A.nobreak) wbits[k] = word & ~broke;
             }
             // undo the power-of-two scale of T (exact)
-            fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
-            fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
-            if (DIM == 3) fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.st_scale;
+            fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.st_exp);
+            fyr = f64_of_pair_scaled(fya.h, fya.l, A.st_exp);
+            if (DIM == 3) fzr = f64_of_pair_scaled(fza.h, fza.l, A.st_exp);
             if (force_row) row_epilogue<DIM, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
@@ -1329,9 +1329,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force3_p
         }
         if (ph == 0 && force_row) {
             // undo the power-of-two scale of T (exact)
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
-            const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.st_scale;
+            const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.st_exp);
+            const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.st_exp);
+            const double fzr = f64_of_pair_scaled(fza.h, fza.l, A.st_exp);
             row_epilogue<3, EPI_NONE>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
     }
@@ -1417,7 +1417,7 @@ __global__ void __launch_bounds__(kForceBlock) k_theta_compact(const ForceArgs A
         if (row && ph == 0) {
             // theta = acc / m and theta / m through 1/m (nb, IEEE-rounded at set-up)
             const double m = A.m[r], rm = A.nb[r];
-            const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
+            const double a = f64_of_pair_scaled(acc.h, acc.l, -A.sth_exp);
             const double th = div_recip(a, m, rm);
             A.theta[r] = th;
             const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
@@ -1515,8 +1515,8 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
             }
             if (ph == 0) {
                 // undo the power-of-two scale of T (exact)
-                const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
-                const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
+                const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.st_exp);
+                const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.st_exp);
                 if (force_row) row_epilogue<2, EPI>(A, r, fxr, fyr, 0.0, xi, yi, 0.0, uxi, uyi, 0.0, red);
             }
         }
@@ -1586,7 +1586,7 @@ __global__ void __launch_bounds__(kForceBlock, 5) k_theta_compact3(const ForceAr
         }
         if (row) {
             const double m = A.m[r], rm = A.nb[r];
-            const double a = (f64_of_f32s(acc.h) + f64_of_f32s(acc.l)) * A.sth_inv;
+            const double a = f64_of_pair_scaled(acc.h, acc.l, -A.sth_exp);
             const double th = div_recip(a, m, rm);
             A.theta[r] = th;
             const ff na = ff_split(div_recip(th, m, rm) * A.sn_scale);
@@ -1685,9 +1685,9 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
             fza = bt::add(fza, bt::f2{__shfl_xor_sync(0xffffffffu, fza.h, off), __shfl_xor_sync(0xffffffffu, fza.l, off)});
         }
         if (ph == 0 && force_row) {
-            const double fxr = (f64_of_f32s(fxa.h) + f64_of_f32s(fxa.l)) * A.st_scale;
-            const double fyr = (f64_of_f32s(fya.h) + f64_of_f32s(fya.l)) * A.st_scale;
-            const double fzr = (f64_of_f32s(fza.h) + f64_of_f32s(fza.l)) * A.st_scale;
+            const double fxr = f64_of_pair_scaled(fxa.h, fxa.l, A.st_exp);
+            const double fyr = f64_of_pair_scaled(fya.h, fya.l, A.st_exp);
+            const double fzr = f64_of_pair_scaled(fza.h, fza.l, A.st_exp);
             row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
     }
@@ -1775,14 +1775,14 @@ static ForceArgs make_args(pd_ctx* c) {
     A.base = S.base;
     A.fbase = S.fbase;
     A.rec = S.rec;
-    A.kscale = S.kscale;
     A.sgeo = S.sgeo;
     A.sth = S.sth;
     A.sfo = S.sfo;
     A.e = S.e;
     A.sn_scale = std::ldexp(1.0, -S.sn_exp);
-    A.sth_inv = std::ldexp(1.0, -S.sth_exp);
-    A.st_scale = std::ldexp(1.0, S.st_exp);
+    A.kexp = S.kexp;
+    A.sth_exp = S.sth_exp;
+    A.st_exp = S.st_exp;
     A.bits = S.bits;
     A.S = S.S;
     A.NN = c->NN;

@@ -180,22 +180,34 @@ __global__ void k_load_tensile(NodeArgs A) {
     }
 }
 
-// kernel_cal_dmg_2D/3D on CSR rows; one warp per node.
+// kernel_cal_dmg_2D/3D (Base_Function.cu:149-217): dmg = 1 - (sum of vol fac
+// over intact bonds) / (sum of vol fac over all bonds), vol cancelled.  One
+// thread per row summing its bonds in order: the reference's warp per node
+// with a shuffle tree spends about 25 FP64 warp instructions per row, most of
+// them on lanes without a bond, and on this GPU's FP64 pipe that took 2.2 ms
+// per call on the 1.6M-node plate; here it is two FP64 additions per bond.
+// The sums differ from the reference's order by rounding only (relative
+// 1e-16).  The intact flag of bond q comes from the CSR flags or (BITS)
+// straight from the step loop's SELL words: slot k of row r is bond
+// rowptr[r] + k, and word fbase[r / 32] + k holds the flags of slot k of the
+// slice's 32 rows (the same word for the 32 lanes of a warp), so no
+// conversion pass is needed.  Both forms give the same bits.
+template <bool BITS>
 __global__ void k_damage(KParams P, const int64_t* __restrict__ rowptr, const int* __restrict__ fail,
+                         const int64_t* __restrict__ fbase, const uint32_t* __restrict__ bits,
                          const double* __restrict__ fac, double* __restrict__ dmg) {
-    const int64_t i = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    const int lane = threadIdx.x & 31;
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= P.N_int) return;
+    const int64_t q0 = rowptr[i], n = rowptr[i + 1] - q0;
+    const uint32_t* wb = BITS ? bits + fbase[i >> 5] : nullptr;
     double d1 = 0.0, d2 = 0.0;
-    for (int64_t q = rowptr[i] + lane; q < rowptr[i + 1]; q += 32) {
-        d1 += fail[q] * P.vol * fac[q];
-        d2 += P.vol * fac[q];
+    for (int64_t k = 0; k < n; k++) {
+        const double f = fac[q0 + k];
+        const bool alive = BITS ? ((wb[k] >> (i & 31)) & 1u) != 0u : fail[q0 + k] != 0;
+        d2 += f;
+        if (alive) d1 += f;
     }
-    for (int off = 16; off > 0; off >>= 1) {
-        d1 += __shfl_down_sync(0xffffffffu, d1, off);
-        d2 += __shfl_down_sync(0xffffffffu, d2, off);
-    }
-    if (lane == 0) dmg[i] = 1.0 - d1 / d2;
+    dmg[i] = 1.0 - d1 / d2;
 }
 
 // Deterministic two-pass sum: block partials in block order, then one block.
@@ -394,10 +406,17 @@ int launch_load_tensile(pd_ctx* c, cudaStream_t s) {
 }
 
 int launch_damage(pd_ctx* c, cudaStream_t s) {
-    int rc = sync_fail_to_csr(c, s);
-    if (rc) return rc;
     const KParams P = kparams(c->p);
-    k_damage<<<(unsigned)((P.N_int * 32 + T - 1) / T), T, 0, s>>>(P, c->rowptr, c->fail, c->fac, c->nf[PD_F_DMG]);
+    const Sell& S = c->sell;
+    const unsigned grid = (unsigned)std::max<int64_t>(1, (P.N_int + T - 1) / T);
+    if (c->bits_current && S.bits) {
+        // the step loop's flags as they stand (no conversion to the CSR flags)
+        k_damage<true><<<grid, T, 0, s>>>(P, c->rowptr, nullptr, S.fbase, S.bits, c->fac, c->nf[PD_F_DMG]);
+    } else {
+        int rc = sync_fail_to_csr(c, s);
+        if (rc) return rc;
+        k_damage<false><<<grid, T, 0, s>>>(P, c->rowptr, c->fail, nullptr, nullptr, c->fac, c->nf[PD_F_DMG]);
+    }
     c->launches++;
     return cuda_err(c, cudaGetLastError(), "damage");
 }

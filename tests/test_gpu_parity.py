@@ -812,3 +812,29 @@ def test_count_broken_matches_the_flags(E):
         n = eng.count_broken()
         assert n == int((eng.get("FAIL") == 0).sum())
         assert n > n0  # bonds broke
+
+
+def test_damage_from_intact_bits_equals_csr_path(E):
+    """pd_damage after force passes reads the step loop's SELL intact bits
+    directly; after the flags are set through the CSR field it converts them
+    and reads the CSR flags.  Both give the same damage field bit for bit, on
+    the crack-branching plate (2-D bond-based) and the impact slab's
+    state-based model (3-D) after bonds broke, and the explicit loop's damage
+    dumps (inside its CUDA graphs) equal a damage call afterwards."""
+    from pd_gpu1_gb300 import presets
+
+    cases = [presets.build_crack_branching(scale=0.1, nt=200),
+             presets.build_kalthoff_winkler(scale=0.3, dx=2e-3, nt=100)]
+    for p, setup, meta in cases:
+        with E.Engine(p) as eng:
+            setup(eng)
+            eng.run_explicit(100, load=meta["load"], dmg_every=50)
+            d_loop = eng.get("DMG")
+            eng.damage()
+            d_bits = eng.get("DMG")
+            np.testing.assert_array_equal(d_loop, d_bits)
+            fail = eng.get("FAIL")
+            assert (fail == 0).sum() > 0
+            eng.set("FAIL", fail)  # the CSR flags become the current copy
+            eng.damage()
+            np.testing.assert_array_equal(eng.get("DMG"), d_bits)
