@@ -275,6 +275,30 @@ __device__ __forceinline__ void contact_node(const KParams& P, const CylDev& cy,
     }
 }
 
+// One component's term of kernel_cnn (Integrate.cu:17-33),
+//   -u^2 (F/m - F_old/m) / (dt vh),
+// as -u^2 ((F - F_old) / m) / (dt vh) with both divisions through
+// reciprocals: 1/m (IEEE-rounded on the host) and 1/(dt vh) from the FP32
+// estimate of the divisor's leading bits refined by two Newton steps in FP64
+// (relative error near 2^-53).  About eleven FP64 instructions instead of the
+// reference's two quotients and one IEEE division (about 24).  The term
+// differs from the reference's in its last bits; the damping coefficient sums
+// these terms over all nodes in another order than the reference's in any
+// case.  Divisors outside [2^-100, 2^101) in magnitude take the IEEE division.
+__device__ __forceinline__ double damping_term(double u, double f, double fo, double rmass, double dt, double vh) {
+    const double d = dt * vh;
+    const double n = -1.0 * u * u * ((f - fo) * rmass);
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned mag = hi & 0x7fffffffu, E = mag >> 20;
+    if (E < 923u || E > 1123u) return n / d;
+    // d's leading bits as a float (truncated), then its reciprocal estimate
+    const float df = __uint_as_float((hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29));
+    double y = f64_of_f32s(rcp_approx_f32(df));
+    y = fma(y, fma(-d, y, 1.0), y);
+    y = fma(y, fma(-d, y, 1.0), y);
+    return __dmul_rn(n, y);  // a product of its own (no contraction into the caller's sum)
+}
+
 // Epilogue of one force-computed row r (r < nforce).
 template <int DIM, int EPI>
 __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, double fxr, double fyr, double fzr,
@@ -285,25 +309,18 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
     A.fy[r] = fyr;
     if (DIM == 3) A.fz[r] = fzr;
     if (EPI == EPI_ADR) {
-        // kernel_cnn (Integrate.cu:17-33), same operand order; a batch of
-        // specimens carries its fictitious mass per node.  The divisions by
-        // the mass go through its reciprocal (div_recip: bit for bit the
-        // quotient); the one by dt * vh is a plain division.
-        const double mass = A.node_mass ? A.node_mass[r] : P.mass;
+        // kernel_cnn (Integrate.cu:17-33) through damping_term; a batch of
+        // specimens carries its fictitious mass per node.
         const double rmass = A.node_mass ? A.node_rmass[r] : P.rmass;
         const double vhx = A.vhx[r], vhy = A.vhy[r];
         double cn = 0.0, disp;
-        if (vhx != 0.0)
-            cn = -1.0 * uxi * uxi * (div_recip(fxr, mass, rmass) - div_recip(A.fox[r], mass, rmass)) / (P.dt * vhx);
+        if (vhx != 0.0) cn = damping_term(uxi, fxr, A.fox[r], rmass, P.dt, vhx);
         disp = uxi * uxi;
-        if (vhy != 0.0)
-            cn -= 1.0 * uyi * uyi * (div_recip(fyr, mass, rmass) - div_recip(A.foy[r], mass, rmass)) / (P.dt * vhy);
+        if (vhy != 0.0) cn += damping_term(uyi, fyr, A.foy[r], rmass, P.dt, vhy);
         disp += uyi * uyi;
         if (DIM == 3) {
             const double vhz = A.vhz[r];
-            if (vhz != 0.0)
-                cn -= 1.0 * uzi * uzi * (div_recip(fzr, mass, rmass) - div_recip(A.foz[r], mass, rmass)) /
-                      (P.dt * vhz);
+            if (vhz != 0.0) cn += damping_term(uzi, fzr, A.foz[r], rmass, P.dt, vhz);
             disp += uzi * uzi;
         }
         red[0] += cn;
@@ -1701,13 +1718,15 @@ __global__ void __launch_bounds__(kForceBlock) k_adr_cnn(const ForceArgs A) {
     const KParams& P = A.P;
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < P.N_int; r += (int64_t)gridDim.x * blockDim.x) {
         const double uxi = A.ux[r], uyi = A.uy[r], uzi = DIM == 3 ? A.uz[r] : 0.0;
+        // the damping terms as the fused epilogue forms them (damping_term)
+        const double rmass = A.node_mass ? A.node_rmass[r] : P.rmass;
         double cn = 0.0, disp;
-        if (A.vhx[r] != 0.0) cn = -1.0 * uxi * uxi * (A.fx[r] / P.mass - A.fox[r] / P.mass) / (P.dt * A.vhx[r]);
+        if (A.vhx[r] != 0.0) cn = damping_term(uxi, A.fx[r], A.fox[r], rmass, P.dt, A.vhx[r]);
         disp = uxi * uxi;
-        if (A.vhy[r] != 0.0) cn -= 1.0 * uyi * uyi * (A.fy[r] / P.mass - A.foy[r] / P.mass) / (P.dt * A.vhy[r]);
+        if (A.vhy[r] != 0.0) cn += damping_term(uyi, A.fy[r], A.foy[r], rmass, P.dt, A.vhy[r]);
         disp += uyi * uyi;
         if (DIM == 3) {
-            if (A.vhz[r] != 0.0) cn -= 1.0 * uzi * uzi * (A.fz[r] / P.mass - A.foz[r] / P.mass) / (P.dt * A.vhz[r]);
+            if (A.vhz[r] != 0.0) cn += damping_term(uzi, A.fz[r], A.foz[r], rmass, P.dt, A.vhz[r]);
             disp += uzi * uzi;
         }
         red[0] += cn;

@@ -32,6 +32,7 @@ struct NodeArgs {
     double* pz;
     const double* cn;
     CylDev* cyl;
+    double adr_c0, adr_c1;  // 1.0 * dt / mass and 2.0 * dt / mass (host IEEE operations, the same bits)
 };
 
 NodeArgs node_args(pd_ctx* c) {
@@ -49,6 +50,8 @@ NodeArgs node_args(pd_ctx* c) {
     a.pxy = c->posxy[c->parity], a.pz = c->posz[c->parity];
     a.cn = c->cn;
     a.cyl = c->cyl;
+    a.adr_c0 = 1.0 * c->p.dt / c->p.mass;
+    a.adr_c1 = 2.0 * c->p.dt / c->p.mass;
     return a;
 }
 
@@ -98,11 +101,20 @@ __global__ void k_prologue(NodeArgs A, double load, int first_verlet, int cyl_st
 // kernel_integrate (Integrate.cu:54-106), same operand order.
 __global__ void k_adr_update(NodeArgs A, int ct, int do_next, double load) {
     const KParams& P = A.P;
-    const double cn = *A.cn;
-    const double c0 = 1.0 * P.dt / P.mass;       // ct == 0
-    const double c1 = 2.0 * P.dt / P.mass;
-    const double num = 2.0 - cn * P.dt, den = 2.0 + cn * P.dt;
-    const double rden = 1.0 / den;  // one IEEE division per thread; per node div_recip (bit for bit the quotient)
+    // per step: 2 - cn dt, 2 + cn dt and its IEEE reciprocal, once per block
+    // (per node the division goes through div_recip, bit for bit the
+    // quotient); dt / mass comes from the host
+    __shared__ double sk[3];
+    if (threadIdx.x == 0) {
+        const double cn = *A.cn;
+        sk[0] = 2.0 - cn * P.dt;
+        sk[1] = 2.0 + cn * P.dt;
+        sk[2] = 1.0 / sk[1];
+    }
+    __syncthreads();
+    const double num = sk[0], den = sk[1], rden = sk[2];
+    const double c0 = A.adr_c0;  // ct == 0
+    const double c1 = A.adr_c1;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < P.N; i += (int64_t)gridDim.x * blockDim.x) {
         if (i < P.N_int) {
             double* vh[3] = {A.vhx, A.vhy, A.vhz};
