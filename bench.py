@@ -851,6 +851,7 @@ def warm_measure(scale, K, smooth, n_plain=1, e2e=True, with_clocks=True):
     with E.Engine(p) as eng:
         setup(eng)
         B = int(eng.get("ROWPTR")[p.N_int])
+        tuned = eng.autotune(reps=5)  # the bond kernel's launch shape, at the initial state
         first = warm.run_increments(eng, meta, 1, mode="plain")[0]  # increment 0; clears the history
         eng.snapshot_save(snap)
         if clocks:
@@ -917,7 +918,8 @@ def warm_measure(scale, K, smooth, n_plain=1, e2e=True, with_clocks=True):
         "config": {"workload": meta["workload"], "nodes": p.N, "bonds": B, "dx": p.dx, "increment_m": delta,
                    "tol": 1e-6, "timed_increments": list(range(1, K + 1)), "smooth_passes": smooth,
                    "untimed": "increment 0 (plain start, %d ADR steps); every chain starts from its state"
-                              % first["iters"]},
+                              % first["iters"],
+                   "launch": {"block": tuned[0], "chunked": tuned[1], "waves": tuned[2], "split": tuned[3]}},
         "plain": {"ms_per_increment": plain_ms, "iters": [s["iters"] for s in plain],
                   "what": "increment 1 from the previous solution"},
         "skip_only": {"ms_per_increment": skip_ms / K, "iters": [s["iters"] for s in skip],

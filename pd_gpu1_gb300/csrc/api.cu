@@ -689,6 +689,7 @@ int pd_run_adr(pd_ctx* c, int ct0, int nsteps, double load, void* stream) {
     auto step = [&](int ct, int last) -> int {
         StepFlags f;
         f.epi = EPI_ADR;
+        f.residual = last;  // read after the call (pd_adr_solve); not formed on the other steps
         int r = launch_force(c, f, s);
         if (r) return r;
         return launch_adr_update(c, ct, last ? 0 : 1, load, s);
@@ -981,6 +982,7 @@ int pd_profile_steps(pd_ctx* c, int kind, int ct0, int nsteps, double load, doub
         StepFlags f;
         if (kind == 0) {
             f.epi = EPI_ADR;
+            f.residual = last;
             rc = launch_force(c, f, s);
             cudaEventRecord(ev[3 * t + 1], s);
             if (!rc) rc = batch ? batch_finish(c, ct0 + t, last, load, s)

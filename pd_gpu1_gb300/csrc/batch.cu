@@ -189,6 +189,7 @@ int batch_prologue(pd_ctx* c, double load, cudaStream_t s) {
 int batch_force(pd_ctx* c, cudaStream_t s) {
     StepFlags f;
     f.epi = EPI_ADR;
+    f.residual = 0;  // a batch has no convergence check
     return launch_force(c, f, s);
 }
 

@@ -299,6 +299,9 @@ __device__ __forceinline__ double damping_term(double u, double f, double fo, do
     return __dmul_rn(n, y);  // a product of its own (no contraction into the caller's sum)
 }
 
+// v != 0.0 on the integer pipe (+0 and -0 compare equal to zero, NaN does not).
+__device__ __forceinline__ bool nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }
+
 // Epilogue of one force-computed row r (r < nforce).
 template <int DIM, int EPI>
 __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, double fxr, double fyr, double fzr,
@@ -314,25 +317,27 @@ __device__ __forceinline__ void row_epilogue(const ForceArgs& A, int64_t r, doub
         const double rmass = A.node_mass ? A.node_rmass[r] : P.rmass;
         const double vhx = A.vhx[r], vhy = A.vhy[r];
         double cn = 0.0, disp;
-        if (vhx != 0.0) cn = damping_term(uxi, fxr, A.fox[r], rmass, P.dt, vhx);
+        if (nonzero(vhx)) cn = damping_term(uxi, fxr, A.fox[r], rmass, P.dt, vhx);
         disp = uxi * uxi;
-        if (vhy != 0.0) cn += damping_term(uyi, fyr, A.foy[r], rmass, P.dt, vhy);
+        if (nonzero(vhy)) cn += damping_term(uyi, fyr, A.foy[r], rmass, P.dt, vhy);
         disp += uyi * uyi;
         if (DIM == 3) {
             const double vhz = A.vhz[r];
-            if (vhz != 0.0) cn += damping_term(uzi, fzr, A.foz[r], rmass, P.dt, vhz);
+            if (nonzero(vhz)) cn += damping_term(uzi, fzr, A.foz[r], rmass, P.dt, vhz);
             disp += uzi * uzi;
         }
         red[0] += cn;
         red[1] += disp;
-        // residual of the iterate: |F + b|^2 over the force rows (free nodes)
-        const double rx = fxr + A.bx[r], ry = fyr + A.by[r];
-        double rr = rx * rx + ry * ry;
-        if (DIM == 3) {
-            const double rz = fzr + A.bz[r];
-            rr += rz * rz;
+        if (A.res_out) {
+            // residual of the iterate: |F + b|^2 over the force rows (free nodes)
+            const double rx = fxr + A.bx[r], ry = fyr + A.by[r];
+            double rr = rx * rx + ry * ry;
+            if (DIM == 3) {
+                const double rz = fzr + A.bz[r];
+                rr += rz * rz;
+            }
+            red[2] += rr;
         }
-        red[2] += rr;
         return;
     }
     if (EPI == EPI_VERLET) {
@@ -611,7 +616,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_force(co
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
     }
-    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -683,7 +688,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split(co
         if (sub == 0 && EPI == EPI_VERLET && A.do_next && in && !force_row && r < P.N) boundary_row<2>(A, r);
         __syncthreads();
     }
-    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -831,7 +836,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<2>(A, r);
     }
-    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -950,7 +955,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kCompactMinBlocks) k_bond_compa
         }
         if (EPI == EPI_VERLET && A.do_next && ph == 0 && !force_row && r < P.N) boundary_row<3>(A, r);
     }
-    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -1024,7 +1029,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_compact_
         if (sub == 0 && EPI == EPI_VERLET && A.do_next && in && !force_row && r < P.N) boundary_row<2>(A, r);
         __syncthreads();
     }
-    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -1112,7 +1117,7 @@ __global__ void __launch_bounds__(kMaxBondBlock, kBondMinBlocks) k_bond_split3(c
         if (sub == 0 && EPI == EPI_VERLET && A.do_next && in && !force_row && r < P.N) boundary_row<3>(A, r);
         __syncthreads();
     }
-    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR && !A.slice_part) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -1256,7 +1261,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_force(co
         }
         if (EPI == EPI_VERLET && A.do_next && !force_row && r < P.N) boundary_row<DIM>(A, r);
     }
-    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -1539,7 +1544,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact(
         }
         if (EPI == EPI_VERLET && A.do_next && ph == 0 && !force_row && r < P.N) boundary_row<2>(A, r);
     }
-    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
     if (EPI == EPI_VERLET && A.contact) finish_reduction<EPI>(A, red, 3);
 }
 
@@ -1708,7 +1713,7 @@ __global__ void __launch_bounds__(kForceBlock, kStateMinBlocks) k_state_compact3
             row_epilogue<3, EPI>(A, r, fxr, fyr, fzr, xi, yi, zi, uxi, uyi, uzi, red);
         }
     }
-    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, 3);
+    if (EPI == EPI_ADR) finish_reduction<EPI>(A, red, A.res_out ? 3 : 2);
 }
 
 // Standalone kernel_cnn + cal_cn (Integrate.cu:7-49, :108-129) on the current forces.
@@ -1721,12 +1726,12 @@ __global__ void __launch_bounds__(kForceBlock) k_adr_cnn(const ForceArgs A) {
         // the damping terms as the fused epilogue forms them (damping_term)
         const double rmass = A.node_mass ? A.node_rmass[r] : P.rmass;
         double cn = 0.0, disp;
-        if (A.vhx[r] != 0.0) cn = damping_term(uxi, A.fx[r], A.fox[r], rmass, P.dt, A.vhx[r]);
+        if (nonzero(A.vhx[r])) cn = damping_term(uxi, A.fx[r], A.fox[r], rmass, P.dt, A.vhx[r]);
         disp = uxi * uxi;
-        if (A.vhy[r] != 0.0) cn += damping_term(uyi, A.fy[r], A.foy[r], rmass, P.dt, A.vhy[r]);
+        if (nonzero(A.vhy[r])) cn += damping_term(uyi, A.fy[r], A.foy[r], rmass, P.dt, A.vhy[r]);
         disp += uyi * uyi;
         if (DIM == 3) {
-            if (A.vhz[r] != 0.0) cn += damping_term(uzi, A.fz[r], A.foz[r], rmass, P.dt, A.vhz[r]);
+            if (nonzero(A.vhz[r])) cn += damping_term(uzi, A.fz[r], A.foz[r], rmass, P.dt, A.vhz[r]);
             disp += uzi * uzi;
         }
         red[0] += cn;
@@ -1959,6 +1964,7 @@ int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s) {
     A.load = f.load;
     A.contact = f.contact;
     A.nobreak = f.nobreak;
+    if (!f.residual) A.res_out = nullptr;
     if (f.epi != EPI_VERLET || !f.do_next) {
         // without the next step's half-kick only the force rows are visited
         A.nslices = (A.nforce + 31) / 32;

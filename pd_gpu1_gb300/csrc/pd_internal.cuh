@@ -314,6 +314,7 @@ struct StepFlags {
     double load = 0.0;    // boundary-row speed of the next step (quick_load)
     int contact = 0;      // rigid impactor contact in the epilogue
     int nobreak = 0;      // leave the intact flags unchanged (residual evaluations)
+    int residual = 1;     // ADR: also reduce |F + b|^2 (the convergence checks read the last step's)
 };
 int launch_force(pd_ctx* c, const StepFlags& f, cudaStream_t s);
 int launch_theta(pd_ctx* c, cudaStream_t s);

@@ -838,3 +838,25 @@ def test_damage_from_intact_bits_equals_csr_path(E):
             eng.set("FAIL", fail)  # the CSR flags become the current copy
             eng.damage()
             np.testing.assert_array_equal(eng.get("DMG"), d_bits)
+
+
+def test_adr_solve_residual_is_the_last_steps(E):
+    """pd_adr_solve's residual is |F + b| over the free nodes of the iterate
+    its last ADR step started from: the force arrays hold that step's forces
+    after the call (the update does not change them).  The residual is formed
+    only on the last step of each chunk of steps."""
+    from pd_gpu1_gb300 import presets
+
+    p, setup, meta = presets.build_plate_tensile(scale=0.3)
+    with E.Engine(p) as eng:
+        setup(eng)
+        eng.run_adr(0, 20, load=meta["load"])
+        for check_every in (100, 37):
+            it, r = eng.adr_solve(20, 200, check_every, 0.0)
+            assert it == 200
+            n = p.N_int
+            fx = eng.get("FX")[:n] + eng.get("BX")[:n]
+            fy = eng.get("FY")[:n] + eng.get("BY")[:n]
+            want = float(np.sqrt(np.sum(fx * fx) + np.sum(fy * fy)))
+            assert want > 0.0
+            assert r == pytest.approx(want, rel=1e-12)
