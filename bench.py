@@ -701,8 +701,6 @@ def batch_arm(args):
     alg_bytes = ALG_BYTES_PER_NODE_2D_ADR * p.N_int + ALG_BYTES_PER_BOND_2D * B
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
-    gfma = C.c_double()
-    L.pd_probe_fp64(C.byref(gfma))
     traffic, traffic_src = traffic_of(meta["workload"], B, p.N_int)
 
     # end to end through the C ABI with host buffers: the initial state goes up
@@ -729,6 +727,10 @@ def batch_arm(args):
     e2e = {"value": e2e_work / e2e_s, "unit": "bond-updates/s", "h2d_bytes_per_step": h2d / args.steps,
            "d2h_bytes_per_step": d2h / args.steps}
     bat.close()
+    # the FP64 instruction rate, after the timed runs (the probe saturates the
+    # FP64 pipe of every SM for ~60 ms)
+    gfma = C.c_double()
+    L.pd_probe_fp64(C.byref(gfma))
 
     sequential = ref_cuda = cpu = None
     if rank == 0 and world == 1:
@@ -1109,8 +1111,6 @@ def gb300_arm(args):
             (ALG_BYTES_PER_BOND_3D if is3d else ALG_BYTES_PER_BOND_2D) * B
     peaks, peak_kind = measured_peaks()
     achieved = alg_bytes / (kern_ms * 1e-3) / 1e9
-    gfma = C.c_double()
-    lib().pd_probe_fp64(C.byref(gfma))
     # DRAM bytes per launch from one ncu capture of the same kernel (the case
     # and date are carried in the line), scaled by bonds and nodes
     traffic, traffic_src = traffic_of(meta["workload"], B, p.N_int)
@@ -1131,7 +1131,8 @@ def gb300_arm(args):
     def e2e_run():
         """The job from the initial state: inputs uploaded from pinned host
         memory, the steps, the damage dumps and the final displacement read
-        back; returns (seconds, bytes up, bytes down)."""
+        back; returns (seconds, bytes up, bytes down, phase seconds: uploads,
+        steps with the dumps, final downloads)."""
         eng.snapshot_load(snap0)
         barrier()
         up = down = 0
@@ -1139,6 +1140,7 @@ def gb300_arm(args):
         for k in names_up:
             eng._c(L.pd_set_field(eng.ctx, FIELD[k], pin[k].data_ptr(), n, eng.stream), "pd_set_field")
             up += n * 8
+        t1 = time.perf_counter()
         every = meta.get("dmg_every") or args.steps
         done = 0
         while done < args.steps:
@@ -1148,18 +1150,32 @@ def gb300_arm(args):
             if meta.get("dmg_every"):
                 eng._c(L.pd_get_field(eng.ctx, FIELD["DMG"], pin["DMG"].data_ptr(), n, eng.stream), "pd_get_field")
                 down += n * 8
+        eng.sync()
+        t2 = time.perf_counter()
         for k in ["UX", "UY"] + (["UZ"] if is3d else []):
             eng._c(L.pd_get_field(eng.ctx, FIELD[k], pin[k].data_ptr(), n, eng.stream), "pd_get_field")
             down += n * 8
-        return time.perf_counter() - t0, up, down
+        t3 = time.perf_counter()
+        return t3 - t0, up, down, (t1 - t0, t2 - t1, t3 - t2)
 
-    e2e_run()  # warm-up, as for the device-timed steps: the step graphs of this run's chunks
-    secs, h2d, d2h = e2e_run()
+    with torch.cuda.stream(stream):
+        e2e_run()  # warm-up, as for the device-timed steps: the step graphs of this run's chunks
+        e2e_clocks = ClockSampler(torch.cuda.current_device())
+        e2e_clocks.start()
+        secs, h2d, d2h, phases = e2e_run()
+        e2e_clk = e2e_clocks.stop()
     e2e_s, e2e_work = aggregate_replicas(secs, B * args.steps, dist, "cuda")
     os.remove(snap0)
     os.rmdir(snap_dir)
     e2e = {"value": e2e_work / e2e_s, "unit": "bond-updates/s",
-           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps}
+           "h2d_bytes_per_step": h2d / args.steps, "d2h_bytes_per_step": d2h / args.steps,
+           "phases_ms": {"upload": phases[0] * 1e3, "steps_and_dumps": phases[1] * 1e3,
+                         "download": phases[2] * 1e3},
+           "clocks": e2e_clk}
+    # the FP64 instruction rate, after the timed runs (the probe saturates the
+    # FP64 pipe of every SM for ~60 ms)
+    gfma = C.c_double()
+    lib().pd_probe_fp64(C.byref(gfma))
 
     # the reference's own CUDA kernels on the same GPU and plate, when their
     # cubin was built (oracle/_ref/ref_kernels.cubin, from the reference sources)
