@@ -467,6 +467,10 @@ __global__ void k_combine(int64_t n, const double* __restrict__ corr, double U, 
 // 32 KB (two 64-wide K chunks, written by the epilogues), the input tile 4 KB
 // and the biases: 110 KB, two CTAs per SM.
 constexpr int kFusedSmem = 4096 + 2 * 32768 + 4096 + 32768 + 4096 + 2048;  // + the biases (1,600 bytes)
+// Eight warps: warps w and w + 4 read the same 32 TMEM lanes (a warp reaches
+// the lane quarter w % 4), the first the columns [0, 64) of each layer, the
+// second [64, 128), so sixteen warps per SM share the epilogues.
+constexpr int kFusedThreads = 256;
 constexpr uint32_t kWeightBytes = 4096 + 2 * 32768 + 4096, kXBytes = 4096;
 
 __device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t da, uint64_t db, uint32_t idesc, uint32_t acc) {
@@ -514,7 +518,7 @@ struct FusedArgs {
     long long spin_limit;
 };
 
-__global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ FusedArgs g) {
+__global__ void __launch_bounds__(kFusedThreads) k_mlp_fused(const __grid_constant__ FusedArgs g) {
     extern __shared__ __align__(1024) unsigned char fsm[];
     unsigned char* sW1 = fsm;                  // 2 boxes x 2 KB (128 rows)
     unsigned char* sW2 = sW1 + 4096;           // 16 boxes x 2 KB
@@ -527,6 +531,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ 
     __shared__ uint32_t tmem_slot;
     __shared__ int failed;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int quarter = warp & 3, half = warp >> 2;  // TMEM lane quarter, column half
     const uint32_t bar_a = smem_addr(&bar), tbar_a = smem_addr(&tbar);
     const uint32_t a0 = smem_addr(sH), x0 = smem_addr(sX), w1 = smem_addr(sW1), w2 = smem_addr(sW2),
                    w3 = smem_addr(sW3), w4 = smem_addr(sW4);
@@ -558,7 +563,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ 
             tma_load_2d(w4 + b * 256, &g.mW4, 8 * b, 0, tbar_a);
         }
     }
-    for (int i = threadIdx.x; i < kHid; i += kThreads) {
+    for (int i = threadIdx.x; i < kHid; i += kFusedThreads) {
         sb[i] = g.b1[i];
         sb[kHid + i] = g.b2[i];
         sb[2 * kHid + i] = g.b3[i];
@@ -571,7 +576,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ 
     constexpr uint32_t kIdH = make_idesc(kTileM, kHid), kIdO = make_idesc(kTileM, kOutPad);
     uint32_t phase = 0, tphase = 0;
     bool pending = true;  // a TMA transaction on tbar not yet waited for (uniform across the CTA)
-    const int r = 32 * warp + lane;  // this thread's row of the tile
+    const int r = 32 * quarter + lane;  // this thread's row of the tile
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t m = tile * kTileM + r;
         // this tile's input rows (and, on the first tile, the weights)
@@ -619,11 +624,12 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ 
                 }
                 pending = true;
             }
-            const uint32_t trow = tmem + ((uint32_t)(32 * warp) << 16);
+            const uint32_t trow = tmem + ((uint32_t)(32 * quarter) << 16);
             if (layer < 3) {
-                // bias, GELU, BF16 -> the next product's A operand
+                // bias, GELU, BF16 -> the next product's A operand (this warp's
+                // half of the columns)
                 const float* bias = sb + layer * kHid;
-                for (int c0 = 0; c0 < kHid; c0 += 16) {
+                for (int c0 = half * (kHid / 2); c0 < (half + 1) * (kHid / 2); c0 += 16) {
                     uint32_t v[16];
                     tmem_ld16(trow + (uint32_t)c0, v);
                     uint32_t h[8];
@@ -638,7 +644,7 @@ __global__ void __launch_bounds__(kThreads) k_mlp_fused(const __grid_constant__ 
                     *reinterpret_cast<uint4*>(chunk + tile_off(r, c0 % kChunkK + 8)) =
                         make_uint4(h[4], h[5], h[6], h[7]);
                 }
-            } else {
+            } else if (half == 0) {
                 uint32_t v[16];
                 tmem_ld16(trow, v);
                 if (m < g.M)
@@ -999,7 +1005,7 @@ int pd_mlp_forward(pd_mlp* n, const void* dev_x, int64_t M, float* dev_y, void* 
     a.b1 = n->b1, a.b2 = n->b2, a.b3 = n->b3, a.b4 = n->b4;
     a.Y = dev_y, a.err = n->err, a.spin_limit = kSpinLimit;
     const unsigned grid = (unsigned)std::max<int64_t>(1, std::min<int64_t>(ntiles, 2 * (int64_t)sms));
-    k_mlp_fused<<<grid, kThreads, kFusedSmem, s>>>(a);
+    k_mlp_fused<<<grid, kFusedThreads, kFusedSmem, s>>>(a);
     n->launches++;
     if (cudaGetLastError() != cudaSuccess) return PD_ERR_CUDA;
     int herr = 0;
