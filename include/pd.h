@@ -113,6 +113,12 @@ typedef struct pd_ctx pd_ctx;
 pd_ctx* pd_create(const pd_params* p, int* status);
 /* Base_Free (Memory.cu:276-284, which re-allocates instead of freeing). */
 int pd_destroy(pd_ctx* ctx);
+/* Test hook (no reference counterpart): from now on, the n-th device
+ * allocation of pd_create (counting from 0) is refused once, as if the device
+ * were out of memory, and that pd_create returns NULL with PD_ERR_NOMEM after
+ * releasing what it had allocated; n = -1 clears the hook.  Lets a caller
+ * check the clean-up of a partly built context without exhausting a GPU. */
+int pd_debug_fail_allocation(int n);
 int pd_get_params(const pd_ctx* ctx, pd_params* out);
 /* Replace the parameters (same N/dim/model; a batch keeps its dt);
  * cudaMemcpyToSymbol(dp, ...) of the drivers. */

@@ -27,6 +27,7 @@ _SIGS = {
     "pd_params_derive": (I32, [P(PDParams), I32, I32, I32] + [D] * 12 + [I32]),
     "pd_create": (VP, [P(PDParams), P(I32)]),
     "pd_destroy": (I32, [VP]),
+    "pd_debug_fail_allocation": (I32, [I32]),
     "pd_get_params": (I32, [VP, P(PDParams)]),
     "pd_set_params": (I32, [VP, P(PDParams)]),
     "pd_get_field": (I32, [VP, I32, VP, SZ, VP]),

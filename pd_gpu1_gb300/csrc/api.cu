@@ -5,6 +5,7 @@
 // Host arithmetic that must match the reference (parameter derivation,
 // coordinates) is written with the reference's operand order and this file's
 // host code is compiled with -ffp-contract=off.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 
@@ -201,6 +202,21 @@ static int graph_chunk(pd_ctx* c, const Key& k, cudaStream_t s, F body) {
 using namespace pdg;
 
 // ---------------------------------------------------------------------------
+// Test hook (pd_debug_fail_allocation): device allocations of pd_create
+// still to go before one is refused as if the device were out of memory; -1:
+// none is refused.
+static std::atomic<int> g_alloc_countdown{-1};
+
+template <class T>
+static bool ctx_alloc(T** ptr, size_t bytes) {
+    const int k = g_alloc_countdown.load();
+    if (k >= 0) {
+        g_alloc_countdown.store(k - 1);
+        if (k == 0) return false;
+    }
+    return cudaMalloc(ptr, bytes) == cudaSuccess;
+}
+
 extern "C" {
 
 const char* pd_status_string(int status) {
@@ -277,6 +293,12 @@ int pd_params_derive(pd_params* p, int dim, int model, int mode, double dt, doub
     return PD_OK;
 }
 
+int pd_debug_fail_allocation(int n) {
+    if (n < -1) return PD_ERR_ARG;
+    g_alloc_countdown.store(n);
+    return PD_OK;
+}
+
 pd_ctx* pd_create(const pd_params* p, int* status) {
     auto fail = [&](int st) -> pd_ctx* {
         if (status) *status = st;
@@ -295,17 +317,17 @@ pd_ctx* pd_create(const pd_params* p, int* status) {
     }
     const size_t nb = (size_t)p->N * 8;
     bool ok = true;
-    for (int f = 0; f < kNodeDoubleFields && ok; f++) ok = cudaMalloc(&c->nf[f], nb) == cudaSuccess;
+    for (int f = 0; f < kNodeDoubleFields && ok; f++) ok = ctx_alloc(&c->nf[f], nb);
     for (int b = 0; b < 2 && ok; b++)
-        ok = cudaMalloc(&c->posxy[b], 2 * nb) == cudaSuccess && cudaMalloc(&c->posz[b], nb) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->NN, (size_t)p->N * 4) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->rowptr, ((size_t)p->N + 1) * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->node_a, 2 * nb) == cudaSuccess && cudaMalloc(&c->node_b, nb) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->partials, (size_t)kMaxPartials * 4 * 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->ticket, 4 * sizeof(unsigned)) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->cn, 8) == cudaSuccess && cudaMalloc(&c->red_out, 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->res, 8) == cudaSuccess;
-    ok = ok && cudaMalloc(&c->cyl, sizeof(CylDev)) == cudaSuccess;
+        ok = ctx_alloc(&c->posxy[b], 2 * nb) && ctx_alloc(&c->posz[b], nb);
+    ok = ok && ctx_alloc(&c->NN, (size_t)p->N * 4);
+    ok = ok && ctx_alloc(&c->rowptr, ((size_t)p->N + 1) * 8);
+    ok = ok && ctx_alloc(&c->node_a, 2 * nb) && ctx_alloc(&c->node_b, nb);
+    ok = ok && ctx_alloc(&c->partials, (size_t)kMaxPartials * 4 * 8);
+    ok = ok && ctx_alloc(&c->ticket, 4 * sizeof(unsigned));
+    ok = ok && ctx_alloc(&c->cn, 8) && ctx_alloc(&c->red_out, 8);
+    ok = ok && ctx_alloc(&c->res, 8);
+    ok = ok && ctx_alloc(&c->cyl, sizeof(CylDev));
     if (!ok) {
         pd_destroy(c);
         cudaGetLastError();

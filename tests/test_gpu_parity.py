@@ -860,3 +860,42 @@ def test_adr_solve_residual_is_the_last_steps(E):
             want = float(np.sqrt(np.sum(fx * fx) + np.sum(fy * fy)))
             assert want > 0.0
             assert r == pytest.approx(want, rel=1e-12)
+
+
+def test_failed_create_releases_its_allocations(E):
+    """Allocation failure, injected on the host (pd_debug_fail_allocation):
+    pd_create refused at every one of its device allocations in turn returns
+    NULL with PD_ERR_NOMEM (-6), frees what it had allocated (device memory
+    back to where it started), and the next pd_create succeeds."""
+    import ctypes as C
+
+    import torch
+
+    from pd_gpu1_gb300._lib import lib
+
+    L = lib()
+    p = E.derive_params(2, 1, 2, 1e-7, 3, 5e-4, 0.0, 5e-4, 0.02, 0.015, 0.0, 192e9, 1.0 / 3.0, 8000.0, 0.04472)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    refused = 0
+    try:
+        for n in range(200):
+            assert L.pd_debug_fail_allocation(n) == 0
+            st = C.c_int(0)
+            ctx = L.pd_create(C.byref(p), C.byref(st))
+            if ctx:  # n is past the last allocation
+                assert st.value == 0
+                assert L.pd_destroy(ctx) == 0
+                break
+            assert st.value == -6, (n, st.value)
+            refused += 1
+    finally:
+        L.pd_debug_fail_allocation(-1)
+    assert refused > 30  # every node field, the position buffers and the scratch
+    torch.cuda.synchronize()
+    free1 = torch.cuda.mem_get_info()[0]
+    assert abs(free1 - free0) <= 16 << 20, (free0, free1)
+    with E.Engine(p) as eng:  # the hook is off again
+        eng.coord_plate()
+        eng.find_neighbor_gpu()
+        assert eng.num_bonds > 0
