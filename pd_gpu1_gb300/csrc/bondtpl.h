@@ -375,5 +375,46 @@ PD_BT_HD bool exceeds(f2 e, double s0, float s0f, const TT& T, float dl) {
     return pair_sum_f64(e) > ecrit;
 }
 
+// The exact double of a float from its IEEE fields (zero and subnormal
+// floats give zero): no FP64 conversion instruction.
+PD_BT_HD double f64_exact(float f) {
+    const uint32_t b = fbits(f), mag = b & 0x7fffffffu;
+    if (mag < 0x00800000u) return 0.0;
+    const uint32_t hi = (b & 0x80000000u) | ((mag >> 3) + (896u << 20));
+    return dfrom(((uint64_t)hi << 32) | (uint64_t)(uint32_t)(mag << 29));
+}
+
+// One component's term of the ADR damping numerator (kernel_cnn,
+// Integrate.cu:17-33),
+//   -u^2 (F/m - F_old/m) / (dt vh),
+// as -u^2 ((F - F_old) (1/m)) / (dt vh) with both divisions through
+// reciprocals: 1/m (IEEE-rounded, rmass) and 1/(dt vh) from the FP32
+// estimate of the divisor's leading bits refined by two Newton steps in FP64
+// (relative error near 2^-53).  About eleven FP64 instructions instead of the
+// reference's two quotients and one IEEE division (about 24).  The term is
+// within a few units in the last place of the exact value of the reference's
+// formula (the reference's own evaluation loses more when F and F_old are
+// close); the damping coefficient sums these terms over all nodes in another
+// order than the reference's in any case.  Divisors outside [2^-100, 2^101)
+// in magnitude take the IEEE division.
+PD_BT_HD double damping_term(double u, double f, double fo, double rmass, double dt, double vh) {
+    const double d = dt * vh;
+    const double n = -1.0 * u * u * ((f - fo) * rmass);
+    const uint64_t b = dbits(d);
+    const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+    const uint32_t mag = hi & 0x7fffffffu, E = mag >> 20;
+    if (E < 923u || E > 1123u) return n / d;
+    // d's leading bits as a float (truncated), then its reciprocal estimate
+    const float df = ffrom((hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29));
+    double y = f64_exact(rcp_seed(df));
+    y = fma(y, fma(-d, y, 1.0), y);
+    y = fma(y, fma(-d, y, 1.0), y);
+#if defined(__CUDA_ARCH__)
+    return __dmul_rn(n, y);  // a product of its own (no contraction into the caller's sum)
+#else
+    return n * y;
+#endif
+}
+
 }  // namespace bt
 }  // namespace pdg

@@ -275,29 +275,9 @@ __device__ __forceinline__ void contact_node(const KParams& P, const CylDev& cy,
     }
 }
 
-// One component's term of kernel_cnn (Integrate.cu:17-33),
-//   -u^2 (F/m - F_old/m) / (dt vh),
-// as -u^2 ((F - F_old) / m) / (dt vh) with both divisions through
-// reciprocals: 1/m (IEEE-rounded on the host) and 1/(dt vh) from the FP32
-// estimate of the divisor's leading bits refined by two Newton steps in FP64
-// (relative error near 2^-53).  About eleven FP64 instructions instead of the
-// reference's two quotients and one IEEE division (about 24).  The term
-// differs from the reference's in its last bits; the damping coefficient sums
-// these terms over all nodes in another order than the reference's in any
-// case.  Divisors outside [2^-100, 2^101) in magnitude take the IEEE division.
-__device__ __forceinline__ double damping_term(double u, double f, double fo, double rmass, double dt, double vh) {
-    const double d = dt * vh;
-    const double n = -1.0 * u * u * ((f - fo) * rmass);
-    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    const unsigned mag = hi & 0x7fffffffu, E = mag >> 20;
-    if (E < 923u || E > 1123u) return n / d;
-    // d's leading bits as a float (truncated), then its reciprocal estimate
-    const float df = __uint_as_float((hi & 0x80000000u) | ((mag - (896u << 20)) << 3) | (lo >> 29));
-    double y = f64_of_f32s(rcp_approx_f32(df));
-    y = fma(y, fma(-d, y, 1.0), y);
-    y = fma(y, fma(-d, y, 1.0), y);
-    return __dmul_rn(n, y);  // a product of its own (no contraction into the caller's sum)
-}
+// The ADR damping terms (kernel_cnn) through reciprocals: bt::damping_term
+// (bondtpl.h, checked on the host against quadruple precision).
+using bt::damping_term;
 
 // v != 0.0 on the integer pipe (+0 and -0 compare equal to zero, NaN does not).
 __device__ __forceinline__ bool nonzero(double v) { return (__double_as_longlong(v) << 1) != 0; }

@@ -3,8 +3,9 @@
 quadruple precision: the 2-D bond on three million lattice bonds (extension
 and force within 2e-13 of the strain scale, hardware-like reciprocal seeds),
 its break decision against the double test on two million extensions around
-the threshold, and the 3-D stretch (extension, 1/L and direction) on the
-bonds of a 3-D lattice."""
+the threshold, the 3-D stretch (extension, 1/L and direction) on the
+bonds of a 3-D lattice, and the ADR damping term (within 8 units of 2^-53 of
+the exact value of the reference's formula)."""
 import os
 import shutil
 import subprocess
@@ -28,3 +29,4 @@ def test_bond_arithmetic_against_quad_precision(tmp_path):
     assert out.returncode == 0, out.stdout + out.stderr
     assert "break decisions: 2000000 checked, 0 differ" in out.stdout
     assert "3-D stretch: worst extension" in out.stdout
+    assert "damping terms: " in out.stdout
