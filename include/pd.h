@@ -299,8 +299,10 @@ int pd_mlp_num_params(void);
 int pd_mlp_set_params(pd_mlp* net, const float* host, int64_t count);
 int pd_mlp_get_params(pd_mlp* net, float* host, int64_t count);
 /* y[M][2] = net(x[M][16]) (device pointers, x 16-byte and y 8-byte aligned;
- * any M): one persistent kernel runs the four layers per 128-row tile with
- * the weights resident in shared memory and the activations kept on chip. */
+ * 1 <= M <= 2^31 - 129, else PD_ERR_ARG): one persistent kernel runs the four
+ * layers per 128-row tile with the weights resident in shared memory and the
+ * activations kept on chip; weights and input tiles arrive by TMA (tensor
+ * maps encoded per call; PD_ERR_CUDA if the driver cannot encode them). */
 int pd_mlp_forward(pd_mlp* net, const void* dev_x, int64_t M, float* dev_y, void* stream);
 /* The same forward pass layer by layer (one tensor-core product per layer
  * over max_rows blocks, activations through device memory): a check of
