@@ -71,3 +71,30 @@ def test_damage_parity_of_a_short_precracked_run():
     # a reference field that was never computed (all zero) is reported as a mismatch
     bad = bench.damage_parity(d, np.zeros_like(d), x[: p.N_int], None, p.delta, 20)
     assert bad["damaged_nodes"] == 0 and bad["damage_nodes_equal"] < 1.0
+
+
+def test_roofline_tables_cover_the_step_workloads():
+    """The ncu-derived tables behind the bench line's roofline: every explicit
+    workload has a DRAM-traffic and an FP64-count entry, each at least the
+    bond loop's own count (kernel source) and within a sane range, and the
+    FP64 block takes the ncu count (per-node work included) where there is
+    one."""
+    sys.path[:0] = [ROOT]
+    import bench
+
+    for w in ["crack_branching_2d_pmb_verlet", "kalthoff_winkler_3d_pmb_verlet", "plate_crack_grow_2d_state_verlet",
+              "kalthoff_winkler_3d_state_verlet"]:
+        assert w in bench.TRAFFIC and w in bench.FP64_NCU_PER_BOND, w
+        per_bond, per_node, src = bench.TRAFFIC[w]
+        assert 12.125 <= per_bond <= 200.0 and per_node >= 0.0 and src
+    loop = {"crack_branching_2d_pmb_verlet": (1, 2), "kalthoff_winkler_3d_pmb_verlet": (1, 3),
+            "plate_crack_grow_2d_state_verlet": (2, 2), "kalthoff_winkler_3d_state_verlet": (2, 3)}
+    for w, (model, dim) in loop.items():
+        n_ncu, src = bench.FP64_NCU_PER_BOND[w]
+        assert bench.FP64_EXEC_PER_BOND[(model, dim)] <= n_ncu <= 2.0 * bench.FP64_EXEC_PER_BOND[(model, dim)], w
+        blk = bench.fp64_block(model, dim, 1_000_000, 1.0, 500.0, w)
+        assert blk["executed_per_bond_ncu"] == n_ncu
+        assert abs(blk["achieved_ginst_s"] - n_ncu) < 1e-9  # 1e6 bonds in 1 ms: n per ns
+        assert abs(blk["frac"] - n_ncu / 500.0) < 1e-12
+    blk = bench.fp64_block(1, 2, 1_000_000, 1.0, 500.0, "batch_plate_adr_2d_pmb")  # no ncu count
+    assert "executed_per_bond_ncu" not in blk and blk["executed_per_bond"] == 4
